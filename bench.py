@@ -1,0 +1,387 @@
+"""Benchmark: Canvas.points count (and mean) over 1e8 points at 1024x1024 on GB300.
+
+Workload (the full-reduction-set config, 1e8 rows): x, y float32 from a
+seeded 5-Gaussian mixture, v float64 ~ lognormal(0, 1), cat int8 over 8
+categories; Canvas 1024x1024 over [-4, 4]^2.  One step = one
+``Canvas.points(frame, 'x', 'y', ds.count())`` call through the public API
+with the columns resident in HBM.  The inputs (800 MB of x/y) are larger
+than L2, so no flush is needed between steps.
+
+The JSON line also carries:
+  roofline      -- the count kernel alone: algorithmic bytes (8 B/point read
+                   + 4 B/pixel written) / CUDA-event kernel time vs the
+                   measured HBM copy bandwidth;
+  mean          -- the same for Canvas.points(..., ds.mean('v'));
+  full_set      -- the whole reduction set of the config plus eq_hist;
+  e2e           -- count with host (pinned) inputs: H2D of x/y, the call, D2H
+                   of the aggregate, all inside the timed region;
+  cpu_baseline  -- the CPU oracle (a restatement of the reference's numba
+                   loop) on one host core, on a bounded sample;
+  clocks        -- nvidia-smi samples taken during the timed region.
+
+``--impl reference`` times the reference's CPU algorithm (the oracle port,
+the reference itself cannot be imported on this machine) over the same
+workload with all host threads: rows split into one partition per thread,
+partial aggregates summed, as datashader's dask path does.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gpoints/s, Canvas.points count/mean 1e8 pts @1024²; viewport p50/p99 ms"
+WORKLOAD = "Canvas.points count, 1e8 float32 points (5-Gaussian mixture), 1024x1024 canvas over [-4,4]^2"
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.gpu), "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def _dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU side
+
+def _oracle_count_threads(xs, ys, threads, width, height, x_range, y_range):
+    """The reference's CPU algorithm (oracle port) over row partitions, one per thread."""
+    import oracle
+    n = xs.size
+    bounds = np.linspace(0, n, threads + 1).astype(np.int64)
+    parts = [None] * threads
+
+    def work(k):
+        a, b = bounds[k], bounds[k + 1]
+        parts[k] = oracle.points({"x": xs[a:b], "y": ys[a:b]}, "x", "y", width, height,
+                                 x_range, y_range, [oracle.spec("count")])[0]
+
+    ts = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return np.sum(parts, axis=0, dtype=np.uint32)
+
+
+def cpu_baseline(sample_n=20_000_000, threads=1):
+    from datashader_gb300 import synthetic
+    x, y = synthetic.gaussian_mixture_np(sample_n, seed=0, dtype=np.float32)
+    xs, ys = x.astype(np.float64), y.astype(np.float64)
+    _oracle_count_threads(xs[:100_000], ys[:100_000], 1, 1024, 1024, (-4, 4), (-4, 4))   # warm
+    t0 = time.perf_counter()
+    _oracle_count_threads(xs, ys, threads, 1024, 1024, (-4, 4), (-4, 4))
+    dt = time.perf_counter() - t0
+    return sample_n / dt / 1e9, dt
+
+
+def run_reference(args):
+    world, rank, _ = _dist_init(args)
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    from datashader_gb300 import synthetic
+    n = min(args.n, args.reference_sample)
+    x, y = synthetic.gaussian_mixture_np(n, seed=0, dtype=np.float32)
+    xs, ys = x.astype(np.float64), y.astype(np.float64)
+    for _ in range(args.warmup):
+        _oracle_count_threads(xs, ys, threads, 1024, 1024, (-4, 4), (-4, 4))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _oracle_count_threads(xs, ys, threads, 1024, 1024, (-4, 4), (-4, 4))
+    dt = time.perf_counter() - t0
+    v = n * args.steps / dt / 1e9
+    sample = f"{n} rows of the same distribution per step, {threads} threads, one row partition per thread"
+    line = {"metric": METRIC, "value": v, "unit": "Gpoints/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "n_points": n, "canvas": [1024, 1024]},
+            "cpu_baseline": {"value": v, "unit": "Gpoints/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "datashader cannot be imported here (numba/pandas/xarray absent): the timed CPU "
+                    "implementation is the C restatement of its numba CPU loop (oracle/)"}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU side
+
+def _events_time(fn, k, stream):
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    for i in range(k):
+        starts[i].record(stream)
+        fn()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def run_gpu(args):
+    import torch
+    world, rank, local = _dist_init(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import datashader_gb300 as ds
+    from datashader_gb300 import _native as N
+    from datashader_gb300 import synthetic
+    from datashader_gb300.compiler import compile_plan
+    from datashader_gb300.core import Executor, dsgb_dtype
+    from datashader_gb300.glyphs import Point
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    n = args.n
+    x, y = synthetic.gaussian_mixture_torch(n, seed=rank, device=dev)
+    v = synthetic.lognormal_torch(n, seed=100 + rank, device=dev)
+    cat = synthetic.categories_torch(n, 8, seed=200 + rank, device=dev)
+    frame = ds.TensorFrame({"x": x, "y": y, "v": v, "cat": cat}, categories={"cat": list(range(8))})
+    cvs = ds.Canvas(plot_width=1024, plot_height=1024, x_range=(-4, 4), y_range=(-4, 4))
+    peak, peak_kind = measured_peak()
+
+    def step_count():
+        return cvs.points(frame, "x", "y", ds.count())
+
+    # ---- headline: count through the public API, inputs resident in HBM
+    for _ in range(args.warmup):
+        step_count()
+    torch.cuda.synchronize()
+    _barrier(world)
+    with ClockSampler(local) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t_start.record(stream)
+        for _ in range(args.steps):
+            step_count()
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        elapsed_ms = t_start.elapsed_time(t_end)
+    _barrier(world)
+    elapsed_ms = _max_over_ranks(world, elapsed_ms)
+    value = n * world * args.steps / (elapsed_ms / 1e3) / 1e9
+
+    # ---- kernel-only timing for the roofline (count and mean kernels)
+    def kernel_runner(agg):
+        plan = compile_plan(agg, frame)
+        ex = Executor(frame, plan, Point("x", "y"))
+        ex.allocate(1024, 1024, dev)
+        x_st = cvs.x_axis.compute_scale_and_translate((-4, 4), 1024)
+        y_st = cvs.y_axis.compute_scale_and_translate((-4, 4), 1024)
+        cv = N.CanvasDesc(1024, 1024, 0, 0, x_st[0], x_st[1], y_st[0], y_st[1], -4.0, 4.0, -4.0, 4.0)
+        L = N.lib()
+        N.check(L.dsgb_bases_init(ex.bases, len(plan.bases), 1024 * 1024, stream.cuda_stream), "init")
+
+        def launch():
+            N.check(L.dsgb_points(ex.cols, len(ex.names), n, 0, 0, 1, ctypes.byref(cv), ex.bases,
+                                  len(plan.bases), ex.outs, 0, N.FLAG_NO_INIT | N.FLAG_NO_FINALIZE,
+                                  stream.cuda_stream), "dsgb_points")
+        return launch
+
+    def roofline(agg, bytes_per_point, bytes_per_pixel, k):
+        launch = kernel_runner(agg)
+        for _ in range(3):
+            launch()
+        times = _events_time(launch, k, stream)
+        avg_ms = sum(times) / len(times)
+        alg = n * bytes_per_point + 1024 * 1024 * bytes_per_pixel
+        achieved = alg / (avg_ms / 1e3) / 1e9
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": alg, "kernel_ms": avg_ms,
+                "kernel_gpts": n / (avg_ms / 1e3) / 1e9}
+
+    rl_count = roofline(ds.count(), 8, 4, args.steps)
+    rl_mean = roofline(ds.mean("v"), 16, 12, args.steps)
+
+    # mean through the public API
+    for _ in range(2):
+        cvs.points(frame, "x", "y", ds.mean("v"))
+    mean_ms = _events_time(lambda: cvs.points(frame, "x", "y", ds.mean("v")), args.steps, stream)
+    mean_ms = sum(mean_ms) / len(mean_ms)
+
+    # the whole reduction set of the config + eq_hist on the count
+    full = ds.summary(count=ds.count(), sum=ds.sum("v"), mean=ds.mean("v"), max=ds.max("v"),
+                      min=ds.min("v"), first=ds.first("v"), where=ds.where(ds.max("v")),
+                      by_cat=ds.by("cat", ds.count()))
+
+    def step_full():
+        a = cvs.points(frame, "x", "y", full)
+        ds.tf.shade(a["count"], how="eq_hist")
+
+    step_full()
+    full_ms = _events_time(step_full, max(2, args.steps // 4), stream)
+    full_ms = sum(full_ms) / len(full_ms)
+
+    # ---- e2e: host (pinned) inputs -> H2D -> Canvas.points -> D2H, per step
+    xh = x.cpu().pin_memory()
+    yh = y.cpu().pin_memory()
+    xd = torch.empty_like(x)
+    yd = torch.empty_like(y)
+
+    def step_e2e():
+        xd.copy_(xh, non_blocking=True)
+        yd.copy_(yh, non_blocking=True)
+        agg = cvs.points(ds.TensorFrame({"x": xd, "y": yd}), "x", "y", ds.count())
+        return agg.data.cpu()
+
+    for _ in range(2):
+        step_e2e()
+    torch.cuda.synchronize()
+    _barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    e2e_s = _max_over_ranks(world, time.perf_counter() - t0)
+    e2e = {"value": n * world * args.steps / e2e_s / 1e9, "unit": "Gpoints/s",
+           "h2d_bytes_per_step": int(xh.numel() * 4 + yh.numel() * 4),
+           "d2h_bytes_per_step": 1024 * 1024 * 4}
+
+    if rank == 0:
+        base = None
+        if world == 1 and not args.no_cpu_baseline:
+            gpts, dt = cpu_baseline(args.cpu_sample)
+            base = {"value": gpts, "unit": "Gpoints/s", "cores": 1, "kind": "port",
+                    "sample": f"{args.cpu_sample} rows of the same distribution, count, one thread, "
+                              f"{dt:.2f} s"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gpoints/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_points": n, "canvas": [1024, 1024],
+                       "x_range": [-4, 4], "coords": "float32", "reduction": "count",
+                       "l2": "inputs (800 MB) larger than L2, no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {k: rl_count[k] for k in ("bound", "achieved", "peak", "unit", "frac", "traffic")},
+            "roofline_detail": rl_count,
+            "mean": {"value": n / (mean_ms / 1e3) / 1e9, "unit": "Gpoints/s", "ms_per_step": mean_ms,
+                     "roofline": rl_mean},
+            "full_set": {"ms_per_step": full_ms, "value": n / (full_ms / 1e3) / 1e9, "unit": "Gpoints/s",
+                         "reductions": "count,sum,mean,max,min,first,where(max),by(cat,count) + eq_hist"},
+            "cpu_baseline": base,
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=100_000_000)
+    ap.add_argument("--cpu-sample", type=int, default=20_000_000)
+    ap.add_argument("--reference-sample", type=int, default=100_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,424 @@
+"""Canvas, axes and the bypixel pipeline on the GPU.
+
+Mirrors datashader/core.py (Canvas 163-478, Axis 45-145, bypixel
+1334-1446) and datashader/data_libraries/pandas.py:26-66 (the
+create / extend / finalize orchestration).  Sources are
+:class:`TensorFrame` objects -- named 1-D torch tensors on a CUDA device,
+with category labels for categorical columns -- in place of pandas / cuDF
+frames.  Host (numpy) columns are accepted too and copied to the device
+first.  All aggregation runs in libdsgb's sm_103a kernels; there is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from numbers import Number
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import reductions as rd
+from .compiler import compile_plan
+from .glyphs import Point, LineAxis0
+
+
+# ----------------------------------------------------------------- sources
+
+_TORCH_TO_DSGB = {
+    torch.float32: N.F32, torch.float64: N.F64, torch.int8: N.I8, torch.uint8: N.U8,
+    torch.int16: N.I16, torch.int32: N.I32, torch.int64: N.I64, torch.uint32: N.U32,
+    torch.bool: N.BOOL,
+}
+_KIND = {torch.float32: "f", torch.float64: "f", torch.float16: "f", torch.bfloat16: "f",
+         torch.int8: "i", torch.int16: "i", torch.int32: "i", torch.int64: "i",
+         torch.uint8: "u", torch.uint32: "u", torch.bool: "b"}
+
+
+def dsgb_dtype(t: torch.Tensor) -> int:
+    try:
+        return _TORCH_TO_DSGB[t.dtype]
+    except KeyError:
+        raise TypeError(f"unsupported column dtype {t.dtype}") from None
+
+
+class TensorFrame:
+    """Named, equal-length 1-D columns on one CUDA device.
+
+    ``categories`` maps a column name to its category labels; the column
+    itself then holds integer codes (the pandas Categorical ``.cat.codes``).
+    Numpy columns are copied to ``device`` (pinned staging) on construction.
+    ``row_offset`` is added to row indexes (first/last/where), like the
+    ``_datashader_row_offset`` attribute of a partition (reductions.py:85-113).
+    """
+
+    def __init__(self, columns, categories=None, device=None, row_offset=0):
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(device)
+        self._cols = {}
+        n = None
+        for k, v in dict(columns).items():
+            t = self._to_device(v)
+            if t.dim() != 1:
+                raise ValueError(f"column {k!r} must be 1-D")
+            if n is None:
+                n = t.shape[0]
+            elif t.shape[0] != n:
+                raise ValueError("columns must have equal length")
+            self._cols[k] = t
+        self._n = n or 0
+        self._cats = {k: list(v) for k, v in (categories or {}).items()}
+        for k in self._cats:
+            if k not in self._cols:
+                raise ValueError(f"categories given for unknown column {k!r}")
+        self.row_offset = int(row_offset)
+
+    def _to_device(self, v):
+        if isinstance(v, torch.Tensor):
+            t = v
+        else:
+            a = np.ascontiguousarray(v)
+            t = torch.from_numpy(a)
+            if self.device.type == "cuda":
+                t = t.pin_memory()
+        if t.device != self.device:
+            t = t.to(self.device, non_blocking=True)
+        return t.contiguous()
+
+    # schema interface used by reductions / compiler
+    def __contains__(self, name):
+        return name in self._cols
+
+    def __getitem__(self, name):
+        return self._cols[name]
+
+    def __len__(self):
+        return self._n
+
+    @property
+    def columns(self):
+        return list(self._cols)
+
+    def dtype_kind(self, name):
+        if name in self._cats:
+            return "c"
+        return _KIND.get(self._cols[name].dtype, "?")
+
+    def is_categorical(self, name):
+        return name in self._cats
+
+    def categories(self, name):
+        return self._cats[name]
+
+    def signature(self):
+        return tuple((k, str(v.dtype), tuple(self._cats.get(k, ()))) for k, v in self._cols.items())
+
+
+def as_frame(source):
+    if isinstance(source, TensorFrame):
+        return source
+    if isinstance(source, dict):
+        return TensorFrame(source)
+    raise ValueError("source must be a TensorFrame or a dict of columns")
+
+
+# -------------------------------------------------------------------- axes
+
+class Axis:
+    """core.py:45-111."""
+
+    def compute_scale_and_translate(self, range, n):
+        """core.py:62-81: s = n/(end-start), t = -start*s (Python floats)."""
+        start, end = map(self.mapper, range)
+        s = n / (end - start)
+        t = -start * s
+        return s, t
+
+    def compute_index(self, st, n):
+        """core.py:83-99: pixel-centre coordinates."""
+        px = np.arange(n) + 0.5
+        s, t = st
+        return self.inverse_mapper((px - t) / s)
+
+    def validate(self, range):
+        pass
+
+
+class LinearAxis(Axis):
+    is_log = False
+
+    @staticmethod
+    def mapper(val):
+        return val
+
+    @staticmethod
+    def inverse_mapper(val):
+        return val
+
+
+class LogAxis(Axis):
+    is_log = True
+
+    @staticmethod
+    def mapper(val):
+        return math.log10(float(val))
+
+    @staticmethod
+    def inverse_mapper(val):
+        return 10 ** val
+
+    def validate(self, range):
+        if range is None:
+            return
+        if range[0] <= 0 or range[1] <= 0:
+            raise ValueError("Range values must be >0 for logarithmic axes")
+
+
+_axis_lookup = {"linear": LinearAxis(), "log": LogAxis()}
+
+
+# ----------------------------------------------------------------- results
+
+class Aggregate:
+    """A 2-D (or 3-D categorical) aggregate: the xr.DataArray of the reference
+    (pandas.py:61-66: dims [y, x(, cat)], coords = pixel centres, attrs
+    x_range / y_range), with ``data`` a CUDA tensor."""
+
+    def __init__(self, data, dims, coords, attrs, name=None):
+        self.data = data
+        self.dims = list(dims)
+        self.coords = dict(coords)
+        self.attrs = dict(attrs)
+        self.name = name
+
+    @property
+    def values(self):
+        return self.data.cpu().numpy()
+
+    def to_numpy(self):
+        return self.values
+
+    @property
+    def shape(self):
+        return tuple(self.data.shape)
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+    @property
+    def ndim(self):
+        return self.data.dim()
+
+    @property
+    def x_range(self):
+        return self.attrs.get("x_range")
+
+    @property
+    def y_range(self):
+        return self.attrs.get("y_range")
+
+    def __repr__(self):
+        return f"<Aggregate {self.name or ''} dims={self.dims} shape={self.shape} dtype={self.dtype}>"
+
+
+class AggregateSet(dict):
+    """The xr.Dataset returned for a summary() reduction."""
+
+    def __getattr__(self, k):
+        try:
+            return self[k]
+        except KeyError:
+            raise AttributeError(k) from None
+
+
+# ------------------------------------------------------------------ canvas
+
+def _validate_xy(glyph, x, y, geometry):
+    if geometry is not None:
+        raise NotImplementedError("geometry columns are not supported on the GPU path")
+    if x is None or y is None:
+        raise ValueError(f"{glyph} coordinates may be specified by providing both the x and y arguments")
+
+
+class Canvas:
+    """An abstract canvas representing the space in which to bin (core.py:163-185)."""
+
+    def __init__(self, plot_width=600, plot_height=600, x_range=None, y_range=None,
+                 x_axis_type="linear", y_axis_type="linear"):
+        self.plot_width = plot_width
+        self.plot_height = plot_height
+        self.x_range = None if x_range is None else tuple(x_range)
+        self.y_range = None if y_range is None else tuple(y_range)
+        self.x_axis = _axis_lookup[x_axis_type]
+        self.y_axis = _axis_lookup[y_axis_type]
+
+    def points(self, source, x=None, y=None, agg=None, geometry=None):
+        """Compute a reduction by pixel, mapping data to pixels as points (core.py:187-232)."""
+        _validate_xy("Point", x, y, geometry)
+        if agg is None:
+            agg = rd.count()
+        return bypixel(source, self, Point(x, y), agg)
+
+    def line(self, source, x=None, y=None, agg=None, axis=0, geometry=None,
+             line_width=0, antialias=False):
+        """Compute a reduction by pixel, mapping data to pixels as one line
+        (LineAxis0 glyph, core.py:234-478)."""
+        _validate_xy("Line", x, y, geometry)
+        if agg is None:
+            agg = rd.any()
+        if line_width is None:
+            line_width = 0
+        if antialias and line_width != 0:
+            raise ValueError("Do not specify values for both the line_width and \n"
+                             "antialias keyword arguments; use line_width instead.")
+        if antialias:
+            line_width = 1.0
+        if axis != 0 or not (isinstance(x, (Number, str)) and isinstance(y, (Number, str))):
+            raise NotImplementedError("only the LineAxis0 glyph (axis=0, one x and one y column) "
+                                      "is on the GPU path")
+        glyph = LineAxis0(x, y)
+        glyph.set_line_width(line_width)
+        if glyph.antialiased:
+            non_cat = agg.reduction if isinstance(agg, rd.by) else agg
+            if not isinstance(non_cat, (rd.any, rd.count, rd.max, rd.min, rd.sum, rd.summary,
+                                        rd._sum_zero, rd._first_or_last, rd.mean,
+                                        rd._max_or_min_row_index, rd.where)):
+                raise NotImplementedError(
+                    f"{type(non_cat)} reduction not implemented for antialiased lines")
+        return bypixel(source, self, glyph, agg, antialias=glyph.antialiased)
+
+    def validate_ranges(self, x_range, y_range):
+        self.x_axis.validate(x_range)
+        self.y_axis.validate(y_range)
+
+    def validate_size(self, width, height):
+        if width <= 0 or height <= 0:
+            raise ValueError("Invalid size: plot_width and plot_height must be bigger than 0")
+
+    def validate(self):
+        self.validate_ranges(self.x_range, self.y_range)
+        self.validate_size(self.plot_width, self.plot_height)
+
+
+def bypixel(source, canvas, glyph, agg, *, antialias=False):
+    """core.py:1334-1359: validate, then run the GPU pipeline."""
+    frame = as_frame(source)
+    glyph.validate(frame)
+    agg.validate(frame)
+    canvas.validate()
+    return gpu_pipeline(frame, canvas, glyph, agg, antialias=antialias)
+
+
+def _column_bounds(frame, name, stream):
+    """Glyph._compute_bounds (glyph.py:51-78) on the device, then
+    maybe_expand_bounds (glyph.py:42-49)."""
+    t = frame[name]
+    col = N.Column(t.data_ptr(), dsgb_dtype(t), 0)
+    out = torch.empty(2, dtype=torch.float64, device=t.device)
+    N.check(N.lib().dsgb_bounds(ctypes.byref(col), t.numel(), out.data_ptr(), stream), "dsgb_bounds")
+    mn, mx = out.cpu().tolist()
+    if not (np.isfinite(mn) and np.isfinite(mx)):
+        mn, mx = -1.0, 1.0
+    elif mn == mx:
+        mn, mx = mn - 1, mn + 1
+    return mn, mx
+
+
+def _derived_columns(frame, plan):
+    cols = {}
+    for name, (col, modulo, offset) in plan.derived.items():
+        cols[name] = torch.remainder(frame[col].to(torch.int64) - offset, modulo).to(torch.int32)
+    return cols
+
+
+class Executor:
+    """Allocates the bases and outputs of a plan and calls the C ABI."""
+
+    def __init__(self, frame, plan, glyph):
+        self.frame = frame
+        self.plan = plan
+        self.glyph = glyph
+        derived = _derived_columns(frame, plan)
+        names = [glyph.x, glyph.y] + [c for c in plan.columns if c not in (glyph.x, glyph.y)]
+        self.names = names
+        self.tensors = [derived[n] if n in derived else frame[n] for n in names]
+        self.col_index = {n: i for i, n in enumerate(names)}
+        self.cols = (N.Column * len(names))(*[N.Column(t.data_ptr(), dsgb_dtype(t), 0) for t in self.tensors])
+
+    def allocate(self, height, width, device):
+        plan = self.plan
+        self.base_tensors = []
+        for b in plan.bases:
+            n = height * width * b.ncat * b.words
+            self.base_tensors.append(torch.empty(n, dtype=b.torch_dtype, device=device))
+        self.bases = (N.Base * max(1, len(plan.bases)))()
+        for i, (b, t) in enumerate(zip(plan.bases, self.base_tensors)):
+            self.bases[i] = N.Base(b.op, self.col_index[b.col] if b.col is not None else -1,
+                                   self.col_index[b.cat] if b.cat is not None else -1,
+                                   b.ncat, b.flags, 0, t.data_ptr())
+        outs = []
+        self.out_tensors = []
+        for key, o in plan.outputs:
+            nc = plan.bases[o.b0].ncat
+            shape = (height, width, nc) if o.categories is not None else (height, width)
+            if o.fin == 0:
+                t = self.base_tensors[o.b0].view(shape)
+            else:
+                t = torch.empty(shape, dtype=o.dtype, device=device)
+                outs.append(N.Output(o.fin, o.b0, o.b1,
+                                     self.col_index[o.col] if o.col is not None else -1, t.data_ptr()))
+            if o.as_bool:
+                t = t.view(torch.bool)
+            self.out_tensors.append(t)
+        self.outs = (N.Output * max(1, len(outs)))(*outs)
+        self.nouts = len(outs)
+
+
+def _results(plan, ex, coords, dims, attrs):
+    items = []
+    for (key, o), t in zip(plan.outputs, ex.out_tensors):
+        d = list(dims)
+        c = dict(coords)
+        if o.categories is not None:
+            d.append(o.cat_dim)
+            c[o.cat_dim] = list(o.categories)
+        items.append((key, Aggregate(t, d, c, attrs, name=key)))
+    if plan.outputs[0][0] is None:
+        return items[0][1]
+    return AggregateSet(items)
+
+
+def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=None):
+    """pandas.py:26-66 on the GPU: ranges, scale/translate, create+extend+finalize."""
+    if stream is None:
+        stream = torch.cuda.current_stream(frame.device).cuda_stream
+    plan = compile_plan(agg, frame, antialias=antialias)
+    x_range = canvas.x_range or _column_bounds(frame, glyph.x, stream)
+    y_range = canvas.y_range or _column_bounds(frame, glyph.y, stream)
+    canvas.validate_ranges(x_range, y_range)
+    width, height = canvas.plot_width, canvas.plot_height
+    x_st = canvas.x_axis.compute_scale_and_translate(x_range, width)
+    y_st = canvas.y_axis.compute_scale_and_translate(y_range, height)
+    x_axis = canvas.x_axis.compute_index(x_st, width)
+    y_axis = canvas.y_axis.compute_index(y_st, height)
+    ex = Executor(frame, plan, glyph)
+    ex.allocate(height, width, frame.device)
+    cv = N.CanvasDesc(width, height, int(canvas.x_axis.is_log), int(canvas.y_axis.is_log),
+                      x_st[0], x_st[1], y_st[0], y_st[1],
+                      float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]))
+    L = N.lib()
+    if isinstance(glyph, LineAxis0):
+        rc = L.dsgb_line_axis0(ex.cols, len(ex.names), len(frame), frame.row_offset, 0, 1, ctypes.byref(cv),
+                               float(glyph.line_width), 1, int(plan.overwrite), int(plan.use_2_stage),
+                               ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
+        N.check(rc, "dsgb_line_axis0")
+    else:
+        rc = L.dsgb_points(ex.cols, len(ex.names), len(frame), frame.row_offset, 0, 1, ctypes.byref(cv),
+                           ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
+        N.check(rc, "dsgb_points")
+    coords = {glyph.x_label: x_axis, glyph.y_label: y_axis}
+    dims = [glyph.y_label, glyph.x_label]
+    return _results(plan, ex, coords, dims, dict(x_range=x_range, y_range=y_range))

@@ -1,0 +1,327 @@
+// common.cu -- error reporting, base initialisation, finalize, autorange.
+//
+// bases_init restates the initial values of Reduction._create_*
+// (datashader/reductions.py:397-472) in their GPU base forms; finalize
+// restates the _finalize functions (reductions.py: sum 1091-1096, mean
+// 1290-1296, first/last 1369-1373, where 2152-2162) and make_finalize
+// (datashader/compiler.py:510-536).
+#include "dsgb_internal.cuh"
+
+#include <stdarg.h>
+#include <cmath>
+
+namespace dsgb {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_status(cudaError_t e, const char *what) {
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    return DSGB_E_CUDA;
+}
+
+int sm_count() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+    return n;
+}
+
+// ------------------------------------------------------------------ init
+
+__global__ void fill_u64_kernel(unsigned long long *p, int64_t n, unsigned long long v) {
+    for (int64_t i = gtid(); i < n; i += gstride()) p[i] = v;
+}
+__global__ void fill_pair_kernel(long long *p, int64_t n, long long a, long long b) {
+    for (int64_t i = gtid(); i < n; i += gstride()) { p[2 * i] = a; p[2 * i + 1] = b; }
+}
+
+static unsigned grid_for(int64_t n, int threads = 256) {
+    int sms = sm_count();
+    if (sms <= 0) sms = 148;
+    int64_t g = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)sms * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (unsigned)g;
+}
+
+int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st) {
+    for (int b = 0; b < nbases; ++b) {
+        const dsgb_base &B = bases[b];
+        const int64_t n = ncells * (B.ncat < 1 ? 1 : B.ncat);
+        if (!B.agg) { set_error("dsgb_bases_init: base %d has null agg", b); return DSGB_E_INVALID; }
+        cudaError_t e = cudaSuccess;
+        switch (B.op) {
+        case DSGB_BASE_COUNT: case DSGB_BASE_AA_CNT0:
+            e = cudaMemsetAsync(B.agg, 0, (size_t)n * 4, st); break;
+        case DSGB_BASE_ANY:
+            e = cudaMemsetAsync(B.agg, 0, (size_t)n, st); break;
+        case DSGB_BASE_SUM: case DSGB_BASE_AA_SUM:
+            e = cudaMemsetAsync(B.agg, 0, (size_t)n * 8, st); break;
+        case DSGB_BASE_MAX: case DSGB_BASE_AA_MAX:
+            fill_u64_kernel<<<grid_for(n), 256, 0, st>>>((unsigned long long *)B.agg, n,
+                                                          (unsigned long long)KEY_EMPTY_MAX);
+            break;
+        case DSGB_BASE_MIN:
+            fill_u64_kernel<<<grid_for(n), 256, 0, st>>>((unsigned long long *)B.agg, n,
+                                                          (unsigned long long)KEY_EMPTY_MIN);
+            break;
+        case DSGB_BASE_MIN_ROW:
+            fill_u64_kernel<<<grid_for(n), 256, 0, st>>>((unsigned long long *)B.agg, n,
+                                                          (unsigned long long)ROW_EMPTY_MIN);
+            break;
+        case DSGB_BASE_MAX_ROW:
+            e = cudaMemsetAsync(B.agg, 0xff, (size_t)n * 8, st); break;   // -1
+        case DSGB_BASE_ARGMAX: case DSGB_BASE_AA_ARGMAX:
+            fill_pair_kernel<<<grid_for(n), 256, 0, st>>>((long long *)B.agg, n, KEY_EMPTY_MAX, ROW_EMPTY_MIN);
+            break;
+        case DSGB_BASE_ARGMIN:
+            fill_pair_kernel<<<grid_for(n), 256, 0, st>>>((long long *)B.agg, n, KEY_EMPTY_MIN, ROW_EMPTY_MIN);
+            break;
+        default:
+            set_error("dsgb_bases_init: unknown base op %d", B.op);
+            return DSGB_E_INVALID;
+        }
+        if (e != cudaSuccess) return cuda_status(e, "dsgb_bases_init memset");
+        DSGB_CHECK_LAUNCH("dsgb_bases_init fill");
+    }
+    return DSGB_OK;
+}
+
+// -------------------------------------------------------------- finalize
+
+struct FinArgs {
+    int32_t op;
+    int32_t b0op, b1op;
+    const void *b0, *b1;
+    ColumnRef col;
+    int64_t row_offset;
+    int64_t ncol_rows;
+    void *out;
+    int64_t n;
+    int32_t out_bytes;
+};
+
+__device__ __forceinline__ double nan_d() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+// Row index held by a row-valued base, or -1.
+__device__ __forceinline__ long long base_row(int op, const void *b, int64_t i) {
+    const long long *q = (const long long *)b;
+    switch (op) {
+    case DSGB_BASE_MIN_ROW: { long long r = q[i]; return r == ROW_EMPTY_MIN ? -1 : r; }
+    case DSGB_BASE_MAX_ROW: return q[i];
+    case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: case DSGB_BASE_AA_ARGMAX: {
+        long long r = q[2 * i + 1]; return r == ROW_EMPTY_MIN ? -1 : r; }
+    default: return -1;
+    }
+}
+
+// Key held by a key-valued base, with empty = false.
+__device__ __forceinline__ bool base_key(int op, const void *b, int64_t i, long long &k) {
+    const long long *q = (const long long *)b;
+    switch (op) {
+    case DSGB_BASE_MAX: case DSGB_BASE_AA_MAX: k = q[i]; return k != KEY_EMPTY_MAX;
+    case DSGB_BASE_MIN: k = q[i]; return k != KEY_EMPTY_MIN;
+    case DSGB_BASE_ARGMAX: case DSGB_BASE_AA_ARGMAX: k = q[2 * i]; return k != KEY_EMPTY_MAX;
+    case DSGB_BASE_ARGMIN: k = q[2 * i]; return k != KEY_EMPTY_MIN;
+    default: return false;
+    }
+}
+
+// Whether something landed in cell i, from a count/any base.
+__device__ __forceinline__ bool base_hit(int op, const void *b, int64_t i, unsigned &cnt) {
+    if (op == DSGB_BASE_ANY) { cnt = ((const uint8_t *)b)[i]; return cnt != 0; }
+    cnt = ((const unsigned *)b)[i];
+    return cnt != 0;
+}
+
+__global__ void finalize_kernel(const FinArgs a) {
+    for (int64_t i = gtid(); i < a.n; i += gstride()) {
+        switch (a.op) {
+        case DSGB_FIN_SUM_NAN: {
+            unsigned c; bool hit = base_hit(a.b1op, a.b1, i, c);
+            ((double *)a.out)[i] = hit ? ((const double *)a.b0)[i] : nan_d();
+            break; }
+        case DSGB_FIN_SUM_F32: {
+            unsigned c; bool hit = base_hit(a.b1op, a.b1, i, c);
+            ((float *)a.out)[i] = hit ? (float)((const double *)a.b0)[i] : __int_as_float(0x7fc00000);
+            break; }
+        case DSGB_FIN_MEAN: {
+            unsigned c; base_hit(a.b1op, a.b1, i, c);
+            // reductions.py:1293-1296: where(counts > 0, sums/counts, nan)
+            ((double *)a.out)[i] = c > 0 ? ((const double *)a.b0)[i] / (double)c : nan_d();
+            break; }
+        case DSGB_FIN_KEY_F64: {
+            long long k; bool ok = base_key(a.b0op, a.b0, i, k);
+            ((double *)a.out)[i] = ok ? key_f64(k) : nan_d();
+            break; }
+        case DSGB_FIN_KEY_F32: {
+            long long k; bool ok = base_key(a.b0op, a.b0, i, k);
+            ((float *)a.out)[i] = ok ? (float)key_f64(k) : __int_as_float(0x7fc00000);
+            break; }
+        case DSGB_FIN_ROW:
+            ((long long *)a.out)[i] = base_row(a.b0op, a.b0, i);
+            break;
+        case DSGB_FIN_GATHER: {
+            long long r = base_row(a.b0op, a.b0, i);
+            long long j = r - a.row_offset;
+            ((double *)a.out)[i] = (r >= 0 && j >= 0 && j < a.ncol_rows) ? load_f64(a.col, j) : nan_d();
+            break; }
+        case DSGB_FIN_COPY: {
+            if (a.out_bytes == 4) ((unsigned *)a.out)[i] = ((const unsigned *)a.b0)[i];
+            else if (a.out_bytes == 1) ((uint8_t *)a.out)[i] = ((const uint8_t *)a.b0)[i];
+            else ((unsigned long long *)a.out)[i] = ((const unsigned long long *)a.b0)[i];
+            break; }
+        default: break;
+        }
+    }
+}
+
+static int base_elem_bytes(int op) {
+    switch (op) {
+    case DSGB_BASE_COUNT: case DSGB_BASE_AA_CNT0: return 4;
+    case DSGB_BASE_ANY: return 1;
+    case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: case DSGB_BASE_AA_ARGMAX: return 16;
+    default: return 8;
+    }
+}
+
+int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
+                     const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                     int64_t ncells, cudaStream_t st, int64_t ncol_rows) {
+    for (int o = 0; o < nouts; ++o) {
+        const dsgb_output &O = outs[o];
+        if (!O.out || O.base0 < 0 || O.base0 >= nbases) {
+            set_error("dsgb_finalize: output %d invalid", o);
+            return DSGB_E_INVALID;
+        }
+        FinArgs a;
+        memset(&a, 0, sizeof(a));
+        a.op = O.op;
+        const dsgb_base &B0 = bases[O.base0];
+        a.b0op = B0.op; a.b0 = B0.agg;
+        if (O.op == DSGB_FIN_SUM_NAN || O.op == DSGB_FIN_MEAN || O.op == DSGB_FIN_SUM_F32) {
+            if (O.base1 < 0 || O.base1 >= nbases) { set_error("dsgb_finalize: output %d needs base1", o); return DSGB_E_INVALID; }
+            a.b1op = bases[O.base1].op; a.b1 = bases[O.base1].agg;
+        }
+        if (O.op == DSGB_FIN_GATHER) {
+            if (O.col < 0 || O.col >= ncols || !cols) { set_error("dsgb_finalize: output %d gather column", o); return DSGB_E_INVALID; }
+            a.col.data = cols[O.col].data; a.col.dtype = cols[O.col].dtype;
+        }
+        if (O.op < DSGB_FIN_SUM_NAN || O.op > DSGB_FIN_COPY) { set_error("dsgb_finalize: bad op %d", O.op); return DSGB_E_INVALID; }
+        a.row_offset = row_offset;
+        a.ncol_rows = ncol_rows;
+        a.out = O.out;
+        a.n = ncells * (B0.ncat < 1 ? 1 : B0.ncat);
+        a.out_bytes = base_elem_bytes(B0.op);
+        finalize_kernel<<<grid_for(a.n), 256, 0, st>>>(a);
+        DSGB_CHECK_LAUNCH("finalize kernel");
+    }
+    return DSGB_OK;
+}
+
+// Compatibility overload used by the glyph entry points: the gather bound
+// is the number of rows of the call.
+int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
+                     const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                     int64_t ncells, cudaStream_t st) {
+    return finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st,
+                            (int64_t)1 << 62);
+}
+
+// ------------------------------------------------------------- autorange
+
+__device__ __forceinline__ unsigned long long ord_u64(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unord_u64(unsigned long long u) {
+    unsigned long long b = (u >> 63) ? (u & 0x7fffffffffffffffull) : ~u;
+    return __longlong_as_double((long long)b);
+}
+
+// glyph.py:66-78: NaN-skipping min/max.  mm[0] = ordered min, mm[1] = ordered max.
+__global__ void bounds_kernel(const ColumnRef c, int64_t n, unsigned long long *mm) {
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (int64_t i = gtid(); i < n; i += gstride()) {
+        double v = load_f64(c, i);
+        if (v == v) {
+            unsigned long long u = ord_u64(v);
+            lo = u < lo ? u : lo;
+            hi = u > hi ? u : hi;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (lo != ~0ull) atomicMin(&mm[0], lo);
+        if (hi != 0ull) atomicMax(&mm[1], hi);
+    }
+}
+
+__global__ void bounds_finish_kernel(unsigned long long *mm, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        unsigned long long lo = mm[0], hi = mm[1];
+        double a = (lo == ~0ull) ? __longlong_as_double(0x7ff0000000000000ll) : unord_u64(lo);
+        double b = (hi == 0ull) ? __longlong_as_double((long long)0xfff0000000000000ull) : unord_u64(hi);
+        out[0] = a;
+        out[1] = b;
+    }
+}
+
+__global__ void bounds_init_kernel(unsigned long long *mm) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) { mm[0] = ~0ull; mm[1] = 0ull; }
+}
+
+}  // namespace dsgb
+
+using namespace dsgb;
+
+extern "C" int dsgb_abi_version(void) { return DSGB_ABI_VERSION; }
+extern "C" const char *dsgb_last_error(void) { return g_err; }
+extern "C" int dsgb_device_sm_count(void) {
+    int n = sm_count();
+    if (n < 0) { set_error("no CUDA device"); return DSGB_E_CUDA; }
+    return n;
+}
+
+extern "C" int dsgb_bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, void *stream) {
+    if ((nbases > 0 && !bases) || nbases < 0 || ncells < 0) { set_error("dsgb_bases_init: bad args"); return DSGB_E_INVALID; }
+    return bases_init(bases, nbases, ncells, as_stream(stream));
+}
+
+extern "C" int dsgb_finalize(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
+                             const dsgb_base *bases, int32_t nbases,
+                             const dsgb_output *outs, int32_t nouts, int64_t ncells, void *stream) {
+    if ((nbases > 0 && !bases) || (nouts > 0 && !outs) || ncells < 0) { set_error("dsgb_finalize: bad args"); return DSGB_E_INVALID; }
+    return finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, as_stream(stream));
+}
+
+// The min/max travel as order-preserving uint64 in the first 16 bytes of
+// out_minmax (used as scratch), then are decoded in place.
+extern "C" int dsgb_bounds(const dsgb_column *col, int64_t n, double *out_minmax, void *stream) {
+    if (!col || !out_minmax || n < 0 || dtype_size(col->dtype) == 0 || (n > 0 && !col->data)) {
+        set_error("dsgb_bounds: bad args");
+        return DSGB_E_INVALID;
+    }
+    cudaStream_t st = as_stream(stream);
+    unsigned long long *mm = (unsigned long long *)out_minmax;
+    bounds_init_kernel<<<1, 32, 0, st>>>(mm);
+    ColumnRef c{col->data, col->dtype};
+    if (n > 0) bounds_kernel<<<grid_for(n), 256, 0, st>>>(c, n, mm);
+    bounds_finish_kernel<<<1, 32, 0, st>>>(mm, out_minmax);
+    DSGB_CHECK_LAUNCH("dsgb_bounds");
+    return DSGB_OK;
+}

@@ -1,0 +1,423 @@
+// eq_hist.cu -- histogram equalisation (tf.shade(how='eq_hist')) on GB300.
+//
+// Restates datashader/transfer_functions/__init__.py:
+//   _interpolate prologue (251-297): mask = data == 0 (uint) / isnan (float),
+//       offset = min of the unmasked values, data -= offset;
+//   eq_hist (148-223): integer data with ptp < nbins -> exact per-value
+//       counts over [vmin, vmax]; otherwise numpy.histogram(data, nbins)
+//       with empty bins dropped; cdf = cumsum / total; np.interp(data,
+//       bin_centers, cdf); masked -> NaN; discrete_levels = #non-empty bins;
+//   span / _rescale_discrete_levels (299-316, 234-248) and the list-colormap
+//       RGBA branch (317-351).
+//
+// numpy.histogram's bin assignment (numpy/lib/_histograms_impl.py: estimate
+// from (x - first) / (last - first) * nbins, then correct against the
+// linspace edges) and numpy.linspace's edges (i*step + start, last = stop)
+// are reproduced exactly, so the histogram is bit-identical.
+//
+// Four launches: min/max, histogram (shared-memory privatised low bins),
+// one-block scan (cdf, levels, span), apply (cdf lookup / interp + RGBA).
+#include "dsgb_internal.cuh"
+
+#include <cmath>
+
+namespace dsgb {
+
+struct EqHeader {
+    unsigned long long lo, hi;     // ordered min / max of the unmasked values
+    unsigned long long total;      // unmasked count
+    long long levels;
+    int32_t path;                  // 0 = no data, 1 = integer counts, 2 = binned
+    int32_t nkept;                 // float path: non-empty bins
+    double first, last, step;      // float path: outer edges and linspace step
+    double span0, span1;           // colormap span
+    double offset;                 // offset (float data)
+    double dmax;                   // largest unmasked value after the offset
+    unsigned int uoffset;          // offset (uint32 data)
+    unsigned int ptp;
+};
+
+constexpr int SMEM_BINS = 8192;
+constexpr size_t HDR_BYTES = 256;
+static_assert(sizeof(EqHeader) <= HDR_BYTES, "header");
+
+struct EqLayout {
+    EqHeader *hdr;
+    unsigned int *hist;   // nbins
+    double *cdf;          // nbins
+    double *centers;      // nbins (float path, compacted)
+};
+
+static size_t ws_bytes(int nbins) {
+    return HDR_BYTES + (size_t)nbins * (4 + 8 + 8) + 64;
+}
+
+static EqLayout layout(void *ws, int nbins) {
+    char *b = (char *)ws;
+    EqLayout L;
+    L.hdr = (EqHeader *)b;
+    L.hist = (unsigned int *)(b + HDR_BYTES);
+    size_t off = HDR_BYTES + (((size_t)nbins * 4 + 15) & ~(size_t)15);
+    L.cdf = (double *)(b + off);
+    L.centers = (double *)(b + off + (size_t)nbins * 8);
+    return L;
+}
+
+__device__ __forceinline__ unsigned long long ord64(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unord64(unsigned long long u) {
+    unsigned long long b = (u >> 63) ? (u & 0x7fffffffffffffffull) : ~u;
+    return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ double dnan() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+template <typename T> __device__ __forceinline__ bool masked(T v);
+template <> __device__ __forceinline__ bool masked<unsigned int>(unsigned int v) { return v == 0u; }
+template <> __device__ __forceinline__ bool masked<double>(double v) { return v != v; }
+
+__global__ void eqh_init(EqHeader *h) {
+    if (threadIdx.x == 0) {
+        memset(h, 0, sizeof(EqHeader));
+        h->lo = ~0ull;
+        h->hi = 0ull;
+    }
+}
+
+template <typename T>
+__global__ void eqh_minmax(const T *data, int64_t n, EqHeader *h) {
+    unsigned long long lo = ~0ull, hi = 0ull, cnt = 0;
+    for (int64_t i = gtid(); i < n; i += gstride()) {
+        T v = data[i];
+        if (masked<T>(v)) continue;
+        unsigned long long u = sizeof(T) == 4 ? (unsigned long long)v : ord64((double)v);
+        lo = u < lo ? u : lo;
+        hi = u > hi ? u : hi;
+        ++cnt;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if ((threadIdx.x & 31) == 0 && cnt) {
+        atomicMin(&h->lo, lo);
+        atomicMax(&h->hi, hi);
+        atomicAdd(&h->total, cnt);
+    }
+}
+
+// numpy.linspace(first, last, nbins+1)[j] (function_base.py: i*step + start,
+// the endpoint set to stop; a zero step falls back to i/div*delta).
+__device__ __forceinline__ double lin_edge(const EqHeader &h, int j, int nbins) {
+    if (j >= nbins) return h.last;
+    if (h.step == 0.0) return __dadd_rn(__dmul_rn(__ddiv_rn((double)j, (double)nbins), h.last - h.first), h.first);
+    return __dadd_rn(__dmul_rn((double)j, h.step), h.first);
+}
+
+// numpy.histogram uniform-bin index of x (within [first, last]).
+__device__ __forceinline__ int np_hist_index(const EqHeader &h, double x, int nbins) {
+    double denom = __dsub_rn(h.last, h.first);
+    double f = __dmul_rn(__ddiv_rn(__dsub_rn(x, h.first), denom), (double)nbins);
+    long long idx = (long long)f;
+    if (idx == nbins) idx -= 1;
+    if (idx < 0) idx = 0;
+    if (idx > nbins - 1) idx = nbins - 1;
+    if (x < lin_edge(h, (int)idx, nbins)) idx -= 1;
+    if (idx < 0) idx = 0;
+    if (idx != nbins - 1 && x >= lin_edge(h, (int)idx + 1, nbins)) idx += 1;
+    return (int)idx;
+}
+
+// Decide the path and the float-path edges (one thread).
+template <typename T>
+__global__ void eqh_plan(EqHeader *h, int nbins) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (h->total == 0) { h->path = 0; return; }
+    if (sizeof(T) == 4) {
+        unsigned int lo = (unsigned int)h->lo, hi = (unsigned int)h->hi;
+        h->uoffset = lo;
+        h->ptp = hi - lo;
+        if ((long long)(hi - lo) < (long long)nbins) { h->path = 1; return; }
+        // binned path on uint32: edges over [0, ptp] in float64
+        h->first = 0.0;
+        h->last = (double)(hi - lo);
+        h->dmax = h->last;
+    } else {
+        double lo = unord64(h->lo), hi = unord64(h->hi);
+        h->offset = lo;
+        // data -= offset happens elementwise: the extremes become these
+        h->first = __dsub_rn(lo, lo);
+        h->last = __dsub_rn(hi, lo);
+        h->dmax = h->last;
+    }
+    if (h->first == h->last) { h->first = h->first - 0.5; h->last = h->last + 0.5; }
+    h->step = __ddiv_rn(__dsub_rn(h->last, h->first), (double)nbins);
+    h->path = 2;
+}
+
+template <typename T>
+__device__ __forceinline__ double shifted(const EqHeader &h, T v) {
+    if (sizeof(T) == 4) return (double)(unsigned int)((unsigned int)v - h.uoffset);
+    return __dsub_rn((double)v, h.offset);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) eqh_hist(const T *data, int64_t n, const EqHeader *hp,
+                                                unsigned int *hist, int nbins) {
+    __shared__ unsigned int sh[SMEM_BINS];
+    const EqHeader h = *hp;
+    if (h.path == 0) return;
+    for (int j = threadIdx.x; j < SMEM_BINS; j += blockDim.x) sh[j] = 0;
+    __syncthreads();
+    for (int64_t i = gtid(); i < n; i += gstride()) {
+        T v = data[i];
+        if (masked<T>(v)) continue;
+        int bin;
+        if (h.path == 1) bin = (int)((unsigned int)v - h.uoffset);
+        else bin = np_hist_index(h, shifted<T>(h, v), nbins);
+        if (bin < SMEM_BINS) atomicAdd(&sh[bin], 1u);
+        else atomicAdd(&hist[bin], 1u);
+    }
+    __syncthreads();
+    const int lim = nbins < SMEM_BINS ? nbins : SMEM_BINS;
+    for (int j = threadIdx.x; j < lim; j += blockDim.x)
+        if (sh[j]) atomicAdd(&hist[j], sh[j]);
+}
+
+// np.interp(x, xp, fp) for sorted xp (left = fp[0], right = fp[-1]).
+__device__ __forceinline__ double np_interp(double x, const double *xp, const double *fp, int len,
+                                            double left, double right) {
+    if (x != x) return x;
+    if (x > xp[len - 1]) return right;
+    if (x < xp[0]) return left;
+    int lo = 0, hi = len - 1;          // invariant xp[lo] <= x, and x < xp[hi] or hi = len-1
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (xp[mid] <= x) lo = mid; else hi = mid;
+    }
+    int j = lo;
+    if (x >= xp[len - 1]) j = len - 1;
+    if (j == len - 1) return fp[j];
+    if (xp[j] == x) return fp[j];
+    double slope = __ddiv_rn(__dsub_rn(fp[j + 1], fp[j]), __dsub_rn(xp[j + 1], xp[j]));
+    double r = __dadd_rn(__dmul_rn(slope, __dsub_rn(x, xp[j])), fp[j]);
+    if (r != r) {
+        r = __dadd_rn(__dmul_rn(slope, __dsub_rn(x, xp[j + 1])), fp[j + 1]);
+        if (r != r && fp[j] == fp[j + 1]) r = fp[j];
+    }
+    return r;
+}
+
+// One block: cumulative sums, cdf, levels, the float-path compaction and the span.
+__global__ void __launch_bounds__(1024) eqh_scan(EqHeader *hp, const unsigned int *hist, double *cdf,
+                                                 double *centers, int nbins, int rescale) {
+    __shared__ unsigned long long wsum[32];
+    __shared__ int wkept[32];
+    EqHeader &h = *hp;
+    if (h.path == 0) return;
+    const int path = h.path;
+    const int nb = path == 1 ? (int)h.ptp + 1 : nbins;
+    const int per = (nb + blockDim.x - 1) / blockDim.x;
+    const int j0 = threadIdx.x * per;
+    const int j1 = min(nb, j0 + per);
+    unsigned long long s = 0;
+    int kept = 0;
+    for (int j = j0; j < j1; ++j) { s += hist[j]; kept += hist[j] != 0; }
+    // block exclusive scan of (s, kept)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long xs = s;
+    int xk = kept;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long t = __shfl_up_sync(0xffffffffu, xs, o);
+        int tk = __shfl_up_sync(0xffffffffu, xk, o);
+        if (lane >= o) { xs += t; xk += tk; }
+    }
+    if (lane == 31) { wsum[warp] = xs; wkept[warp] = xk; }
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long a = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+        int ak = lane < (int)(blockDim.x >> 5) ? wkept[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long t = __shfl_up_sync(0xffffffffu, a, o);
+            int tk = __shfl_up_sync(0xffffffffu, ak, o);
+            if (lane >= o) { a += t; ak += tk; }
+        }
+        wsum[lane] = a;
+        wkept[lane] = ak;
+    }
+    __syncthreads();
+    unsigned long long run = xs - s + (warp > 0 ? wsum[warp - 1] : 0);
+    int krun = xk - kept + (warp > 0 ? wkept[warp - 1] : 0);
+    const unsigned long long total = wsum[31];
+    const int nkept = wkept[31];
+    const double ftotal = (double)total;
+    for (int j = j0; j < j1; ++j) {
+        unsigned int c = hist[j];
+        run += c;
+        if (path == 1) {
+            cdf[j] = __ddiv_rn((double)run, ftotal);          // (:200-201)
+        } else if (c) {
+            cdf[krun] = __ddiv_rn((double)run, ftotal);
+            double e0 = lin_edge(h, j, nbins), e1 = lin_edge(h, j + 1, nbins);
+            centers[krun] = __ddiv_rn(__dadd_rn(e0, e1), 2.0);  // (:194)
+            ++krun;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        h.levels = (long long)nkept;
+        h.nkept = nkept;
+        // span = (min, max) of the equalised unmasked values: the output is
+        // monotone in the value, so they are the images of the extremes.
+        double s0, s1;
+        if (path == 1) {
+            s0 = cdf[0];
+            s1 = cdf[h.ptp];
+        } else {
+            // the shifted extremes of the unmasked data are 0 and dmax
+            s0 = np_interp(0.0, centers, cdf, nkept, cdf[0], cdf[nkept - 1]);
+            s1 = np_interp(h.dmax, centers, cdf, nkept, cdf[0], cdf[nkept - 1]);
+        }
+        if (rescale) {
+            // _rescale_discrete_levels (:234-248)
+            double m = __ddiv_rn(-0.5, 98.0);
+            double c = __dsub_rn(1.5, __dmul_rn(2.0, m));
+            double multiple = __dadd_rn(__dmul_rn(m, (double)h.levels), c);
+            if (multiple > 1) {
+                double lower = __dsub_rn(s1, __dmul_rn(multiple, __dsub_rn(s1, s0)));
+                s0 = lower > 0 ? lower : 0;
+                s1 = 1;
+            }
+        }
+        h.span0 = s0;
+        h.span1 = s1;
+    }
+}
+
+struct Cmap {
+    double r[16], g[16], b[16];
+    int n;
+    int alpha;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) eqh_apply(const T *data, int64_t n, const EqHeader *hp,
+                                                 const double *cdf, const double *centers, double *out,
+                                                 uint32_t *rgba, const Cmap cm, int nbins) {
+    const EqHeader h = *hp;
+    // np.linspace(span0, span1, ncolors) (:320)
+    double xs[16];
+    if (rgba) {
+        const int div = cm.n - 1;
+        const double delta = __dsub_rn(h.span1, h.span0);
+        const double step = div > 0 ? __ddiv_rn(delta, (double)div) : 0.0;
+        for (int k = 0; k < cm.n; ++k) {
+            double y;
+            if (div > 0 && step == 0.0) y = __dmul_rn(__ddiv_rn((double)k, (double)div), delta);
+            else y = __dmul_rn((double)k, step);
+            xs[k] = __dadd_rn(y, h.span0);
+        }
+        if (div > 0) xs[cm.n - 1] = h.span1;
+    }
+    for (int64_t i = gtid(); i < n; i += gstride()) {
+        T v = data[i];
+        double o;
+        if (h.path == 0 || masked<T>(v)) {
+            o = dnan();
+        } else if (h.path == 1) {
+            o = cdf[(unsigned int)v - h.uoffset];
+        } else {
+            o = np_interp(shifted<T>(h, v), centers, cdf, h.nkept, cdf[0], cdf[h.nkept - 1]);
+        }
+        out[i] = o;
+        if (rgba) {
+            uint32_t px = 0;
+            if (o == o) {
+                // interp(data, span, chan, left=255), nan_to_num, astype(uint8)
+                double r = np_interp(o, xs, cm.r, cm.n, 255.0, cm.r[cm.n - 1]);
+                double g = np_interp(o, xs, cm.g, cm.n, 255.0, cm.g[cm.n - 1]);
+                double b = np_interp(o, xs, cm.b, cm.n, 255.0, cm.b[cm.n - 1]);
+                px = (uint32_t)(uint8_t)(int)r | ((uint32_t)(uint8_t)(int)g << 8) |
+                     ((uint32_t)(uint8_t)(int)b << 16) | ((uint32_t)(uint8_t)cm.alpha << 24);
+            }
+            rgba[i] = px;
+        }
+    }
+}
+
+__global__ void eqh_levels(const EqHeader *h, long long *levels) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *levels = h->path == 0 ? 0 : h->levels;
+}
+
+static unsigned grid_cap(int64_t n, int threads, int mult) {
+    int sms = sm_count();
+    if (sms <= 0) sms = 148;
+    int64_t g = (n + threads - 1) / threads;
+    if (g > (int64_t)sms * mult) g = (int64_t)sms * mult;
+    if (g < 1) g = 1;
+    return (unsigned)g;
+}
+
+template <typename T>
+static int eq_hist_impl(const T *data, int64_t n, int32_t nbins, double *out, int64_t *levels,
+                        uint32_t *rgba, const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                        int32_t rescale, void *workspace, size_t wsb, void *stream) {
+    if ((!data && n > 0) || n < 0 || !out || !levels || nbins < 1 || nbins > (1 << 24) || !workspace) {
+        set_error("dsgb_eq_hist: invalid arguments");
+        return DSGB_E_INVALID;
+    }
+    if (wsb < ws_bytes(nbins)) {
+        set_error("dsgb_eq_hist: workspace of %zu bytes, %zu needed", wsb, ws_bytes(nbins));
+        return DSGB_E_NOSPACE;
+    }
+    if (rgba && (!cmap_rgb || ncolors < 1 || ncolors > 16)) {
+        set_error("dsgb_eq_hist: colormap must have 1..16 colours");
+        return DSGB_E_INVALID;
+    }
+    Cmap cm;
+    memset(&cm, 0, sizeof(cm));
+    if (rgba) {
+        cm.n = ncolors;
+        for (int k = 0; k < ncolors; ++k) {
+            cm.r[k] = cmap_rgb[3 * k]; cm.g[k] = cmap_rgb[3 * k + 1]; cm.b[k] = cmap_rgb[3 * k + 2];
+        }
+        cm.alpha = alpha;
+    }
+    cudaStream_t st = as_stream(stream);
+    EqLayout L = layout(workspace, nbins);
+    eqh_init<<<1, 32, 0, st>>>(L.hdr);
+    cudaError_t e = cudaMemsetAsync(L.hist, 0, (size_t)nbins * 4, st);
+    if (e != cudaSuccess) return cuda_status(e, "dsgb_eq_hist memset");
+    if (n > 0) eqh_minmax<T><<<grid_cap(n, 256, 4), 256, 0, st>>>(data, n, L.hdr);
+    eqh_plan<T><<<1, 32, 0, st>>>(L.hdr, nbins);
+    if (n > 0) eqh_hist<T><<<grid_cap(n, 512, 2), 512, 0, st>>>(data, n, L.hdr, L.hist, nbins);
+    eqh_scan<<<1, 1024, 0, st>>>(L.hdr, L.hist, L.cdf, L.centers, nbins, rescale);
+    if (n > 0) eqh_apply<T><<<grid_cap(n, 256, 8), 256, 0, st>>>(data, n, L.hdr, L.cdf, L.centers, out, rgba, cm, nbins);
+    eqh_levels<<<1, 32, 0, st>>>(L.hdr, (long long *)levels);
+    DSGB_CHECK_LAUNCH("dsgb_eq_hist");
+    return DSGB_OK;
+}
+
+}  // namespace dsgb
+
+using namespace dsgb;
+
+extern "C" size_t dsgb_eq_hist_workspace_size(int32_t nbins) { return ws_bytes(nbins < 1 ? 1 : nbins); }
+
+extern "C" int dsgb_eq_hist_u32(const uint32_t *data, int64_t n, int32_t nbins, double *out, int64_t *levels,
+                                uint32_t *rgba, const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                                int32_t rescale, void *workspace, size_t wsb, void *stream) {
+    return eq_hist_impl<unsigned int>((const unsigned int *)data, n, nbins, out, levels, rgba, cmap_rgb,
+                                      ncolors, alpha, rescale, workspace, wsb, stream);
+}
+
+extern "C" int dsgb_eq_hist_f64(const double *data, int64_t n, int32_t nbins, double *out, int64_t *levels,
+                                uint32_t *rgba, const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                                int32_t rescale, void *workspace, size_t wsb, void *stream) {
+    return eq_hist_impl<double>(data, n, nbins, out, levels, rgba, cmap_rgb, ncolors, alpha, rescale,
+                                workspace, wsb, stream);
+}

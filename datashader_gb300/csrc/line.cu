@@ -1,0 +1,418 @@
+// line.cu -- Canvas.line, LineAxis0 glyph, on GB300.
+//
+// Replaces LineAxis0._internal_build_extend / _build_extend_line_axis0
+// (datashader/glyphs/line.py:59-103, 1099-1149) with draw_segment
+// (1033-1097), Liang-Barsky clipping (734-800), pixel mapping (688-731),
+// Bresenham (986-1031) and the antialiased wide-line scan conversion
+// _full_antialias (826-981).
+//
+// One thread draws one segment (rows i, i+1); the pixel appends are
+// atomics on the caller's bases.  This file is compiled with -fmad=false:
+// numba contracts no multiply-adds, so every product and sum is rounded
+// separately and the coverage values are bit-identical to the reference's.
+// Only the order of the floating-point accumulation differs (atomics).
+#include "dsgb_internal.cuh"
+
+#include <cmath>
+
+namespace dsgb {
+
+struct LineParams {
+    ColumnRef cols[MAX_COLS];
+    BaseDev bases[MAX_BASES];
+    int32_t ncols, nbases;
+    int64_t n, row_offset;
+    int32_t x_col, y_col;
+    int32_t width, height;
+    double sx, tx, sy, ty;
+    double xmin, xmax, ymin, ymax;
+    double line_width;
+    int32_t plot_start, overwrite, use_2_stage;
+};
+
+// One append of row i (field row = segment start) at pixel (x, y).
+// aa / pa are aa_factor / prev_aa_factor (1, 0 for Bresenham lines).
+__device__ void line_append(const LineParams &p, int64_t i, long long x, long long y,
+                            double aa, double pa) {
+    if (x < 0 || y < 0 || x >= p.width || y >= p.height) return;  // memory safety only
+    const int64_t pix = (int64_t)y * p.width + x;
+    const long long row = (long long)(i + p.row_offset);
+#pragma unroll 1
+    for (int b = 0; b < p.nbases; ++b) {
+        const BaseDev &B = p.bases[b];
+        int64_t cell = pix;
+        if (B.cat_col >= 0) {
+            long long c = load_i64(p.cols[B.cat_col], i);
+            if (c < 0) c += B.ncat;
+            if (c < 0 || c >= B.ncat) continue;
+            cell = pix * B.ncat + c;
+        }
+        double field = 1.0;
+        bool has = true;
+        if (B.col >= 0) {
+            field = load_f64(p.cols[B.col], i);
+            has = !isnull(field);
+        }
+        const bool unweighted = (B.flags & DSGB_BASEF_UNWEIGHTED) || B.col < 0;
+        switch (B.op) {
+        case DSGB_BASE_COUNT: if (has) atomicAdd((unsigned *)B.agg + cell, 1u); break;
+        case DSGB_BASE_ANY: if (has) ((volatile uint8_t *)B.agg)[cell] = 1; break;
+        case DSGB_BASE_SUM: if (has) atomicAdd((double *)B.agg + cell, field); break;
+        case DSGB_BASE_MAX: if (has) atomic_max_key((long long *)B.agg + cell, f64_key(field)); break;
+        case DSGB_BASE_MIN: if (has) atomic_min_key((long long *)B.agg + cell, f64_key(field)); break;
+        case DSGB_BASE_MIN_ROW: if (has) atomic_min_key((long long *)B.agg + cell, row); break;
+        case DSGB_BASE_MAX_ROW: if (has) atomic_max_key((long long *)B.agg + cell, row); break;
+        case DSGB_BASE_ARGMAX: if (has) pair_update<true>((long long *)B.agg + 2 * cell, f64_key(field), row); break;
+        case DSGB_BASE_ARGMIN: if (has) pair_update<false>((long long *)B.agg + 2 * cell, f64_key(field), row); break;
+        case DSGB_BASE_AA_SUM: {
+            // reductions.py:966-973, 1065-1075, 560-569: value = field*(aa - prev)
+            if (!has) break;
+            double d = aa - pa;
+            double value = unweighted ? d : field * d;
+            if (!isnull(value)) atomicAdd((double *)B.agg + cell, value);
+            break; }
+        case DSGB_BASE_AA_CNT0:
+            // reductions.py:680-685: count once per row (prev_aa_factor == 0)
+            if (has && pa == 0.0) atomicAdd((unsigned *)B.agg + cell, 1u);
+            break;
+        case DSGB_BASE_AA_MAX: {
+            // reductions.py:1186-1192 and siblings: keep the largest field*aa
+            if (!has) break;
+            double value = unweighted ? aa : field * aa;
+            if (!isnull(value)) atomic_max_key((long long *)B.agg + cell, f64_key(value));
+            break; }
+        case DSGB_BASE_AA_ARGMAX: {
+            if (!has) break;
+            double value = unweighted ? aa : field * aa;
+            if (!isnull(value)) pair_update<true>((long long *)B.agg + 2 * cell, f64_key(value), row);
+            break; }
+        default: break;
+        }
+    }
+}
+
+// line.py:783-800
+__device__ __forceinline__ bool clipt(double p, double q, double &t0, double &t1) {
+    bool accept = true;
+    if (p < 0 && q < 0) {
+        double r = q / p;
+        if (r > t1) accept = false;
+        else if (r > t0) t0 = r;
+    } else if (p > 0 && q < p) {
+        double r = q / p;
+        if (r < t0) accept = false;
+        else if (r < t1) t1 = r;
+    } else if (q < 0) {
+        accept = false;
+    }
+    return accept;
+}
+
+// line.py:734-780
+__device__ __forceinline__ void liang_barsky(double xmin, double xmax, double ymin, double ymax,
+                                             double &x0, double &x1, double &y0, double &y1,
+                                             bool &skip, bool &cs, bool &ce) {
+    if (x0 < xmin && x1 < xmin) skip = true;
+    else if (x0 > xmax && x1 > xmax) skip = true;
+    else if (y0 < ymin && y1 < ymin) skip = true;
+    else if (y0 > ymax && y1 > ymax) skip = true;
+    double t0 = 0, t1 = 1;
+    double dx1 = x1 - x0;
+    if (!clipt(-dx1, x0 - xmin, t0, t1)) skip = true;
+    if (!clipt(dx1, xmax - x0, t0, t1)) skip = true;
+    double dy1 = y1 - y0;
+    if (!clipt(-dy1, y0 - ymin, t0, t1)) skip = true;
+    if (!clipt(dy1, ymax - y0, t0, t1)) skip = true;
+    if (t1 < 1) { ce = true; x1 = x0 + t1 * dx1; y1 = y0 + t1 * dy1; } else ce = false;
+    if (t0 > 0) { cs = true; x0 = x0 + t0 * dx1; y0 = y0 + t0 * dy1; } else cs = false;
+}
+
+__device__ __forceinline__ double clampd(double x, double lo, double hi) {
+    double m = x < hi ? x : hi;
+    return lo > m ? lo : m;
+}
+__device__ __forceinline__ long long clampi(long long x, long long lo, long long hi) {
+    long long m = x < hi ? x : hi;
+    return lo > m ? lo : m;
+}
+// line.py:808-811
+__device__ __forceinline__ double linearstep(double e0, double e1, double x) {
+    return clampd((x - e0) / (e1 - e0), 0.0, 1.0);
+}
+// line.py:814-821
+__device__ __forceinline__ double x_intercept(double y, double cx0, double cy0, double cx1, double cy1) {
+    if (cy0 == cy1) return cx1;
+    double frac = (y - cy0) / (cy1 - cy0);
+    return cx0 + frac * (cx1 - cx0);
+}
+__device__ __forceinline__ double sq(double v) { return v * v; }
+
+// line.py:826-981 -- _full_antialias.
+__device__ void full_antialias(const LineParams &p, double line_width, bool overwrite, int64_t i,
+                               double x0, double x1, double y0, double y1,
+                               bool segment_start, bool segment_end, double xm, double ym,
+                               long long nx, long long ny) {
+    if (x0 == x1 && y0 == y1) return;
+    const bool flip_xy = fabs(x0 - x1) < fabs(y0 - y1);
+    if (flip_xy) {
+        double t;
+        t = x0; x0 = y0; y0 = t;
+        t = x1; x1 = y1; y1 = t;
+        t = xm; xm = ym; ym = t;
+    }
+    double scale = 1.0;
+    if (line_width < 1.0) { scale *= line_width; line_width = 1.0; }
+    const double aa = 1.0;
+    const double halfwidth = 0.5 * (line_width + aa);
+    const bool flip_order = y1 < y0 || (y1 == y0 && x1 < x0);
+    double alongx = x1 - x0;
+    double alongy = y1 - y0;
+    const double length = sqrt(sq(alongx) + sq(alongy));
+    alongx /= length;
+    alongy /= length;
+    const double rightx = alongy;
+    const double righty = -alongx;
+    double b[8];
+    if (flip_order) {
+        b[0] = x1 - halfwidth * (rightx - alongx);
+        b[1] = x1 - halfwidth * (-rightx - alongx);
+        b[2] = x0 - halfwidth * (-rightx + alongx);
+        b[3] = x0 - halfwidth * (rightx + alongx);
+        b[4] = y1 - halfwidth * (righty - alongy);
+        b[5] = y1 - halfwidth * (-righty - alongy);
+        b[6] = y0 - halfwidth * (-righty + alongy);
+        b[7] = y0 - halfwidth * (righty + alongy);
+    } else {
+        b[0] = x0 + halfwidth * (rightx - alongx);
+        b[1] = x0 + halfwidth * (-rightx - alongx);
+        b[2] = x1 + halfwidth * (-rightx + alongx);
+        b[3] = x1 + halfwidth * (rightx + alongx);
+        b[4] = y0 + halfwidth * (righty - alongy);
+        b[5] = y0 + halfwidth * (-righty - alongy);
+        b[6] = y1 + halfwidth * (-righty + alongy);
+        b[7] = y1 + halfwidth * (righty + alongy);
+    }
+    long long xmaxi = nx - 1, ymaxi = ny - 1;
+    if (flip_xy) { long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
+    const int lowindex = flip_order ? (x0 > x1 ? 0 : 1) : (x1 > x0 ? 0 : 1);
+    double prev_alongx = 0, prev_alongy = 0, prev_length = 0, prev_rightx = 0, prev_righty = 0;
+    if (!overwrite && !segment_start) {
+        prev_alongx = x0 - xm;
+        prev_alongy = y0 - ym;
+        prev_length = sqrt(sq(prev_alongx) + sq(prev_alongy));
+        if (prev_length > 0.0) {
+            prev_alongx /= prev_length;
+            prev_alongy /= prev_length;
+            prev_rightx = prev_alongy;
+            prev_righty = -prev_alongx;
+        } else {
+            overwrite = true;
+        }
+    }
+    const long long ystart = clampi((long long)ceil(b[4 + lowindex]), 0, ymaxi);
+    const long long yend = clampi((long long)floor(b[4 + (lowindex + 2) % 4]), 0, ymaxi);
+    int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
+    const double lw_lo = 0.5 * (line_width - aa);
+    for (long long y = ystart; y <= yend; ++y) {
+        const double yd = (double)y;
+        if (ll == lowindex && yd > b[4 + lu]) { ll = lu; lu = (ll + 1) % 4; }
+        if (rl == lowindex && yd > b[4 + ru]) { rl = ru; ru = (rl + 3) % 4; }
+        const long long xleft = clampi((long long)ceil(x_intercept(yd, b[ll], b[4 + ll], b[lu], b[4 + lu])), 0, xmaxi);
+        const long long xright = clampi((long long)floor(x_intercept(yd, b[rl], b[4 + rl], b[ru], b[4 + ru])), 0, xmaxi);
+        for (long long x = xleft; x <= xright; ++x) {
+            const double xd = (double)x;
+            const double along = (xd - x0) * alongx + (yd - y0) * alongy;
+            bool prev_correction = false;
+            double distance;
+            if (along < 0.0) {
+                if (overwrite || segment_start || (xd - x0) * prev_alongx + (yd - y0) * prev_alongy > 0.0)
+                    distance = sqrt(sq(xd - x0) + sq(yd - y0));
+                else continue;
+            } else if (along > length) {
+                if (overwrite || segment_end) distance = sqrt(sq(xd - x1) + sq(yd - y1));
+                else continue;
+            } else {
+                distance = fabs((xd - x0) * rightx + (yd - y0) * righty);
+                if (!overwrite && !segment_start) {
+                    const double pd = (xd - x0) * prev_alongx + (yd - y0) * prev_alongy;
+                    if (-prev_length <= pd && pd <= 0.0 &&
+                        fabs((xd - x0) * prev_rightx + (yd - y0) * prev_righty) <= halfwidth)
+                        prev_correction = true;
+                }
+            }
+            double value = 1.0 - linearstep(lw_lo, halfwidth, distance);
+            value *= scale;
+            double prev_value = 0.0;
+            if (prev_correction) {
+                const double prev_distance = fabs((xd - x0) * prev_rightx + (yd - y0) * prev_righty);
+                prev_value = 1.0 - linearstep(lw_lo, halfwidth, prev_distance);
+                prev_value *= scale;
+                if (value <= prev_value) value = 0.0;
+            }
+            if (value > 0.0) {
+                if (flip_xy) line_append(p, i, y, x, value, prev_value);
+                else line_append(p, i, x, y, value, prev_value);
+            }
+        }
+    }
+}
+
+// line.py:986-1031 -- integer Bresenham.
+__device__ void bresenham(const LineParams &p, int64_t i, bool segment_start, long long x0, long long x1,
+                          long long y0, long long y1, bool clipped) {
+    long long dx = x1 - x0;
+    const long long ix = (dx > 0) - (dx < 0);
+    dx = (dx < 0 ? -dx : dx) * 2;
+    long long dy = y1 - y0;
+    const long long iy = (dy > 0) - (dy < 0);
+    dy = (dy < 0 ? -dy : dy) * 2;
+    if (!clipped && !(dx | dy)) { line_append(p, i, x0, y0, 1.0, 0.0); return; }
+    if (segment_start) line_append(p, i, x0, y0, 1.0, 0.0);
+    if (dx >= dy) {
+        long long error = 2 * dy - dx;
+        while (x0 != x1) {
+            if (error >= 0 && (error || ix > 0)) { error -= 2 * dx; y0 += iy; }
+            error += 2 * dy;
+            x0 += ix;
+            line_append(p, i, x0, y0, 1.0, 0.0);
+        }
+    } else {
+        long long error = 2 * dx - dy;
+        while (y0 != y1) {
+            if (error >= 0 && (error || iy > 0)) { error -= 2 * dy; x0 += ix; }
+            error += 2 * dx;
+            y0 += iy;
+            line_append(p, i, x0, y0, 1.0, 0.0);
+        }
+    }
+}
+
+__device__ __forceinline__ long long pyround(double v) { return (long long)rint(v); }
+
+// line.py:688-721 -- map_onto_pixel_snap
+__device__ __forceinline__ void map_snap(const LineParams &p, double x, double y, long long &xo, long long &yo) {
+    long long xx = (long long)(x * p.sx + p.tx);
+    long long yy = (long long)(y * p.sy + p.ty);
+    long long xxmax = pyround(p.xmax * p.sx + p.tx);
+    long long yymax = pyround(p.ymax * p.sy + p.ty);
+    xo = xx == xxmax ? xx - 1 : xx;
+    yo = yy == yymax ? yy - 1 : yy;
+}
+
+// line.py:1104-1124 + 1045-1095, one segment.
+__global__ void __launch_bounds__(256) line_axis0_kernel(const LineParams p) {
+    const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
+    const bool antialias = p.line_width > 0.0;
+    for (int64_t i = gtid(); i + 1 < p.n; i += gstride()) {
+        double x0 = load_f64(X, i), y0 = load_f64(Y, i);
+        double x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
+        bool segment_start = (i == 0) ? (p.plot_start != 0)
+                                      : (isnull(load_f64(X, i - 1)) || isnull(load_f64(Y, i - 1)));
+        bool segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
+        double xm = 0.0, ym = 0.0;
+        if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, i - 1); ym = load_f64(Y, i - 1); }
+        bool skip = isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1);
+        bool cs = false, ce = false;
+        liang_barsky(p.xmin, p.xmax, p.ymin, p.ymax, x0, x1, y0, y1, skip, cs, ce);
+        if (skip) continue;
+        const bool clipped = cs || ce;
+        segment_start = segment_start || cs;
+        if (antialias) {
+            // line.py:723-726 map_onto_pixel_no_snap
+            const double px0 = x0 * p.sx + p.tx - 0.5, py0 = y0 * p.sy + p.ty - 0.5;
+            const double px1 = x1 * p.sx + p.tx - 0.5, py1 = y1 * p.sy + p.ty - 0.5;
+            double pxm = 0.0, pym = 0.0;
+            if (!segment_start) { pxm = xm * p.sx + p.tx - 0.5; pym = ym * p.sy + p.ty - 0.5; }
+            const long long nx = pyround((p.xmax - p.xmin) * p.sx);
+            const long long ny = pyround((p.ymax - p.ymin) * p.sy);
+            full_antialias(p, p.line_width, p.overwrite != 0, i, px0, px1, py0, py1,
+                           segment_start, segment_end, pxm, pym, nx, ny);
+        } else {
+            long long ix0, iy0, ix1, iy1;
+            map_snap(p, x0, y0, ix0, iy0);
+            map_snap(p, x1, y1, ix1, iy1);
+            bresenham(p, i, segment_start, ix0, ix1, iy0, iy1, clipped);
+        }
+    }
+}
+
+int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st);
+int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
+                     const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                     int64_t ncells, cudaStream_t st);
+
+int build_line_params(LineParams &p, const dsgb_column *cols, int32_t ncols, int64_t n,
+                      int64_t row_offset, int32_t x_col, int32_t y_col, const dsgb_canvas *cv,
+                      const dsgb_base *bases, int32_t nbases) {
+    if (!cols || !cv || ncols <= 0 || ncols > MAX_COLS || n < 0 || nbases < 0 || nbases > MAX_BASES ||
+        (nbases > 0 && !bases) || x_col < 0 || x_col >= ncols || y_col < 0 || y_col >= ncols ||
+        cv->width <= 0 || cv->height <= 0) {
+        set_error("dsgb_line_axis0: invalid arguments");
+        return DSGB_E_INVALID;
+    }
+    if (cv->x_log || cv->y_log) {
+        set_error("dsgb_line_axis0: log axes are not supported for lines");
+        return DSGB_E_UNSUPPORTED;
+    }
+    memset(&p, 0, sizeof(p));
+    for (int c = 0; c < ncols; ++c) {
+        if (dtype_size(cols[c].dtype) == 0 || (n > 0 && !cols[c].data)) {
+            set_error("dsgb_line_axis0: column %d invalid", c);
+            return DSGB_E_INVALID;
+        }
+        p.cols[c].data = cols[c].data;
+        p.cols[c].dtype = cols[c].dtype;
+    }
+    for (int b = 0; b < nbases; ++b) {
+        const dsgb_base &B = bases[b];
+        if (!B.agg || B.col >= ncols || B.cat_col >= ncols || B.ncat < 1 || B.op < DSGB_BASE_COUNT ||
+            B.op > DSGB_BASE_AA_ARGMAX) {
+            set_error("dsgb_line_axis0: base %d invalid", b);
+            return DSGB_E_INVALID;
+        }
+        p.bases[b] = BaseDev{B.op, B.col, B.cat_col < 0 ? -1 : B.cat_col, B.ncat, B.flags, B.agg};
+    }
+    p.ncols = ncols; p.nbases = nbases; p.n = n; p.row_offset = row_offset;
+    p.x_col = x_col; p.y_col = y_col; p.width = cv->width; p.height = cv->height;
+    p.sx = cv->sx; p.tx = cv->tx; p.sy = cv->sy; p.ty = cv->ty;
+    p.xmin = cv->xmin; p.xmax = cv->xmax; p.ymin = cv->ymin; p.ymax = cv->ymax;
+    return DSGB_OK;
+}
+
+}  // namespace dsgb
+
+using namespace dsgb;
+
+extern "C" int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                               int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                               double line_width, int32_t plot_start, int32_t overwrite,
+                               int32_t use_2_stage_agg,
+                               const dsgb_base *bases, int32_t nbases,
+                               const dsgb_output *outs, int32_t nouts,
+                               uint32_t flags, void *stream) {
+    LineParams p;
+    int rc = build_line_params(p, cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases);
+    if (rc) return rc;
+    if (!(line_width >= 0.0)) { set_error("dsgb_line_axis0: line_width must be >= 0"); return DSGB_E_INVALID; }
+    p.line_width = line_width;
+    p.plot_start = plot_start;
+    p.overwrite = overwrite;
+    p.use_2_stage = use_2_stage_agg;
+    cudaStream_t st = as_stream(stream);
+    const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    if (!(flags & DSGB_FLAG_NO_INIT)) {
+        rc = bases_init(bases, nbases, ncells, st);
+        if (rc) return rc;
+    }
+    if (n > 1 && nbases > 0) {
+        int sms = sm_count();
+        if (sms <= 0) sms = 148;
+        int64_t blocks = (n + 255) / 256;
+        if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+        line_axis0_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
+        DSGB_CHECK_LAUNCH("line_axis0 kernel");
+    }
+    if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+        rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+    return rc;
+}

@@ -1,0 +1,432 @@
+// points.cu -- Canvas.points on GB300: projection + fused aggregation.
+//
+// Replaces Point._build_extend (datashader/glyphs/points.py:182-242) and the
+// per-reduction append functions that compiler.make_append fuses
+// (datashader/compiler.py:321-475).
+//
+// Binning semantics (points.py:190-204): a row is kept when
+// xmin <= x <= xmax and ymin <= y <= ymax (inclusive, float64 compares);
+// xx = int(x*sx + tx) with the product and the sum each rounded in float64
+// (numba emits no FMA) and int() truncating toward zero; xx >= width maps to
+// width-1.
+//
+// GB300 has little float64 throughput, so the kernel bins in float32 and
+// proves the result: with E a host-computed bound on |float32 result -
+// float64 result| (binning_error_bound below), a point whose float32 value is
+// farther than E from every integer lands in the same bin as the float64
+// computation.  Points within E of a pixel edge (about 1 in 2000 at
+// 1024 px) are recomputed with the exact float64 formula.  The result is
+// bit-identical to the reference's binning.
+#include "dsgb_internal.cuh"
+
+#include <cmath>
+#include <float.h>
+#include <math.h>
+
+namespace dsgb {
+
+
+struct PointsParams {
+    ColumnRef cols[MAX_COLS];
+    BaseDev bases[MAX_BASES];
+    int32_t ncols, nbases;
+    int64_t n, row_offset;
+    int32_t x_col, y_col;
+    int32_t width, height;
+    int32_t x_log, y_log;
+    double sx, tx, sy, ty;
+    double xmin, xmax, ymin, ymax;
+    // float32 fast path
+    float xminf, xmaxf, yminf, ymaxf;  // exact float images of the inclusive bounds
+    float sxf, txf, syf, tyf;
+    float ex, ey;                      // proven |float32 - float64| bounds (pixels)
+    long long kxmin, kxmax, kymin, kymax;  // order-preserving keys of the bounds
+};
+
+// ------------------------------------------------------------------ binning
+
+// Exact float64 binning of one coordinate (points.py:199-203).
+__device__ __forceinline__ int bin_exact(double m, double s, double t, int n) {
+    double v = __dadd_rn(__dmul_rn(m, s), t);
+    long long xx = __double2ll_rz(v);
+    if (xx >= n) xx = n - 1;
+    if (xx < 0) xx += n;           // numba indexes negative positions from the end
+    if (xx < 0) xx = 0;            // not reachable after the bounds test; memory safety
+    return (int)xx;
+}
+
+// float32 binning with the exact fallback near pixel edges.
+__device__ __forceinline__ int bin_fast(float xf, double xd, float sf, float tf, float e,
+                                        double s, double t, int n) {
+    float v = __fmaf_rn(xf, sf, tf);
+    float fl = floorf(v);
+    float d = fminf(v - fl, (fl + 1.0f) - v);
+    if (d > e) {
+        int xx = __float2int_rz(v);
+        if (xx >= n) xx = n - 1;
+        if (xx < 0) xx += n;
+        if (xx < 0) xx = 0;
+        return xx;
+    }
+    return bin_exact(xd, s, t, n);
+}
+
+// Float32 image of a double by mantissa truncation, integer ops only.
+// Returns false (caller uses the exact path) outside the normal float range.
+__device__ __forceinline__ bool f64_to_f32_trunc(double x, float &out) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if ((b << 1) == 0) { out = 0.0f; return true; }
+    int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+    if (e <= 0 || e >= 255) return false;
+    unsigned m = (unsigned)((b >> 29) & 0x7fffffu);
+    out = __uint_as_float(((unsigned)(b >> 63) << 31) | ((unsigned)e << 23) | m);
+    return true;
+}
+
+__device__ __forceinline__ long long key_canon(double v) {
+    long long b = __double_as_longlong(v);
+    if (b == (long long)0x8000000000000000ull) b = 0;  // -0.0 compares equal to +0.0
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+
+// Each binning routine returns false for rows outside the bounds.
+__device__ __forceinline__ bool bin_f32_fast(const PointsParams &p, float x, float y, int &xi, int &yi) {
+    if (!(x >= p.xminf && x <= p.xmaxf && y >= p.yminf && y <= p.ymaxf)) return false;
+    xi = bin_fast(x, (double)x, p.sxf, p.txf, p.ex, p.sx, p.tx, p.width);
+    yi = bin_fast(y, (double)y, p.syf, p.tyf, p.ey, p.sy, p.ty, p.height);
+    return true;
+}
+
+__device__ __forceinline__ bool bin_f64_fast(const PointsParams &p, double x, double y, int &xi, int &yi) {
+    long long kx = key_canon(x), ky = key_canon(y);
+    // NaN keys fall outside every finite-or-infinite bound interval.
+    if (!(kx >= p.kxmin && kx <= p.kxmax && ky >= p.kymin && ky <= p.kymax)) return false;
+    float xf, yf;
+    if (f64_to_f32_trunc(x, xf)) xi = bin_fast(xf, x, p.sxf, p.txf, p.ex, p.sx, p.tx, p.width);
+    else xi = bin_exact(x, p.sx, p.tx, p.width);
+    if (f64_to_f32_trunc(y, yf)) yi = bin_fast(yf, y, p.syf, p.tyf, p.ey, p.sy, p.ty, p.height);
+    else yi = bin_exact(y, p.sy, p.ty, p.height);
+    return true;
+}
+
+__device__ __forceinline__ bool bin_exact_xy(const PointsParams &p, double x, double y, int &xi, int &yi) {
+    if (!((p.xmin <= x && x <= p.xmax) && (p.ymin <= y && y <= p.ymax))) return false;
+    double mx = p.x_log ? log10(x) : x;   // LogAxis.mapper (core.py:131-134)
+    double my = p.y_log ? log10(y) : y;
+    xi = bin_exact(mx, p.sx, p.tx, p.width);
+    yi = bin_exact(my, p.sy, p.ty, p.height);
+    return true;
+}
+
+// ---------------------------------------------------------------- appends
+
+// The GPU form of the fused append: one pass over the bases for row i.
+__device__ __forceinline__ void accumulate(const PointsParams &p, int64_t i, int64_t pix) {
+    const long long row = (long long)(i + p.row_offset);
+#pragma unroll 1
+    for (int b = 0; b < p.nbases; ++b) {
+        const BaseDev &B = p.bases[b];
+        int64_t cell = pix;
+        if (B.cat_col >= 0) {
+            // compiler.py:379-390 -- agg[:, :, int(code)], negative codes wrap
+            long long c = load_i64(p.cols[B.cat_col], i);
+            if (c < 0) c += B.ncat;
+            if (c < 0 || c >= B.ncat) continue;
+            cell = pix * B.ncat + c;
+        }
+        double field = 0.0;
+        bool has = true;
+        if (B.col >= 0) {
+            field = load_f64(p.cols[B.col], i);
+            has = !isnull(field);
+        }
+        if (!has) continue;
+        switch (B.op) {
+        case DSGB_BASE_COUNT: atomicAdd((unsigned *)B.agg + cell, 1u); break;
+        case DSGB_BASE_ANY: ((volatile uint8_t *)B.agg)[cell] = 1; break;
+        case DSGB_BASE_SUM: atomicAdd((double *)B.agg + cell, field); break;
+        case DSGB_BASE_MAX: atomic_max_key((long long *)B.agg + cell, f64_key(field)); break;
+        case DSGB_BASE_MIN: atomic_min_key((long long *)B.agg + cell, f64_key(field)); break;
+        case DSGB_BASE_MIN_ROW: atomic_min_key((long long *)B.agg + cell, row); break;
+        case DSGB_BASE_MAX_ROW: atomic_max_key((long long *)B.agg + cell, row); break;
+        case DSGB_BASE_ARGMAX: pair_update<true>((long long *)B.agg + 2 * cell, f64_key(field), row); break;
+        case DSGB_BASE_ARGMIN: pair_update<false>((long long *)B.agg + 2 * cell, f64_key(field), row); break;
+        default: break;
+        }
+    }
+}
+
+enum Mode { MODE_GENERIC = 0, MODE_COUNT = 1, MODE_MEAN = 2 };
+
+// Per-row work of one kernel instantiation.  MEAN: bases[0] = SUM(v), bases[1] = COUNT(v).
+template <int MODE>
+__device__ __forceinline__ void emit(const PointsParams &p, int64_t i, int xi, int yi, double v) {
+    int64_t pix = (int64_t)yi * p.width + xi;
+    if (MODE == MODE_COUNT) {
+        atomicAdd((unsigned *)p.bases[0].agg + pix, 1u);
+    } else if (MODE == MODE_MEAN) {
+        if (!isnull(v)) {
+            atomicAdd((double *)p.bases[0].agg + pix, v);
+            atomicAdd((unsigned *)p.bases[1].agg + pix, 1u);
+        }
+    } else {
+        accumulate(p, i, pix);
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ double mean_value(const PointsParams &p, int64_t i) {
+    if (MODE != MODE_MEAN) return 0.0;
+    return load_f64(p.cols[p.bases[0].col], i);
+}
+
+// float32 coordinates, 4 rows per thread per iteration (float4 streaming loads).
+template <int MODE, bool FAST, bool WARPAGG>
+__global__ void __launch_bounds__(256) points_f32_kernel(const PointsParams p) {
+    const float *xs = (const float *)p.cols[p.x_col].data;
+    const float *ys = (const float *)p.cols[p.y_col].data;
+    const int64_t n4 = p.n >> 2;
+    const float4 *x4 = (const float4 *)xs;
+    const float4 *y4 = (const float4 *)ys;
+    const int lane = threadIdx.x & 31;
+    // Warp-uniform trip count so that the warp-level match below is legal.
+    for (int64_t base = gtid() - lane; base < n4; base += gstride()) {
+        const int64_t v = base + lane;
+        const bool live = v < n4;
+        float4 a = make_float4(0, 0, 0, 0), b = a;
+        if (live) { a = __ldcs(x4 + v); b = __ldcs(y4 + v); }
+        float xa[4] = {a.x, a.y, a.z, a.w};
+        float ya[4] = {b.x, b.y, b.z, b.w};
+        double va[4] = {0, 0, 0, 0};
+        if (MODE == MODE_MEAN && live) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) va[k] = mean_value<MODE>(p, 4 * v + k);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int xi = 0, yi = 0;
+            bool in = live && (FAST ? bin_f32_fast(p, xa[k], ya[k], xi, yi)
+                                    : bin_exact_xy(p, (double)xa[k], (double)ya[k], xi, yi));
+            if (WARPAGG && MODE == MODE_COUNT) {
+                unsigned key = in ? (unsigned)(yi * p.width + xi) : (0x80000000u | (unsigned)lane);
+                unsigned peers = __match_any_sync(0xffffffffu, key);
+                if (in && lane == __ffs(peers) - 1)
+                    atomicAdd((unsigned *)p.bases[0].agg + key, (unsigned)__popc(peers));
+            } else if (in) {
+                emit<MODE>(p, 4 * v + k, xi, yi, va[k]);
+            }
+        }
+    }
+    // tail rows (n not a multiple of 4)
+    for (int64_t i = 4 * n4 + gtid(); i < p.n; i += gstride()) {
+        int xi, yi;
+        float x = xs[i], y = ys[i];
+        bool in = FAST ? bin_f32_fast(p, x, y, xi, yi) : bin_exact_xy(p, (double)x, (double)y, xi, yi);
+        if (in) emit<MODE>(p, i, xi, yi, mean_value<MODE>(p, i));
+    }
+}
+
+// float64 coordinates, 2 rows per thread per iteration (double2 streaming loads).
+template <int MODE, bool FAST>
+__global__ void __launch_bounds__(256) points_f64_kernel(const PointsParams p) {
+    const double *xs = (const double *)p.cols[p.x_col].data;
+    const double *ys = (const double *)p.cols[p.y_col].data;
+    const int64_t n2 = p.n >> 1;
+    const double2 *x2 = (const double2 *)xs;
+    const double2 *y2 = (const double2 *)ys;
+    for (int64_t v = gtid(); v < n2; v += gstride()) {
+        double2 a = __ldcs(x2 + v), b = __ldcs(y2 + v);
+        double xa[2] = {a.x, a.y}, ya[2] = {b.x, b.y};
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            int xi, yi;
+            bool in = FAST ? bin_f64_fast(p, xa[k], ya[k], xi, yi) : bin_exact_xy(p, xa[k], ya[k], xi, yi);
+            if (in) emit<MODE>(p, 2 * v + k, xi, yi, mean_value<MODE>(p, 2 * v + k));
+        }
+    }
+    for (int64_t i = 2 * n2 + gtid(); i < p.n; i += gstride()) {
+        int xi, yi;
+        bool in = FAST ? bin_f64_fast(p, xs[i], ys[i], xi, yi) : bin_exact_xy(p, xs[i], ys[i], xi, yi);
+        if (in) emit<MODE>(p, i, xi, yi, mean_value<MODE>(p, i));
+    }
+}
+
+// Any coordinate dtype (integers, unaligned columns): scalar loads, exact binning.
+template <int MODE>
+__global__ void __launch_bounds__(256) points_any_kernel(const PointsParams p) {
+    for (int64_t i = gtid(); i < p.n; i += gstride()) {
+        int xi, yi;
+        double x = load_f64(p.cols[p.x_col], i), y = load_f64(p.cols[p.y_col], i);
+        if (bin_exact_xy(p, x, y, xi, yi)) emit<MODE>(p, i, xi, yi, mean_value<MODE>(p, i));
+    }
+}
+
+// ------------------------------------------------------------- host side
+
+// Smallest float >= v (as a double compare) / largest float <= v.
+static float float_ceil_of(double v) {
+    if (std::isnan(v)) return NAN;
+    float f = (float)v;
+    if ((double)f < v) f = nextafterf(f, INFINITY);
+    return f;
+}
+static float float_floor_of(double v) {
+    if (std::isnan(v)) return NAN;
+    float f = (float)v;
+    if ((double)f > v) f = nextafterf(f, -INFINITY);
+    return f;
+}
+static long long host_key_canon(double v) {
+    long long b; memcpy(&b, &v, 8);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+
+// Bound on |fma32(x, (float)s, (float)t) - fl64(fl64(x*s) + t)| over
+// lo <= x <= hi, in output units, including the float32 truncation of a
+// float64 x.  Terms: rounding of the float32 result, of (float)s and
+// (float)t, of the float32 image of x, and the two float64 roundings; the
+// factor 4 covers their sum with margin.  Returns +inf when the fast path
+// must not be used.
+static double binning_error_bound(double lo, double hi, double s, double t, int n) {
+    if (!std::isfinite(lo) || !std::isfinite(hi) || !std::isfinite(s) || !std::isfinite(t))
+        return INFINITY;
+    double xm = std::fmax(std::fabs(lo), std::fabs(hi));
+    double mag = xm * std::fabs(s) + std::fabs(t) + (double)n + 1.0;
+    if (!(mag < 1e6) || std::fabs(s) > 1e30 || xm > 1e30) return INFINITY;
+    return 4.0 * ldexp(1.0, -23) * mag;
+}
+
+static int build_params(PointsParams &p, const dsgb_column *cols, int32_t ncols, int64_t n,
+                        int64_t row_offset, int32_t x_col, int32_t y_col,
+                        const dsgb_canvas *cv, const dsgb_base *bases, int32_t nbases) {
+    if (!cols || !cv || ncols <= 0 || ncols > MAX_COLS || n < 0 || nbases < 0 || nbases > MAX_BASES ||
+        (nbases > 0 && !bases)) {
+        set_error("dsgb_points: invalid arguments (ncols=%d, n=%lld, nbases=%d)", ncols, (long long)n, nbases);
+        return DSGB_E_INVALID;
+    }
+    if (x_col < 0 || x_col >= ncols || y_col < 0 || y_col >= ncols) {
+        set_error("dsgb_points: x_col/y_col out of range");
+        return DSGB_E_INVALID;
+    }
+    if (cv->width <= 0 || cv->height <= 0) {
+        set_error("dsgb_points: invalid canvas size %dx%d", cv->width, cv->height);
+        return DSGB_E_INVALID;
+    }
+    memset(&p, 0, sizeof(p));
+    for (int c = 0; c < ncols; ++c) {
+        if (dtype_size(cols[c].dtype) == 0 || (n > 0 && !cols[c].data)) {
+            set_error("dsgb_points: column %d has bad dtype %d or null data", c, cols[c].dtype);
+            return DSGB_E_INVALID;
+        }
+        p.cols[c].data = cols[c].data;
+        p.cols[c].dtype = cols[c].dtype;
+    }
+    for (int b = 0; b < nbases; ++b) {
+        const dsgb_base &B = bases[b];
+        if (!B.agg || B.col >= ncols || B.cat_col >= ncols || B.ncat < 1 ||
+            B.op < DSGB_BASE_COUNT || B.op > DSGB_BASE_ARGMIN) {
+            set_error("dsgb_points: base %d invalid (op=%d col=%d cat=%d ncat=%d)", b, B.op, B.col,
+                      B.cat_col, B.ncat);
+            return DSGB_E_INVALID;
+        }
+        p.bases[b] = BaseDev{B.op, B.col, B.cat_col < 0 ? -1 : B.cat_col, B.ncat, B.flags, B.agg};
+    }
+    p.ncols = ncols; p.nbases = nbases; p.n = n; p.row_offset = row_offset;
+    p.x_col = x_col; p.y_col = y_col;
+    p.width = cv->width; p.height = cv->height; p.x_log = cv->x_log; p.y_log = cv->y_log;
+    p.sx = cv->sx; p.tx = cv->tx; p.sy = cv->sy; p.ty = cv->ty;
+    p.xmin = cv->xmin; p.xmax = cv->xmax; p.ymin = cv->ymin; p.ymax = cv->ymax;
+    p.xminf = float_ceil_of(cv->xmin); p.xmaxf = float_floor_of(cv->xmax);
+    p.yminf = float_ceil_of(cv->ymin); p.ymaxf = float_floor_of(cv->ymax);
+    p.sxf = (float)cv->sx; p.txf = (float)cv->tx; p.syf = (float)cv->sy; p.tyf = (float)cv->ty;
+    p.kxmin = host_key_canon(cv->xmin); p.kxmax = host_key_canon(cv->xmax);
+    p.kymin = host_key_canon(cv->ymin); p.kymax = host_key_canon(cv->ymax);
+    p.ex = (float)binning_error_bound(cv->xmin, cv->xmax, cv->sx, cv->tx, cv->width);
+    p.ey = (float)binning_error_bound(cv->ymin, cv->ymax, cv->sy, cv->ty, cv->height);
+    return DSGB_OK;
+}
+
+static bool aligned16(const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; }
+
+int launch_points(const PointsParams &p, uint32_t flags, cudaStream_t st) {
+    if (p.n == 0 || p.nbases == 0) return DSGB_OK;
+    int mode = MODE_GENERIC;
+    if (p.nbases == 1 && p.bases[0].op == DSGB_BASE_COUNT && p.bases[0].col < 0 && p.bases[0].cat_col < 0)
+        mode = MODE_COUNT;
+    else if (p.nbases == 2 && p.bases[0].op == DSGB_BASE_SUM && p.bases[1].op == DSGB_BASE_COUNT &&
+             p.bases[0].col >= 0 && p.bases[0].col == p.bases[1].col &&
+             p.bases[0].cat_col < 0 && p.bases[1].cat_col < 0)
+        mode = MODE_MEAN;
+    const int xdt = p.cols[p.x_col].dtype, ydt = p.cols[p.y_col].dtype;
+    const void *xp = p.cols[p.x_col].data, *yp = p.cols[p.y_col].data;
+    const bool fast = !(flags & DSGB_FLAG_EXACT_BIN) && !p.x_log && !p.y_log &&
+                      std::isfinite(p.ex) && std::isfinite(p.ey) && p.ex < 0.01f && p.ey < 0.01f;
+    const bool warpagg = (flags & DSGB_FLAG_WARP_AGG) != 0;
+    const int threads = 256;
+    int sms = sm_count();
+    if (sms <= 0) sms = 148;
+    int64_t blocks = (int64_t)sms * 8;
+    if (xdt == DSGB_F32 && ydt == DSGB_F32 && aligned16(xp) && aligned16(yp)) {
+        int64_t need = ((p.n >> 2) + threads - 1) / threads;
+        if (need < 1) need = 1;
+        if (blocks > need) blocks = need;
+#define DSGB_L32(M, F, W) points_f32_kernel<M, F, W><<<(unsigned)blocks, threads, 0, st>>>(p)
+        if (mode == MODE_COUNT) {
+            if (fast) { if (warpagg) DSGB_L32(MODE_COUNT, true, true); else DSGB_L32(MODE_COUNT, true, false); }
+            else { if (warpagg) DSGB_L32(MODE_COUNT, false, true); else DSGB_L32(MODE_COUNT, false, false); }
+        } else if (mode == MODE_MEAN) {
+            if (fast) DSGB_L32(MODE_MEAN, true, false); else DSGB_L32(MODE_MEAN, false, false);
+        } else {
+            if (fast) DSGB_L32(MODE_GENERIC, true, false); else DSGB_L32(MODE_GENERIC, false, false);
+        }
+#undef DSGB_L32
+    } else if (xdt == DSGB_F64 && ydt == DSGB_F64 && aligned16(xp) && aligned16(yp)) {
+        int64_t need = ((p.n >> 1) + threads - 1) / threads;
+        if (need < 1) need = 1;
+        if (blocks > need) blocks = need;
+#define DSGB_L64(M, F) points_f64_kernel<M, F><<<(unsigned)blocks, threads, 0, st>>>(p)
+        if (mode == MODE_COUNT) { if (fast) DSGB_L64(MODE_COUNT, true); else DSGB_L64(MODE_COUNT, false); }
+        else if (mode == MODE_MEAN) { if (fast) DSGB_L64(MODE_MEAN, true); else DSGB_L64(MODE_MEAN, false); }
+        else { if (fast) DSGB_L64(MODE_GENERIC, true); else DSGB_L64(MODE_GENERIC, false); }
+#undef DSGB_L64
+    } else {
+        int64_t need = (p.n + threads - 1) / threads;
+        if (blocks > need) blocks = need;
+        if (mode == MODE_COUNT) points_any_kernel<MODE_COUNT><<<(unsigned)blocks, threads, 0, st>>>(p);
+        else if (mode == MODE_MEAN) points_any_kernel<MODE_MEAN><<<(unsigned)blocks, threads, 0, st>>>(p);
+        else points_any_kernel<MODE_GENERIC><<<(unsigned)blocks, threads, 0, st>>>(p);
+    }
+    DSGB_CHECK_LAUNCH("points kernel launch");
+    return DSGB_OK;
+}
+
+int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st);
+int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
+                     const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                     int64_t ncells, cudaStream_t st);
+
+}  // namespace dsgb
+
+using namespace dsgb;
+
+extern "C" int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                           int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                           const dsgb_base *bases, int32_t nbases,
+                           const dsgb_output *outs, int32_t nouts,
+                           uint32_t flags, void *stream) {
+    PointsParams p;
+    int rc = build_params(p, cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases);
+    if (rc) return rc;
+    cudaStream_t st = as_stream(stream);
+    const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    if (!(flags & DSGB_FLAG_NO_INIT)) {
+        rc = bases_init(bases, nbases, ncells, st);
+        if (rc) return rc;
+    }
+    rc = launch_points(p, flags, st);
+    if (rc) return rc;
+    if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+        rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+    return rc;
+}

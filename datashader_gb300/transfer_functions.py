@@ -1,0 +1,136 @@
+"""tf.shade(how='eq_hist') and eq_hist on the GPU.
+
+Mirrors datashader/transfer_functions/__init__.py: shade (616-745) for 2-D
+aggregates with a list colormap, the _interpolate prologue (251-297),
+eq_hist (148-223), _rescale_discrete_levels (234-248) and the list-colormap
+RGBA branch (317-351).  The histogram, CDF, lookup and colouring run in one
+libdsgb call (eq_hist.cu); other ``how`` values and colormap kinds are
+outside the GPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _native as N
+from .core import Aggregate
+
+# CSS named colours (the subset most used with datashader palettes).
+_CSS = {
+    "aliceblue": "#F0F8FF", "antiquewhite": "#FAEBD7", "aqua": "#00FFFF", "aquamarine": "#7FFFD4",
+    "azure": "#F0FFFF", "beige": "#F5F5DC", "black": "#000000", "blue": "#0000FF",
+    "blueviolet": "#8A2BE2", "brown": "#A52A2A", "cadetblue": "#5F9EA0", "chartreuse": "#7FFF00",
+    "coral": "#FF7F50", "cornflowerblue": "#6495ED", "crimson": "#DC143C", "cyan": "#00FFFF",
+    "darkblue": "#00008B", "darkcyan": "#008B8B", "darkgray": "#A9A9A9", "darkgreen": "#006400",
+    "darkgrey": "#A9A9A9", "darkorange": "#FF8C00", "darkred": "#8B0000", "darkviolet": "#9400D3",
+    "deeppink": "#FF1493", "deepskyblue": "#00BFFF", "dodgerblue": "#1E90FF", "firebrick": "#B22222",
+    "forestgreen": "#228B22", "fuchsia": "#FF00FF", "gold": "#FFD700", "gray": "#808080",
+    "green": "#008000", "greenyellow": "#ADFF2F", "grey": "#808080", "hotpink": "#FF69B4",
+    "indigo": "#4B0082", "ivory": "#FFFFF0", "khaki": "#F0E68C", "lavender": "#E6E6FA",
+    "lightblue": "#ADD8E6", "lightcoral": "#F08080", "lightcyan": "#E0FFFF", "lightgray": "#D3D3D3",
+    "lightgreen": "#90EE90", "lightgrey": "#D3D3D3", "lightpink": "#FFB6C1", "lightyellow": "#FFFFE0",
+    "lime": "#00FF00", "magenta": "#FF00FF", "maroon": "#800000", "navy": "#000080",
+    "olive": "#808000", "orange": "#FFA500", "orangered": "#FF4500", "orchid": "#DA70D6",
+    "pink": "#FFC0CB", "plum": "#DDA0DD", "purple": "#800080", "red": "#FF0000",
+    "royalblue": "#4169E1", "salmon": "#FA8072", "seagreen": "#2E8B57", "silver": "#C0C0C0",
+    "skyblue": "#87CEEB", "steelblue": "#4682B4", "tan": "#D2B48C", "teal": "#008080",
+    "tomato": "#FF6347", "turquoise": "#40E0D0", "violet": "#EE82EE", "white": "#FFFFFF",
+    "yellow": "#FFFF00", "yellowgreen": "#9ACD32",
+}
+
+
+def rgb(x):
+    """colors.py:99-128: colour name, '#RRGGBB' or an (r, g, b) tuple."""
+    if isinstance(x, str):
+        h = x if x.startswith("#") else _CSS.get(x)
+        if h is None:
+            raise ValueError(f"Unknown color: '{x}'")
+        if not (h.startswith("#") and len(h) == 7):
+            raise ValueError("Invalid hex color")
+        return int(h[1:3], 16), int(h[3:5], 16), int(h[5:7], 16)
+    if isinstance(x, tuple) and len(x) == 3:
+        if min(x) < 0 or max(x) > 255:
+            raise ValueError("Invalid RGB tuple")
+        return x
+    raise TypeError(f"Don't know how to convert {x} to RGB")
+
+
+class Image(Aggregate):
+    """A uint32 RGBA image (transfer_functions/__init__.py:25-58)."""
+
+
+_WS = {}
+
+
+def _workspace(device, nbins):
+    size = int(N.lib().dsgb_eq_hist_workspace_size(nbins))
+    key = (device, nbins)
+    t = _WS.get(key)
+    if t is None or t.numel() < size:
+        t = torch.empty(size, dtype=torch.uint8, device=device)
+        _WS[key] = t
+    return t
+
+
+def _run_eq_hist(data, nbins=256 * 256, cmap=None, alpha=255, rescale_discrete_levels=False,
+                 stream=None):
+    """One libdsgb eq_hist call.  Returns (equalised f64, levels tensor, rgba or None)."""
+    if data.dtype == torch.uint32:
+        fn = N.lib().dsgb_eq_hist_u32
+    elif data.dtype == torch.float64:
+        fn = N.lib().dsgb_eq_hist_f64
+    else:
+        raise NotImplementedError(f"eq_hist on the GPU path takes uint32 or float64 aggregates, not {data.dtype}")
+    data = data.contiguous()
+    dev = data.device
+    if stream is None:
+        stream = torch.cuda.current_stream(dev).cuda_stream
+    out = torch.empty(data.shape, dtype=torch.float64, device=dev)
+    levels = torch.empty(1, dtype=torch.int64, device=dev)
+    rgba = None
+    cmap_buf = None
+    ncol = 0
+    if cmap is not None:
+        cols = [rgb(c) for c in cmap]
+        if not 1 <= len(cols) <= 16:
+            raise ValueError("colormap must have 1..16 colours")
+        ncol = len(cols)
+        cmap_buf = (ctypes.c_uint8 * (3 * ncol))(*[v for c in cols for v in c])
+        rgba = torch.empty(data.shape, dtype=torch.uint32, device=dev)
+    ws = _workspace(dev, nbins)
+    rc = fn(data.data_ptr(), data.numel(), nbins, out.data_ptr(), levels.data_ptr(),
+            rgba.data_ptr() if rgba is not None else None, cmap_buf, ncol, int(alpha),
+            int(bool(rescale_discrete_levels)), ws.data_ptr(), ws.numel(), stream)
+    N.check(rc, "dsgb_eq_hist")
+    return out, levels, rgba
+
+
+def eq_hist_agg(agg, nbins=256 * 256):
+    """The eq_hist step of shade: mask (0 / NaN), offset, equalise.
+
+    Returns (equalised float64 tensor with NaN where masked, discrete_levels)."""
+    data = agg.data if isinstance(agg, Aggregate) else agg
+    out, levels, _ = _run_eq_hist(data, nbins)
+    return out, int(levels.item())
+
+
+def shade(agg, cmap=("lightblue", "darkblue"), color_key=None, how="eq_hist", alpha=255,
+          min_alpha=40, span=None, name=None, color_baseline=None, rescale_discrete_levels=False):
+    """tf.shade for a 2-D aggregate, how='eq_hist', list colormap."""
+    if not isinstance(agg, Aggregate):
+        raise TypeError("agg must be instance of DataArray")
+    name = agg.name if name is None else name
+    if not ((0 <= min_alpha <= 255) and (0 <= alpha <= 255)):
+        raise ValueError(f"min_alpha ({min_alpha}) and alpha ({alpha}) must be between 0 and 255")
+    if agg.ndim != 2:
+        raise NotImplementedError("only 2-D aggregates are shaded on the GPU path")
+    if how != "eq_hist":
+        raise NotImplementedError("only how='eq_hist' is on the GPU path")
+    if span is not None:
+        raise ValueError("span is not (yet) valid to use with eq_hist")
+    if isinstance(cmap, str) or not isinstance(cmap, (list, tuple)):
+        raise NotImplementedError("only list colormaps are on the GPU path")
+    _, _, rgba = _run_eq_hist(agg.data, cmap=list(cmap), alpha=alpha,
+                              rescale_discrete_levels=rescale_discrete_levels)
+    return Image(rgba, agg.dims, agg.coords, agg.attrs, name=name)

@@ -1,0 +1,239 @@
+/*
+ * dsgb.h -- C ABI of libdsgb, the GB300 (sm_103a) projection + aggregation
+ * library behind datashader's Canvas.points / Canvas.line / tf.shade(eq_hist).
+ *
+ * Plain C: pointers, sizes and PODs only, no C++ or torch types.  Every
+ * entry point returns DSGB_OK (0) or a negative DSGB_E_* code and never
+ * aborts; dsgb_last_error() gives a thread-local message.  All device memory
+ * (columns, base accumulators, outputs, workspaces) is owned by the caller;
+ * calls are asynchronous on the caller's stream (a cudaStream_t passed as
+ * void*, NULL = legacy default stream).
+ *
+ * Mapping onto the reference (datashader 0.19.1):
+ *   - dsgb_points      replaces Point._build_extend's extend()
+ *                      (datashader/glyphs/points.py:182-242) together with
+ *                      the create/append/finalize functions that
+ *                      compiler.compile_components builds
+ *                      (datashader/compiler.py:36-150, 294-536).
+ *   - dsgb_line_axis0  replaces LineAxis0._internal_build_extend's extend()
+ *                      (datashader/glyphs/line.py:59-103, 1033-1149).
+ *   - dsgb_eq_hist_u32 / dsgb_eq_hist_f64 replace tf.eq_hist
+ *                      (datashader/transfer_functions/__init__.py:148-223)
+ *                      plus the mask/offset prologue of _interpolate
+ *                      (:251-297) and, optionally, the list-colormap RGBA
+ *                      step (:317-351).
+ *   - dsgb_bounds      replaces Glyph._compute_bounds_numba
+ *                      (datashader/glyphs/glyph.py:66-78).
+ *   - dsgb_pyramid     renders a quadtree of tiles in one persistent launch
+ *                      (each tile equal to a Canvas.points call, see
+ *                      datashader/tiles.py:70-130 for the reference's
+ *                      per-tile driver).
+ *   - dsgb_line_axis0_backward is the adjoint of dsgb_line_axis0 for the
+ *                      antialiased sum reduction (no reference counterpart;
+ *                      it differentiates line.py:826-981).
+ */
+#ifndef DSGB_H
+#define DSGB_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DSGB_ABI_VERSION 1
+
+/* Status codes. */
+#define DSGB_OK             0
+#define DSGB_E_INVALID     -1  /* bad argument (null pointer, size, index) */
+#define DSGB_E_UNSUPPORTED -2  /* dtype / op combination not implemented */
+#define DSGB_E_CUDA        -3  /* CUDA runtime error (message in dsgb_last_error) */
+#define DSGB_E_TIMEOUT     -4  /* a bounded device wait gave up */
+#define DSGB_E_NOSPACE     -5  /* workspace too small */
+
+/* Column element types. */
+typedef enum {
+    DSGB_F32 = 1, DSGB_F64 = 2, DSGB_I8 = 3, DSGB_U8 = 4, DSGB_I16 = 5,
+    DSGB_I32 = 6, DSGB_I64 = 7, DSGB_U32 = 8, DSGB_BOOL = 9
+} dsgb_dtype;
+
+typedef struct {
+    const void *data;   /* device pointer, n elements, contiguous */
+    int32_t dtype;      /* dsgb_dtype */
+    int32_t reserved;
+} dsgb_column;
+
+/* The canvas of one aggregation.  s/t are computed by the caller exactly as
+ * Axis.compute_scale_and_translate (datashader/core.py:62-81):
+ * s = n/(end-start), t = -start*s on the mapped range; x_log / y_log select
+ * LogAxis.mapper (core.py:127-145) on the device. */
+typedef struct {
+    int32_t width, height;
+    int32_t x_log, y_log;
+    double sx, tx, sy, ty;
+    double xmin, xmax, ymin, ymax;   /* inclusive bounds (points.py:198) */
+} dsgb_canvas;
+
+/* Base accumulator operations (the GPU form of Reduction._build_bases,
+ * reductions.py).  Each base owns one caller-allocated device array of
+ * height*width*ncat elements, laid out [y][x][cat] (row 0 = y_min). */
+typedef enum {
+    DSGB_BASE_COUNT     = 1,  /* uint32: rows (col<0) or non-NaN col values      */
+    DSGB_BASE_ANY       = 2,  /* uint8 : 1 where some row (non-NaN col) landed  */
+    DSGB_BASE_SUM       = 3,  /* double: sum of non-NaN col values, zero-init   */
+    DSGB_BASE_MAX       = 4,  /* int64 : order-preserving key of the max value  */
+    DSGB_BASE_MIN       = 5,  /* int64 : order-preserving key of the min value  */
+    DSGB_BASE_MIN_ROW   = 6,  /* int64 : smallest row index with non-NaN col    */
+    DSGB_BASE_MAX_ROW   = 7,  /* int64 : largest row index with non-NaN col     */
+    DSGB_BASE_ARGMAX    = 8,  /* 2 x int64 {key,row}: max value, first row on ties */
+    DSGB_BASE_ARGMIN    = 9,  /* 2 x int64 {key,row}: min value, first row on ties */
+    /* antialiased-line forms (value = col * coverage) */
+    DSGB_BASE_AA_SUM    = 10, /* double: sum of w*(aa - prev_aa), w = col or 1    */
+    DSGB_BASE_AA_CNT0   = 11, /* uint32: rows whose prev_aa == 0 (mean count)   */
+    DSGB_BASE_AA_MAX    = 12, /* int64 key: max of w*aa, w = col or 1            */
+    DSGB_BASE_AA_ARGMAX = 13  /* {key,row}: max of w*aa, first row on ties       */
+} dsgb_base_op;
+
+#define DSGB_BASEF_UNWEIGHTED 0x1  /* antialiased forms: the column only gates NaN rows,
+                                       the value is the coverage itself */
+
+typedef struct {
+    int32_t op;        /* dsgb_base_op */
+    int32_t col;       /* value column index, -1 = none (count/any of every row) */
+    int32_t cat_col;   /* category-code column index, -1 = not categorical */
+    int32_t ncat;      /* categories (>= 1) */
+    int32_t flags;     /* DSGB_BASEF_* */
+    int32_t reserved;
+    void *agg;         /* device accumulator */
+} dsgb_base;
+
+/* Finalize operations (Reduction._finalize / make_finalize, compiler.py:510-536). */
+typedef enum {
+    DSGB_FIN_SUM_NAN    = 1,  /* f64 out = any ? sum : NaN          (b0 SUM/AA_SUM, b1 COUNT/ANY) */
+    DSGB_FIN_MEAN       = 2,  /* f64 out = cnt>0 ? sum/cnt : NaN    (b0 SUM/AA_SUM, b1 COUNT/AA_CNT0) */
+    DSGB_FIN_KEY_F64    = 3,  /* f64 out = decode(key) or NaN       (b0 MAX/MIN/ARGMAX/ARGMIN/AA_MAX) */
+    DSGB_FIN_ROW        = 4,  /* i64 out = row or -1                (b0 MIN_ROW/MAX_ROW/ARGMAX/ARGMIN) */
+    DSGB_FIN_GATHER     = 5,  /* f64 out = col[row-row_offset] or NaN (b0 row-valued base, col) */
+    DSGB_FIN_KEY_F32    = 6,  /* f32 out = (float)decode(key) or NaN (b0 AA_MAX) */
+    DSGB_FIN_SUM_F32    = 7,  /* f32 out = any ? (float)sum : NaN   (b0 AA_SUM, b1 ANY) */
+    DSGB_FIN_COPY       = 8   /* out = base bytes (count, any)       (b0) */
+} dsgb_fin_op;
+
+typedef struct {
+    int32_t op;        /* dsgb_fin_op */
+    int32_t base0, base1;
+    int32_t col;       /* DSGB_FIN_GATHER: lookup column */
+    void *out;         /* device output, height*width*ncat elements of the op's type */
+} dsgb_output;
+
+/* Flags. */
+#define DSGB_FLAG_NO_INIT      0x1u  /* accumulate into the bases as they are */
+#define DSGB_FLAG_NO_FINALIZE  0x2u  /* skip the finalize step */
+#define DSGB_FLAG_EXACT_BIN    0x4u  /* always bin in float64 (disable the float32 fast path) */
+#define DSGB_FLAG_WARP_AGG     0x8u  /* warp-level pre-aggregation of identical pixels */
+
+/* ---- informational ---------------------------------------------------- */
+int dsgb_abi_version(void);
+const char *dsgb_last_error(void);
+/* Number of SMs of the current device (grid sizing), or a negative code. */
+int dsgb_device_sm_count(void);
+
+/* ---- bases ------------------------------------------------------------ */
+/* Fill each base with its initial value (reductions.py:397-472). */
+int dsgb_bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, void *stream);
+/* Run the finalize step for bases that were filled by earlier calls. */
+int dsgb_finalize(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
+                  const dsgb_base *bases, int32_t nbases,
+                  const dsgb_output *outs, int32_t nouts, int64_t ncells, void *stream);
+
+/* ---- Canvas.points ------------------------------------------------------
+ * Replaces points.py:182-242 (+ compiler.py create/append/finalize).
+ * n rows of columns cols[0..ncols); x_col / y_col index the coordinates;
+ * row_offset is added to row indexes (first/last/where). */
+int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                const dsgb_base *bases, int32_t nbases,
+                const dsgb_output *outs, int32_t nouts,
+                uint32_t flags, void *stream);
+
+/* ---- Canvas.line, LineAxis0 glyph ----------------------------------------
+ * Replaces line.py:59-103 + 1033-1149.  line_width == 0 draws Bresenham
+ * lines, > 0 antialiased lines; overwrite / use_2_stage_agg follow
+ * antialias.py:30-58 (two_stage_agg) for the reductions in `bases`. */
+int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                    int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                    double line_width, int32_t plot_start, int32_t overwrite,
+                    int32_t use_2_stage_agg,
+                    const dsgb_base *bases, int32_t nbases,
+                    const dsgb_output *outs, int32_t nouts,
+                    uint32_t flags, void *stream);
+
+/* Adjoint of the antialiased LineAxis0 sum('v') aggregate (self-intersecting
+ * form): given dL/dagg (f64, height*width), accumulate dL/dv (f64, n) and
+ * dL/dy (f64, n, y in data units) with coverage recomputed, not stored.
+ * `agg_any` (uint8, may be NULL) masks pixels that the forward left NaN. */
+int dsgb_line_axis0_backward(const dsgb_column *cols, int32_t ncols, int64_t n,
+                             int32_t x_col, int32_t y_col, int32_t v_col,
+                             const dsgb_canvas *canvas, double line_width,
+                             int32_t plot_start, const double *grad_agg,
+                             const uint8_t *agg_any, double *grad_v, double *grad_y,
+                             void *stream);
+
+/* Adjoint of points sum / mean w.r.t. the value column (gather):
+ * grad_v[i] = grad_agg[p(i)] (sum) or grad_agg[p(i)]/count[p(i)] (mean when
+ * counts != NULL); rows that are NaN or out of bounds get 0. */
+int dsgb_points_backward(const dsgb_column *cols, int32_t ncols, int64_t n,
+                         int32_t x_col, int32_t y_col, int32_t v_col,
+                         const dsgb_canvas *canvas, const double *grad_agg,
+                         const uint32_t *counts, double *grad_v, uint32_t flags, void *stream);
+
+/* ---- autorange ----------------------------------------------------------
+ * glyph.py:66-78: NaN-skipping min and max of a column into out_minmax[0..1]
+ * (device, double).  Empty / all-NaN gives (+inf, -inf). */
+int dsgb_bounds(const dsgb_column *col, int64_t n, double *out_minmax, void *stream);
+
+/* ---- eq_hist (transfer_functions/__init__.py:148-223, 251-297) -----------
+ * Input: a uint32 aggregate (count) or a float64 aggregate; masked pixels are
+ * 0 (uint32) or NaN (float64).  Output: out (f64, NaN where masked) = the
+ * equalised value; *levels (device int64) = discrete_levels; when rgba != NULL
+ * the list-colormap RGBA image (uint32) is also written, with `ncolors` colour
+ * stops in `cmap_rgb` (host, 3*ncolors bytes) and `alpha`, `rescale` as in
+ * tf.shade.  `workspace` must hold dsgb_eq_hist_workspace_size() bytes. */
+size_t dsgb_eq_hist_workspace_size(int32_t nbins);
+int dsgb_eq_hist_u32(const uint32_t *data, int64_t n, int32_t nbins,
+                     double *out, int64_t *levels, uint32_t *rgba,
+                     const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                     int32_t rescale_discrete_levels,
+                     void *workspace, size_t workspace_bytes, void *stream);
+int dsgb_eq_hist_f64(const double *data, int64_t n, int32_t nbins,
+                     double *out, int64_t *levels, uint32_t *rgba,
+                     const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                     int32_t rescale_discrete_levels,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---- batched tile pyramid --------------------------------------------------
+ * Every tile (z, tx, ty) for z in [zmin, zmax] of the [x0,x1)x[y0,y1) square
+ * is a tile_size x tile_size Canvas.points aggregate with inclusive bounds
+ * (points on a shared edge count in both tiles).  Tiles are stored level by
+ * level, row-major by (ty, tx), each [tile_size][tile_size].  Computes count
+ * (uint32) and, when v_col >= 0, max(v) as an int64 key array (decode with
+ * DSGB_FIN_KEY_F64 semantics, done by dsgb_pyramid_finalize).
+ * `config` selects the shared-memory privatisation (autotuned by the caller):
+ * smem_levels = number of coarse levels privatised per block. */
+typedef struct {
+    int32_t zmin, zmax, tile_size, smem_levels;
+    int32_t blocks_per_sm, threads;
+    double x0, x1, y0, y1;
+} dsgb_pyramid_config;
+int64_t dsgb_pyramid_tile_offset(int32_t zmin, int32_t z, int32_t tile_size);
+int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n,
+                 int32_t x_col, int32_t y_col, int32_t v_col,
+                 const dsgb_pyramid_config *config,
+                 uint32_t *counts, int64_t *max_keys, uint32_t flags, void *stream);
+int dsgb_pyramid_finalize(const int64_t *max_keys, double *max_out, int64_t ncells, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DSGB_H */

@@ -1,0 +1,294 @@
+"""CPU oracle for the datashader aggregation hot path -- TEST INFRASTRUCTURE ONLY.
+
+This package restates the reference's CPU algorithm (datashader 0.19.1, the
+numba path) so that the GPU kernels can be checked against it:
+
+* ``dsgb_oracle.c`` -- points binning, the reduction append functions, and
+  LineAxis0 (clipping, Bresenham, antialiased coverage), row by row, serial,
+  compiled with ``-ffp-contract=off``;
+* ``eq_hist.py`` -- the eq_hist histogram/CDF step and the list-colormap
+  shading of ``tf.shade`` restated with numpy (the reference calls numpy for
+  these steps itself).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this package, and only as the checker / baseline.
+The product path (``datashader_gb300``) never imports it.
+
+Parity is pinned by ``tests/test_oracle_golden.py`` against the golden
+vectors of the reference's own test-suite (extracted to ``tests/golden/``).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+KIND = {
+    "count": 1, "any": 2, "sum": 3, "sum_zero": 4, "mean": 5, "min": 6, "max": 7,
+    "first": 8, "last": 9, "min_row": 10, "max_row": 11, "where": 12,
+    "count_ignore_aa": 13,
+}
+
+
+class _Red(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32), ("col", ctypes.c_int32), ("sel_kind", ctypes.c_int32),
+        ("sel_col", ctypes.c_int32), ("lookup_col", ctypes.c_int32), ("cat_col", ctypes.c_int32),
+        ("ncat", ctypes.c_int32), ("self_intersect", ctypes.c_int32),
+        ("agg", ctypes.c_void_p), ("agg2", ctypes.c_void_p),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile the C oracle (gcc, -ffp-contract=off) into oracle/_build."""
+    src = os.path.join(_HERE, "dsgb_oracle.c")
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(src)):
+        return _LIB_PATH
+    os.makedirs(os.path.dirname(_LIB_PATH), exist_ok=True)
+    tmp = _LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call([
+        os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+        "-std=c11", "-shared", "-o", tmp, src, "-lm"])
+    os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(_LIB_PATH)
+            L.oracle_init.argtypes = [ctypes.POINTER(_Red), ctypes.c_int, ctypes.c_int64, ctypes.c_int]
+            L.oracle_points.argtypes = [
+                ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 8 + [
+                ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
+            L.oracle_line_axis0.argtypes = [
+                ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 9 + [
+                ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
+            L.oracle_bounds.argtypes = [ctypes.c_int64, ctypes.c_void_p,
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+            _lib = L
+    return _lib
+
+
+# --------------------------------------------------------------------------
+# Reduction specs.  A spec is a dict:
+#   {"kind": <KIND key>, "column": name|None, "selector": spec|None,
+#    "lookup": name|None, "cat": name|None, "ncat": int, "self_intersect": bool}
+# --------------------------------------------------------------------------
+
+def spec(kind, column=None, *, selector=None, lookup=None, cat=None, ncat=1,
+         self_intersect=True):
+    return dict(kind=kind, column=column, selector=selector, lookup=lookup, cat=cat,
+                ncat=ncat, self_intersect=self_intersect)
+
+
+def scale_translate(rng, n, log=False):
+    """core.py:62-81 -- s = n/(end-start), t = -start*s, in Python floats."""
+    start, end = rng
+    if log:
+        start, end = math.log10(float(start)), math.log10(float(end))
+    s = n / (end - start)
+    t = -start * s
+    return s, t
+
+
+def maybe_expand_bounds(bounds):
+    """glyph.py:42-49."""
+    mn, mx = bounds
+    if not (np.isfinite(mn) and np.isfinite(mx)):
+        mn, mx = -1.0, 1.0
+    elif mn == mx:
+        mn, mx = mn - 1, mn + 1
+    return mn, mx
+
+
+def compute_bounds(v):
+    """glyph.py:66-78 via the C restatement."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    mn, mx = ctypes.c_double(), ctypes.c_double()
+    lib().oracle_bounds(v.size, v.ctypes.data, ctypes.byref(mn), ctypes.byref(mx))
+    return mn.value, mx.value
+
+
+def _agg_dtype(kind, antialias, lookup_is_row=False):
+    if kind == "count":
+        return np.float32 if antialias else np.uint32
+    if kind == "count_ignore_aa":
+        return np.uint32
+    if kind == "any":
+        return np.float32 if antialias else np.uint8
+    if kind in ("min_row", "max_row"):
+        return np.int64
+    if kind == "where":
+        return np.int64 if lookup_is_row else np.float64
+    return np.float64
+
+
+def _prepare(cols, specs, shape, antialias):
+    names = []
+
+    def cidx(name):
+        if name is None:
+            return -1
+        if name not in names:
+            names.append(name)
+        return names.index(name)
+
+    H, W = shape
+    reds = (_Red * len(specs))()
+    keep = []
+    for k, s in enumerate(specs):
+        ncat = int(s.get("ncat") or 1) if s.get("cat") is not None else 1
+        r = reds[k]
+        r.kind = KIND[s["kind"]]
+        r.col = cidx(s.get("column"))
+        r.cat_col = cidx(s.get("cat"))
+        r.ncat = ncat
+        r.self_intersect = 1 if s.get("self_intersect", True) else 0
+        r.sel_kind = 0
+        r.sel_col = -1
+        r.lookup_col = -1
+        full = (H, W, ncat) if s.get("cat") is not None else (H, W)
+        if s["kind"] == "where":
+            sel = s["selector"]
+            r.sel_kind = KIND[sel["kind"]]
+            r.sel_col = cidx(sel.get("column"))
+            r.lookup_col = cidx(s.get("lookup"))
+            agg = np.empty(full, _agg_dtype("where", antialias, s.get("lookup") is None))
+            agg2 = np.empty(full, np.int64 if sel["kind"] in ("min_row", "max_row") else np.float64)
+        elif s["kind"] == "mean":
+            agg = np.empty(full, np.float64)
+            agg2 = np.empty(full, np.uint32)
+        else:
+            agg = np.empty(full, _agg_dtype(s["kind"], antialias))
+            agg2 = None
+        r.agg = agg.ctypes.data
+        r.agg2 = agg2.ctypes.data if agg2 is not None else None
+        keep.append((agg, agg2))
+    colarrs = [np.ascontiguousarray(cols[n], dtype=np.float64) for n in names]
+    ptrs = (ctypes.c_void_p * max(1, len(colarrs)))(*[a.ctypes.data for a in colarrs])
+    return reds, keep, colarrs, ptrs
+
+
+def _finalize(specs, keep):
+    out = []
+    for s, (agg, agg2) in zip(specs, keep):
+        if s["kind"] == "mean":
+            with np.errstate(divide="ignore", invalid="ignore"):
+                out.append(np.where(agg2 > 0, agg / agg2, np.nan))     # reductions.py:1290-1296
+        elif s["kind"] == "any" and agg.dtype == np.uint8:
+            out.append(agg.astype(bool))
+        else:
+            out.append(agg)
+    return out
+
+
+def points(cols, x, y, width, height, x_range, y_range, specs, row_offset=0,
+           x_axis="linear", y_axis="linear"):
+    """Canvas.points via pandas.default + Point.extend_cpu (pandas.py:26-66, points.py:182-212)."""
+    xs = np.ascontiguousarray(cols[x], dtype=np.float64)
+    ys = np.ascontiguousarray(cols[y], dtype=np.float64)
+    if x_range is None:
+        x_range = maybe_expand_bounds(compute_bounds(xs))
+    if y_range is None:
+        y_range = maybe_expand_bounds(compute_bounds(ys))
+    sx, tx = scale_translate(x_range, width, x_axis == "log")
+    sy, ty = scale_translate(y_range, height, y_axis == "log")
+    reds, keep, colarrs, ptrs = _prepare(cols, specs, (height, width), False)
+    L = lib()
+    L.oracle_init(reds, len(specs), height * width, 0)
+    L.oracle_points(xs.size, xs.ctypes.data, ys.ctypes.data, ptrs, row_offset, width, height,
+                    sx, tx, sy, ty, float(x_range[0]), float(x_range[1]),
+                    float(y_range[0]), float(y_range[1]),
+                    1 if x_axis == "log" else 0, 1 if y_axis == "log" else 0,
+                    reds, len(specs))
+    return _finalize(specs, keep)
+
+
+# AntialiasCombination values (antialias.py:8-14).
+SUM_1AGG, SUM_2AGG, MIN, MAX, FIRST, LAST = range(1, 7)
+
+
+def _requires_2_stages(s):
+    """Reduction._antialias_requires_2_stages overrides (reductions.py)."""
+    k = s["kind"]
+    if k in ("count", "sum"):
+        return not s.get("self_intersect", True)
+    return k in ("min", "first", "last", "min_row")
+
+
+def _combinations(s, self_intersect):
+    """Reduction._antialias_stage_2 of each base of a spec."""
+    k = s["kind"]
+    if k in ("count", "sum", "sum_zero", "count_ignore_aa"):
+        return [SUM_1AGG if self_intersect else SUM_2AGG]
+    if k == "mean":
+        return [SUM_1AGG if self_intersect else SUM_2AGG] * 2
+    if k in ("any", "max", "max_row"):
+        return [MAX]
+    if k in ("min", "min_row"):
+        return [MIN]
+    if k == "first":
+        return [FIRST]
+    if k == "last":
+        return [LAST]
+    if k == "where":
+        sel = _combinations(s["selector"], self_intersect)
+        return sel + sel
+    raise ValueError(k)
+
+
+def aa_flags(specs):
+    """compiler.py:539-554 (make_antialias_stage_2) + antialias.py:30-58 (two_stage_agg).
+
+    Returns (self_intersect, overwrite, use_2_stage_agg)."""
+    self_intersect = not any(_requires_2_stages(s) for s in specs)
+    combos = [c for s in specs for c in _combinations(s, self_intersect)]
+    use_2_stage = any(c in (SUM_2AGG, MIN, FIRST, LAST) for c in combos)
+    overwrite = not any(c == SUM_1AGG for c in combos)
+    return self_intersect, overwrite, use_2_stage
+
+
+def line_axis0(cols, x, y, width, height, x_range, y_range, specs, line_width=0.0,
+               plot_start=True, row_offset=0):
+    """Canvas.line with the LineAxis0 glyph (core.py:234-478, line.py:59-103, 1099-1136)."""
+    xs = np.ascontiguousarray(cols[x], dtype=np.float64)
+    ys = np.ascontiguousarray(cols[y], dtype=np.float64)
+    if x_range is None:
+        x_range = maybe_expand_bounds(compute_bounds(xs))
+    if y_range is None:
+        y_range = maybe_expand_bounds(compute_bounds(ys))
+    sx, tx = scale_translate(x_range, width)
+    sy, ty = scale_translate(y_range, height)
+    antialias = line_width > 0
+    if antialias:
+        self_intersect, overwrite, use_2_stage = aa_flags(specs)
+        specs = [dict(s, self_intersect=self_intersect) for s in specs]
+    else:
+        overwrite, use_2_stage = False, False
+    reds, keep, colarrs, ptrs = _prepare(cols, specs, (height, width), antialias)
+    L = lib()
+    L.oracle_init(reds, len(specs), height * width, 1 if antialias else 0)
+    L.oracle_line_axis0(xs.size, xs.ctypes.data, ys.ctypes.data, ptrs, row_offset, width, height,
+                        sx, tx, sy, ty, float(x_range[0]), float(x_range[1]),
+                        float(y_range[0]), float(y_range[1]), float(line_width),
+                        1 if plot_start else 0, 1 if overwrite else 0, 1 if use_2_stage else 0,
+                        reds, len(specs))
+    return _finalize(specs, keep)
+
+
+from .eq_hist import eq_hist, shade_eq_hist, interpolate_prologue  # noqa: E402,F401

@@ -1,0 +1,115 @@
+"""Extract golden vectors from the reference's own test files into JSON fixtures.
+
+Reads (as text, via ``ast``; nothing from the reference is imported or run):
+
+* ``datashader/tests/test_pandas.py``      -- the antialiased-line solution
+  arrays (``line_antialias_sol_*``, ``line_antialias_nan_sol_*``), the
+  ``line_antialias_df`` input frame and the LineAxis0 entry of
+  ``line_antialias_nan_params``;
+* ``datashader/tests/test_transfer_functions.py`` -- ``eq_hist_sol`` and
+  ``eq_hist_sol_rescale_discrete_levels`` (uint32 RGBA images).
+
+Usage::
+
+    python tests/golden/make_golden.py /path/to/reference
+
+The output files (``tests/golden/*.json``) are committed; the GPU machine never
+needs the reference checkout.
+"""
+from __future__ import annotations
+
+import ast
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+class _FakePd:
+    """Stand-in for the ``pd`` names the literal expressions use."""
+
+    @staticmethod
+    def DataFrame(data=None, dtype=None, **kw):
+        data = dict(data if data is not None else kw)
+        return {k: np.asarray(v, dtype=dtype) if dtype else np.asarray(v) for k, v in data.items()}
+
+    @staticmethod
+    def array(v, dtype=None):
+        return v
+
+
+def _literal_assignments(path, wanted_prefixes, extra_names=()):
+    src = open(path).read()
+    tree = ast.parse(src)
+    ns = {"np": np, "nan": np.nan, "pd": _FakePd, "sp": None}
+    out = {}
+    for node in tree.body:
+        if not isinstance(node, ast.Assign) or len(node.targets) != 1:
+            continue
+        tgt = node.targets[0]
+        if isinstance(tgt, ast.Name):
+            name = tgt.id
+            if name.startswith(wanted_prefixes) or name in extra_names:
+                code = compile(ast.Expression(node.value), path, "eval")
+                ns[name] = eval(code, ns)  # literal numpy expressions only
+                out[name] = (ns[name], node.lineno)
+        elif isinstance(tgt, ast.Subscript) and isinstance(tgt.value, ast.Name):
+            # e.g. eq_hist_sol_rescale_discrete_levels['c'] = ...['b']
+            name = tgt.value.id
+            if name in out:
+                code = compile(ast.Module([node], []), path, "exec")
+                exec(code, ns)
+    return out
+
+
+def _jsonable(a):
+    a = np.asarray(a)
+    if a.dtype.kind == "f":
+        return {"dtype": str(a.dtype), "shape": list(a.shape),
+                "data": [None if np.isnan(v) else float(v) for v in a.ravel()]}
+    return {"dtype": str(a.dtype), "shape": list(a.shape), "data": [int(v) for v in a.ravel()]}
+
+
+def main(ref_root):
+    tests = os.path.join(ref_root, "datashader", "tests")
+    pandas_path = os.path.join(tests, "test_pandas.py")
+    found = _literal_assignments(
+        pandas_path, ("line_antialias_sol_", "line_antialias_nan_sol_"),
+        extra_names=("line_antialias_df", "line_antialias_nan_params"))
+    goldens = {}
+    for name, (val, line) in found.items():
+        if name == "line_antialias_df":
+            goldens[name] = {"source": f"datashader/tests/test_pandas.py:{line}",
+                             "columns": {k: _jsonable(v) for k, v in val.items()}}
+        elif name == "line_antialias_nan_params":
+            frame, kw, sol_false, sol_true = val[0]   # the LineAxis0 entry
+            goldens["line_antialias_nan_axis0"] = {
+                "source": f"datashader/tests/test_pandas.py:{line}",
+                "columns": {k: _jsonable(np.asarray(v, dtype=frame.get("dtype", "float64")))
+                            for k, v in frame["data"].items()},
+                "sol_self_intersect_false": _jsonable(sol_false),
+                "sol_self_intersect_true": _jsonable(sol_true)}
+        else:
+            goldens[name] = dict(_jsonable(val), source=f"datashader/tests/test_pandas.py:{line}")
+    with open(os.path.join(HERE, "line_antialias.json"), "w") as f:
+        json.dump(goldens, f, indent=0)
+
+    tf_path = os.path.join(tests, "test_transfer_functions.py")
+    found = _literal_assignments(tf_path, ("eq_hist_sol",))
+    eq = {}
+    for name, (val, line) in found.items():
+        src = f"datashader/tests/test_transfer_functions.py:{line}"
+        if isinstance(val, dict):
+            eq[name] = {k: dict(_jsonable(v), source=src) for k, v in val.items()}
+        else:
+            eq[name] = dict(_jsonable(val), source=src)
+    with open(os.path.join(HERE, "eq_hist.json"), "w") as f:
+        json.dump(eq, f, indent=0)
+    print("wrote", sorted(goldens), sorted(eq))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

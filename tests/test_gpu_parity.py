@@ -1,0 +1,246 @@
+"""GPU vs CPU oracle on seeded synthetic inputs shaped like the benchmark configs.
+
+Tolerances: integer / index / min / max / first / last / where / by-count
+results and the eq_hist histogram are bit-exact.  float64 sums and means are
+accumulated by atomics in a different order than the oracle's row-order
+fold: 1e-12 relative.  Antialiased line sums: 1e-12 relative (the coverage
+values themselves are bit-identical; only the summation order differs).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import datashader_gb300 as ds
+import oracle
+from datashader_gb300 import synthetic
+from gpu_helpers import assert_same, frame_from_numpy, to_numpy
+from oracle_bridge import run_line, run_points
+
+pytestmark = pytest.mark.gpu
+
+CANVAS2 = dict(plot_width=1024, plot_height=1024, x_range=(-4, 4), y_range=(-4, 4))
+RTOL_SUM = 1e-12
+
+
+def _cfg2_frame(n, seed=0, xy_dtype=np.float32):
+    x, y = synthetic.gaussian_mixture_np(n, seed, dtype=xy_dtype)
+    rng = np.random.default_rng(seed + 1)
+    v = rng.lognormal(0.0, 1.0, n)
+    v[rng.integers(0, n, n // 100)] = np.nan          # NaN values are skipped by every reduction
+    cat = rng.integers(0, 8, n).astype(np.int8)
+    idx = np.arange(n, dtype=np.int64)
+    # rows exactly on the bounds, on pixel edges, just inside/outside, NaN coordinates
+    k = np.arange(64)
+    edge = (-4 + k / 128.0).astype(xy_dtype)
+    x[:64] = edge
+    y[:64] = edge[::-1]
+    x[64:70] = np.array([-4, 4, 4, -4, np.nan, 4.0000001], dtype=xy_dtype)
+    y[64:70] = np.array([-4, 4, -4, 4, 0, 0], dtype=xy_dtype)
+    nxt = np.nextafter(edge, np.array(np.inf, dtype=xy_dtype))
+    x[70:134] = nxt
+    y[70:134] = np.nextafter(edge, np.array(-np.inf, dtype=xy_dtype))
+    cols = {"x": x, "y": y, "v": v, "cat": cat, "index": idx}
+    return cols, {"cat": list(range(8))}
+
+
+def _cfg2_summary():
+    return ds.summary(
+        count=ds.count(), sum=ds.sum("v"), mean=ds.mean("v"), max=ds.max("v"), min=ds.min("v"),
+        first=ds.first("v"), last=ds.last("v"), where_row=ds.where(ds.max("v")),
+        where_index=ds.where(ds.max("v"), "index"), by_cat=ds.by("cat", ds.count()))
+
+
+@pytest.mark.parametrize("xy_dtype", [np.float32, np.float64])
+def test_points_cfg2_summary_vs_oracle(xy_dtype):
+    cols, cats = _cfg2_frame(300_000, seed=3, xy_dtype=xy_dtype)
+    agg = _cfg2_summary()
+    got = to_numpy(ds.Canvas(**CANVAS2).points(frame_from_numpy(cols, cats), "x", "y", agg))
+    ref = run_points(cols, cats, agg, CANVAS2)
+    for k in ("count", "max", "min", "first", "last", "where_row", "where_index", "by_cat"):
+        assert_same(got[k], ref[k], what=k)
+    for k in ("sum", "mean"):
+        assert_same(got[k], ref[k], rtol=RTOL_SUM, what=k)
+
+
+@pytest.mark.parametrize("warp_agg", [False, True])
+def test_points_cfg1_count_f64(warp_agg):
+    x, y = synthetic.gaussian_mixture_np(500_000, seed=7)
+    cols = {"x": x, "y": y}
+    canvas = dict(plot_width=512, plot_height=512, x_range=(-4, 4), y_range=(-4, 4))
+    frame = frame_from_numpy(cols)
+    from datashader_gb300.core import gpu_pipeline
+    from datashader_gb300 import _native as N
+    from datashader_gb300.glyphs import Point
+    flags = N.FLAG_WARP_AGG if warp_agg else 0
+    got = to_numpy(gpu_pipeline(frame, ds.Canvas(**canvas), Point("x", "y"), ds.count(), flags=flags))
+    ref = run_points(cols, {}, ds.count(), canvas)
+    assert_same(got, ref)
+
+
+def test_points_exact_flag_matches_fast_path():
+    cols, cats = _cfg2_frame(200_000, seed=11)
+    frame = frame_from_numpy(cols, cats)
+    from datashader_gb300.core import gpu_pipeline
+    from datashader_gb300 import _native as N
+    from datashader_gb300.glyphs import Point
+    cv = ds.Canvas(**CANVAS2)
+    a = to_numpy(gpu_pipeline(frame, cv, Point("x", "y"), ds.count()))
+    b = to_numpy(gpu_pipeline(frame, cv, Point("x", "y"), ds.count(), flags=N.FLAG_EXACT_BIN))
+    assert_same(a, b)
+
+
+def test_points_pixel_edges_dense():
+    """Every float32 value within a few ulp of every pixel edge of a 1024 px axis."""
+    edges = (-4 + np.arange(1025) / 128.0).astype(np.float32)
+    vals = [edges]
+    up, dn = edges.copy(), edges.copy()
+    for _ in range(3):
+        up = np.nextafter(up, np.float32(np.inf))
+        dn = np.nextafter(dn, np.float32(-np.inf))
+        vals += [up.copy(), dn.copy()]
+    xs = np.concatenate(vals)
+    rng = np.random.default_rng(5)
+    ys = rng.permutation(xs)
+    cols = {"x": xs, "y": ys}
+    got = to_numpy(ds.Canvas(**CANVAS2).points(frame_from_numpy(cols), "x", "y", ds.count()))
+    ref = run_points(cols, {}, ds.count(), CANVAS2)
+    assert_same(got, ref)
+
+
+def test_points_offset_range_uses_exact_path():
+    """A range far from zero (float32 binning error bound too large): exact path."""
+    rng = np.random.default_rng(9)
+    x = 1e6 + rng.uniform(0, 1, 100_000)
+    y = rng.uniform(0, 1, 100_000)
+    cols = {"x": x, "y": y, "v": rng.normal(size=100_000)}
+    canvas = dict(plot_width=300, plot_height=200, x_range=(1e6, 1e6 + 1), y_range=(0, 1))
+    agg = ds.summary(c=ds.count(), m=ds.max("v"))
+    got = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", agg))
+    ref = run_points(cols, {}, agg, canvas)
+    assert_same(got, ref)
+
+
+def test_points_row_offset_and_unaligned_columns():
+    cols, cats = _cfg2_frame(50_001, seed=13)
+    # a frame of column views starting one element in (not 16-byte aligned)
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in cols.items()}
+    sl = {k: v[1:] for k, v in t.items()}
+    frame = ds.TensorFrame(sl, categories=cats, row_offset=1000)
+    agg = ds.summary(first=ds.first("v"), where_row=ds.where(ds.max("v")), c=ds.count())
+    got = to_numpy(ds.Canvas(**CANVAS2).points(frame, "x", "y", agg))
+    sub = {k: v[1:] for k, v in cols.items()}
+    ref = run_points(sub, cats, agg, CANVAS2, row_offset=1000)
+    assert_same(got, ref)
+
+
+def test_points_empty_and_all_outside():
+    for n in (0, 17):
+        cols = {"x": np.full(n, 100.0), "y": np.full(n, 100.0), "v": np.ones(n)}
+        agg = ds.summary(c=ds.count(), s=ds.sum("v"), m=ds.max("v"), w=ds.where(ds.min("v")))
+        got = to_numpy(ds.Canvas(**CANVAS2).points(frame_from_numpy(cols), "x", "y", agg))
+        ref = run_points(cols, {}, agg, CANVAS2)
+        assert_same(got, ref)
+
+
+def test_points_autorange():
+    x, y = synthetic.gaussian_mixture_np(10_000, seed=21)
+    x[5] = np.nan
+    cols = {"x": x, "y": y}
+    canvas = dict(plot_width=200, plot_height=100)
+    got = ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", ds.count())
+    ref = run_points(cols, {}, ds.count(), canvas)
+    assert_same(to_numpy(got), ref)
+    assert got.x_range == oracle.maybe_expand_bounds(oracle.compute_bounds(x))
+
+
+def test_points_deterministic_repeat():
+    cols, cats = _cfg2_frame(100_000, seed=17)
+    frame = frame_from_numpy(cols, cats)
+    cvs = ds.Canvas(**CANVAS2)
+    agg = ds.summary(c=ds.count(), w=ds.where(ds.max("v")), f=ds.first("v"), b=ds.by("cat", ds.count()))
+    a = to_numpy(cvs.points(frame, "x", "y", agg))
+    b = to_numpy(cvs.points(frame, "x", "y", agg))
+    assert_same(a, b)
+
+
+# ------------------------------------------------------------------ lines
+
+def _series(nseries, length, seed=0):
+    x, y, v, _ = synthetic.time_series_np(nseries, length, seed)
+    return {"x": x, "y": y, "v": v}
+
+
+@pytest.mark.parametrize("line_width", [1.5, 1.0, 0.5, 2.0])
+def test_line_aa_sum_vs_oracle(line_width):
+    cols = _series(40, 400, seed=1)
+    canvas = dict(plot_width=256, plot_height=128)
+    got = ds.Canvas(**canvas).line(frame_from_numpy(cols), "x", "y", agg=ds.sum("v"), line_width=line_width)
+    ref = run_line(cols, {}, ds.sum("v"), canvas, line_width)
+    assert_same(to_numpy(got), ref, rtol=RTOL_SUM, atol=1e-13)
+
+
+@pytest.mark.parametrize("agg_name", ["count", "any", "max", "mean", "min_row", "summary2stage"])
+def test_line_aa_reductions_vs_oracle(agg_name):
+    cols = _series(10, 300, seed=2)
+    canvas = dict(plot_width=200, plot_height=100)
+    agg = {"count": ds.count(), "any": ds.any(), "max": ds.max("v"), "mean": ds.mean("v"),
+           "min_row": ds._min_row_index(),
+           "summary2stage": ds.summary(c=ds.count(), mn=ds.min("v"), w=ds.where(ds.max("v")))}[agg_name]
+    got = to_numpy(ds.Canvas(**canvas).line(frame_from_numpy(cols), "x", "y", agg=agg, line_width=1.5))
+    ref = run_line(cols, {}, agg, canvas, 1.5)
+    pairs = ref.items() if isinstance(ref, dict) else [(None, ref)]
+    for k, r in pairs:
+        g = got[k] if k is not None else got
+        if r.dtype == np.float32:      # the reference sums float32 aggregates in float32
+            assert_same(g, r, rtol=3e-7, atol=1e-7, what=str(k))
+        elif r.dtype.kind == "f":
+            assert_same(g, r, rtol=RTOL_SUM, atol=1e-13, what=str(k))
+        else:
+            assert_same(g, r, what=str(k))
+
+
+def test_line_bresenham_vs_oracle():
+    cols = _series(30, 500, seed=3)
+    canvas = dict(plot_width=300, plot_height=150)
+    agg = ds.summary(c=ds.count(), s=ds.sum("v"), l=ds.last("v"))
+    got = to_numpy(ds.Canvas(**canvas).line(frame_from_numpy(cols), "x", "y", agg=agg))
+    ref = run_line(cols, {}, agg, canvas, 0)
+    assert_same(got["c"], ref["c"])
+    assert_same(got["l"], ref["l"])
+    assert_same(got["s"], ref["s"], rtol=RTOL_SUM)
+
+
+# ---------------------------------------------------------------- eq_hist
+
+def test_eq_hist_count_agg_vs_oracle():
+    cols, cats = _cfg2_frame(400_000, seed=23)
+    agg = ds.Canvas(**CANVAS2).points(frame_from_numpy(cols, cats), "x", "y", ds.count())
+    out, levels = ds.tf.eq_hist_agg(agg)
+    data, mask = oracle.interpolate_prologue(to_numpy(agg))
+    ref, ref_levels = oracle.eq_hist(data, mask)
+    assert levels == ref_levels
+    assert_same(out.cpu().numpy(), ref)
+    img = ds.tf.shade(agg, cmap=["lightblue", "darkblue"], how="eq_hist")
+    got = img.data.view(torch.int32).cpu().numpy().view(np.uint32)
+    assert_same(got, oracle.shade_eq_hist(to_numpy(agg), ["lightblue", "darkblue"]))
+
+
+def test_eq_hist_binned_paths_vs_oracle():
+    """uint32 data with ptp >= 65536 and float64 data take numpy.histogram's binned path."""
+    rng = np.random.default_rng(31)
+    u = rng.integers(0, 3_000_000, size=(300, 400)).astype(np.uint32)
+    u[rng.random(u.shape) < 0.1] = 0
+    f = rng.lognormal(0, 2, size=(300, 400))
+    f[rng.random(f.shape) < 0.1] = np.nan
+    for data in (u, f):
+        t = torch.from_numpy(data.view(np.int32) if data.dtype == np.uint32 else data).cuda()
+        if data.dtype == np.uint32:
+            t = t.view(torch.uint32)
+        out, levels = ds.tf.eq_hist_agg(t)
+        d, mask = oracle.interpolate_prologue(data)
+        ref, ref_levels = oracle.eq_hist(d, mask)
+        assert levels == ref_levels
+        # np.interp between bin centres: FMA contraction differs between numpy builds
+        assert_same(out.cpu().numpy(), ref, rtol=1e-12, atol=1e-15)

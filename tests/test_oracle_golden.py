@@ -1,0 +1,117 @@
+"""Pin the CPU oracle against the reference test-suite's golden vectors (no GPU)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+import refcases
+from oracle_bridge import run_line, run_points
+
+POINT_CASES = refcases.point_cases()
+LINE_CASES = refcases.line_cases()
+
+
+def _check(got, exp, close):
+    if isinstance(exp, dict):
+        assert sorted(got) == sorted(exp)
+        for k in exp:
+            _check(got[k], exp[k], close)
+        return
+    got = np.asarray(got)
+    assert got.shape == np.shape(exp)
+    if close:
+        # the reference's assert_eq_ndarray(close=True): 5 decimals
+        np.testing.assert_array_almost_equal(got, exp, decimal=5)
+    else:
+        np.testing.assert_array_equal(got, exp)
+
+
+@pytest.mark.parametrize("case", POINT_CASES, ids=[c["id"] for c in POINT_CASES])
+def test_oracle_points_golden(case):
+    if case["frame"] is None:
+        cols, cats = refcases.pandas_frame()
+    else:
+        cols, cats = case["frame"], {}
+    got = run_points(cols, cats, case["agg"], case["canvas"], case["x"], case["y"])
+    _check(got, case["expected"], case["close"])
+
+
+@pytest.mark.parametrize("case", LINE_CASES, ids=[c["id"] for c in LINE_CASES])
+def test_oracle_line_golden(case):
+    got = run_line(case["frame"], case.get("categories", {}), case["agg"], case["canvas"], case["line_width"])
+    _check(got, case["expected"], case["close"])
+
+
+@pytest.mark.parametrize("high", [9, 10, 99, 100])
+def test_oracle_uniform_diagonal_points(high):
+    """test_pandas.py:1147-1168."""
+    import datashader_gb300 as ds
+    low = 0
+    width = height = high - low
+    n = width * height
+    cols = {"time": np.ones(n, dtype="i4"),
+            "x": np.array([np.arange(low, high, dtype="f8")] * width).flatten(),
+            "y": np.array([np.arange(low, high, dtype="f8")] * height).flatten()}
+    agg = run_points(cols, {}, ds.count("time"),
+                     dict(plot_width=2, plot_height=2, x_range=(low, high), y_range=(low, high)))
+    diagonal = agg.diagonal(0)
+    assert diagonal.sum() == n
+    assert abs(high - low) % 2 == abs(diagonal[1] / high - diagonal[0] / high)
+
+
+def _eq_sol(name):
+    return refcases.golden_array(refcases.load_golden("eq_hist.json", name))
+
+
+def test_oracle_eq_hist_rgba_golden():
+    """test_transfer_functions.py:194-201: shade(how='eq_hist') exact RGBA for u4 and f8 aggs."""
+    a, c = refcases.eq_hist_agg_a()
+    sol = _eq_sol("eq_hist_sol")
+    cmap = ["pink", "red"]
+    np.testing.assert_array_equal(oracle.shade_eq_hist(a, cmap), sol)
+    np.testing.assert_array_equal(oracle.shade_eq_hist(c, cmap), sol)
+
+
+def test_oracle_eq_hist_rescale_golden():
+    """test_transfer_functions.py:113-120, 199-201 (tolerance 1 per channel)."""
+    a, c = refcases.eq_hist_agg_a()
+    g = refcases.load_golden("eq_hist.json", "eq_hist_sol_rescale_discrete_levels")
+    for data, key in ((a, "a"), (c, "c")):
+        sol = refcases.golden_array(g[key]).view(np.uint8).astype(int)
+        got = oracle.shade_eq_hist(data, ["pink", "red"], rescale_discrete_levels=True).view(np.uint8).astype(int)
+        assert np.abs(got - sol).max() <= 1
+
+
+def _check_cdf_slope(eq):
+    """test_transfer_functions.py:1131-1137."""
+    cdf = np.histogram(eq[~np.isnan(eq)], bins=256)[0].cumsum()
+    cdf = cdf / cdf[-1]
+    slope = np.polyfit(np.linspace(0, 1, cdf.size), cdf, 1)[0]
+    assert 0.9 < slope < 1.1
+
+
+def test_oracle_eq_hist_slope(rng):
+    """test_transfer_functions.py:1140-1153."""
+    data = rng.normal(size=300 ** 2)
+    data[rng.integers(300 ** 2, size=100)] = np.nan
+    data = (data - np.nanmin(data)).reshape((300, 300))
+    mask = np.isnan(data)
+    eq, _ = oracle.eq_hist(data, mask)
+    _check_cdf_slope(eq)
+    assert (np.isnan(eq) == mask).all()
+    data = rng.normal(scale=100, size=(300, 300)).astype("i8")
+    data = data - data.min()
+    eq, _ = oracle.eq_hist(data)
+    _check_cdf_slope(eq)
+
+
+def test_oracle_mutation_is_caught():
+    """A mistake planted in the oracle's inputs must change the golden comparison."""
+    import datashader_gb300 as ds
+    cols, cats = refcases.pandas_frame()
+    cols = dict(cols)
+    cols["x"] = cols["x"].copy()
+    cols["x"][0] = 1.0           # move one row to the other column of pixels
+    got = run_points(cols, cats, ds.count(), refcases.C2)
+    assert not np.array_equal(got, np.array([[5, 5], [5, 5]]))
