@@ -265,10 +265,13 @@ def run_gpu(args):
         L = N.lib()
         N.check(L.dsgb_bases_init(ex.bases, len(plan.bases), 1024 * 1024, stream.cuda_stream), "init")
 
+        wsz = int(L.dsgb_points_workspace_size(n, ctypes.byref(cv), ex.bases, len(plan.bases)))
+        ws = torch.empty(max(wsz, 1), dtype=torch.uint8, device=dev)
+
         def launch():
-            N.check(L.dsgb_points(ex.cols, len(ex.names), n, 0, 0, 1, ctypes.byref(cv), ex.bases,
-                                  len(plan.bases), ex.outs, 0, N.FLAG_NO_INIT | N.FLAG_NO_FINALIZE,
-                                  stream.cuda_stream), "dsgb_points")
+            N.check(L.dsgb_points_ws(ex.cols, len(ex.names), n, 0, 0, 1, ctypes.byref(cv), ex.bases,
+                                     len(plan.bases), ex.outs, 0, ws.data_ptr() if wsz else None, wsz,
+                                     N.FLAG_NO_INIT | N.FLAG_NO_FINALIZE, stream.cuda_stream), "dsgb_points_ws")
         return launch
 
     def roofline(agg, bytes_per_point, bytes_per_pixel, k):

@@ -391,6 +391,22 @@ def _results(plan, ex, coords, dims, attrs):
     return AggregateSet(items)
 
 
+_WORKSPACES = {}
+
+
+def workspace(device, stream, nbytes):
+    """A device scratch buffer of at least ``nbytes`` owned by (device, stream).
+
+    Calls on one stream run in order, so they may share it; another stream
+    gets its own buffer."""
+    key = (str(device), int(stream))
+    t = _WORKSPACES.get(key)
+    if t is None or t.numel() < nbytes:
+        t = torch.empty(max(nbytes, 1 << 20), dtype=torch.uint8, device=device)
+        _WORKSPACES[key] = t
+    return t
+
+
 def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=None):
     """pandas.py:26-66 on the GPU: ranges, scale/translate, create+extend+finalize."""
     if stream is None:
@@ -416,9 +432,12 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
                                ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
         N.check(rc, "dsgb_line_axis0")
     else:
-        rc = L.dsgb_points(ex.cols, len(ex.names), len(frame), frame.row_offset, 0, 1, ctypes.byref(cv),
-                           ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
-        N.check(rc, "dsgb_points")
+        wsz = int(L.dsgb_points_workspace_size(len(frame), ctypes.byref(cv), ex.bases, len(plan.bases)))
+        ws = workspace(frame.device, stream, wsz) if wsz else None
+        rc = L.dsgb_points_ws(ex.cols, len(ex.names), len(frame), frame.row_offset, 0, 1, ctypes.byref(cv),
+                              ex.bases, len(plan.bases), ex.outs, ex.nouts,
+                              ws.data_ptr() if ws is not None else None, wsz, flags, stream)
+        N.check(rc, "dsgb_points_ws")
     coords = {glyph.x_label: x_axis, glyph.y_label: y_axis}
     dims = [glyph.y_label, glyph.x_label]
     return _results(plan, ex, coords, dims, dict(x_range=x_range, y_range=y_range))

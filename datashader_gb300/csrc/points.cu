@@ -402,6 +402,21 @@ int launch_points(const PointsParams &p, uint32_t flags, cudaStream_t st) {
 }
 
 int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st);
+size_t binned_workspace_size(int64_t n, int width, int height);
+int launch_points_binned(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
+                         float xminf, float xmaxf, float yminf, float ymaxf, float ex, float ey,
+                         long long kx0, long long kx1, long long ky0, long long ky1,
+                         uint32_t *out, bool accumulate, void *ws, size_t ws_bytes, cudaStream_t st);
+
+// The binned (two-pass, shared-memory) path serves a plain count() of every
+// row on a float32/float64 canvas that the float32 fast path may bin.
+static bool binned_eligible(const PointsParams &p, uint32_t flags) {
+    return p.nbases == 1 && p.bases[0].op == DSGB_BASE_COUNT && p.bases[0].col < 0 &&
+           p.bases[0].cat_col < 0 && !(flags & (DSGB_FLAG_EXACT_BIN | DSGB_FLAG_WARP_AGG)) &&
+           !p.x_log && !p.y_log && std::isfinite(p.ex) && std::isfinite(p.ey) && p.ex < 0.01f &&
+           p.ey < 0.01f;
+}
+
 int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
                      const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
                      int64_t ncells, cudaStream_t st);
@@ -410,16 +425,23 @@ int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
 
 using namespace dsgb;
 
-extern "C" int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
-                           int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
-                           const dsgb_base *bases, int32_t nbases,
-                           const dsgb_output *outs, int32_t nouts,
-                           uint32_t flags, void *stream) {
+static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                       int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                       const dsgb_base *bases, int32_t nbases,
+                       const dsgb_output *outs, int32_t nouts,
+                       void *workspace, size_t ws_bytes, uint32_t flags, void *stream) {
     PointsParams p;
     int rc = build_params(p, cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases);
     if (rc) return rc;
     cudaStream_t st = as_stream(stream);
     const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    if (workspace && binned_eligible(p, flags)) {
+        rc = launch_points_binned(p.cols[x_col], p.cols[y_col], n, canvas, p.xminf, p.xmaxf, p.yminf,
+                                  p.ymaxf, p.ex, p.ey, p.kxmin, p.kxmax, p.kymin, p.kymax,
+                                  (uint32_t *)p.bases[0].agg, (flags & DSGB_FLAG_NO_INIT) != 0,
+                                  workspace, ws_bytes, st);
+        if (rc != DSGB_E_UNSUPPORTED) return rc;
+    }
     if (!(flags & DSGB_FLAG_NO_INIT)) {
         rc = bases_init(bases, nbases, ncells, st);
         if (rc) return rc;
@@ -429,4 +451,30 @@ extern "C" int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, in
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
         rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
     return rc;
+}
+
+extern "C" int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                           int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                           const dsgb_base *bases, int32_t nbases,
+                           const dsgb_output *outs, int32_t nouts,
+                           uint32_t flags, void *stream) {
+    return points_impl(cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases, outs, nouts,
+                       nullptr, 0, flags, stream);
+}
+
+extern "C" size_t dsgb_points_workspace_size(int64_t n, const dsgb_canvas *canvas,
+                                             const dsgb_base *bases, int32_t nbases) {
+    if (!canvas || n < 0 || nbases != 1 || !bases || bases[0].op != DSGB_BASE_COUNT ||
+        bases[0].col >= 0 || bases[0].cat_col >= 0)
+        return 0;
+    return binned_workspace_size(n, canvas->width, canvas->height);
+}
+
+extern "C" int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                              int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                              const dsgb_base *bases, int32_t nbases,
+                              const dsgb_output *outs, int32_t nouts,
+                              void *workspace, size_t workspace_bytes, uint32_t flags, void *stream) {
+    return points_impl(cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases, outs, nouts,
+                       workspace, workspace_bytes, flags, stream);
 }

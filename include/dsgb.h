@@ -157,6 +157,21 @@ int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_o
                 const dsgb_output *outs, int32_t nouts,
                 uint32_t flags, void *stream);
 
+/* Canvas.points with a caller-provided workspace.  A plain count() of every
+ * row takes a two-pass path that never touches global atomics (rows are
+ * binned into row bands in the workspace, then each band is counted in
+ * shared memory and added to the output with TMA bulk reductions); every
+ * other plan, or a workspace smaller than dsgb_points_workspace_size(),
+ * runs exactly as dsgb_points.  The workspace must be 256-byte aligned and
+ * must not be used by another call in flight. */
+size_t dsgb_points_workspace_size(int64_t n, const dsgb_canvas *canvas,
+                                  const dsgb_base *bases, int32_t nbases);
+int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                   int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                   const dsgb_base *bases, int32_t nbases,
+                   const dsgb_output *outs, int32_t nouts,
+                   void *workspace, size_t workspace_bytes, uint32_t flags, void *stream);
+
 /* ---- Canvas.line, LineAxis0 glyph ----------------------------------------
  * Replaces line.py:59-103 + 1033-1149.  line_width == 0 draws Bresenham
  * lines, > 0 antialiased lines; overwrite / use_2_stage_agg follow

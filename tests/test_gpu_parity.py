@@ -244,3 +244,44 @@ def test_eq_hist_binned_paths_vs_oracle():
         assert levels == ref_levels
         # np.interp between bin centres: FMA contraction differs between numpy builds
         assert_same(out.cpu().numpy(), ref, rtol=1e-12, atol=1e-15)
+
+
+# ------------------------------------------- two-pass binned count (workspace path)
+
+@pytest.mark.parametrize("shape", [(1024, 1024), (512, 256), (1920, 1080), (4096, 2160), (1000, 1000),
+                                   (1002, 100), (4, 4)])
+@pytest.mark.parametrize("n", [1, 8191, 8193, 250_003])
+def test_binned_count_shapes_vs_oracle(shape, n):
+    w, h = shape
+    x, y = synthetic.gaussian_mixture_np(n, seed=n + w, dtype=np.float32)
+    cols = {"x": x, "y": y}
+    canvas = dict(plot_width=w, plot_height=h, x_range=(-4, 4), y_range=(-3, 3))
+    got = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", ds.count()))
+    ref = run_points(cols, {}, ds.count(), canvas)
+    assert_same(got, ref)
+
+
+def test_binned_count_f64_and_accumulate():
+    import ctypes
+    from datashader_gb300 import _native as N
+    from datashader_gb300.compiler import compile_plan
+    from datashader_gb300.core import Executor
+    from datashader_gb300.glyphs import Point
+    x, y = synthetic.gaussian_mixture_np(300_001, seed=4)
+    cols = {"x": x, "y": y}
+    frame = frame_from_numpy(cols)
+    plan = compile_plan(ds.count(), frame)
+    ex = Executor(frame, plan, Point("x", "y"))
+    ex.allocate(1024, 1024, frame.device)
+    cv = N.CanvasDesc(1024, 1024, 0, 0, 128.0, 512.0, 128.0, 512.0, -4.0, 4.0, -4.0, 4.0)
+    L = N.lib()
+    wsz = int(L.dsgb_points_workspace_size(len(frame), ctypes.byref(cv), ex.bases, 1))
+    assert wsz > 0
+    ws = torch.empty(wsz, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    for flags in (0, N.FLAG_NO_INIT):   # the second call adds onto the first
+        N.check(L.dsgb_points_ws(ex.cols, len(ex.names), len(frame), 0, 0, 1, ctypes.byref(cv), ex.bases, 1,
+                                 ex.outs, 0, ws.data_ptr(), wsz, flags, st), "dsgb_points_ws")
+    got = to_numpy(type("A", (), {"data": ex.out_tensors[0]})())
+    ref = run_points(cols, {}, ds.count(), CANVAS2)
+    assert_same(got, 2 * ref)
