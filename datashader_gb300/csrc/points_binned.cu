@@ -29,8 +29,10 @@
 namespace dsgb {
 
 constexpr int ROUND = 8192;           // rows per round (1024 threads x 8 rows)
-constexpr int MAX_BANDS = 1024;
-constexpr int BAND_CELLS = 16384;     // cells per band held in shared memory (64 KB)
+constexpr int MAX_BANDS = 256;
+constexpr int ROUND_CAP = 10240;      // entry slots per round: 8192 + padding of every band to 8
+constexpr int MAX_BAND_CELLS = 49152; // band-local index < 65535 (0xFFFF pads a run)
+constexpr uint16_t PAD = 0xFFFFu;
 
 struct BinnedParams {
     const float *xs32, *ys32;         // float32 coordinates (or null)
@@ -42,13 +44,44 @@ struct BinnedParams {
     double sx, tx, sy, ty;
     float xminf, xmaxf, yminf, ymaxf, sxf, txf, syf, tyf, ex, ey;
     long long kxmin, kxmax, kymin, kymax;
-    uint16_t *entries;                // nrounds * ROUND
-    uint32_t *dir;                    // nrounds * nbands: (offset << 16) | count
+    uint16_t *entries;                // nrounds * ROUND_CAP
+    uint32_t *dir;                    // nrounds * nbands: (offset in 8-entry units << 16) | count
     unsigned long long *totals;       // nbands
     int4 *items;                      // (band, r0, r1, -)
     int *nitems;
+    int *status;                      // 0, or 1 when a bounded wait gave up
     uint32_t *out;                    // height * width counts
 };
+
+// ---- mbarrier / bulk-copy helpers (sm_90+ PTX)
+__device__ __forceinline__ unsigned smem_addr(const void *ptr) {
+    return (unsigned)__cvta_generic_to_shared(ptr);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    unsigned long long state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state) : "r"(smem_addr(bar)), "r"(bytes) : "memory");
+    (void)state;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+// Wait for the phase with the given parity; false when the limit runs out.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
+    for (int it = 0; it < (1 << 20); ++it) {
+        unsigned done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
 
 // ---- binning (the same arithmetic as points.cu; see its header comment)
 __device__ __forceinline__ int bb_exact(double m, double s, double t, int n) {
@@ -103,7 +136,7 @@ __device__ __forceinline__ bool bb_f64(const BinnedParams &p, double x, double y
 // ---- pass 1
 template <bool F64>
 __global__ void __launch_bounds__(1024, 1) binned_pass1(const BinnedParams p) {
-    __shared__ uint16_t stage[ROUND];
+    __shared__ __align__(16) uint16_t stage[ROUND_CAP];
     __shared__ unsigned hist[MAX_BANDS];
     __shared__ unsigned offs[MAX_BANDS];
     __shared__ unsigned wsum[32];
@@ -187,9 +220,10 @@ __global__ void __launch_bounds__(1024, 1) binned_pass1(const BinnedParams p) {
             rank[k] = (int)(base + __popc(peers & ((1u << lane) - 1u)));
         }
         __syncthreads();
-        // exclusive scan of hist[0..B) (B <= 1024: one value per thread)
+        // exclusive scan of the band runs padded to 8 entries (B <= 256)
         {
-            unsigned v = threadIdx.x < (unsigned)B ? hist[threadIdx.x] : 0u;
+            const unsigned cnt = threadIdx.x < (unsigned)B ? hist[threadIdx.x] : 0u;
+            const unsigned v = (cnt + 7u) & ~7u;
             unsigned s = v;
             for (int o = 1; o < 32; o <<= 1) {
                 unsigned t = __shfl_up_sync(0xffffffffu, s, o);
@@ -206,11 +240,12 @@ __global__ void __launch_bounds__(1024, 1) binned_pass1(const BinnedParams p) {
                 wsum[lane] = w;
             }
             __syncthreads();
-            unsigned excl = s - v + (warp > 0 ? wsum[warp - 1] : 0u);
+            const unsigned excl = s - v + (warp > 0 ? wsum[warp - 1] : 0u);
             if (threadIdx.x < (unsigned)B) {
                 offs[threadIdx.x] = excl;
-                p.dir[r * B + threadIdx.x] = (excl << 16) | v;
-                my_total += v;
+                p.dir[r * B + threadIdx.x] = ((excl >> 3) << 16) | cnt;
+                my_total += cnt;
+                for (unsigned j = excl + cnt; j < excl + v; ++j) stage[j] = PAD;
             }
         }
         __syncthreads();
@@ -218,36 +253,176 @@ __global__ void __launch_bounds__(1024, 1) binned_pass1(const BinnedParams p) {
         for (int k = 0; k < 8; ++k)
             if (band[k] >= 0) stage[offs[band[k]] + rank[k]] = (uint16_t)local[k];
         __syncthreads();
-        // the sorted round, coalesced (16 KB = 1024 x uint4)
+        // the sorted, padded round (coalesced uint4 stores)
         const unsigned total = wsum[31];
-        uint4 *dst = (uint4 *)(p.entries + row0);
+        uint4 *dst = (uint4 *)(p.entries + r * ROUND_CAP);
         const uint4 *src = (const uint4 *)stage;
-        const unsigned nvec = (total + 7) / 8;
-        for (unsigned v = threadIdx.x; v < nvec; v += blockDim.x) __stcs(dst + v, src[v]);
+        for (unsigned v = threadIdx.x; v < total / 8; v += blockDim.x) __stcs(dst + v, src[v]);
         for (int b = threadIdx.x; b < B; b += blockDim.x) hist[b] = 0;
         __syncthreads();
     }
     if (threadIdx.x < (unsigned)B && my_total) atomicAdd(&p.totals[threadIdx.x], my_total);
 }
 
+// float32 coordinates: the rounds stream in through a two-slot TMA bulk-copy
+// ring (x and y, 32 KB each per round) so that HBM reads overlap the binning
+// and sorting of the previous round.
+__global__ void __launch_bounds__(1024, 1) binned_pass1_tma(const BinnedParams p) {
+    extern __shared__ __align__(128) unsigned char dyn[];
+    float *xb = (float *)dyn;                       // [2][ROUND]
+    float *yb = xb + 2 * ROUND;                     // [2][ROUND]
+    uint16_t *stage = (uint16_t *)(yb + 2 * ROUND); // [ROUND_CAP]
+    __shared__ unsigned hist[MAX_BANDS];
+    __shared__ unsigned offs[MAX_BANDS];
+    __shared__ unsigned wsum[32];
+    __shared__ __align__(8) unsigned long long bar[2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int B = p.nbands;
+    const int64_t nfull = p.n / ROUND;              // rounds fully inside the columns
+    for (int b = tid; b < B; b += blockDim.x) hist[b] = 0;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int64_t r, int slot) {
+        if (r < nfull) {
+            mbar_expect_tx(&bar[slot], 2u * ROUND * 4u);
+            bulk_g2s(xb + slot * ROUND, p.xs32 + r * ROUND, ROUND * 4u, &bar[slot]);
+            bulk_g2s(yb + slot * ROUND, p.ys32 + r * ROUND, ROUND * 4u, &bar[slot]);
+        }
+    };
+    if (tid == 0) {
+        issue(blockIdx.x, 0);
+        issue(blockIdx.x + gridDim.x, 1);
+    }
+    unsigned parity[2] = {0u, 0u};
+    unsigned long long my_total = 0;
+    int i = 0;
+    for (int64_t r = blockIdx.x; r < p.nrounds; r += gridDim.x, ++i) {
+        const int slot = i & 1;
+        const int64_t row0 = r * ROUND;
+        float xf[8], yf[8];
+        if (r < nfull) {
+            const bool ok = mbar_wait_bounded(&bar[slot], parity[slot]);
+            parity[slot] ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                // a bulk copy did not land within the limit: report and stop
+                if (tid == 0) atomicExch(p.status, 1);
+                return;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                xf[k] = xb[slot * ROUND + tid + 1024 * k];
+                yf[k] = yb[slot * ROUND + tid + 1024 * k];
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int64_t ii = row0 + tid + 1024 * k;
+                xf[k] = ii < p.n ? p.xs32[ii] : __int_as_float(0x7fc00000);
+                yf[k] = ii < p.n ? p.ys32[ii] : 0.0f;
+            }
+        }
+        int band[8], local[8], rank[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int xi, yi, bnd = -1, loc = 0;
+            if (bb_f32(p, xf[k], yf[k], xi, yi)) {
+                bnd = yi / p.rows_per_band;
+                loc = (yi - bnd * p.rows_per_band) * p.width + xi;
+            }
+            band[k] = bnd;
+            local[k] = loc;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int bnd = band[k];
+            const unsigned peers = __match_any_sync(0xffffffffu, bnd);
+            const int leader = __ffs(peers) - 1;
+            unsigned base = 0;
+            if (lane == leader && bnd >= 0) base = atomicAdd(&hist[bnd], (unsigned)__popc(peers));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            rank[k] = (int)(base + __popc(peers & ((1u << lane) - 1u)));
+        }
+        __syncthreads();   // hist complete; every thread is done with this slot's buffers
+        if (tid == 0) issue(r + 2 * (int64_t)gridDim.x, slot);
+        {
+            const unsigned cnt = tid < B ? hist[tid] : 0u;
+            const unsigned v = (cnt + 7u) & ~7u;
+            unsigned sc = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned t = __shfl_up_sync(0xffffffffu, sc, o);
+                if (lane >= o) sc += t;
+            }
+            if (lane == 31) wsum[warp] = sc;
+            __syncthreads();
+            if (warp == 0) {
+                unsigned w = wsum[lane];
+                for (int o = 1; o < 32; o <<= 1) {
+                    unsigned t = __shfl_up_sync(0xffffffffu, w, o);
+                    if (lane >= o) w += t;
+                }
+                wsum[lane] = w;
+            }
+            __syncthreads();
+            const unsigned excl = sc - v + (warp > 0 ? wsum[warp - 1] : 0u);
+            if (tid < B) {
+                offs[tid] = excl;
+                p.dir[r * B + tid] = ((excl >> 3) << 16) | cnt;
+                my_total += cnt;
+                for (unsigned j = excl + cnt; j < excl + v; ++j) stage[j] = PAD;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (band[k] >= 0) stage[offs[band[k]] + rank[k]] = (uint16_t)local[k];
+        __syncthreads();
+        const unsigned total = wsum[31];
+        uint4 *dst = (uint4 *)(p.entries + r * ROUND_CAP);
+        const uint4 *src = (const uint4 *)stage;
+        for (unsigned v = tid; v < total / 8; v += blockDim.x) __stcs(dst + v, src[v]);
+        if (tid < B) hist[tid] = 0;
+        __syncthreads();
+    }
+    if (tid < B && my_total) atomicAdd(&p.totals[tid], my_total);
+}
+
 // ---- plan: work items of similar size
-__global__ void binned_plan(const BinnedParams p, int target_items) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(256) binned_plan(const BinnedParams p, int target_items) {
+    __shared__ unsigned long long s_all[8];
+    __shared__ int s_k[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned long long t = tid < p.nbands ? p.totals[tid] : 0ull;
+    unsigned long long a = t;
+    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) s_all[warp] = a;
+    __syncthreads();
     unsigned long long all = 0;
-    for (int b = 0; b < p.nbands; ++b) all += p.totals[b];
-    int n = 0;
-    for (int b = 0; b < p.nbands; ++b) {
-        unsigned long long t = p.totals[b];
-        if (!t) continue;
-        long long k = all ? (long long)((t * (unsigned long long)target_items + all - 1) / all) : 1;
+    for (int w = 0; w < 8; ++w) all += s_all[w];
+    long long k = 0;
+    if (t) {
+        k = (long long)((t * (unsigned long long)target_items + all - 1) / all);
         if (k < 1) k = 1;
         if (k > p.nrounds) k = p.nrounds;
-        for (long long j = 0; j < k; ++j) {
-            int r0 = (int)(p.nrounds * j / k), r1 = (int)(p.nrounds * (j + 1) / k);
-            if (r1 > r0) p.items[n++] = make_int4(b, r0, r1, 0);
-        }
     }
-    *p.nitems = n;
+    int inc = (int)k;
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane == 31) s_k[warp] = inc;
+    __syncthreads();
+    int base = inc - (int)k;
+    for (int w = 0; w < warp; ++w) base += s_k[w];
+    for (long long j = 0; j < k; ++j) {
+        const int r0 = (int)(p.nrounds * j / k), r1 = (int)(p.nrounds * (j + 1) / k);
+        p.items[base + j] = make_int4(tid, r0, r1, 0);
+    }
+    if (tid == 255) *p.nitems = base + (int)k;
 }
 
 // ---- pass 2
@@ -262,11 +437,42 @@ __global__ void __launch_bounds__(512) binned_pass2(const BinnedParams p) {
     for (int i = threadIdx.x; i < cells; i += blockDim.x) band_sm[i] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int r = it.y + warp; r < it.z; r += nwarps) {
-        const uint32_t d = __ldg(&p.dir[(int64_t)r * p.nbands + b]);
-        const unsigned off = d >> 16, cnt = d & 0xffffu;
-        const uint16_t *src = p.entries + (int64_t)r * ROUND + off;
-        for (unsigned j = lane; j < cnt; j += 32) atomicAdd(&band_sm[__ldcs(src + j)], 1u);
+    const uint4 *ent = (const uint4 *)p.entries;
+    // 32 rounds per warp step: lane j owns round rbase + j; the runs of the 32
+    // rounds are flattened into one index space of 8-entry vectors.
+    for (int rbase = it.y + warp * 32; rbase < it.z; rbase += nwarps * 32) {
+        const int r = rbase + lane;
+        const uint32_t d = r < it.z ? __ldg(&p.dir[(int64_t)r * p.nbands + b]) : 0u;
+        const unsigned nv = ((d & 0xffffu) + 7u) >> 3;
+        const unsigned offv = d >> 16;
+        unsigned incl = nv;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const unsigned excl = incl - nv;
+        const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+        for (unsigned vb = 0; vb < total; vb += 32) {
+            const unsigned e = vb + lane;
+            int j = 0;
+#pragma unroll
+            for (int st = 16; st >= 1; st >>= 1) {
+                const unsigned x = __shfl_sync(0xffffffffu, excl, j + st);
+                if (x <= e) j += st;
+            }
+            const unsigned offj = __shfl_sync(0xffffffffu, offv, j);
+            const unsigned exj = __shfl_sync(0xffffffffu, excl, j);
+            if (e < total) {
+                const uint4 q = __ldcs(ent + (int64_t)(rbase + j) * (ROUND_CAP / 8) + offj + (e - exj));
+                const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const unsigned lo = w[k] & 0xffffu, hi = w[k] >> 16;
+                    if (lo != PAD) atomicAdd(&band_sm[lo], 1u);
+                    if (hi != PAD) atomicAdd(&band_sm[hi], 1u);
+                }
+            }
+        }
     }
     __syncthreads();
     // add the band into the output with TMA bulk reductions (16-byte granules);
@@ -294,27 +500,31 @@ __global__ void __launch_bounds__(512) binned_pass2(const BinnedParams p) {
 struct BinnedLayout {
     int rows_per_band, nbands;
     int64_t nrounds;
-    size_t off_entries, off_dir, off_totals, off_items, off_nitems, total;
+    size_t off_entries, off_dir, off_totals, off_items, off_nitems, off_status, total;
 };
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 static bool binned_layout(int64_t n, int width, int height, int target_items, BinnedLayout &L) {
-    if (width <= 0 || height <= 0 || width > BAND_CELLS || (width % 4) != 0) return false;
-    int rpb = BAND_CELLS / width;
+    if (width <= 0 || height <= 0 || width > MAX_BAND_CELLS || (width % 4) != 0) return false;
+    // rows per band: about 16K cells (64 KB of shared memory, several CTAs per
+    // SM in pass 2), more when needed to keep at most MAX_BANDS bands
+    int rpb = 16384 / width;
+    if (rpb < 1) rpb = 1;
+    while ((height + rpb - 1) / rpb > MAX_BANDS && (int64_t)(rpb + 1) * width <= MAX_BAND_CELLS) ++rpb;
     if (rpb > height) rpb = height;
-    while (rpb > 1 && ((int64_t)rpb * width) % 4) --rpb;
     int nb = (height + rpb - 1) / rpb;
     if (nb > MAX_BANDS) return false;
     L.rows_per_band = rpb;
     L.nbands = nb;
     L.nrounds = (n + ROUND - 1) / ROUND;
     size_t o = 0;
-    L.off_entries = o; o = align_up(o + (size_t)L.nrounds * ROUND * 2, 256);
+    L.off_entries = o; o = align_up(o + (size_t)L.nrounds * ROUND_CAP * 2, 256);
     L.off_dir = o; o = align_up(o + (size_t)L.nrounds * nb * 4, 256);
     L.off_totals = o; o = align_up(o + (size_t)nb * 8, 256);
     L.off_items = o; o = align_up(o + (size_t)(nb + target_items + 8) * 16, 256);
     L.off_nitems = o; o = align_up(o + 16, 256);
+    L.off_status = o; o = align_up(o + 16, 256);
     L.total = o;
     return true;
 }
@@ -363,8 +573,10 @@ int launch_points_binned(const ColumnRef &xc, const ColumnRef &yc, int64_t n, co
     p.totals = (unsigned long long *)(w + L.off_totals);
     p.items = (int4 *)(w + L.off_items);
     p.nitems = (int *)(w + L.off_nitems);
+    p.status = (int *)(w + L.off_status);
     p.out = out;
     cudaError_t e = cudaMemsetAsync(p.totals, 0, (size_t)L.nbands * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.status, 0, 16, st);
     if (e == cudaSuccess && !accumulate) e = cudaMemsetAsync(out, 0, (size_t)cv->width * cv->height * 4, st);
     if (e != cudaSuccess) return cuda_status(e, "binned memset");
     if (n == 0) return DSGB_OK;
@@ -372,9 +584,15 @@ int launch_points_binned(const ColumnRef &xc, const ColumnRef &yc, int64_t n, co
     if (sms <= 0) sms = 148;
     int64_t g1 = (int64_t)sms;
     if (g1 > L.nrounds) g1 = L.nrounds;
-    if (f32) binned_pass1<false><<<(unsigned)g1, 1024, 0, st>>>(p);
-    else binned_pass1<true><<<(unsigned)g1, 1024, 0, st>>>(p);
-    binned_plan<<<1, 32, 0, st>>>(p, target);
+    if (f32) {
+        const size_t smem1 = (size_t)4 * ROUND * 4 + (size_t)ROUND_CAP * 2;
+        e = cudaFuncSetAttribute(binned_pass1_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+        if (e != cudaSuccess) return cuda_status(e, "binned pass1 smem attribute");
+        binned_pass1_tma<<<(unsigned)g1, 1024, smem1, st>>>(p);
+    } else {
+        binned_pass1<true><<<(unsigned)g1, 1024, 0, st>>>(p);
+    }
+    binned_plan<<<1, 256, 0, st>>>(p, target);
     const size_t smem = (size_t)L.rows_per_band * cv->width * 4;
     e = cudaFuncSetAttribute(binned_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "binned pass2 smem attribute");
