@@ -4,24 +4,10 @@
 // per-reduction append functions that compiler.make_append fuses
 // (datashader/compiler.py:321-475).
 //
-// Binning semantics (points.py:190-204): a row is kept when
-// xmin <= x <= xmax and ymin <= y <= ymax (inclusive, float64 compares);
-// xx = int(x*sx + tx) with the product and the sum each rounded in float64
-// (numba emits no FMA) and int() truncating toward zero; xx >= width maps to
-// width-1.
-//
-// GB300 has little float64 throughput, so the kernel bins in float32 and
-// proves the result: with E a host-computed bound on |float32 result -
-// float64 result| (binning_error_bound below), a point whose float32 value is
-// farther than E from every integer lands in the same bin as the float64
-// computation.  Points within E of a pixel edge (about 1 in 2000 at
-// 1024 px) are recomputed with the exact float64 formula.  The result is
-// bit-identical to the reference's binning.
+// Binning is exact (binning.cuh): a float32 fast path proven against the
+// float64 formula of points.py:199-203, with a float64 fallback.
 #include "dsgb_internal.cuh"
-
-#include <cmath>
-#include <float.h>
-#include <math.h>
+#include "binning.cuh"
 
 namespace dsgb {
 
@@ -36,85 +22,26 @@ struct PointsParams {
     int32_t x_log, y_log;
     double sx, tx, sy, ty;
     double xmin, xmax, ymin, ymax;
-    // float32 fast path
-    float xminf, xmaxf, yminf, ymaxf;  // exact float images of the inclusive bounds
-    float sxf, txf, syf, tyf;
-    float ex, ey;                      // proven |float32 - float64| bounds (pixels)
-    long long kxmin, kxmax, kymin, kymax;  // order-preserving keys of the bounds
+    BinAxis ax, ay;                    // float32 fast path (binning.cuh)
+    BinBounds bb;
 };
 
 // ------------------------------------------------------------------ binning
 
-// Exact float64 binning of one coordinate (points.py:199-203).
-__device__ __forceinline__ int bin_exact(double m, double s, double t, int n) {
-    double v = __dadd_rn(__dmul_rn(m, s), t);
-    long long xx = __double2ll_rz(v);
-    if (xx >= n) xx = n - 1;
-    if (xx < 0) xx += n;           // numba indexes negative positions from the end
-    if (xx < 0) xx = 0;            // not reachable after the bounds test; memory safety
-    return (int)xx;
-}
-
-// float32 binning with the exact fallback near pixel edges.
-__device__ __forceinline__ int bin_fast(float xf, double xd, float sf, float tf, float e,
-                                        double s, double t, int n) {
-    float v = __fmaf_rn(xf, sf, tf);
-    float fl = floorf(v);
-    float d = fminf(v - fl, (fl + 1.0f) - v);
-    if (d > e) {
-        int xx = __float2int_rz(v);
-        if (xx >= n) xx = n - 1;
-        if (xx < 0) xx += n;
-        if (xx < 0) xx = 0;
-        return xx;
-    }
-    return bin_exact(xd, s, t, n);
-}
-
-// Float32 image of a double by mantissa truncation, integer ops only.
-// Returns false (caller uses the exact path) outside the normal float range.
-__device__ __forceinline__ bool f64_to_f32_trunc(double x, float &out) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    if ((b << 1) == 0) { out = 0.0f; return true; }
-    int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
-    if (e <= 0 || e >= 255) return false;
-    unsigned m = (unsigned)((b >> 29) & 0x7fffffu);
-    out = __uint_as_float(((unsigned)(b >> 63) << 31) | ((unsigned)e << 23) | m);
-    return true;
-}
-
-__device__ __forceinline__ long long key_canon(double v) {
-    long long b = __double_as_longlong(v);
-    if (b == (long long)0x8000000000000000ull) b = 0;  // -0.0 compares equal to +0.0
-    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
-}
-
-// Each binning routine returns false for rows outside the bounds.
 __device__ __forceinline__ bool bin_f32_fast(const PointsParams &p, float x, float y, int &xi, int &yi) {
-    if (!(x >= p.xminf && x <= p.xmaxf && y >= p.yminf && y <= p.ymaxf)) return false;
-    xi = bin_fast(x, (double)x, p.sxf, p.txf, p.ex, p.sx, p.tx, p.width);
-    yi = bin_fast(y, (double)y, p.syf, p.tyf, p.ey, p.sy, p.ty, p.height);
-    return true;
+    return bin_point_f32(x, y, p.bb, p.ax, p.ay, xi, yi);
 }
 
 __device__ __forceinline__ bool bin_f64_fast(const PointsParams &p, double x, double y, int &xi, int &yi) {
-    long long kx = key_canon(x), ky = key_canon(y);
-    // NaN keys fall outside every finite-or-infinite bound interval.
-    if (!(kx >= p.kxmin && kx <= p.kxmax && ky >= p.kymin && ky <= p.kymax)) return false;
-    float xf, yf;
-    if (f64_to_f32_trunc(x, xf)) xi = bin_fast(xf, x, p.sxf, p.txf, p.ex, p.sx, p.tx, p.width);
-    else xi = bin_exact(x, p.sx, p.tx, p.width);
-    if (f64_to_f32_trunc(y, yf)) yi = bin_fast(yf, y, p.syf, p.tyf, p.ey, p.sy, p.ty, p.height);
-    else yi = bin_exact(y, p.sy, p.ty, p.height);
-    return true;
+    return bin_point_f64(x, y, p.bb, p.ax, p.ay, xi, yi);
 }
 
 __device__ __forceinline__ bool bin_exact_xy(const PointsParams &p, double x, double y, int &xi, int &yi) {
     if (!((p.xmin <= x && x <= p.xmax) && (p.ymin <= y && y <= p.ymax))) return false;
     double mx = p.x_log ? log10(x) : x;   // LogAxis.mapper (core.py:131-134)
     double my = p.y_log ? log10(y) : y;
-    xi = bin_exact(mx, p.sx, p.tx, p.width);
-    yi = bin_exact(my, p.sy, p.ty, p.height);
+    xi = bin_exact64(mx, p.ax);
+    yi = bin_exact64(my, p.ay);
     return true;
 }
 
@@ -202,11 +129,30 @@ __global__ void __launch_bounds__(256) points_f32_kernel(const PointsParams p) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) va[k] = mean_value<MODE>(p, 4 * v + k);
         }
+        int xs_[4], ys_[4];
+        unsigned inm = 0;
+        if (FAST) {
+            unsigned need = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int r = live ? bin_try_f32(xa[k], ya[k], p.bb, p.ax, p.ay, xs_[k], ys_[k]) : 0;
+                inm |= (unsigned)(r != 0) << k;
+                need |= (unsigned)(r == 2) << k;
+            }
+            if (need) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if ((need >> k) & 1u) bin_exact_f32(xa[k], ya[k], p.ax, p.ay, xs_[k], ys_[k]);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                inm |= (unsigned)(live && bin_exact_xy(p, (double)xa[k], (double)ya[k], xs_[k], ys_[k])) << k;
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            int xi = 0, yi = 0;
-            bool in = live && (FAST ? bin_f32_fast(p, xa[k], ya[k], xi, yi)
-                                    : bin_exact_xy(p, (double)xa[k], (double)ya[k], xi, yi));
+            const bool in = (inm >> k) & 1u;
+            const int xi = in ? xs_[k] : 0, yi = in ? ys_[k] : 0;
             if (WARPAGG && MODE == MODE_COUNT) {
                 unsigned key = in ? (unsigned)(yi * p.width + xi) : (0x80000000u | (unsigned)lane);
                 unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -263,40 +209,6 @@ __global__ void __launch_bounds__(256) points_any_kernel(const PointsParams p) {
 
 // ------------------------------------------------------------- host side
 
-// Smallest float >= v (as a double compare) / largest float <= v.
-static float float_ceil_of(double v) {
-    if (std::isnan(v)) return NAN;
-    float f = (float)v;
-    if ((double)f < v) f = nextafterf(f, INFINITY);
-    return f;
-}
-static float float_floor_of(double v) {
-    if (std::isnan(v)) return NAN;
-    float f = (float)v;
-    if ((double)f > v) f = nextafterf(f, -INFINITY);
-    return f;
-}
-static long long host_key_canon(double v) {
-    long long b; memcpy(&b, &v, 8);
-    if (b == (long long)0x8000000000000000ull) b = 0;
-    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
-}
-
-// Bound on |fma32(x, (float)s, (float)t) - fl64(fl64(x*s) + t)| over
-// lo <= x <= hi, in output units, including the float32 truncation of a
-// float64 x.  Terms: rounding of the float32 result, of (float)s and
-// (float)t, of the float32 image of x, and the two float64 roundings; the
-// factor 4 covers their sum with margin.  Returns +inf when the fast path
-// must not be used.
-static double binning_error_bound(double lo, double hi, double s, double t, int n) {
-    if (!std::isfinite(lo) || !std::isfinite(hi) || !std::isfinite(s) || !std::isfinite(t))
-        return INFINITY;
-    double xm = std::fmax(std::fabs(lo), std::fabs(hi));
-    double mag = xm * std::fabs(s) + std::fabs(t) + (double)n + 1.0;
-    if (!(mag < 1e6) || std::fabs(s) > 1e30 || xm > 1e30) return INFINITY;
-    return 4.0 * ldexp(1.0, -23) * mag;
-}
-
 static int build_params(PointsParams &p, const dsgb_column *cols, int32_t ncols, int64_t n,
                         int64_t row_offset, int32_t x_col, int32_t y_col,
                         const dsgb_canvas *cv, const dsgb_base *bases, int32_t nbases) {
@@ -337,13 +249,9 @@ static int build_params(PointsParams &p, const dsgb_column *cols, int32_t ncols,
     p.width = cv->width; p.height = cv->height; p.x_log = cv->x_log; p.y_log = cv->y_log;
     p.sx = cv->sx; p.tx = cv->tx; p.sy = cv->sy; p.ty = cv->ty;
     p.xmin = cv->xmin; p.xmax = cv->xmax; p.ymin = cv->ymin; p.ymax = cv->ymax;
-    p.xminf = float_ceil_of(cv->xmin); p.xmaxf = float_floor_of(cv->xmax);
-    p.yminf = float_ceil_of(cv->ymin); p.ymaxf = float_floor_of(cv->ymax);
-    p.sxf = (float)cv->sx; p.txf = (float)cv->tx; p.syf = (float)cv->sy; p.tyf = (float)cv->ty;
-    p.kxmin = host_key_canon(cv->xmin); p.kxmax = host_key_canon(cv->xmax);
-    p.kymin = host_key_canon(cv->ymin); p.kymax = host_key_canon(cv->ymax);
-    p.ex = (float)binning_error_bound(cv->xmin, cv->xmax, cv->sx, cv->tx, cv->width);
-    p.ey = (float)binning_error_bound(cv->ymin, cv->ymax, cv->sy, cv->ty, cv->height);
+    p.ax = make_axis(cv->sx, cv->tx, cv->xmin, cv->xmax, cv->width);
+    p.ay = make_axis(cv->sy, cv->ty, cv->ymin, cv->ymax, cv->height);
+    p.bb = make_bounds(cv->xmin, cv->xmax, cv->ymin, cv->ymax);
     return DSGB_OK;
 }
 
@@ -360,8 +268,7 @@ int launch_points(const PointsParams &p, uint32_t flags, cudaStream_t st) {
         mode = MODE_MEAN;
     const int xdt = p.cols[p.x_col].dtype, ydt = p.cols[p.y_col].dtype;
     const void *xp = p.cols[p.x_col].data, *yp = p.cols[p.y_col].data;
-    const bool fast = !(flags & DSGB_FLAG_EXACT_BIN) && !p.x_log && !p.y_log &&
-                      std::isfinite(p.ex) && std::isfinite(p.ey) && p.ex < 0.01f && p.ey < 0.01f;
+    const bool fast = !(flags & DSGB_FLAG_EXACT_BIN) && !p.x_log && !p.y_log && fast_path_ok(p.ax, p.ay);
     const bool warpagg = (flags & DSGB_FLAG_WARP_AGG) != 0;
     const int threads = 256;
     int sms = sm_count();
@@ -402,19 +309,17 @@ int launch_points(const PointsParams &p, uint32_t flags, cudaStream_t st) {
 }
 
 int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st);
-size_t binned_workspace_size(int64_t n, int width, int height);
-int launch_points_binned(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
-                         float xminf, float xmaxf, float yminf, float ymaxf, float ex, float ey,
-                         long long kx0, long long kx1, long long ky0, long long ky1,
+size_t cached_workspace_size(int64_t n, int width, int height);
+int launch_points_cached(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
+                         const BinAxis &ax, const BinAxis &ay, const BinBounds &bb,
                          uint32_t *out, bool accumulate, void *ws, size_t ws_bytes, cudaStream_t st);
 
-// The binned (two-pass, shared-memory) path serves a plain count() of every
-// row on a float32/float64 canvas that the float32 fast path may bin.
-static bool binned_eligible(const PointsParams &p, uint32_t flags) {
+// The hot-tile path (points_cached.cu) serves a plain count() of every row
+// on a canvas that the float32 fast path may bin.
+static bool cached_eligible(const PointsParams &p, uint32_t flags) {
     return p.nbases == 1 && p.bases[0].op == DSGB_BASE_COUNT && p.bases[0].col < 0 &&
            p.bases[0].cat_col < 0 && !(flags & (DSGB_FLAG_EXACT_BIN | DSGB_FLAG_WARP_AGG)) &&
-           !p.x_log && !p.y_log && std::isfinite(p.ex) && std::isfinite(p.ey) && p.ex < 0.01f &&
-           p.ey < 0.01f;
+           !p.x_log && !p.y_log && fast_path_ok(p.ax, p.ay);
 }
 
 int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
@@ -435,9 +340,8 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
     if (rc) return rc;
     cudaStream_t st = as_stream(stream);
     const int64_t ncells = (int64_t)canvas->width * canvas->height;
-    if (workspace && binned_eligible(p, flags)) {
-        rc = launch_points_binned(p.cols[x_col], p.cols[y_col], n, canvas, p.xminf, p.xmaxf, p.yminf,
-                                  p.ymaxf, p.ex, p.ey, p.kxmin, p.kxmax, p.kymin, p.kymax,
+    if (workspace && cached_eligible(p, flags)) {
+        rc = launch_points_cached(p.cols[x_col], p.cols[y_col], n, canvas, p.ax, p.ay, p.bb,
                                   (uint32_t *)p.bases[0].agg, (flags & DSGB_FLAG_NO_INIT) != 0,
                                   workspace, ws_bytes, st);
         if (rc != DSGB_E_UNSUPPORTED) return rc;
@@ -467,7 +371,7 @@ extern "C" size_t dsgb_points_workspace_size(int64_t n, const dsgb_canvas *canva
     if (!canvas || n < 0 || nbases != 1 || !bases || bases[0].op != DSGB_BASE_COUNT ||
         bases[0].col >= 0 || bases[0].cat_col >= 0)
         return 0;
-    return binned_workspace_size(n, canvas->width, canvas->height);
+    return cached_workspace_size(n, canvas->width, canvas->height);
 }
 
 extern "C" int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
