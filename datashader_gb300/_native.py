@@ -136,8 +136,7 @@ FLAG_NO_INIT, FLAG_NO_FINALIZE, FLAG_EXACT_BIN, FLAG_WARP_AGG = 0x1, 0x2, 0x4, 0
 # every symbol include/dsgb.h declares
 EXPORTED = (
     "dsgb_abi_version", "dsgb_last_error", "dsgb_device_sm_count", "dsgb_bases_init",
-    "dsgb_finalize", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_ws",
-    "dsgb_points_ws_status", "dsgb_line_axis0", "dsgb_line_axis0_backward",
+    "dsgb_finalize", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_ws", "dsgb_line_axis0", "dsgb_line_axis0_backward",
     "dsgb_points_backward", "dsgb_bounds", "dsgb_eq_hist_workspace_size", "dsgb_eq_hist_u32",
     "dsgb_eq_hist_f64", "dsgb_pyramid_tile_offset", "dsgb_pyramid", "dsgb_pyramid_finalize",
 )
@@ -164,7 +163,6 @@ def _declare(L):
     L.dsgb_points_workspace_size.restype = ctypes.c_size_t
     L.dsgb_points_ws.argtypes = [PC, i32, i64, i64, i32, i32, ctypes.POINTER(CanvasDesc), PB, i32, PO, i32,
                                  P, ctypes.c_size_t, u32, P]
-    L.dsgb_points_ws_status.argtypes = [P, ctypes.POINTER(ctypes.c_int), P]
     L.dsgb_line_axis0.argtypes = [PC, i32, i64, i64, i32, i32, ctypes.POINTER(CanvasDesc), dbl, i32, i32, i32,
                                   PB, i32, PO, i32, u32, P]
     L.dsgb_line_axis0_backward.argtypes = [PC, i32, i64, i32, i32, i32, ctypes.POINTER(CanvasDesc), dbl, i32,

@@ -9,22 +9,12 @@
 //   sample  -- bin ~1% of the rows (evenly spaced chunks) into a histogram of
 //              tiles (16x16 px, 32x32 or 64x64 for large canvases);
 //   select  -- one block picks the K most populated tiles that fit in shared
-//              memory (a uint16 counter per pixel) and writes tile -> slot;
+//              memory (a uint32 counter per pixel) and writes tile -> slot;
 //   main    -- one CTA per SM streams x/y (float4 loads), bins each row
 //              (binning.cuh: exact), and increments the tile's shared-memory
 //              counter when the tile is cached, the output with an L2
-//              reduction otherwise; every CTA then stores its cached tiles to
-//              a per-CTA partial array;
-//   reduce  -- adds the per-CTA partials of each cached pixel into the output.
-//
-// Counters are uint16 pairs in 32-bit words.  The increment that takes a
-// counter from 0x7FFF to 0x8000 moves 0x8000 to the output and subtracts it
-// from the counter, so a counter stays below 0x10000 unless 0x8000 more
-// increments of the same pixel are served by the shared-memory atomic unit
-// before that subtraction (three instructions later in the same thread):
-// same-address shared atomics serialise, so that would take over 32768
-// cycles.  A wrap would still be detected (the returned old value is 0xFFFF)
-// and reported through the workspace status word, never silently.
+//              reduction otherwise; at the end every CTA adds its non-zero
+//              cached counters into the output.
 //
 // Every result is exact: integer counts in any order.
 #include "dsgb_internal.cuh"
@@ -51,8 +41,6 @@ struct CachedParams {
     unsigned *hist;             // ntiles
     short *slot;                // ntiles
     int *slot_tile;             // K
-    uint16_t *partials;         // gridDim(main) * K * tile cells
-    int *status;
 };
 
 __device__ __forceinline__ int tile_cells(const CachedParams &p) { return 1 << (2 * p.ts); }
@@ -127,16 +115,7 @@ __device__ __forceinline__ void cached_emit(const CachedParams &p, const short *
     const int s = tab[(yi >> p.ts) * p.tiles_x + (xi >> p.ts)];
     if (s >= 0) {
         const int tm = (1 << p.ts) - 1;
-        const unsigned cell = ((unsigned)s << (2 * p.ts)) + ((unsigned)(yi & tm) << p.ts) + (unsigned)(xi & tm);
-        const unsigned sh = (cell & 1u) * 16u;
-        const unsigned old = atomicAdd(&cache[cell >> 1], 1u << sh);
-        const unsigned h = (old >> sh) & 0xffffu;
-        if (h == 0x7fffu) {
-            atomicSub(&cache[cell >> 1], 0x8000u << sh);
-            atomicAdd(&p.out[(int64_t)yi * p.width + xi], 0x8000u);
-        } else if (h == 0xffffu) {
-            atomicExch(p.status, 1);
-        }
+        atomicAdd(&cache[((unsigned)s << (2 * p.ts)) + ((unsigned)(yi & tm) << p.ts) + (unsigned)(xi & tm)], 1u);
     } else {
         atomicAdd(&p.out[(int64_t)yi * p.width + xi], 1u);
     }
@@ -147,9 +126,10 @@ __global__ void __launch_bounds__(1024, 1) cached_main(const CachedParams p) {
     short *tab = (short *)smem;
     const int tab_bytes = ((p.ntiles * 2) + 15) & ~15;
     unsigned *cache = (unsigned *)(smem + tab_bytes);
-    const int cells = p.K * tile_cells(p);
+    const int tc = tile_cells(p);
+    const int cells = p.K * tc;
     for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x) tab[i] = p.slot[i];
-    for (int i = threadIdx.x; i < cells / 2; i += blockDim.x) cache[i] = 0;
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) cache[i] = 0;
     __syncthreads();
     const float4 *x4 = (const float4 *)p.xs;
     const float4 *y4 = (const float4 *)p.ys;
@@ -167,8 +147,8 @@ __global__ void __launch_bounds__(1024, 1) cached_main(const CachedParams p) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int r = (k < 4 || two) ? bin_try_f32(xs[k], ys[k], p.bb, p.ax, p.ay, xi[k], yi[k]) : 0;
-            in |= (r != 0) << k;
-            need |= (r == 2) << k;
+            in |= (unsigned)(r != 0) << k;
+            need |= (unsigned)(r == 2) << k;
         }
         if (need) {
 #pragma unroll
@@ -187,26 +167,14 @@ __global__ void __launch_bounds__(1024, 1) cached_main(const CachedParams p) {
         if (r) cached_emit(p, tab, cache, xi, yi);
     }
     __syncthreads();
-    uint4 *dst = (uint4 *)(p.partials + (int64_t)blockIdx.x * cells);
-    const uint4 *src = (const uint4 *)cache;
-    for (int i = threadIdx.x; i < cells / 8; i += blockDim.x) __stcs(dst + i, src[i]);
-}
-
-// ---- reduce: out[pixel of (slot, cell)] += sum over CTAs of the partials
-__global__ void __launch_bounds__(256) cached_reduce(const CachedParams p, int nparts) {
-    const int tc = tile_cells(p);
-    const int64_t cells = (int64_t)p.K * tc;
-    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
-        const int s = (int)(c >> (2 * p.ts));
-        const int t = p.slot_tile[s];
-        if (t < 0) continue;
-        const int within = (int)(c & (tc - 1));
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+        const unsigned c = cache[i];
+        if (!c) continue;
+        const int t = p.slot_tile[i >> (2 * p.ts)];
+        const int within = i & (tc - 1);
         const int yi = (t / p.tiles_x) * (1 << p.ts) + (within >> p.ts);
         const int xi = (t % p.tiles_x) * (1 << p.ts) + (within & ((1 << p.ts) - 1));
-        if (yi >= p.height || xi >= p.width) continue;
-        unsigned sum = 0;
-        for (int g = 0; g < nparts; ++g) sum += __ldcs(p.partials + (int64_t)g * cells + c);
-        if (sum) p.out[(int64_t)yi * p.width + xi] += sum;
+        atomicAdd(&p.out[(int64_t)yi * p.width + xi], c);
     }
 }
 
@@ -214,7 +182,7 @@ __global__ void __launch_bounds__(256) cached_reduce(const CachedParams p, int n
 
 struct CachedLayout {
     int ts, tiles_x, ntiles, K, grid;
-    size_t off_status, off_hist, off_slot, off_slot_tile, off_partials, total;
+    size_t off_hist, off_slot, off_slot_tile, total;
 };
 
 static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
@@ -232,18 +200,16 @@ static bool cached_layout(int64_t n, int width, int height, CachedLayout &L) {
     L.tiles_x = (width + (1 << ts) - 1) >> ts;
     L.ntiles = L.tiles_x * ((height + (1 << ts) - 1) >> ts);
     const int tab = ((L.ntiles * 2) + 15) & ~15;
-    const int tile_bytes = (1 << (2 * ts)) * 2;
+    const int tile_bytes = (1 << (2 * ts)) * 4;
     L.K = (SMEM_BUDGET - tab) / tile_bytes;
     if (L.K > L.ntiles) L.K = L.ntiles;
     if (L.K < 1) return false;
-    int sms = sm_count();
+    const int sms = sm_count();
     L.grid = sms > 0 ? sms : 148;
     size_t o = 0;
-    L.off_status = o; o = align256(o + 16);
     L.off_hist = o; o = align256(o + (size_t)L.ntiles * 4);
     L.off_slot = o; o = align256(o + (size_t)L.ntiles * 2);
     L.off_slot_tile = o; o = align256(o + (size_t)L.K * 4);
-    L.off_partials = o; o = align256(o + (size_t)L.grid * L.K * (1 << (2 * ts)) * 2);
     L.total = o;
     return true;
 }
@@ -270,41 +236,21 @@ int launch_points_cached(const ColumnRef &xc, const ColumnRef &yc, int64_t n, co
     p.ax = ax; p.ay = ay; p.bb = bb;
     p.out = out;
     char *w = (char *)ws;
-    p.status = (int *)(w + L.off_status);
     p.hist = (unsigned *)(w + L.off_hist);
     p.slot = (short *)(w + L.off_slot);
     p.slot_tile = (int *)(w + L.off_slot_tile);
-    p.partials = (uint16_t *)(w + L.off_partials);
-    cudaError_t e = cudaMemsetAsync(p.status, 0, 16, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p.hist, 0, (size_t)L.ntiles * 4, st);
+    cudaError_t e = cudaMemsetAsync(p.hist, 0, (size_t)L.ntiles * 4, st);
     if (e == cudaSuccess && !accumulate) e = cudaMemsetAsync(out, 0, (size_t)cv->width * cv->height * 4, st);
     if (e != cudaSuccess) return cuda_status(e, "cached count memset");
     const int64_t chunk = SAMPLE_CHUNK < n / SAMPLE_BLOCKS ? SAMPLE_CHUNK : n / SAMPLE_BLOCKS;
     cached_sample<<<SAMPLE_BLOCKS, 256, (size_t)L.ntiles * 4, st>>>(p, chunk);
     cached_select<<<1, 1024, 0, st>>>(p);
-    const size_t smem = (((size_t)L.ntiles * 2 + 15) & ~(size_t)15) + (size_t)L.K * (1 << (2 * L.ts)) * 2;
+    const size_t smem = (((size_t)L.ntiles * 2 + 15) & ~(size_t)15) + (size_t)L.K * (1 << (2 * L.ts)) * 4;
     e = cudaFuncSetAttribute(cached_main, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "cached count smem attribute");
     cached_main<<<L.grid, 1024, smem, st>>>(p);
-    const int64_t cells = (int64_t)L.K * (1 << (2 * L.ts));
-    int rg = (int)((cells + 255) / 256);
-    if (rg > L.grid * 8) rg = L.grid * 8;
-    cached_reduce<<<rg, 256, 0, st>>>(p, L.grid);
     DSGB_CHECK_LAUNCH("cached count launch");
     return DSGB_OK;
 }
 
 }  // namespace dsgb
-
-using namespace dsgb;
-
-// Reads the status word a cached count left in its workspace (0 = fine,
-// 1 = a shared-memory counter wrapped: the aggregate is not valid).
-extern "C" int dsgb_points_ws_status(const void *workspace, int *status, void *stream) {
-    if (!workspace || !status) { set_error("dsgb_points_ws_status: null argument"); return DSGB_E_INVALID; }
-    cudaStream_t st = as_stream(stream);
-    cudaError_t e = cudaMemcpyAsync(status, workspace, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return cuda_status(e, "dsgb_points_ws_status");
-    return DSGB_OK;
-}

@@ -161,12 +161,10 @@ int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_o
  * row of float32 coordinates (at least 2^20 rows) takes a path that keeps
  * the densest canvas tiles in shared memory: a 1% sample picks the tiles,
  * one CTA per SM counts rows of cached tiles with shared-memory atomics and
- * the others with L2 reductions, and the per-CTA tiles are summed at the
- * end.  Every other plan, or a workspace smaller than
+ * the others with L2 reductions, and each CTA adds its tiles into the output
+ * at the end.  Every other plan, or a workspace smaller than
  * dsgb_points_workspace_size(), runs exactly as dsgb_points.  The workspace
- * must be 256-byte aligned and not used by another call in flight; after
- * the call, dsgb_points_ws_status() reads its status word (0 = valid, 1 = a
- * shared-memory counter wrapped and the aggregate must not be used). */
+ * must be 256-byte aligned and not used by another call in flight. */
 size_t dsgb_points_workspace_size(int64_t n, const dsgb_canvas *canvas,
                                   const dsgb_base *bases, int32_t nbases);
 int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
@@ -174,7 +172,6 @@ int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t ro
                    const dsgb_base *bases, int32_t nbases,
                    const dsgb_output *outs, int32_t nouts,
                    void *workspace, size_t workspace_bytes, uint32_t flags, void *stream);
-int dsgb_points_ws_status(const void *workspace, int *status, void *stream);
 
 /* ---- Canvas.line, LineAxis0 glyph ----------------------------------------
  * Replaces line.py:59-103 + 1033-1149.  line_width == 0 draws Bresenham

@@ -246,12 +246,12 @@ def test_eq_hist_binned_paths_vs_oracle():
         assert_same(out.cpu().numpy(), ref, rtol=1e-12, atol=1e-15)
 
 
-# ------------------------------------------- two-pass binned count (workspace path)
+# ----------------------------------------- hot-tile count path (workspace path)
 
-@pytest.mark.parametrize("shape", [(1024, 1024), (512, 256), (1920, 1080), (4096, 2160), (1000, 1000),
-                                   (1002, 100), (4, 4)])
-@pytest.mark.parametrize("n", [1, 8191, 8193, 250_003])
-def test_binned_count_shapes_vs_oracle(shape, n):
+@pytest.mark.parametrize("shape", [(1024, 1024), (512, 256), (1920, 1080), (4096, 2160), (1000, 999),
+                                   (3, 5)])
+@pytest.mark.parametrize("n", [8191, (1 << 20) + 3, 1_500_000])
+def test_cached_count_shapes_vs_oracle(shape, n):
     w, h = shape
     x, y = synthetic.gaussian_mixture_np(n, seed=n + w, dtype=np.float32)
     cols = {"x": x, "y": y}
@@ -261,27 +261,47 @@ def test_binned_count_shapes_vs_oracle(shape, n):
     assert_same(got, ref)
 
 
-def test_binned_count_f64_and_accumulate():
+def _count_ws(frame, width, height, x_range, y_range, flags_seq=(0,)):
     import ctypes
     from datashader_gb300 import _native as N
     from datashader_gb300.compiler import compile_plan
     from datashader_gb300.core import Executor
     from datashader_gb300.glyphs import Point
-    x, y = synthetic.gaussian_mixture_np(300_001, seed=4)
-    cols = {"x": x, "y": y}
-    frame = frame_from_numpy(cols)
     plan = compile_plan(ds.count(), frame)
     ex = Executor(frame, plan, Point("x", "y"))
-    ex.allocate(1024, 1024, frame.device)
-    cv = N.CanvasDesc(1024, 1024, 0, 0, 128.0, 512.0, 128.0, 512.0, -4.0, 4.0, -4.0, 4.0)
+    ex.allocate(height, width, frame.device)
+    cvs = ds.Canvas(width, height, x_range, y_range)
+    sx, tx = cvs.x_axis.compute_scale_and_translate(x_range, width)
+    sy, ty = cvs.y_axis.compute_scale_and_translate(y_range, height)
+    cv = N.CanvasDesc(width, height, 0, 0, sx, tx, sy, ty, float(x_range[0]), float(x_range[1]),
+                      float(y_range[0]), float(y_range[1]))
     L = N.lib()
     wsz = int(L.dsgb_points_workspace_size(len(frame), ctypes.byref(cv), ex.bases, 1))
     assert wsz > 0
     ws = torch.empty(wsz, dtype=torch.uint8, device="cuda")
     st = torch.cuda.current_stream().cuda_stream
-    for flags in (0, N.FLAG_NO_INIT):   # the second call adds onto the first
+    for flags in flags_seq:
         N.check(L.dsgb_points_ws(ex.cols, len(ex.names), len(frame), 0, 0, 1, ctypes.byref(cv), ex.bases, 1,
                                  ex.outs, 0, ws.data_ptr(), wsz, flags, st), "dsgb_points_ws")
-    got = to_numpy(type("A", (), {"data": ex.out_tensors[0]})())
+    return to_numpy(type("A", (), {"data": ex.out_tensors[0]})())
+
+
+def test_cached_count_accumulate():
+    from datashader_gb300 import _native as N
+    x, y = synthetic.gaussian_mixture_np(1_300_001, seed=4, dtype=np.float32)
+    cols = {"x": x, "y": y}
+    got = _count_ws(frame_from_numpy(cols), 1024, 1024, (-4, 4), (-4, 4), (0, N.FLAG_NO_INIT))
     ref = run_points(cols, {}, ds.count(), CANVAS2)
     assert_same(got, 2 * ref)
+
+
+def test_cached_count_single_hot_pixel():
+    """Nearly every row on two pixels: the cached counters take every row."""
+    n = 12_000_000
+    x = np.full(n, 0.1, dtype=np.float32)
+    y = np.full(n, -0.2, dtype=np.float32)
+    x[::7] = 0.7                      # a second hot pixel
+    got = _count_ws(frame_from_numpy({"x": x, "y": y}), 1024, 1024, (-4, 4), (-4, 4))
+    ref = run_points({"x": x, "y": y}, {}, ds.count(), CANVAS2)
+    assert_same(got, ref)
+    assert int(got.astype(np.int64).sum()) == n
