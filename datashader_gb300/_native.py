@@ -138,7 +138,7 @@ EXPORTED = (
     "dsgb_abi_version", "dsgb_last_error", "dsgb_device_sm_count", "dsgb_bases_init",
     "dsgb_finalize", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_ws", "dsgb_line_axis0", "dsgb_line_axis0_backward",
     "dsgb_points_backward", "dsgb_bounds", "dsgb_eq_hist_workspace_size", "dsgb_eq_hist_u32",
-    "dsgb_eq_hist_f64", "dsgb_pyramid_tile_offset", "dsgb_pyramid", "dsgb_pyramid_finalize",
+    "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_pyramid_tile_offset", "dsgb_pyramid", "dsgb_pyramid_finalize",
 )
 
 _lock = threading.Lock()
@@ -173,6 +173,7 @@ def _declare(L):
     L.dsgb_eq_hist_workspace_size.restype = ctypes.c_size_t
     for nm in ("dsgb_eq_hist_u32", "dsgb_eq_hist_f64"):
         getattr(L, nm).argtypes = [P, i64, i32, P, P, P, P, i32, i32, i32, P, ctypes.c_size_t, P]
+    L.dsgb_eq_hist_u32_static.argtypes = [P, i64, i32, P, P, P, P, i32, i32, i32, P]
     L.dsgb_pyramid_tile_offset.argtypes = [i32, i32, i32]
     L.dsgb_pyramid_tile_offset.restype = i64
     L.dsgb_pyramid.argtypes = [PC, i32, i64, i32, i32, i32, ctypes.POINTER(PyramidConfig), P, P, u32, P]

@@ -20,6 +20,7 @@
 #include "dsgb_internal.cuh"
 
 #include <cmath>
+#include <mutex>
 
 namespace dsgb {
 
@@ -402,9 +403,61 @@ static int eq_hist_impl(const T *data, int64_t n, int32_t nbins, double *out, in
     return DSGB_OK;
 }
 
+// ---- allocation-free variant --------------------------------------------
+//
+// Some callers cannot allocate device memory at the moment they need an
+// equalised image: a host thread with a latency budget (cudaMalloc may
+// synchronise the whole device), code that runs where allocation is not
+// allowed (inside a stream callback or another library's allocator hook),
+// or a plugin whose host process owns every device allocation.  For them
+// the scratch of eq_hist lives in this file-scope device array instead of a
+// caller workspace.  It is sized for the largest histogram the reference
+// uses (nbins = 65536, about 1.25 MiB); every GPU that loads the library
+// holds it until the process exits.
+constexpr int STATIC_MAX_BINS = 65536;
+static __device__ __align__(256) unsigned char g_eq_hist_scratch[HDR_BYTES + (size_t)STATIC_MAX_BINS * 20 + 64];
+static_assert(sizeof(g_eq_hist_scratch) >= HDR_BYTES + (size_t)STATIC_MAX_BINS * 20 + 64, "scratch size");
+
+// In host code `g_eq_hist_scratch` names a host-side shadow, not device
+// memory, so the device address is looked up once per device, with that
+// device current, and cached.
+static std::mutex g_scratch_mu;
+static void *g_scratch_ptr[128];
+
+static int static_scratch(void **ptr) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "dsgb_eq_hist_u32_static: cudaGetDevice");
+    if (dev < 0 || dev >= 128) { set_error("dsgb_eq_hist_u32_static: device ordinal %d out of range", dev); return DSGB_E_INVALID; }
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_eq_hist_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "dsgb_eq_hist_u32_static: cudaGetSymbolAddress");
+        g_scratch_ptr[dev] = p;
+    }
+    *ptr = g_scratch_ptr[dev];
+    return DSGB_OK;
+}
+
 }  // namespace dsgb
 
 using namespace dsgb;
+
+extern "C" int dsgb_eq_hist_u32_static(const uint32_t *data, int64_t n, int32_t nbins, double *out,
+                                       int64_t *levels, uint32_t *rgba, const uint8_t *cmap_rgb,
+                                       int32_t ncolors, int32_t alpha, int32_t rescale, void *stream) {
+    if (nbins < 1 || nbins > STATIC_MAX_BINS) {
+        set_error("dsgb_eq_hist_u32_static: nbins=%d is outside 1..%d, the size of the static scratch",
+                  nbins, STATIC_MAX_BINS);
+        return DSGB_E_INVALID;
+    }
+    void *scratch = nullptr;
+    int rc = static_scratch(&scratch);
+    if (rc) return rc;
+    return eq_hist_impl<unsigned int>((const unsigned int *)data, n, nbins, out, levels, rgba, cmap_rgb,
+                                      ncolors, alpha, rescale, scratch, sizeof(g_eq_hist_scratch), stream);
+}
 
 extern "C" size_t dsgb_eq_hist_workspace_size(int32_t nbins) { return ws_bytes(nbins < 1 ? 1 : nbins); }
 

@@ -228,6 +228,21 @@ int dsgb_eq_hist_f64(const double *data, int64_t n, int32_t nbins,
                      int32_t rescale_discrete_levels,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+/* dsgb_eq_hist_u32 for callers that cannot allocate device memory (no
+ * counterpart in the reference).  The scratch is a file-scope device array
+ * inside libdsgb sized for nbins <= 65536 (about 1.25 MiB, held on every GPU
+ * that loads the library until the process exits); larger nbins are
+ * rejected with DSGB_E_INVALID.  Nothing is allocated: the first call on a
+ * device looks up the array's device address (with that device current)
+ * and caches it, so make that first call before any stream capture.  Every
+ * call shares the one array and resets what must start at zero, so calls
+ * whose work overlaps on the GPU (different streams, or host threads racing
+ * on one device) corrupt each other: serialise them. */
+int dsgb_eq_hist_u32_static(const uint32_t *data, int64_t n, int32_t nbins,
+                            double *out, int64_t *levels, uint32_t *rgba,
+                            const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                            int32_t rescale_discrete_levels, void *stream);
+
 /* ---- batched tile pyramid --------------------------------------------------
  * Every tile (z, tx, ty) for z in [zmin, zmax] of the [x0,x1)x[y0,y1) square
  * is a tile_size x tile_size Canvas.points aggregate with inclusive bounds
