@@ -306,11 +306,13 @@ __global__ void __launch_bounds__(256) line_axis0_kernel(const LineParams p) {
     for (int64_t i = gtid(); i + 1 < p.n; i += gstride()) {
         double x0 = load_f64(X, i), y0 = load_f64(Y, i);
         double x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
+        // the previous row, with numba's wrap of index -1 onto the last row
+        const int64_t im = i > 0 ? i - 1 : p.n - 1;
         bool segment_start = (i == 0) ? (p.plot_start != 0)
-                                      : (isnull(load_f64(X, i - 1)) || isnull(load_f64(Y, i - 1)));
+                                      : (isnull(load_f64(X, im)) || isnull(load_f64(Y, im)));
         bool segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
         double xm = 0.0, ym = 0.0;
-        if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, i - 1); ym = load_f64(Y, i - 1); }
+        if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, im); ym = load_f64(Y, im); }
         bool skip = isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1);
         bool cs = false, ce = false;
         liang_barsky(p.xmin, p.xmax, p.ymin, p.ymax, x0, x1, y0, y1, skip, cs, ce);

@@ -1,0 +1,378 @@
+// line_backward.cu -- adjoints of the aggregation (no reference counterpart).
+//
+// dsgb_line_axis0_backward: the adjoint of the antialiased LineAxis0 sum('v')
+// aggregate (self-intersecting form, overwrite == False: every pixel of
+// segment i receives v_i * (aa - prev_aa), line.py:826-981 with
+// reductions.py:1065-1075).  For a loss L with dL/dagg = g:
+//
+//   dL/dv_i  = sum over the pixels p that segment i appends of g[p] * (aa - prev_aa)
+//   dL/dy_k  = sum over segments i-1, i, i+1 touching y_k of g[p] * v_i * d(aa - prev_aa)/dy_k
+//
+// Segment i depends on y_{i-1} (the previous vertex, used by the previous-
+// segment correction), y_i and y_{i+1}.  The coverage is recomputed, never
+// stored: each thread re-runs the segment's scan conversion in forward-mode
+// dual arithmetic (a value and its three tangents), through the pixel
+// mapping, Liang-Barsky clipping and _full_antialias.  Every branch is taken
+// on the value, computed with the same operations as the forward kernel
+// (this file is compiled without FMA contraction), so the pixels and
+// decisions are exactly the forward pass's; the gradient is the derivative
+// almost everywhere (clamps, abs, the integer scanline limits and the
+// "value <= prev_value" choice are kinks with one-sided derivatives).
+//
+// dsgb_points_backward: the gather adjoint of points sum / mean with respect
+// to the value column: dL/dv_i = g[p(i)] (sum) or g[p(i)] / count[p(i)] (mean)
+// for rows that land on a pixel with a non-NaN value, 0 otherwise.
+#include "dsgb_internal.cuh"
+#include "binning.cuh"
+
+#include <cmath>
+
+namespace dsgb {
+
+// ---------------------------------------------------------------- duals
+
+struct D3 {
+    double v, g0, g1, g2;
+};
+__device__ __forceinline__ D3 dc(double v) { return D3{v, 0.0, 0.0, 0.0}; }
+__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return D3{a.v + b.v, a.g0 + b.g0, a.g1 + b.g1, a.g2 + b.g2}; }
+__device__ __forceinline__ D3 operator-(D3 a, D3 b) { return D3{a.v - b.v, a.g0 - b.g0, a.g1 - b.g1, a.g2 - b.g2}; }
+__device__ __forceinline__ D3 operator-(D3 a) { return D3{-a.v, -a.g0, -a.g1, -a.g2}; }
+__device__ __forceinline__ D3 operator*(D3 a, D3 b) {
+    return D3{a.v * b.v, a.g0 * b.v + a.v * b.g0, a.g1 * b.v + a.v * b.g1, a.g2 * b.v + a.v * b.g2};
+}
+__device__ __forceinline__ D3 operator/(D3 a, D3 b) {
+    const double q = a.v / b.v;
+    return D3{q, (a.g0 - q * b.g0) / b.v, (a.g1 - q * b.g1) / b.v, (a.g2 - q * b.g2) / b.v};
+}
+__device__ __forceinline__ D3 dsqrt(D3 a) {
+    const double r = sqrt(a.v);
+    const double k = r > 0.0 ? 0.5 / r : 0.0;
+    return D3{r, a.g0 * k, a.g1 * k, a.g2 * k};
+}
+__device__ __forceinline__ D3 dabs(D3 a) { return a.v < 0.0 ? -a : a; }
+__device__ __forceinline__ D3 dsq(D3 a) { return a * a; }
+// max(lo, min(x, hi)) as the forward computes it
+__device__ __forceinline__ D3 dclamp(D3 x, double lo, double hi) {
+    D3 m = x.v < hi ? x : dc(hi);
+    return lo > m.v ? dc(lo) : m;
+}
+__device__ __forceinline__ D3 dlinearstep(double e0, double e1, D3 x) {
+    return dclamp((x - dc(e0)) / dc(e1 - e0), 0.0, 1.0);
+}
+__device__ __forceinline__ D3 dx_intercept(double y, D3 cx0, D3 cy0, D3 cx1, D3 cy1) {
+    if (cy0.v == cy1.v) return cx1;
+    const D3 frac = (dc(y) - cy0) / (cy1 - cy0);
+    return cx0 + frac * (cx1 - cx0);
+}
+__device__ __forceinline__ long long clampi_b(long long x, long long lo, long long hi) {
+    long long m = x < hi ? x : hi;
+    return lo > m ? lo : m;
+}
+
+// line.py:783-800 in duals
+__device__ __forceinline__ bool dclipt(D3 p, D3 q, D3 &t0, D3 &t1) {
+    bool accept = true;
+    if (p.v < 0 && q.v < 0) {
+        const D3 r = q / p;
+        if (r.v > t1.v) accept = false;
+        else if (r.v > t0.v) t0 = r;
+    } else if (p.v > 0 && q.v < p.v) {
+        const D3 r = q / p;
+        if (r.v < t0.v) accept = false;
+        else if (r.v < t1.v) t1 = r;
+    } else if (q.v < 0) {
+        accept = false;
+    }
+    return accept;
+}
+
+struct BwdParams {
+    ColumnRef X, Y, V;
+    int64_t n;
+    int32_t width, height;
+    double sx, tx, sy, ty;
+    double xmin, xmax, ymin, ymax;
+    double line_width;
+    int32_t plot_start;
+    const double *grad;
+    const uint8_t *any;
+    double *grad_v, *grad_y;
+};
+
+// The appends of one segment: accumulates dL/dv_i and the three y tangents.
+__device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3 y0, D3 y1,
+                                 bool segment_start, bool segment_end, D3 xm, D3 ym,
+                                 long long nx, long long ny, double field,
+                                 double &gv, double &gy0, double &gy1, double &gy2) {
+    double line_width = p.line_width;
+    bool overwrite = false;
+    if (x0.v == x1.v && y0.v == y1.v) return;
+    const bool flip_xy = fabs(x0.v - x1.v) < fabs(y0.v - y1.v);
+    if (flip_xy) {
+        D3 t;
+        t = x0; x0 = y0; y0 = t;
+        t = x1; x1 = y1; y1 = t;
+        t = xm; xm = ym; ym = t;
+    }
+    double scale = 1.0;
+    if (line_width < 1.0) { scale *= line_width; line_width = 1.0; }
+    const double aa = 1.0;
+    const double halfwidth = 0.5 * (line_width + aa);
+    const bool flip_order = y1.v < y0.v || (y1.v == y0.v && x1.v < x0.v);
+    D3 alongx = x1 - x0, alongy = y1 - y0;
+    const D3 length = dsqrt(dsq(alongx) + dsq(alongy));
+    alongx = alongx / length;
+    alongy = alongy / length;
+    const D3 rightx = alongy, righty = -alongx;
+    const D3 hw = dc(halfwidth);
+    D3 b[8];
+    if (flip_order) {
+        b[0] = x1 - hw * (rightx - alongx);
+        b[1] = x1 - hw * (-rightx - alongx);
+        b[2] = x0 - hw * (-rightx + alongx);
+        b[3] = x0 - hw * (rightx + alongx);
+        b[4] = y1 - hw * (righty - alongy);
+        b[5] = y1 - hw * (-righty - alongy);
+        b[6] = y0 - hw * (-righty + alongy);
+        b[7] = y0 - hw * (righty + alongy);
+    } else {
+        b[0] = x0 + hw * (rightx - alongx);
+        b[1] = x0 + hw * (-rightx - alongx);
+        b[2] = x1 + hw * (-rightx + alongx);
+        b[3] = x1 + hw * (rightx + alongx);
+        b[4] = y0 + hw * (righty - alongy);
+        b[5] = y0 + hw * (-righty - alongy);
+        b[6] = y1 + hw * (-righty + alongy);
+        b[7] = y1 + hw * (righty + alongy);
+    }
+    long long xmaxi = nx - 1, ymaxi = ny - 1;
+    if (flip_xy) { long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
+    const int lowindex = flip_order ? (x0.v > x1.v ? 0 : 1) : (x1.v > x0.v ? 0 : 1);
+    D3 prev_alongx = dc(0), prev_alongy = dc(0), prev_length = dc(0), prev_rightx = dc(0), prev_righty = dc(0);
+    if (!overwrite && !segment_start) {
+        prev_alongx = x0 - xm;
+        prev_alongy = y0 - ym;
+        prev_length = dsqrt(dsq(prev_alongx) + dsq(prev_alongy));
+        if (prev_length.v > 0.0) {
+            prev_alongx = prev_alongx / prev_length;
+            prev_alongy = prev_alongy / prev_length;
+            prev_rightx = prev_alongy;
+            prev_righty = -prev_alongx;
+        } else {
+            overwrite = true;
+        }
+    }
+    const long long ystart = clampi_b((long long)ceil(b[4 + lowindex].v), 0, ymaxi);
+    const long long yend = clampi_b((long long)floor(b[4 + (lowindex + 2) % 4].v), 0, ymaxi);
+    int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
+    const double lw_lo = 0.5 * (line_width - aa);
+    for (long long y = ystart; y <= yend; ++y) {
+        const double yd = (double)y;
+        if (ll == lowindex && yd > b[4 + lu].v) { ll = lu; lu = (ll + 1) % 4; }
+        if (rl == lowindex && yd > b[4 + ru].v) { rl = ru; ru = (rl + 3) % 4; }
+        const long long xleft = clampi_b((long long)ceil(dx_intercept(yd, b[ll], b[4 + ll], b[lu], b[4 + lu]).v), 0, xmaxi);
+        const long long xright = clampi_b((long long)floor(dx_intercept(yd, b[rl], b[4 + rl], b[ru], b[4 + ru]).v), 0, xmaxi);
+        for (long long x = xleft; x <= xright; ++x) {
+            const D3 xd = dc((double)x), ydd = dc(yd);
+            const D3 along = (xd - x0) * alongx + (ydd - y0) * alongy;
+            bool prev_correction = false;
+            D3 distance;
+            if (along.v < 0.0) {
+                if (overwrite || segment_start || ((xd - x0) * prev_alongx + (ydd - y0) * prev_alongy).v > 0.0)
+                    distance = dsqrt(dsq(xd - x0) + dsq(ydd - y0));
+                else continue;
+            } else if (along.v > length.v) {
+                if (overwrite || segment_end) distance = dsqrt(dsq(xd - x1) + dsq(ydd - y1));
+                else continue;
+            } else {
+                distance = dabs((xd - x0) * rightx + (ydd - y0) * righty);
+                if (!overwrite && !segment_start) {
+                    const D3 pd = (xd - x0) * prev_alongx + (ydd - y0) * prev_alongy;
+                    if (-prev_length.v <= pd.v && pd.v <= 0.0 &&
+                        dabs((xd - x0) * prev_rightx + (ydd - y0) * prev_righty).v <= halfwidth)
+                        prev_correction = true;
+                }
+            }
+            D3 value = dc(1.0) - dlinearstep(lw_lo, halfwidth, distance);
+            value = value * dc(scale);
+            D3 prev_value = dc(0.0);
+            if (prev_correction) {
+                const D3 prev_distance = dabs((xd - x0) * prev_rightx + (ydd - y0) * prev_righty);
+                prev_value = dc(1.0) - dlinearstep(lw_lo, halfwidth, prev_distance);
+                prev_value = prev_value * dc(scale);
+                if (value.v <= prev_value.v) value = dc(0.0);
+            }
+            if (value.v > 0.0) {
+                const long long xx = flip_xy ? y : x, yy = flip_xy ? x : y;
+                if (xx < 0 || yy < 0 || xx >= p.width || yy >= p.height) continue;
+                const int64_t pix = yy * (int64_t)p.width + xx;
+                if (p.any && !p.any[pix]) continue;
+                const double g = p.grad[pix];
+                const D3 d = value - prev_value;
+                gv += g * d.v;
+                gy0 += g * field * d.g0;
+                gy1 += g * field * d.g1;
+                gy2 += g * field * d.g2;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) line_backward_kernel(const BwdParams p) {
+    for (int64_t i = gtid(); i + 1 < p.n; i += gstride()) {
+        const double field = load_f64(p.V, i);
+        const double xv0 = load_f64(p.X, i), yv0 = load_f64(p.Y, i);
+        const double xv1 = load_f64(p.X, i + 1), yv1 = load_f64(p.Y, i + 1);
+        // the previous row, with numba's wrap of index -1 onto the last row
+        const int64_t im = i > 0 ? i - 1 : p.n - 1;
+        bool segment_start = (i == 0) ? (p.plot_start != 0)
+                                      : (isnull(load_f64(p.X, im)) || isnull(load_f64(p.Y, im)));
+        const bool segment_end = (i == p.n - 2) || isnull(load_f64(p.X, i + 2)) || isnull(load_f64(p.Y, i + 2));
+        double xmv = 0.0, ymv = 0.0;
+        if (!segment_start) { xmv = load_f64(p.X, im); ymv = load_f64(p.Y, im); }
+        if (isnull(field) || isnull(xv0) || isnull(yv0) || isnull(xv1) || isnull(yv1)) continue;
+        // tangents: g0 = d/dy_{i-1}, g1 = d/dy_i, g2 = d/dy_{i+1}
+        D3 x0 = dc(xv0), x1 = dc(xv1);
+        D3 y0 = D3{yv0, 0.0, 1.0, 0.0}, y1 = D3{yv1, 0.0, 0.0, 1.0};
+        // line.py:734-780 (Liang-Barsky) in duals
+        bool skip = false;
+        if (x0.v < p.xmin && x1.v < p.xmin) skip = true;
+        else if (x0.v > p.xmax && x1.v > p.xmax) skip = true;
+        else if (y0.v < p.ymin && y1.v < p.ymin) skip = true;
+        else if (y0.v > p.ymax && y1.v > p.ymax) skip = true;
+        D3 t0 = dc(0.0), t1 = dc(1.0);
+        const D3 dx1 = x1 - x0;
+        if (!dclipt(-dx1, x0 - dc(p.xmin), t0, t1)) skip = true;
+        if (!dclipt(dx1, dc(p.xmax) - x0, t0, t1)) skip = true;
+        const D3 dy1 = y1 - y0;
+        if (!dclipt(-dy1, y0 - dc(p.ymin), t0, t1)) skip = true;
+        if (!dclipt(dy1, dc(p.ymax) - y0, t0, t1)) skip = true;
+        if (skip) continue;
+        bool cs = false;
+        if (t1.v < 1) { x1 = x0 + t1 * dx1; y1 = y0 + t1 * dy1; }
+        if (t0.v > 0) { cs = true; x0 = x0 + t0 * dx1; y0 = y0 + t0 * dy1; }
+        segment_start = segment_start || cs;
+        // line.py:723-726 (no snap) in duals
+        const D3 sxd = dc(p.sx), txd = dc(p.tx), syd = dc(p.sy), tyd = dc(p.ty), half = dc(0.5);
+        const D3 px0 = x0 * sxd + txd - half, py0 = y0 * syd + tyd - half;
+        const D3 px1 = x1 * sxd + txd - half, py1 = y1 * syd + tyd - half;
+        D3 pxm = dc(0.0), pym = dc(0.0);
+        if (!segment_start) {
+            pxm = dc(xmv) * sxd + txd - half;
+            pym = D3{ymv, 1.0, 0.0, 0.0} * syd + tyd - half;
+        }
+        const long long nx = (long long)rint((p.xmax - p.xmin) * p.sx);
+        const long long ny = (long long)rint((p.ymax - p.ymin) * p.sy);
+        double gv = 0.0, gy0 = 0.0, gy1 = 0.0, gy2 = 0.0;
+        segment_backward(p, i, px0, px1, py0, py1, segment_start, segment_end, pxm, pym, nx, ny, field,
+                         gv, gy0, gy1, gy2);
+        p.grad_v[i] = gv;   // only segment i appends row i's value
+        if (gy0 != 0.0) atomicAdd(&p.grad_y[im], gy0);
+        if (gy1 != 0.0) atomicAdd(&p.grad_y[i], gy1);
+        if (gy2 != 0.0) atomicAdd(&p.grad_y[i + 1], gy2);
+    }
+}
+
+// ---- points sum / mean gather adjoint
+struct PBwdParams {
+    ColumnRef X, Y, V;
+    int64_t n;
+    BinAxis ax, ay;
+    double xmin, xmax, ymin, ymax;
+    int32_t width;
+    const double *grad;
+    const uint32_t *counts;
+    double *grad_v;
+};
+
+__global__ void __launch_bounds__(256) points_backward_kernel(const PBwdParams p) {
+    for (int64_t i = gtid(); i < p.n; i += gstride()) {
+        const double x = load_f64(p.X, i), y = load_f64(p.Y, i), v = load_f64(p.V, i);
+        double g = 0.0;
+        if (!isnull(v) && (p.xmin <= x && x <= p.xmax) && (p.ymin <= y && y <= p.ymax)) {
+            const int xi = bin_exact64(x, p.ax), yi = bin_exact64(y, p.ay);
+            const int64_t pix = (int64_t)yi * p.width + xi;
+            g = p.grad[pix];
+            if (p.counts) g = g / (double)p.counts[pix];
+        }
+        p.grad_v[i] = g;
+    }
+}
+
+static unsigned grid_of(int64_t n) {
+    int sms = sm_count();
+    if (sms <= 0) sms = 148;
+    int64_t g = (n + 255) / 256;
+    if (g > (int64_t)sms * 16) g = (int64_t)sms * 16;
+    if (g < 1) g = 1;
+    return (unsigned)g;
+}
+
+}  // namespace dsgb
+
+using namespace dsgb;
+
+extern "C" int dsgb_line_axis0_backward(const dsgb_column *cols, int32_t ncols, int64_t n,
+                                        int32_t x_col, int32_t y_col, int32_t v_col,
+                                        const dsgb_canvas *canvas, double line_width,
+                                        int32_t plot_start, const double *grad_agg,
+                                        const uint8_t *agg_any, double *grad_v, double *grad_y,
+                                        void *stream) {
+    if (!cols || !canvas || !grad_agg || !grad_v || !grad_y || n < 0 || x_col < 0 || y_col < 0 || v_col < 0 ||
+        x_col >= ncols || y_col >= ncols || v_col >= ncols || canvas->width <= 0 || canvas->height <= 0) {
+        set_error("dsgb_line_axis0_backward: invalid arguments");
+        return DSGB_E_INVALID;
+    }
+    if (!(line_width > 0.0) || canvas->x_log || canvas->y_log) {
+        set_error("dsgb_line_axis0_backward: needs an antialiased line (line_width > 0) on linear axes");
+        return DSGB_E_UNSUPPORTED;
+    }
+    BwdParams p;
+    memset(&p, 0, sizeof(p));
+    p.X = ColumnRef{cols[x_col].data, cols[x_col].dtype};
+    p.Y = ColumnRef{cols[y_col].data, cols[y_col].dtype};
+    p.V = ColumnRef{cols[v_col].data, cols[v_col].dtype};
+    p.n = n; p.width = canvas->width; p.height = canvas->height;
+    p.sx = canvas->sx; p.tx = canvas->tx; p.sy = canvas->sy; p.ty = canvas->ty;
+    p.xmin = canvas->xmin; p.xmax = canvas->xmax; p.ymin = canvas->ymin; p.ymax = canvas->ymax;
+    p.line_width = line_width; p.plot_start = plot_start;
+    p.grad = grad_agg; p.any = agg_any; p.grad_v = grad_v; p.grad_y = grad_y;
+    cudaStream_t st = as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(grad_y, 0, (size_t)n * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(grad_v, 0, (size_t)n * 8, st);
+    if (e != cudaSuccess) return cuda_status(e, "dsgb_line_axis0_backward memset");
+    if (n > 1) line_backward_kernel<<<grid_of(n), 256, 0, st>>>(p);
+    DSGB_CHECK_LAUNCH("dsgb_line_axis0_backward");
+    return DSGB_OK;
+}
+
+extern "C" int dsgb_points_backward(const dsgb_column *cols, int32_t ncols, int64_t n,
+                                    int32_t x_col, int32_t y_col, int32_t v_col,
+                                    const dsgb_canvas *canvas, const double *grad_agg,
+                                    const uint32_t *counts, double *grad_v, uint32_t flags, void *stream) {
+    (void)flags;
+    if (!cols || !canvas || !grad_agg || !grad_v || n < 0 || x_col < 0 || y_col < 0 || v_col < 0 ||
+        x_col >= ncols || y_col >= ncols || v_col >= ncols || canvas->width <= 0 || canvas->height <= 0) {
+        set_error("dsgb_points_backward: invalid arguments");
+        return DSGB_E_INVALID;
+    }
+    if (canvas->x_log || canvas->y_log) {
+        set_error("dsgb_points_backward: log axes are not supported");
+        return DSGB_E_UNSUPPORTED;
+    }
+    PBwdParams p;
+    memset(&p, 0, sizeof(p));
+    p.X = ColumnRef{cols[x_col].data, cols[x_col].dtype};
+    p.Y = ColumnRef{cols[y_col].data, cols[y_col].dtype};
+    p.V = ColumnRef{cols[v_col].data, cols[v_col].dtype};
+    p.n = n;
+    p.ax = make_axis(canvas->sx, canvas->tx, canvas->xmin, canvas->xmax, canvas->width);
+    p.ay = make_axis(canvas->sy, canvas->ty, canvas->ymin, canvas->ymax, canvas->height);
+    p.xmin = canvas->xmin; p.xmax = canvas->xmax; p.ymin = canvas->ymin; p.ymax = canvas->ymax;
+    p.width = canvas->width;
+    p.grad = grad_agg; p.counts = counts; p.grad_v = grad_v;
+    if (n > 0) points_backward_kernel<<<grid_of(n), 256, 0, as_stream(stream)>>>(p);
+    DSGB_CHECK_LAUNCH("dsgb_points_backward");
+    return DSGB_OK;
+}

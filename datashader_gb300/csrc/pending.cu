@@ -13,13 +13,3 @@ extern "C" int dsgb_pyramid(const dsgb_column *, int32_t, int64_t, int32_t, int3
 extern "C" int dsgb_pyramid_finalize(const int64_t *, double *, int64_t, void *) {
     set_error("dsgb_pyramid_finalize: not built"); return DSGB_E_UNSUPPORTED;
 }
-extern "C" int dsgb_line_axis0_backward(const dsgb_column *, int32_t, int64_t, int32_t, int32_t, int32_t,
-                                        const dsgb_canvas *, double, int32_t, const double *,
-                                        const uint8_t *, double *, double *, void *) {
-    set_error("dsgb_line_axis0_backward: not built"); return DSGB_E_UNSUPPORTED;
-}
-extern "C" int dsgb_points_backward(const dsgb_column *, int32_t, int64_t, int32_t, int32_t, int32_t,
-                                    const dsgb_canvas *, const double *, const uint32_t *, double *,
-                                    uint32_t, void *) {
-    set_error("dsgb_points_backward: not built"); return DSGB_E_UNSUPPORTED;
-}

@@ -582,11 +582,13 @@ int oracle_line_axis0(int64_t n, const double *xs, const double *ys,
     int antialias = line_width > 0.0;
     for (int64_t i = 0; i + 1 < n; ++i) {
         double x0 = xs[i], y0 = ys[i], x1 = xs[i + 1], y1 = ys[i + 1];
-        int segment_start = (i == 0) ? plot_start : (isnull_d(xs[i - 1]) || isnull_d(ys[i - 1]));
+        /* xs[i - 1] with numba's wrap of index -1 onto the last row */
+        const int64_t im = i > 0 ? i - 1 : n - 1;
+        int segment_start = (i == 0) ? plot_start : (isnull_d(xs[im]) || isnull_d(ys[im]));
         int segment_end = (i == n - 2) || isnull_d(xs[i + 2]) || isnull_d(ys[i + 2]);
         double xm, ym;
         if (segment_start || use_2_stage_agg) { xm = 0.0; ym = 0.0; }
-        else { xm = xs[i - 1]; ym = ys[i - 1]; }
+        else { xm = xs[im]; ym = ys[im]; }
         int skip = 0;
         if (isnull_d(x0) || isnull_d(y0) || isnull_d(x1) || isnull_d(y1)) skip = 1;
         int clipped_start = 0, clipped_end = 0;

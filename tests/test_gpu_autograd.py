@@ -1,0 +1,139 @@
+"""Hand-written adjoints against float64 central finite differences.
+
+The loss is the differentiation workload's: the MSE between an aggregate and
+the aggregate of the same series with y perturbed, NaN pixels masked with
+nan_to_num on both sides.  Gradients with respect to v and y from the
+adjoint kernels are compared with central differences of (a) the GPU forward
+and (b) the CPU oracle forward (the reference algorithm) on random
+coordinates.  Coordinates where the one-sided differences disagree sit on a
+kink of the piecewise-smooth coverage (a clamp edge, a scanline limit, the
+previous-segment choice); they are reported and excluded, and must be rare.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import datashader_gb300 as ds
+import oracle
+from datashader_gb300 import autograd as ag
+from datashader_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def _series(nseries=12, length=160, seed=0):
+    x, y, v, _ = synthetic.time_series_np(nseries, length, seed)
+    return x, y, v
+
+
+def _canvas(y):
+    lo, hi = float(np.nanmin(y)), float(np.nanmax(y))
+    pad = 0.05 * (hi - lo)
+    return ds.Canvas(plot_width=160, plot_height=80, x_range=(0.0, 1.0), y_range=(lo - pad, hi + pad))
+
+
+def _loss_gpu(x, y, v, target, cvs, lw=1.5):
+    agg = ag.line_sum(x, y, v, cvs, lw)
+    return torch.mean((torch.nan_to_num(agg) - target) ** 2)
+
+
+def _loss_oracle(x, y, v, target_np, cvs, lw=1.5):
+    agg = oracle.line_axis0({"x": x, "y": y, "v": v}, "x", "y", cvs.plot_width, cvs.plot_height,
+                            cvs.x_range, cvs.y_range, [oracle.spec("sum", "v")], line_width=lw)[0]
+    return float(np.mean((np.nan_to_num(agg) - target_np) ** 2))
+
+
+def test_line_sum_adjoint_vs_finite_differences():
+    x, y, v = _series()
+    rng = np.random.default_rng(7)
+    y_t = y + rng.normal(0, 0.005, y.shape)
+    cvs = _canvas(y)
+    X = torch.from_numpy(x).cuda()
+    target = torch.nan_to_num(ag.line_sum(X, torch.from_numpy(y_t).cuda(), torch.from_numpy(v).cuda(), cvs)).detach()
+    target_np = target.cpu().numpy()
+    Y = torch.from_numpy(y).cuda().requires_grad_(True)
+    V = torch.from_numpy(v).cuda().requires_grad_(True)
+    loss = _loss_gpu(X, Y, V, target, cvs)
+    loss.backward()
+    gy, gv = Y.grad.cpu().numpy(), V.grad.cpu().numpy()
+    valid = np.flatnonzero(~np.isnan(y))
+    picks = rng.choice(valid, 64, replace=False)
+
+    def loss_at(which, k, d):
+        arr = (y if which == "y" else v).copy()
+        arr[k] += d
+        yy, vv = (arr, v) if which == "y" else (y, arr)
+        return float(_loss_gpu(X, torch.from_numpy(yy).cuda(), torch.from_numpy(vv).cuda(), target, cvs))
+
+    kinks, checked = [], 0
+    for which, grad, base in (("y", gy, y), ("v", gv, v)):
+        for k in picks[:32] if which == "y" else picks[32:]:
+            # The loss is exactly quadratic in v (the coverage does not depend
+            # on v): no kinks, and the central difference is exact.  In y it is
+            # piecewise smooth: the one-sided asymmetry a(h) = (f(h) + f(-h) -
+            # 2 f(0)) / h shrinks like h on a smooth piece and stays at the
+            # slope jump on a kink.
+            h = 1e-6 if which == "y" else 1e-3
+            f0, fp, fm = loss_at(which, k, 0.0), loss_at(which, k, h), loss_at(which, k, -h)
+            central = (fp - fm) / (2 * h)
+            scale = max(abs(central), abs(grad[k]), 1e-12)
+            if which == "y":
+                a1 = (fp + fm - 2 * f0) / h
+                q = h / 8
+                a2 = (loss_at(which, k, q) + loss_at(which, k, -q) - 2 * f0) / q
+                if abs(a2) > 0.5 * abs(a1) and abs(a1) > 1e-6 * scale:
+                    kinks.append((which, int(k)))
+                    continue
+            checked += 1
+            assert abs(grad[k] - central) <= 1e-4 * scale + 1e-10, (which, k, grad[k], central)
+            # the reference algorithm's own finite difference (CPU oracle forward)
+            arrp, arrm = base.copy(), base.copy()
+            arrp[k] += h
+            arrm[k] -= h
+            if which == "y":
+                ref = (_loss_oracle(x, arrp, v, target_np, cvs) - _loss_oracle(x, arrm, v, target_np, cvs)) / (2 * h)
+            else:
+                ref = (_loss_oracle(x, y, arrp, target_np, cvs) - _loss_oracle(x, y, arrm, target_np, cvs)) / (2 * h)
+            assert abs(grad[k] - ref) <= 1e-4 * max(abs(ref), abs(grad[k]), 1e-12) + 1e-10, (which, k, grad[k], ref)
+    assert checked >= 56, f"too many kink coordinates: {kinks}"
+
+
+def test_line_sum_adjoint_value_linearity():
+    """The aggregate is linear in v: the v-gradient of <w, agg> is exact."""
+    x, y, v = _series(6, 120, seed=3)
+    cvs = _canvas(y)
+    X, Y = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    V = torch.from_numpy(v).cuda().requires_grad_(True)
+    agg = ag.line_sum(X, Y, V, cvs)
+    w = torch.randn_like(agg)
+    (torch.nan_to_num(agg) * w).sum().backward()
+    # <w, agg(v)> = sum_i v_i * c_i, so c_i = <w, agg(e_i)>
+    for i in (5, 40, 77):
+        e = np.zeros_like(v)
+        e[i] = 1.0
+        ai = torch.nan_to_num(ag.line_sum(X, Y, torch.from_numpy(e).cuda(), cvs))
+        assert abs(float((ai * w).sum()) - float(V.grad[i])) <= 1e-10 * max(1.0, abs(float(V.grad[i])))
+
+
+@pytest.mark.parametrize("mean", [False, True])
+def test_points_adjoint_vs_finite_differences(mean):
+    rng = np.random.default_rng(11)
+    n = 20_000
+    x, y = synthetic.gaussian_mixture_np(n, seed=2, dtype=np.float32)
+    v = rng.lognormal(0, 1, n)
+    cvs = ds.Canvas(plot_width=64, plot_height=64, x_range=(-4, 4), y_range=(-4, 4))
+    X, Y = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    V = torch.from_numpy(v).cuda().requires_grad_(True)
+    f = ag.points_mean if mean else ag.points_sum
+    w = torch.randn(64, 64, dtype=torch.float64, device="cuda")
+    (torch.nan_to_num(f(X, Y, V, cvs)) * w).sum().backward()
+    for i in rng.choice(n, 16, replace=False):
+        h = 1e-3
+        vp, vm = v.copy(), v.copy()
+        vp[i] += h
+        vm[i] -= h
+        lp = float((torch.nan_to_num(f(X, Y, torch.from_numpy(vp).cuda(), cvs)) * w).sum())
+        lm = float((torch.nan_to_num(f(X, Y, torch.from_numpy(vm).cuda(), cvs)) * w).sum())
+        assert abs((lp - lm) / (2 * h) - float(V.grad[i])) <= 1e-7 * max(1.0, abs(float(V.grad[i])))
