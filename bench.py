@@ -43,7 +43,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Gpoints/s, Canvas.points count/mean 1e8 pts @1024²; viewport p50/p99 ms"
-WORKLOAD = "Canvas.points count, 1e8 float32 points (5-Gaussian mixture), 1024x1024 canvas over [-4,4]^2"
+def workload(n):
+    return (f"Canvas.points count, {n:,} float32 points (5-Gaussian mixture), "
+            "1024x1024 canvas over [-4,4]^2")
+
+
+# DRAM bytes (read + write) of one hot-tile count launch, from an ncu capture
+# of cached_main at 2e7 rows (164.54 MB read, 3.08 MB written; profiles/
+# cached_main_count_2e7_1024_full.md): reads scale with rows, writes with the
+# touched pixels of the 1024x1024 canvas.
+def count_traffic(n):
+    return 164.54e6 / 2e7 * n + 3.08e6
 
 
 def measured_peak():
@@ -184,7 +194,7 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "n_points": n, "canvas": [1024, 1024]},
+            "config": {"workload": workload(n), "n_points": n, "canvas": [1024, 1024]},
             "cpu_baseline": {"value": v, "unit": "Gpoints/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -274,7 +284,7 @@ def run_gpu(args):
                                      N.FLAG_NO_INIT | N.FLAG_NO_FINALIZE, stream.cuda_stream), "dsgb_points_ws")
         return launch
 
-    def roofline(agg, bytes_per_point, bytes_per_pixel, k):
+    def roofline(agg, bytes_per_point, bytes_per_pixel, k, traffic=None):
         launch = kernel_runner(agg)
         for _ in range(3):
             launch()
@@ -283,11 +293,11 @@ def run_gpu(args):
         alg = n * bytes_per_point + 1024 * 1024 * bytes_per_pixel
         achieved = alg / (avg_ms / 1e3) / 1e9
         return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg, "kernel_ms": avg_ms,
                 "kernel_gpts": n / (avg_ms / 1e3) / 1e9}
 
-    rl_count = roofline(ds.count(), 8, 4, args.steps)
+    rl_count = roofline(ds.count(), 8, 4, args.steps, traffic=count_traffic(n))
     # kernels of one count call: the hot-tile path launches sample, select and
     # main; the single-kernel path one points kernel
     _probe = Executor(frame, compile_plan(ds.count(), frame), Point("x", "y"))
@@ -352,7 +362,7 @@ def run_gpu(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_points": n, "canvas": [1024, 1024],
+            "config": {"workload": workload(n), "n_points": n, "canvas": [1024, 1024],
                        "x_range": [-4, 4], "coords": "float32", "reduction": "count",
                        "l2": "inputs (800 MB) larger than L2, no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
