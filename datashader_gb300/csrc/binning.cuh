@@ -29,14 +29,15 @@ struct BinAxis {
 };
 
 // Exact float64 binning of one mapped coordinate.
-__device__ __forceinline__ int bin_exact64(double m, const BinAxis &a) {
-    const double v = __dadd_rn(__dmul_rn(m, a.s), a.t);
+__device__ __forceinline__ int bin_exact64_st(double m, double s, double t, int n) {
+    const double v = __dadd_rn(__dmul_rn(m, s), t);
     long long xx = __double2ll_rz(v);
-    if (xx >= a.n) xx = a.n - 1;
-    if (xx < 0) xx += a.n;            // numba indexes negative positions from the end
+    if (xx >= n) xx = n - 1;
+    if (xx < 0) xx += n;              // numba indexes negative positions from the end
     if (xx < 0) xx = 0;               // unreachable after the bounds test; memory safety
     return (int)xx;
 }
+__device__ __forceinline__ int bin_exact64(double m, const BinAxis &a) { return bin_exact64_st(m, a.s, a.t, a.n); }
 
 // float32 binning of a coordinate whose float64 value is `exact` (a float
 // promoted exactly, or the original double).  `xf` is a float32 image of it
@@ -114,11 +115,21 @@ __device__ __forceinline__ int bin_try_f32(float x, float y, const BinBounds &bb
     return (okx & oky) ? 1 : 2;
 }
 
-// The exact float64 binning of an in-bounds float32 point (one copy, not inlined).
-static __device__ __noinline__ void bin_exact_f32(float x, float y, const BinAxis &ax, const BinAxis &ay,
-                                           int &xi, int &yi) {
-    xi = bin_exact64((double)x, ax);
-    yi = bin_exact64((double)y, ay);
+// The exact float64 binning of an in-bounds float32 point: one out-of-line
+// copy, kept out of the unrolled hot loops.  Scalars go in by value and the
+// pair comes back packed in one 64-bit register: reference arguments would
+// force the caller's bins and the axis structs into local memory.
+static __device__ __noinline__ unsigned long long bin_exact_pair(float x, float y, double sx, double tx, int nx,
+                                                                 double sy, double ty, int ny) {
+    const unsigned xi = (unsigned)bin_exact64_st((double)x, sx, tx, nx);
+    const unsigned yi = (unsigned)bin_exact64_st((double)y, sy, ty, ny);
+    return (unsigned long long)xi | ((unsigned long long)yi << 32);
+}
+__device__ __forceinline__ void bin_exact_f32(float x, float y, const BinAxis &ax, const BinAxis &ay,
+                                              int &xi, int &yi) {
+    const unsigned long long r = bin_exact_pair(x, y, ax.s, ax.t, ax.n, ay.s, ay.t, ay.n);
+    xi = (int)(unsigned)r;
+    yi = (int)(unsigned)(r >> 32);
 }
 
 __device__ __forceinline__ bool bin_point_f32(float x, float y, const BinBounds &bb, const BinAxis &ax,

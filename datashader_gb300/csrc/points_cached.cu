@@ -7,14 +7,18 @@
 // L2 slices.  This path absorbs the densest part of the canvas on chip:
 //
 //   sample  -- bin ~1% of the rows (evenly spaced chunks) into a histogram of
-//              tiles (16x16 px, 32x32 or 64x64 for large canvases);
-//   select  -- one block picks the K most populated tiles that fit in shared
-//              memory (a uint32 counter per pixel) and writes tile -> slot;
+//              tiles (16x16 px, 32x32 or 64x64 for large canvases); the last
+//              block to finish picks the K most populated tiles that fit in
+//              shared memory (a uint32 counter per pixel) and writes
+//              tile -> slot;
 //   main    -- one CTA per SM streams x/y (float4 loads), bins each row
 //              (binning.cuh: exact), and increments the tile's shared-memory
 //              counter when the tile is cached, the output with an L2
-//              reduction otherwise; at the end every CTA adds its non-zero
-//              cached counters into the output.
+//              reduction otherwise; at the end every CTA adds its cached
+//              tile rows into the output with TMA bulk reductions
+//              (cp.reduce.async.bulk .add.u32, one per 16-pixel row), or with
+//              per-pixel atomics when the canvas rows are not 16-byte
+//              aligned.
 //
 // Every result is exact: integer counts in any order.
 #include "dsgb_internal.cuh"
@@ -25,7 +29,8 @@ namespace dsgb {
 constexpr int SMEM_BUDGET = 220 * 1024;     // dynamic shared memory of the main kernel
 constexpr int MAX_TABLE_TILES = 8192;       // tile -> slot table entries (16 KB)
 constexpr int SAMPLE_BLOCKS = 128;
-constexpr int SAMPLE_CHUNK = 8192;
+constexpr int SAMPLE_THREADS = 1024;
+constexpr int SAMPLE_CHUNK = 8192;          // rows per sample block: two float4 of x and of y per thread
 constexpr int MIN_ROWS = 1 << 20;           // below this the single kernel is as fast
 
 struct CachedParams {
@@ -38,76 +43,105 @@ struct CachedParams {
     BinAxis ax, ay;
     BinBounds bb;
     uint32_t *out;
-    unsigned *hist;             // ntiles
+    unsigned *hist;             // ntiles, then the sample blocks' done counter
     short *slot;                // ntiles
     int *slot_tile;             // K
+    int32_t bulk_flush;         // canvas rows 16-byte aligned: flush with bulk reductions
 };
 
 __device__ __forceinline__ int tile_cells(const CachedParams &p) { return 1 << (2 * p.ts); }
 
-// ---- sample: tile histogram of evenly spaced chunks
-__global__ void __launch_bounds__(256) cached_sample(const CachedParams p, int64_t chunk) {
+// ---- select: smallest T with #(count > T) <= K; those tiles get slots.
+// Runs in the last sample block; the counts stay in registers (ntiles <=
+// MAX_TABLE_TILES = 8 per thread) and each bisection step costs one barrier.
+constexpr int SEL_PER_THREAD = MAX_TABLE_TILES / SAMPLE_THREADS;
+
+__device__ void select_tiles(const CachedParams &p) {
+    __shared__ unsigned part[2][32];
+    __shared__ unsigned s_next;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned c[SEL_PER_THREAD];
+    unsigned mx = 0;
+#pragma unroll
+    for (int k = 0; k < SEL_PER_THREAD; ++k) {
+        const int i = threadIdx.x + k * blockDim.x;
+        c[k] = i < p.ntiles ? __ldcg(&p.hist[i]) : 0u;
+        mx = max(mx, c[k]);
+    }
+    for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) part[0][warp] = mx;
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    unsigned lo = 0, hi = 0;
+    for (int w = 0; w < nw; ++w) hi = max(hi, part[0][w]);
+    // every thread runs the same bisection on the same block-wide sums
+    for (int it = 0; lo < hi && it < 40; ++it) {
+        const unsigned mid = lo + (hi - lo) / 2;
+        unsigned cnt = 0;
+#pragma unroll
+        for (int k = 0; k < SEL_PER_THREAD; ++k) cnt += c[k] > mid;
+        for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        const int b = 1 - (it & 1);          // part[0] held the maxima: start on part[1]
+        if (lane == 0) part[b][warp] = cnt;
+        __syncthreads();
+        unsigned t = 0;
+        for (int w = 0; w < nw; ++w) t += part[b][w];
+        if (t <= (unsigned)p.K) hi = mid; else lo = mid + 1;
+    }
+    const unsigned T = hi;
+    for (int i = threadIdx.x; i < p.K; i += blockDim.x) p.slot_tile[i] = -1;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SEL_PER_THREAD; ++k) {
+        const int i = threadIdx.x + k * blockDim.x;
+        if (i >= p.ntiles) continue;
+        short s = -1;
+        if (c[k] > T) {
+            const unsigned q = atomicAdd(&s_next, 1u);
+            if (q < (unsigned)p.K) { s = (short)q; p.slot_tile[q] = i; }
+        }
+        p.slot[i] = s;
+    }
+}
+
+// ---- sample: tile histogram of evenly spaced chunks (float4 loads, all
+// issued before any is used), then the last block to finish selects.
+__global__ void __launch_bounds__(SAMPLE_THREADS) cached_sample(const CachedParams p, int64_t chunk) {
     extern __shared__ unsigned sh_hist[];
+    __shared__ bool s_last;
     for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x) sh_hist[i] = 0;
     __syncthreads();
-    const int64_t start = (p.n / gridDim.x) * blockIdx.x;
+    const int64_t start = ((p.n / gridDim.x) * blockIdx.x) & ~(int64_t)3;
     const int64_t end = start + chunk < p.n ? start + chunk : p.n;
-    for (int64_t i = start + threadIdx.x; i < end; i += blockDim.x) {
-        int xi, yi;
-        const float x = p.xs[i], y = p.ys[i];
-        int r = bin_try_f32(x, y, p.bb, p.ax, p.ay, xi, yi);
-        if (r == 2) bin_exact_f32(x, y, p.ax, p.ay, xi, yi);
-        if (r) atomicAdd(&sh_hist[(yi >> p.ts) * p.tiles_x + (xi >> p.ts)], 1u);
+    const float4 *x4 = (const float4 *)p.xs;
+    const float4 *y4 = (const float4 *)p.ys;
+    const int64_t v1 = end >> 2;             // whole float4s of the chunk (a sample: the ragged end is skipped)
+    for (int64_t v = (start >> 2) + threadIdx.x; v < v1; v += 2 * (int64_t)blockDim.x) {
+        const bool two = v + blockDim.x < v1;
+        const float4 a0 = __ldg(x4 + v), b0 = __ldg(y4 + v);
+        float4 a1 = make_float4(0.f, 0.f, 0.f, 0.f), b1 = a1;
+        if (two) { a1 = __ldg(x4 + v + blockDim.x); b1 = __ldg(y4 + v + blockDim.x); }
+        const float xs[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float ys[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (k >= 4 && !two) break;
+            int xi, yi;
+            const int r = bin_try_f32(xs[k], ys[k], p.bb, p.ax, p.ay, xi, yi);
+            if (r == 2) bin_exact_f32(xs[k], ys[k], p.ax, p.ay, xi, yi);
+            if (r) atomicAdd(&sh_hist[(yi >> p.ts) * p.tiles_x + (xi >> p.ts)], 1u);
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
         if (sh_hist[i]) atomicAdd(&p.hist[i], sh_hist[i]);
-}
-
-// ---- select: smallest T with #(count > T) <= K; those tiles get slots
-__global__ void __launch_bounds__(1024) cached_select(const CachedParams p) {
-    __shared__ unsigned red[32];
-    __shared__ unsigned s_lo, s_hi, s_next;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    unsigned mx = 0;
-    for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x) mx = max(mx, p.hist[i]);
-    for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if (lane == 0) red[warp] = mx;
+    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned m = 0;
-        for (int w = 0; w < nw; ++w) m = max(m, red[w]);
-        s_lo = 0; s_hi = m; s_next = 0;
-    }
+    if (threadIdx.x == 0) s_last = atomicAdd(&p.hist[p.ntiles], 1u) == gridDim.x - 1;
     __syncthreads();
-    for (int it = 0; it < 40; ++it) {
-        const unsigned lo = s_lo, hi = s_hi;
-        if (lo >= hi) break;
-        const unsigned mid = lo + (hi - lo) / 2;
-        unsigned c = 0;
-        for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x) c += p.hist[i] > mid;
-        for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-        __syncthreads();
-        if (lane == 0) red[warp] = c;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned t = 0;
-            for (int w = 0; w < nw; ++w) t += red[w];
-            if (t <= (unsigned)p.K) s_hi = mid; else s_lo = mid + 1;
-        }
-        __syncthreads();
-    }
-    const unsigned T = s_hi;
-    for (int i = threadIdx.x; i < p.K; i += blockDim.x) p.slot_tile[i] = -1;
-    __syncthreads();
-    for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x) {
-        short s = -1;
-        if (p.hist[i] > T) {
-            const unsigned k = atomicAdd(&s_next, 1u);
-            if (k < (unsigned)p.K) { s = (short)k; p.slot_tile[k] = i; }
-        }
-        p.slot[i] = s;
-    }
+    if (!s_last) return;
+    __threadfence();
+    select_tiles(p);
 }
 
 // ---- main
@@ -167,6 +201,41 @@ __global__ void __launch_bounds__(1024, 1) cached_main(const CachedParams p) {
         if (r) cached_emit(p, tab, cache, xi, yi);
     }
     __syncthreads();
+    if (p.bulk_flush) {
+        // Each cached tile row (16 B-aligned in shared and global memory, a
+        // multiple of 16 B long) is added into the output by one bulk
+        // reduction.  Every thread orders its shared-memory atomics before
+        // the async proxy reads them.
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        const int side = 1 << p.ts;
+        bool issued = false;
+        for (int r = threadIdx.x; r < p.K * side; r += blockDim.x) {
+            const int slot = r >> p.ts, ry = r & (side - 1);
+            const int t = p.slot_tile[slot];
+            if (t < 0) continue;
+            const int yi = (t / p.tiles_x) * side + ry;
+            const int x0 = (t % p.tiles_x) * side;
+            if (yi >= p.height) continue;
+            const int ncols = p.width - x0 < side ? p.width - x0 : side;   // a multiple of 4
+            const unsigned *src = cache + ((unsigned)slot << (2 * p.ts)) + ((unsigned)ry << p.ts);
+            unsigned any = 0;
+            for (int c = 0; c < ncols; c += 4) {
+                const uint4 q = *(const uint4 *)(src + c);
+                any |= q.x | q.y | q.z | q.w;
+            }
+            if (!any) continue;
+            const unsigned saddr = (unsigned)__cvta_generic_to_shared(src);
+            asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.u32 [%0], [%1], %2;"
+                         :: "l"(p.out + (int64_t)yi * p.width + x0), "r"(saddr), "r"(ncols * 4) : "memory");
+            issued = true;
+        }
+        if (issued) {
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < cells; i += blockDim.x) {
         const unsigned c = cache[i];
         if (!c) continue;
@@ -207,7 +276,7 @@ static bool cached_layout(int64_t n, int width, int height, CachedLayout &L) {
     const int sms = sm_count();
     L.grid = sms > 0 ? sms : 148;
     size_t o = 0;
-    L.off_hist = o; o = align256(o + (size_t)L.ntiles * 4);
+    L.off_hist = o; o = align256(o + (size_t)L.ntiles * 4 + 4);     // + the done counter
     L.off_slot = o; o = align256(o + (size_t)L.ntiles * 2);
     L.off_slot_tile = o; o = align256(o + (size_t)L.K * 4);
     L.total = o;
@@ -239,12 +308,12 @@ int launch_points_cached(const ColumnRef &xc, const ColumnRef &yc, int64_t n, co
     p.hist = (unsigned *)(w + L.off_hist);
     p.slot = (short *)(w + L.off_slot);
     p.slot_tile = (int *)(w + L.off_slot_tile);
-    cudaError_t e = cudaMemsetAsync(p.hist, 0, (size_t)L.ntiles * 4, st);
+    p.bulk_flush = (cv->width % 4 == 0) && (((uintptr_t)out & 15u) == 0);
+    cudaError_t e = cudaMemsetAsync(p.hist, 0, (size_t)L.ntiles * 4 + 4, st);
     if (e == cudaSuccess && !accumulate) e = cudaMemsetAsync(out, 0, (size_t)cv->width * cv->height * 4, st);
     if (e != cudaSuccess) return cuda_status(e, "cached count memset");
     const int64_t chunk = SAMPLE_CHUNK < n / SAMPLE_BLOCKS ? SAMPLE_CHUNK : n / SAMPLE_BLOCKS;
-    cached_sample<<<SAMPLE_BLOCKS, 256, (size_t)L.ntiles * 4, st>>>(p, chunk);
-    cached_select<<<1, 1024, 0, st>>>(p);
+    cached_sample<<<SAMPLE_BLOCKS, SAMPLE_THREADS, (size_t)L.ntiles * 4, st>>>(p, chunk);
     const size_t smem = (((size_t)L.ntiles * 2 + 15) & ~(size_t)15) + (size_t)L.K * (1 << (2 * L.ts)) * 4;
     e = cudaFuncSetAttribute(cached_main, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "cached count smem attribute");
