@@ -114,8 +114,7 @@ class Output(ctypes.Structure):
 
 class PyramidConfig(ctypes.Structure):
     _fields_ = [("zmin", ctypes.c_int32), ("zmax", ctypes.c_int32), ("tile_size", ctypes.c_int32),
-                ("smem_levels", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("threads", ctypes.c_int32),
+                ("split", ctypes.c_int32), ("threads", ctypes.c_int32), ("chunk", ctypes.c_int32),
                 ("x0", ctypes.c_double), ("x1", ctypes.c_double),
                 ("y0", ctypes.c_double), ("y1", ctypes.c_double)]
 
@@ -136,9 +135,10 @@ FLAG_NO_INIT, FLAG_NO_FINALIZE, FLAG_EXACT_BIN, FLAG_WARP_AGG = 0x1, 0x2, 0x4, 0
 # every symbol include/dsgb.h declares
 EXPORTED = (
     "dsgb_abi_version", "dsgb_last_error", "dsgb_device_sm_count", "dsgb_bases_init",
-    "dsgb_finalize", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_ws", "dsgb_line_axis0", "dsgb_line_axis0_backward",
+    "dsgb_finalize", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_ws", "dsgb_points_segments",
+    "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_axis0_backward",
     "dsgb_points_backward", "dsgb_bounds", "dsgb_eq_hist_workspace_size", "dsgb_eq_hist_u32",
-    "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_pyramid_tile_offset", "dsgb_pyramid", "dsgb_pyramid_finalize",
+    "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_pyramid_tile_offset", "dsgb_pyramid_workspace_size", "dsgb_pyramid", "dsgb_pyramid_status",
 )
 
 _lock = threading.Lock()
@@ -163,6 +163,11 @@ def _declare(L):
     L.dsgb_points_workspace_size.restype = ctypes.c_size_t
     L.dsgb_points_ws.argtypes = [PC, i32, i64, i64, i32, i32, ctypes.POINTER(CanvasDesc), PB, i32, PO, i32,
                                  P, ctypes.c_size_t, u32, P]
+    L.dsgb_points_segments.argtypes = [PC, i32, i64, i32, i32, ctypes.POINTER(CanvasDesc), PB, i32, PO, i32,
+                                       P, P, i32, u32, P]
+    L.dsgb_bucket_sort_workspace_size.argtypes = [i32]
+    L.dsgb_bucket_sort_workspace_size.restype = ctypes.c_size_t
+    L.dsgb_bucket_sort.argtypes = [PC, i32, i64, i32, i32, P, i32, P, P, P, ctypes.c_size_t, P]
     L.dsgb_line_axis0.argtypes = [PC, i32, i64, i64, i32, i32, ctypes.POINTER(CanvasDesc), dbl, i32, i32, i32,
                                   PB, i32, PO, i32, u32, P]
     L.dsgb_line_axis0_backward.argtypes = [PC, i32, i64, i32, i32, i32, ctypes.POINTER(CanvasDesc), dbl, i32,
@@ -176,10 +181,13 @@ def _declare(L):
     L.dsgb_eq_hist_u32_static.argtypes = [P, i64, i32, P, P, P, P, i32, i32, i32, P]
     L.dsgb_pyramid_tile_offset.argtypes = [i32, i32, i32]
     L.dsgb_pyramid_tile_offset.restype = i64
-    L.dsgb_pyramid.argtypes = [PC, i32, i64, i32, i32, i32, ctypes.POINTER(PyramidConfig), P, P, u32, P]
-    L.dsgb_pyramid_finalize.argtypes = [P, P, i64, P]
+    L.dsgb_pyramid_workspace_size.argtypes = [i64, i32, ctypes.POINTER(PyramidConfig)]
+    L.dsgb_pyramid_workspace_size.restype = ctypes.c_size_t
+    L.dsgb_pyramid.argtypes = [PC, i32, i64, i32, i32, i32, ctypes.POINTER(PyramidConfig), P, P, P,
+                               ctypes.c_size_t, u32, P]
+    L.dsgb_pyramid_status.argtypes = [P, i64, i32, ctypes.POINTER(PyramidConfig), P, P]
     non_int = ("dsgb_last_error", "dsgb_eq_hist_workspace_size", "dsgb_pyramid_tile_offset",
-               "dsgb_points_workspace_size")
+               "dsgb_points_workspace_size", "dsgb_pyramid_workspace_size", "dsgb_bucket_sort_workspace_size")
     for nm in EXPORTED:
         if nm not in non_int:
             getattr(L, nm).restype = ctypes.c_int

@@ -173,6 +173,32 @@ int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t ro
                    const dsgb_output *outs, int32_t nouts,
                    void *workspace, size_t workspace_bytes, uint32_t flags, void *stream);
 
+/* Canvas.points over the rows in segments [seg_begin[i], seg_end[i]) of the
+ * columns (host arrays, nseg <= 256): the same reductions and flags as
+ * dsgb_points (row index = position in the columns; row_offset 0).  The
+ * serving path uses it on a bucketed store (dsgb_bucket_sort) so that a
+ * viewport reads only the bucket rows it overlaps.  No reference
+ * counterpart (the reference scans every row, glyphs/points.py:210-242). */
+int dsgb_points_segments(const dsgb_column *cols, int32_t ncols, int64_t n,
+                         int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                         const dsgb_base *bases, int32_t nbases,
+                         const dsgb_output *outs, int32_t nouts,
+                         const int64_t *seg_begin, const int64_t *seg_end, int32_t nseg,
+                         uint32_t flags, void *stream);
+
+/* Regroup every column by a grid x grid bucketing of the domain square
+ * (domain = {x0, x1, y0, y1}, host; grid <= 128): bucket (bx, by) is
+ * number by * grid + bx, and bucket grid*grid holds the points outside the
+ * domain or with NaN coordinates.  out_data: one device pointer per column
+ * (same dtype, n rows); bucket_start (device, grid*grid + 2 int64): row
+ * offset of each bucket.  Bucket ids are float64 estimates: a viewport
+ * reading buckets must widen its bucket range by one on each side.  No
+ * reference counterpart. */
+size_t dsgb_bucket_sort_workspace_size(int32_t grid);
+int dsgb_bucket_sort(const dsgb_column *cols, int32_t ncols, int64_t n, int32_t x_col, int32_t y_col,
+                     const double *domain, int32_t grid, void *const *out_data, int64_t *bucket_start,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- Canvas.line, LineAxis0 glyph ----------------------------------------
  * Replaces line.py:59-103 + 1033-1149.  line_width == 0 draws Bresenham
  * lines, > 0 antialiased lines; overwrite / use_2_stage_agg follow
@@ -244,25 +270,38 @@ int dsgb_eq_hist_u32_static(const uint32_t *data, int64_t n, int32_t nbins,
                             int32_t rescale_discrete_levels, void *stream);
 
 /* ---- batched tile pyramid --------------------------------------------------
- * Every tile (z, tx, ty) for z in [zmin, zmax] of the [x0,x1)x[y0,y1) square
- * is a tile_size x tile_size Canvas.points aggregate with inclusive bounds
- * (points on a shared edge count in both tiles).  Tiles are stored level by
- * level, row-major by (ty, tx), each [tile_size][tile_size].  Computes count
- * (uint32) and, when v_col >= 0, max(v) as an int64 key array (decode with
- * DSGB_FIN_KEY_F64 semantics, done by dsgb_pyramid_finalize).
- * `config` selects the shared-memory privatisation (autotuned by the caller):
- * smem_levels = number of coarse levels privatised per block. */
+ * Every tile (z, tx, ty), zmin <= z <= zmax, of the square [x0,x1]x[y0,y1]
+ * in one pass: tile (z, tx, ty) equals
+ *   Canvas(ts, ts, x_range=(lo(tx), lo(tx+1)), y_range=(lo(ty), lo(ty+1)))
+ *       .points(df, 'x', 'y', count() / max('v'))
+ * with lo(t) = x0 + (x1 - x0) * (t / 2^z) in float64, i.e. one reference
+ * call per tile (glyphs/points.py:182-242 with core.py:62-81); points on a
+ * shared edge count in both tiles.  Tiles are stored level by level
+ * (dsgb_pyramid_tile_offset), row-major by (ty, tx), each [ts][ts] with
+ * row 0 at the tile's lower y.  counts: uint32; max_out (when v_col >= 0):
+ * float64, NaN where empty, max of +-0 reported as +0.  x, y, v float32;
+ * zmax <= 6.  The knobs (autotuned by the caller): split (the
+ * shared-memory footprint of the finest level is ts >> (1 + split) pixels
+ * on a side), threads (render CTA size: 256, 512 or 1024) and chunk (points
+ * per work item).  No reference counterpart: the reference renders tiles
+ * one Canvas call at a time (tiles.py:70-130). */
 typedef struct {
-    int32_t zmin, zmax, tile_size, smem_levels;
-    int32_t blocks_per_sm, threads;
+    int32_t zmin, zmax, tile_size, split;
+    int32_t threads, chunk;
     double x0, x1, y0, y1;
 } dsgb_pyramid_config;
 int64_t dsgb_pyramid_tile_offset(int32_t zmin, int32_t z, int32_t tile_size);
+size_t dsgb_pyramid_workspace_size(int64_t n, int32_t has_v, const dsgb_pyramid_config *config);
 int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n,
                  int32_t x_col, int32_t y_col, int32_t v_col,
                  const dsgb_pyramid_config *config,
-                 uint32_t *counts, int64_t *max_keys, uint32_t flags, void *stream);
-int dsgb_pyramid_finalize(const int64_t *max_keys, double *max_out, int64_t ncells, void *stream);
+                 uint32_t *counts, double *max_out,
+                 void *workspace, size_t workspace_bytes, uint32_t flags, void *stream);
+/* Status bits of the last dsgb_pyramid on this workspace (synchronises the
+ * stream): 1 = edge-contribution queue overflowed, 2 = a max update gave up,
+ * 4 = partial slots exhausted.  Non-zero means the pyramid is incomplete. */
+int dsgb_pyramid_status(const void *workspace, int64_t n, int32_t has_v,
+                        const dsgb_pyramid_config *config, uint32_t *flags_out, void *stream);
 
 #ifdef __cplusplus
 }
