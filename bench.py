@@ -218,6 +218,115 @@ def _events_time(fn, k, stream):
     return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
 
+def bench_pyramid(args, dev, peak, peak_kind):
+    """The tile-pyramid workload: 2e8 float32 points in [0,1)^2 (half uniform,
+    half 20 Gaussians), v float32 ~ N(0,1), zoom 0-6 of 256x256 tiles (5,461
+    tiles), count and max(v), one graph replay per pyramid; against one plain
+    Canvas.points call per tile (timed on a sample of tiles, scaled to 5,461)."""
+    import torch
+    import datashader_gb300 as ds
+    from datashader_gb300 import pyramid as P
+    from datashader_gb300 import synthetic
+    n = args.pyramid_n
+    stream = torch.cuda.current_stream(dev)
+    x, y = synthetic.pyramid_points_torch(n, seed=0, device=dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    v = torch.randn(n, generator=g, device=dev, dtype=torch.float32)
+    pyr = P.TilePyramid(x, y, v, zmin=0, zmax=6, tile_size=256)
+    best, results = P.autotune(pyr, repeats=2)
+    pyr.render()
+    torch.cuda.synchronize()
+    status = pyr.status()
+    times = _events_time(pyr.render, max(3, args.steps // 2), stream)
+    ms = sum(times) / len(times)
+    frame = ds.TensorFrame({"x": x, "y": y, "v": v})
+    agg = ds.summary(count=ds.count(), max=ds.max("v"))
+    rng = np.random.default_rng(0)
+    tiles = [(z, int(rng.integers(0, 1 << z)), int(rng.integers(0, 1 << z))) for z in range(7) for _ in range(2)]
+
+    def plain(z, tx, ty):
+        xr, yr = pyr.tile_ranges(z, tx, ty)
+        return ds.Canvas(plot_width=256, plot_height=256, x_range=xr, y_range=yr).points(frame, "x", "y", agg)
+
+    plain(*tiles[0])
+    per_tile = _events_time(lambda: [plain(*t) for t in tiles], 1, stream)[0] / len(tiles)
+    same = True
+    for t in tiles:
+        r = plain(*t)
+        c, m = pyr.tile(*t)
+        same &= bool(torch.equal(r["count"].data.view(torch.int32), c.view(torch.int32)))
+        same &= bool(torch.equal(torch.nan_to_num(r["max"].data, nan=-1e300), torch.nan_to_num(m, nan=-1e300)))
+    ntiles = sum(4 ** z for z in range(7))
+    out_bytes = pyr.counts.numel() * 4 + pyr.max.numel() * 8
+    alg = n * 12 + out_bytes
+    achieved = alg / (ms / 1e3) / 1e9
+    res = {"workload": f"tile pyramid zoom 0-6, 256x256 tiles ({ntiles}), {n:,} float32 points, count + max(v)",
+           "ms_per_pyramid": ms, "gpoints_per_s": n / (ms / 1e3) / 1e9, "status_flags": status,
+           "autotuned": best, "candidates": [[round(t, 4), c] for t, c in results],
+           "plain_ms_per_tile": per_tile, "plain_ms_per_pyramid_est": per_tile * ntiles,
+           "speedup_vs_plain": per_tile * ntiles / ms, "sample_tiles_identical": same,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_kind": peak_kind,
+                        "algorithmic_bytes": alg, "note": "12 B/point read + count/max tiles written once"},
+           "gpu_launches_per_pyramid": 6}
+    del pyr, x, y, v, frame
+    torch.cuda.empty_cache()
+    return res
+
+
+def bench_serving(args, dev):
+    """The viewport workload: 5e8 points resident (float32 x/y of the pyramid
+    distribution, float32 v ~ N(0,1), uint8 cat over 16), Poisson arrivals at
+    200 / 1,000 / 5,000 req/s, zoom log-uniform 1x-1000x, random pan, canvas
+    from {256^2, 512^2, 1024^2, 1920x1080, 4096x2160}, reduction from {count,
+    mean(v), max(v), by(cat, count)}; continuous batching vs the same segment
+    kernels one request at a time vs a plain whole-frame Canvas.points call
+    per request, one at a time."""
+    import torch
+    import datashader_gb300 as ds
+    from datashader_gb300 import serving as S
+    from datashader_gb300 import synthetic
+    n = args.serving_n
+    x, y = synthetic.pyramid_points_torch(n, seed=3, device=dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4)
+    v = torch.randn(n, generator=g, device=dev, dtype=torch.float32)
+    cat = torch.randint(0, 16, (n,), generator=g, device=dev, dtype=torch.uint8)
+    frame = ds.TensorFrame({"x": x, "y": y, "v": v, "cat": cat}, categories={"cat": list(range(16))})
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    store = S.BucketedStore(frame, grid=128, domain=(0.0, 1.0, 0.0, 1.0))
+    torch.cuda.synchronize()
+    sort_s = time.perf_counter() - t0
+    del frame, x, y, v, cat
+    torch.cuda.empty_cache()
+    ex = S.SegmentExecutor(store)
+    server = S.ViewportServer(ex, slots=args.serving_slots, mem_budget=args.serving_mem_gb << 30)
+    warm = S.generate_requests(40, rate=1e6, seed=99)
+    server.run(warm)
+    server.run([S.Request(r.rid, 0.0, r.x_range, r.y_range, r.width, r.height, r.kind) for r in warm[:8]],
+               mode="plain")
+    torch.cuda.synchronize()
+    out = {"workload": f"{n:,} resident points (13 B/point), {args.serving_requests} requests per rate",
+           "store_sort_ms": sort_s * 1e3, "slots": args.serving_slots, "mem_budget_gb": args.serving_mem_gb,
+           "rates": {}}
+    for rate in (200, 1000, 5000):
+        per = {}
+        for mode in ("batched", "sequential", "plain"):
+            reqs = S.generate_requests(args.serving_requests, rate=rate, seed=rate)
+            server.peak_inflight = 0
+            server.run(reqs, mode=mode)
+            torch.cuda.synchronize()
+            st = S.summarize(reqs)
+            st["peak_inflight"] = server.peak_inflight
+            per[mode] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in st.items()}
+        out["rates"][str(rate)] = per
+    del store, ex, server
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args):
     import torch
     world, rank, local = _dist_init(args)
@@ -350,6 +459,14 @@ def run_gpu(args):
            "h2d_bytes_per_step": int(xh.numel() * 4 + yh.numel() * 4),
            "d2h_bytes_per_step": 1024 * 1024 * 4}
 
+    del x, y, v, cat, frame, xh, yh, xd, yd
+    torch.cuda.empty_cache()
+    extras = {}
+    if world == 1 and args.pyramid_n > 0:
+        extras["pyramid"] = bench_pyramid(args, dev, peak, peak_kind)
+    if world == 1 and args.serving_n > 0 and args.serving_requests > 0:
+        extras["serving"] = bench_serving(args, dev)
+
     if rank == 0:
         base = None
         if world == 1 and not args.no_cpu_baseline:
@@ -377,6 +494,7 @@ def run_gpu(args):
             "gpu_launches": args.steps * kernels_per_count,
             "clocks": clk.summary(),
         }
+        line.update(extras)
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
@@ -394,6 +512,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=20_000_000)
     ap.add_argument("--reference-sample", type=int, default=100_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pyramid-n", type=int, default=200_000_000, help="0 skips the tile-pyramid workload")
+    ap.add_argument("--serving-n", type=int, default=500_000_000, help="0 skips the viewport workload")
+    ap.add_argument("--serving-requests", type=int, default=1000)
+    ap.add_argument("--serving-slots", type=int, default=8)
+    ap.add_argument("--serving-mem-gb", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

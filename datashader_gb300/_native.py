@@ -130,12 +130,13 @@ BASEF_UNWEIGHTED = 0x1
 # finalize ops (dsgb_fin_op)
 FIN_SUM_NAN, FIN_MEAN, FIN_KEY_F64, FIN_ROW, FIN_GATHER, FIN_KEY_F32, FIN_SUM_F32, FIN_COPY = range(1, 9)
 
-FLAG_NO_INIT, FLAG_NO_FINALIZE, FLAG_EXACT_BIN, FLAG_WARP_AGG = 0x1, 0x2, 0x4, 0x8
+FLAG_NO_INIT, FLAG_NO_FINALIZE, FLAG_EXACT_BIN, FLAG_WARP_AGG, FLAG_DETERMINISTIC = 0x1, 0x2, 0x4, 0x8, 0x10
 
 # every symbol include/dsgb.h declares
 EXPORTED = (
     "dsgb_abi_version", "dsgb_last_error", "dsgb_device_sm_count", "dsgb_bases_init",
-    "dsgb_finalize", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_ws", "dsgb_points_segments",
+    "dsgb_finalize", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_workspace_size_flags",
+    "dsgb_points_ws", "dsgb_points_segments",
     "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_axis0_backward",
     "dsgb_points_backward", "dsgb_bounds", "dsgb_eq_hist_workspace_size", "dsgb_eq_hist_u32",
     "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_pyramid_tile_offset", "dsgb_pyramid_workspace_size", "dsgb_pyramid", "dsgb_pyramid_status",
@@ -161,6 +162,8 @@ def _declare(L):
     L.dsgb_points.argtypes = [PC, i32, i64, i64, i32, i32, ctypes.POINTER(CanvasDesc), PB, i32, PO, i32, u32, P]
     L.dsgb_points_workspace_size.argtypes = [i64, ctypes.POINTER(CanvasDesc), PB, i32]
     L.dsgb_points_workspace_size.restype = ctypes.c_size_t
+    L.dsgb_points_workspace_size_flags.argtypes = [i64, ctypes.POINTER(CanvasDesc), PB, i32, u32]
+    L.dsgb_points_workspace_size_flags.restype = ctypes.c_size_t
     L.dsgb_points_ws.argtypes = [PC, i32, i64, i64, i32, i32, ctypes.POINTER(CanvasDesc), PB, i32, PO, i32,
                                  P, ctypes.c_size_t, u32, P]
     L.dsgb_points_segments.argtypes = [PC, i32, i64, i32, i32, ctypes.POINTER(CanvasDesc), PB, i32, PO, i32,
@@ -187,7 +190,8 @@ def _declare(L):
                                ctypes.c_size_t, u32, P]
     L.dsgb_pyramid_status.argtypes = [P, i64, i32, ctypes.POINTER(PyramidConfig), P, P]
     non_int = ("dsgb_last_error", "dsgb_eq_hist_workspace_size", "dsgb_pyramid_tile_offset",
-               "dsgb_points_workspace_size", "dsgb_pyramid_workspace_size", "dsgb_bucket_sort_workspace_size")
+               "dsgb_points_workspace_size", "dsgb_pyramid_workspace_size", "dsgb_bucket_sort_workspace_size",
+               "dsgb_points_workspace_size_flags")
     for nm in EXPORTED:
         if nm not in non_int:
             getattr(L, nm).restype = ctypes.c_int

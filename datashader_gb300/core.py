@@ -255,12 +255,18 @@ class Canvas:
         self.x_axis = _axis_lookup[x_axis_type]
         self.y_axis = _axis_lookup[y_axis_type]
 
-    def points(self, source, x=None, y=None, agg=None, geometry=None):
-        """Compute a reduction by pixel, mapping data to pixels as points (core.py:187-232)."""
+    def points(self, source, x=None, y=None, agg=None, geometry=None, *, deterministic=False):
+        """Compute a reduction by pixel, mapping data to pixels as points (core.py:187-232).
+
+        ``deterministic=True`` (an addition to the reference's signature) adds
+        the float64 sums of sum / mean in row order, bit-identical to the
+        reference's CPU loop and from run to run; the other reductions are
+        order-independent already."""
         _validate_xy("Point", x, y, geometry)
         if agg is None:
             agg = rd.count()
-        return bypixel(source, self, Point(x, y), agg)
+        return bypixel(source, self, Point(x, y), agg,
+                       flags=N.FLAG_DETERMINISTIC if deterministic else 0)
 
     def line(self, source, x=None, y=None, agg=None, axis=0, geometry=None,
              line_width=0, antialias=False):
@@ -303,13 +309,13 @@ class Canvas:
         self.validate_size(self.plot_width, self.plot_height)
 
 
-def bypixel(source, canvas, glyph, agg, *, antialias=False):
+def bypixel(source, canvas, glyph, agg, *, antialias=False, flags=0):
     """core.py:1334-1359: validate, then run the GPU pipeline."""
     frame = as_frame(source)
     glyph.validate(frame)
     agg.validate(frame)
     canvas.validate()
-    return gpu_pipeline(frame, canvas, glyph, agg, antialias=antialias)
+    return gpu_pipeline(frame, canvas, glyph, agg, antialias=antialias, flags=flags)
 
 
 def _column_bounds(frame, name, stream):
@@ -432,7 +438,8 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
                                ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
         N.check(rc, "dsgb_line_axis0")
     else:
-        wsz = int(L.dsgb_points_workspace_size(len(frame), ctypes.byref(cv), ex.bases, len(plan.bases)))
+        wsz = int(L.dsgb_points_workspace_size_flags(len(frame), ctypes.byref(cv), ex.bases, len(plan.bases),
+                                                     flags))
         ws = workspace(frame.device, stream, wsz) if wsz else None
         rc = L.dsgb_points_ws(ex.cols, len(ex.names), len(frame), frame.row_offset, 0, 1, ctypes.byref(cv),
                               ex.bases, len(plan.bases), ex.outs, ex.nouts,

@@ -23,6 +23,16 @@ int sm_count();
 
 static inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Blocks of 256 threads for a grid-stride loop over n items (at most 16 per SM).
+static inline unsigned grid_of(int64_t n) {
+    int sms = sm_count();
+    if (sms <= 0) sms = 148;
+    int64_t g = (n + 255) / 256;
+    if (g > (int64_t)sms * 16) g = (int64_t)sms * 16;
+    if (g < 1) g = 1;
+    return (unsigned)g;
+}
+
 static inline int dtype_size(int32_t dt) {
     switch (dt) {
     case DSGB_F32: case DSGB_I32: case DSGB_U32: return 4;

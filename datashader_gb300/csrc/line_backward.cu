@@ -300,14 +300,6 @@ __global__ void __launch_bounds__(256) points_backward_kernel(const PBwdParams p
     }
 }
 
-static unsigned grid_of(int64_t n) {
-    int sms = sm_count();
-    if (sms <= 0) sms = 148;
-    int64_t g = (n + 255) / 256;
-    if (g > (int64_t)sms * 16) g = (int64_t)sms * 16;
-    if (g < 1) g = 1;
-    return (unsigned)g;
-}
 
 }  // namespace dsgb
 

@@ -6,106 +6,10 @@
 //
 // Binning is exact (binning.cuh): a float32 fast path proven against the
 // float64 formula of points.py:199-203, with a float64 fallback.
-#include "dsgb_internal.cuh"
-#include "binning.cuh"
+#include "points_params.cuh"
 
 namespace dsgb {
 
-
-struct PointsParams {
-    ColumnRef cols[MAX_COLS];
-    BaseDev bases[MAX_BASES];
-    int32_t ncols, nbases;
-    int64_t n, row_offset;
-    int32_t x_col, y_col;
-    int32_t width, height;
-    int32_t x_log, y_log;
-    double sx, tx, sy, ty;
-    double xmin, xmax, ymin, ymax;
-    BinAxis ax, ay;                    // float32 fast path (binning.cuh)
-    BinBounds bb;
-};
-
-// ------------------------------------------------------------------ binning
-
-__device__ __forceinline__ bool bin_f32_fast(const PointsParams &p, float x, float y, int &xi, int &yi) {
-    return bin_point_f32(x, y, p.bb, p.ax, p.ay, xi, yi);
-}
-
-__device__ __forceinline__ bool bin_f64_fast(const PointsParams &p, double x, double y, int &xi, int &yi) {
-    return bin_point_f64(x, y, p.bb, p.ax, p.ay, xi, yi);
-}
-
-__device__ __forceinline__ bool bin_exact_xy(const PointsParams &p, double x, double y, int &xi, int &yi) {
-    if (!((p.xmin <= x && x <= p.xmax) && (p.ymin <= y && y <= p.ymax))) return false;
-    double mx = p.x_log ? log10(x) : x;   // LogAxis.mapper (core.py:131-134)
-    double my = p.y_log ? log10(y) : y;
-    xi = bin_exact64(mx, p.ax);
-    yi = bin_exact64(my, p.ay);
-    return true;
-}
-
-// ---------------------------------------------------------------- appends
-
-// The GPU form of the fused append: one pass over the bases for row i.
-__device__ __forceinline__ void accumulate(const PointsParams &p, int64_t i, int64_t pix) {
-    const long long row = (long long)(i + p.row_offset);
-#pragma unroll 1
-    for (int b = 0; b < p.nbases; ++b) {
-        const BaseDev &B = p.bases[b];
-        int64_t cell = pix;
-        if (B.cat_col >= 0) {
-            // compiler.py:379-390 -- agg[:, :, int(code)], negative codes wrap
-            long long c = load_i64(p.cols[B.cat_col], i);
-            if (c < 0) c += B.ncat;
-            if (c < 0 || c >= B.ncat) continue;
-            cell = pix * B.ncat + c;
-        }
-        double field = 0.0;
-        bool has = true;
-        if (B.col >= 0) {
-            field = load_f64(p.cols[B.col], i);
-            has = !isnull(field);
-        }
-        if (!has) continue;
-        switch (B.op) {
-        case DSGB_BASE_COUNT: atomicAdd((unsigned *)B.agg + cell, 1u); break;
-        case DSGB_BASE_ANY: ((volatile uint8_t *)B.agg)[cell] = 1; break;
-        case DSGB_BASE_SUM: atomicAdd((double *)B.agg + cell, field); break;
-        case DSGB_BASE_MAX: atomic_max_key((long long *)B.agg + cell, f64_key(field)); break;
-        case DSGB_BASE_MIN: atomic_min_key((long long *)B.agg + cell, f64_key(field)); break;
-        case DSGB_BASE_MIN_ROW: atomic_min_key((long long *)B.agg + cell, row); break;
-        case DSGB_BASE_MAX_ROW: atomic_max_key((long long *)B.agg + cell, row); break;
-        case DSGB_BASE_ARGMAX: pair_update<true>((long long *)B.agg + 2 * cell, f64_key(field), row); break;
-        case DSGB_BASE_ARGMIN: pair_update<false>((long long *)B.agg + 2 * cell, f64_key(field), row); break;
-        default: break;
-        }
-    }
-}
-
-enum Mode { MODE_GENERIC = 0, MODE_COUNT = 1, MODE_MEAN = 2 };
-
-// Per-row work of one kernel instantiation.  MEAN: bases[0] = SUM(v), bases[1] = COUNT(v).
-template <int MODE>
-__device__ __forceinline__ void emit(const PointsParams &p, int64_t i, int xi, int yi, double v) {
-    int64_t pix = (int64_t)yi * p.width + xi;
-    if (MODE == MODE_COUNT) {
-        atomicAdd((unsigned *)p.bases[0].agg + pix, 1u);
-    } else if (MODE == MODE_MEAN) {
-        if (!isnull(v)) {
-            atomicAdd((double *)p.bases[0].agg + pix, v);
-            atomicAdd((unsigned *)p.bases[1].agg + pix, 1u);
-        }
-    } else {
-        accumulate(p, i, pix);
-    }
-}
-
-template <int MODE>
-__device__ __forceinline__ double mean_value(const PointsParams &p, int64_t i) {
-    if (MODE != MODE_MEAN) return 0.0;
-    return load_f64(p.cols[p.bases[0].col], i);
-}
 
 // float32 coordinates, 4 rows per thread per iteration (float4 streaming loads).
 template <int MODE, bool FAST, bool WARPAGG>
@@ -204,6 +108,32 @@ __global__ void __launch_bounds__(256) points_any_kernel(const PointsParams p) {
         int xi, yi;
         double x = load_f64(p.cols[p.x_col], i), y = load_f64(p.cols[p.y_col], i);
         if (bin_exact_xy(p, x, y, xi, yi)) emit<MODE>(p, i, xi, yi, mean_value<MODE>(p, i));
+    }
+}
+
+// Rows given as segments [begin, end) of the columns (a viewport over a
+// spatially sorted store): blockIdx.y is the segment, blockIdx.x strides it.
+constexpr int MAX_SEGMENTS = 256;
+struct SegList {
+    int64_t begin[MAX_SEGMENTS];
+    int64_t end[MAX_SEGMENTS];
+};
+
+template <int MODE, bool F32, bool FAST>
+__global__ void __launch_bounds__(256) points_seg_kernel(const PointsParams p, const SegList s) {
+    const int64_t b = s.begin[blockIdx.y], e = s.end[blockIdx.y];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = b + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < e; i += stride) {
+        int xi, yi;
+        bool in;
+        if (F32) {
+            const float x = ((const float *)p.cols[p.x_col].data)[i];
+            const float y = ((const float *)p.cols[p.y_col].data)[i];
+            in = FAST ? bin_f32_fast(p, x, y, xi, yi) : bin_exact_xy(p, (double)x, (double)y, xi, yi);
+        } else {
+            in = bin_exact_xy(p, load_f64(p.cols[p.x_col], i), load_f64(p.cols[p.y_col], i), xi, yi);
+        }
+        if (in) emit<MODE>(p, i, xi, yi, mean_value<MODE>(p, i));
     }
 }
 
@@ -308,6 +238,39 @@ int launch_points(const PointsParams &p, uint32_t flags, cudaStream_t st) {
     return DSGB_OK;
 }
 
+static int launch_points_segments(const PointsParams &p, const SegList &s, int nseg, int64_t maxlen,
+                                  uint32_t flags, cudaStream_t st) {
+    if (nseg == 0 || maxlen == 0 || p.nbases == 0) return DSGB_OK;
+    int mode = MODE_GENERIC;
+    if (p.nbases == 1 && p.bases[0].op == DSGB_BASE_COUNT && p.bases[0].col < 0 && p.bases[0].cat_col < 0)
+        mode = MODE_COUNT;
+    else if (p.nbases == 2 && p.bases[0].op == DSGB_BASE_SUM && p.bases[1].op == DSGB_BASE_COUNT &&
+             p.bases[0].col >= 0 && p.bases[0].col == p.bases[1].col &&
+             p.bases[0].cat_col < 0 && p.bases[1].cat_col < 0)
+        mode = MODE_MEAN;
+    const bool f32 = p.cols[p.x_col].dtype == DSGB_F32 && p.cols[p.y_col].dtype == DSGB_F32;
+    const bool fast = f32 && !(flags & DSGB_FLAG_EXACT_BIN) && !p.x_log && !p.y_log && fast_path_ok(p.ax, p.ay);
+    int sms = sm_count();
+    if (sms <= 0) sms = 148;
+    int64_t gx = (maxlen + 255) / 256;
+    const int64_t cap = ((int64_t)sms * 8 + nseg - 1) / nseg;
+    if (gx > cap) gx = cap;
+    if (gx < 1) gx = 1;
+    const dim3 grid((unsigned)gx, (unsigned)nseg);
+#define DSGB_LSEG(M)                                                                        \
+    do {                                                                                    \
+        if (fast) points_seg_kernel<M, true, true><<<grid, 256, 0, st>>>(p, s);            \
+        else if (f32) points_seg_kernel<M, true, false><<<grid, 256, 0, st>>>(p, s);       \
+        else points_seg_kernel<M, false, false><<<grid, 256, 0, st>>>(p, s);               \
+    } while (0)
+    if (mode == MODE_COUNT) DSGB_LSEG(MODE_COUNT);
+    else if (mode == MODE_MEAN) DSGB_LSEG(MODE_MEAN);
+    else DSGB_LSEG(MODE_GENERIC);
+#undef DSGB_LSEG
+    DSGB_CHECK_LAUNCH("points segments kernel launch");
+    return DSGB_OK;
+}
+
 int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st);
 size_t cached_workspace_size(int64_t n, int width, int height);
 int launch_points_cached(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
@@ -320,6 +283,15 @@ static bool cached_eligible(const PointsParams &p, uint32_t flags) {
     return p.nbases == 1 && p.bases[0].op == DSGB_BASE_COUNT && p.bases[0].col < 0 &&
            p.bases[0].cat_col < 0 && !(flags & (DSGB_FLAG_EXACT_BIN | DSGB_FLAG_WARP_AGG)) &&
            !p.x_log && !p.y_log && fast_path_ok(p.ax, p.ay);
+}
+
+size_t det_workspace_size(int64_t n);
+int det_sums(const PointsParams &p, bool fast, void *ws, size_t ws_bytes, cudaStream_t st);
+
+static bool has_sum_base(const PointsParams &p) {
+    for (int b = 0; b < p.nbases; ++b)
+        if (p.bases[b].op == DSGB_BASE_SUM) return true;
+    return false;
 }
 
 int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
@@ -340,6 +312,29 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
     if (rc) return rc;
     cudaStream_t st = as_stream(stream);
     const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    if ((flags & DSGB_FLAG_DETERMINISTIC) && has_sum_base(p)) {
+        // float64 sums in row order (points_det.cu); the other bases as usual
+        if (!(flags & DSGB_FLAG_NO_INIT)) {
+            rc = bases_init(bases, nbases, ncells, st);
+            if (rc) return rc;
+        }
+        const bool fast = !(flags & DSGB_FLAG_EXACT_BIN) && !p.x_log && !p.y_log && fast_path_ok(p.ax, p.ay);
+        PointsParams rest = p;
+        bool any_rest = false;
+        for (int b = 0; b < rest.nbases; ++b) {
+            if (rest.bases[b].op == DSGB_BASE_SUM) rest.bases[b].op = 0;     // skipped by the append
+            else any_rest = true;
+        }
+        if (any_rest) {
+            rc = launch_points(rest, flags & ~DSGB_FLAG_WARP_AGG, st);
+            if (rc) return rc;
+        }
+        rc = det_sums(p, fast, workspace, ws_bytes, st);
+        if (rc) return rc;
+        if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+        return rc;
+    }
     if (workspace && cached_eligible(p, flags)) {
         rc = launch_points_cached(p.cols[x_col], p.cols[y_col], n, canvas, p.ax, p.ay, p.bb,
                                   (uint32_t *)p.bases[0].agg, (flags & DSGB_FLAG_NO_INIT) != 0,
@@ -374,6 +369,21 @@ extern "C" size_t dsgb_points_workspace_size(int64_t n, const dsgb_canvas *canva
     return cached_workspace_size(n, canvas->width, canvas->height);
 }
 
+extern "C" size_t dsgb_points_workspace_size_flags(int64_t n, const dsgb_canvas *canvas, const dsgb_base *bases,
+                                                   int32_t nbases, uint32_t flags) {
+    if (!canvas || n < 0 || nbases < 0 || (nbases > 0 && !bases)) return 0;
+    size_t need = dsgb_points_workspace_size(n, canvas, bases, nbases);
+    if (flags & DSGB_FLAG_DETERMINISTIC) {
+        for (int b = 0; b < nbases; ++b)
+            if (bases[b].op == DSGB_BASE_SUM) {
+                const size_t d = det_workspace_size(n);
+                if (d > need) need = d;
+                break;
+            }
+    }
+    return need;
+}
+
 extern "C" int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
                               int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
                               const dsgb_base *bases, int32_t nbases,
@@ -381,4 +391,45 @@ extern "C" int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n,
                               void *workspace, size_t workspace_bytes, uint32_t flags, void *stream) {
     return points_impl(cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases, outs, nouts,
                        workspace, workspace_bytes, flags, stream);
+}
+
+extern "C" int dsgb_points_segments(const dsgb_column *cols, int32_t ncols, int64_t n, int32_t x_col,
+                                    int32_t y_col, const dsgb_canvas *canvas, const dsgb_base *bases,
+                                    int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                                    const int64_t *seg_begin, const int64_t *seg_end, int32_t nseg,
+                                    uint32_t flags, void *stream) {
+    if (nseg < 0 || nseg > MAX_SEGMENTS || (nseg > 0 && (!seg_begin || !seg_end))) {
+        set_error("dsgb_points_segments: nseg=%d outside 0..%d or null segment arrays", nseg, MAX_SEGMENTS);
+        return DSGB_E_INVALID;
+    }
+    PointsParams p;
+    int rc = build_params(p, cols, ncols, n, 0, x_col, y_col, canvas, bases, nbases);
+    if (rc) return rc;
+    SegList s;
+    memset(&s, 0, sizeof(s));
+    int64_t maxlen = 0;
+    int k = 0;
+    for (int i = 0; i < nseg; ++i) {
+        if (seg_begin[i] < 0 || seg_end[i] < seg_begin[i] || seg_end[i] > n) {
+            set_error("dsgb_points_segments: segment %d [%lld, %lld) outside [0, %lld)", i,
+                      (long long)seg_begin[i], (long long)seg_end[i], (long long)n);
+            return DSGB_E_INVALID;
+        }
+        if (seg_end[i] == seg_begin[i]) continue;
+        s.begin[k] = seg_begin[i];
+        s.end[k] = seg_end[i];
+        if (seg_end[i] - seg_begin[i] > maxlen) maxlen = seg_end[i] - seg_begin[i];
+        ++k;
+    }
+    cudaStream_t st = as_stream(stream);
+    const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    if (!(flags & DSGB_FLAG_NO_INIT)) {
+        rc = bases_init(bases, nbases, ncells, st);
+        if (rc) return rc;
+    }
+    rc = launch_points_segments(p, s, k, maxlen, flags, st);
+    if (rc) return rc;
+    if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+        rc = finalize_outputs(cols, ncols, 0, bases, nbases, outs, nouts, ncells, st);
+    return rc;
 }

@@ -132,6 +132,9 @@ typedef struct {
 #define DSGB_FLAG_NO_FINALIZE  0x2u  /* skip the finalize step */
 #define DSGB_FLAG_EXACT_BIN    0x4u  /* always bin in float64 (disable the float32 fast path) */
 #define DSGB_FLAG_WARP_AGG     0x8u  /* warp-level pre-aggregation of identical pixels */
+#define DSGB_FLAG_DETERMINISTIC 0x10u /* float64 sums in row order (bit-identical to the
+                                         reference's CPU loop and run to run); needs the
+                                         workspace of dsgb_points_workspace_size_flags */
 
 /* ---- informational ---------------------------------------------------- */
 int dsgb_abi_version(void);
@@ -167,6 +170,10 @@ int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_o
  * must be 256-byte aligned and not used by another call in flight. */
 size_t dsgb_points_workspace_size(int64_t n, const dsgb_canvas *canvas,
                                   const dsgb_base *bases, int32_t nbases);
+/* Workspace for dsgb_points_ws under `flags` (the deterministic mode needs
+ * about 16 bytes per row). */
+size_t dsgb_points_workspace_size_flags(int64_t n, const dsgb_canvas *canvas,
+                                        const dsgb_base *bases, int32_t nbases, uint32_t flags);
 int dsgb_points_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
                    int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
                    const dsgb_base *bases, int32_t nbases,
