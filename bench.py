@@ -269,7 +269,7 @@ def bench_pyramid(args, dev, peak, peak_kind):
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "peak_kind": peak_kind,
                         "algorithmic_bytes": alg, "note": "12 B/point read + count/max tiles written once"},
-           "gpu_launches_per_pyramid": 6}
+           "gpu_launches_per_pyramid": 8}
     del pyr, x, y, v, frame
     torch.cuda.empty_cache()
     return res

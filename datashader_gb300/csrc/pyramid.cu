@@ -20,8 +20,11 @@
 //                  bucket is a work unit, not a result);
 //   pyr_plan    -- one block: bucket offsets, work items (bucket, chunk,
 //                  sub-bucket) and partial slots;
-//   pyr_scatter -- the points regrouped by bucket (block-aggregated
-//                  reservations, two reads of x/y per block);
+//   pyr_band / pyr_scatter
+//               -- the points regrouped by bucket in two passes, first by
+//                  bucket row (2^B bands) and then by bucket, so that every
+//                  block writes runs of consecutive rows (block-aggregated
+//                  reservations, two reads of the input per block);
 //   pyr_render  -- persistent: each CTA takes work items off a queue.  The
 //                  item's footprint at level z, (ts >> (B + split - z)) pixels
 //                  on a side, is privatised in shared memory (uint32 count,
@@ -34,6 +37,12 @@
 //                  (edge duplicates in the neighbouring tile, or a bucket
 //                  estimate off by one) are queued;
 //   pyr_spill   -- applies the queued contributions with atomics.
+// Dyadic squares (x0 = y0 = 0, power-of-two spans; checked by the host)
+// have exact tile transforms at every level: a point's pixel at level z is
+// its pixel at zmax shifted right by zmax - z.  There the render bins each
+// point at zmax only and derives the coarser footprints in shared memory by
+// 2x2 sums and maxima; only points on a tile edge (whose extra copies go to
+// the queue) run the per-level code.
 // The autotuned knobs are the shared-memory tile size (split: the finest
 // footprint is ts/2 or ts/4 pixels on a side; a split bucket is rendered by
 // 4 CTAs that each take their quarter of the bucket's points), the render
@@ -47,9 +56,8 @@ namespace dsgb {
 
 constexpr int PYR_MAX_Z = 6;                  // 4^(zmax + 1) buckets <= 16384
 constexpr int PYR_HIST_THREADS = 1024;
-constexpr int PYR_SCATTER_THREADS = 1024;
-constexpr int PYR_SCATTER_ROWS = 32768;       // rows per scatter block
 constexpr int PYR_SMEM_LIMIT = 220 * 1024;
+constexpr int PYR_BAND_ROWS = 8;              // bucket rows per band of the first regroup pass
 constexpr int PYR_SPILL_CAS_LIMIT = 1 << 20;
 
 struct PyrEntry {                             // one tile of one level, one axis
@@ -66,7 +74,8 @@ struct PyrCounters {
     unsigned queue;                           // next work item
     unsigned n_items;
     unsigned n_spill;
-    unsigned flags;                           // bit 0: spill overflow, bit 1: CAS limit
+    unsigned flags;                           // bit 0: spill overflow, bit 1: CAS limit, bit 2: slots
+    unsigned n_slots;                         // accumulation slots in use
 };
 
 struct PyrParams {
@@ -84,16 +93,20 @@ struct PyrParams {
     unsigned *bcount;                         // nbuckets
     unsigned *bstart;                         // nbuckets + 1
     unsigned *cursor;                         // nbuckets
+    unsigned *band_cursor;                    // nbk (bucket rows)
     unsigned *item_base;                      // nbuckets + 1 (items before bucket b)
-    unsigned *slot_base;                      // nbuckets (first partial slot of b)
+    unsigned *slot_base;                      // nbuckets (accumulation slot of b, when split in chunks)
     unsigned *done;                           // nbuckets << (2 * split)
     PyrCounters *ctr;
     float *sx, *sy, *sv;                      // points grouped by bucket
-    unsigned *partials;                       // slots x (2 * footprint) uint32
+    float *bx_, *by_, *bv_;                   // points grouped by bucket row (first pass)
+    int32_t dyadic;                           // exact nesting of the levels (see above)
+    int32_t vec_out;                          // outputs 16-byte aligned: vector stores
+    unsigned *partials;                       // slots x (2 * footprint) uint32: counts, then max keys
     int64_t slot_cap;
     PyrSpill *spill;
     int64_t spill_cap;
-    int32_t footprint;                        // sum over levels of F_z^2
+    int32_t footprint;                        // sum over levels of F_z^2, each rounded up to 4
     int32_t fp_off[PYR_MAX_Z + 2];            // offset of level z in the footprint (z - zmin)
     int64_t level_off[PYR_MAX_Z + 2];         // output offset of level z
     uint32_t *count_out;
@@ -263,7 +276,7 @@ __global__ void __launch_bounds__(1024) pyr_plan(const PyrParams p) {
         const unsigned c = p.bcount[b], ch = chunks_of(c, p.chunk);
         s_cnt += c;
         s_items += ch * nsub;
-        s_slots += ch > 1 ? ch * nsub : 0u;
+        s_slots += ch > 1 ? (unsigned)nsub : 0u;
     }
     unsigned t_cnt, t_items, t_slots;
     unsigned o_cnt = block_exclusive_scan(s_cnt, &t_cnt);
@@ -275,11 +288,12 @@ __global__ void __launch_bounds__(1024) pyr_plan(const PyrParams p) {
         const unsigned c = p.bcount[b], ch = chunks_of(c, p.chunk);
         p.bstart[b] = o_cnt;
         p.cursor[b] = o_cnt;
+        if (b % (p.nbk * PYR_BAND_ROWS) == 0) p.band_cursor[b / (p.nbk * PYR_BAND_ROWS)] = o_cnt;
         p.item_base[b] = o_items;
         p.slot_base[b] = o_slots;
         o_cnt += c;
         o_items += ch * nsub;
-        o_slots += ch > 1 ? ch * nsub : 0u;
+        o_slots += ch > 1 ? (unsigned)nsub : 0u;
         for (int q = 0; q < nsub; ++q) p.done[(int64_t)b * nsub + q] = 0;
     }
     if (threadIdx.x == 0) {
@@ -289,40 +303,179 @@ __global__ void __launch_bounds__(1024) pyr_plan(const PyrParams p) {
         p.ctr->n_items = t_items;
         p.ctr->n_spill = 0;
         p.ctr->flags = (int64_t)t_slots > p.slot_cap ? 4u : 0u;
+        p.ctr->n_slots = t_slots;
     }
+}
+
+__global__ void pyr_zero_slots(const PyrParams p) {
+    const unsigned ns = p.ctr->n_slots;
+    const int64_t n4 = ((int64_t)(ns < p.slot_cap ? ns : p.slot_cap) * 2 * p.footprint) >> 2;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x)
+        ((uint4 *)p.partials)[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // ---------------------------------------------------------------- scatter
 
-__global__ void __launch_bounds__(PYR_SCATTER_THREADS, 1) pyr_scatter(const PyrParams p) {
-    extern __shared__ unsigned h[];
-    for (int i = threadIdx.x; i < p.nbuckets; i += blockDim.x) h[i] = 0;
+// Warp-aggregated slot reservation: the lanes of a warp that share `key`
+// (an index into h, or a value with bit 31 set for lanes that place
+// nothing) take consecutive slots with one shared-memory atomic.
+__device__ __forceinline__ unsigned warp_reserve(unsigned *h, unsigned key, bool live) {
+    const int lane = threadIdx.x & 31;
+    const unsigned k = live ? key : (0x80000000u | lane);
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    const int leader = __ffs(peers) - 1;
+    unsigned base = 0;
+    if (live && lane == leader) base = atomicAdd(&h[key], (unsigned)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+// Regroup passes.  A block takes PYR_STAGE_ROWS consecutive rows, ranks
+// them by destination group in shared memory (warp-aggregated counters),
+// reserves each group's range with one global atomic, stages the rows in
+// shared memory in group order and writes them out as contiguous runs, so
+// that global stores are coalesced instead of one sector per row.
+constexpr int PYR_STAGE_THREADS = 1024;
+constexpr int PYR_STAGE_ITEMS = 8;
+constexpr int PYR_STAGE_ROWS = PYR_STAGE_THREADS * PYR_STAGE_ITEMS;
+constexpr int PYR_STAGE_MAX_GROUPS = 4096;    // 48 KB of counters + 128 KB of staged rows
+
+struct StageIn {
+    const float *x, *y, *v;       // v may be null
+    int64_t r0, r1;               // the block's rows
+};
+
+// Dynamic shared memory: counters (ngroups), group offsets (ngroups + 1),
+// global bases (ngroups), then the staged x, y, v (PYR_STAGE_ROWS each)
+// and their group ids.  `group_of` maps (x, y) to a group in [0, ngroups)
+// or -1 (dropped).
+template <typename G>
+__device__ void stage_and_write(const StageIn in, int ngroups, G group_of, unsigned *gcursor, float *ox,
+                                float *oy, float *ov, unsigned char *sm) {
+    unsigned *cnt = (unsigned *)sm;
+    unsigned *off = cnt + ngroups;
+    unsigned *gbase = off + ngroups + 1;
+    float *sx = (float *)(gbase + ngroups);
+    float *sy = sx + PYR_STAGE_ROWS;
+    float *sv = sy + PYR_STAGE_ROWS;
+    int *sg = (int *)(sv + PYR_STAGE_ROWS);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < ngroups; i += blockDim.x) cnt[i] = 0;
     __syncthreads();
+    float xv[PYR_STAGE_ITEMS], yv[PYR_STAGE_ITEMS], vv[PYR_STAGE_ITEMS];
+    int gv[PYR_STAGE_ITEMS];
+    unsigned rk[PYR_STAGE_ITEMS];
+#pragma unroll
+    for (int k = 0; k < PYR_STAGE_ITEMS; ++k) {
+        const int64_t i = in.r0 + (int64_t)(warp * PYR_STAGE_ITEMS + k) * 32 + lane;
+        const bool live = i < in.r1;
+        xv[k] = live ? __ldcs(in.x + i) : __int_as_float(0x7fc00000);
+        yv[k] = live ? __ldcs(in.y + i) : 0.f;
+        vv[k] = (live && in.v) ? __ldcs(in.v + i) : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < PYR_STAGE_ITEMS; ++k) {
+        gv[k] = group_of(xv[k], yv[k]);
+        rk[k] = warp_reserve(cnt, gv[k] >= 0 ? (unsigned)gv[k] : 0u, gv[k] >= 0);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // exclusive scan of the group counts by one warp
+        unsigned carry = 0;
+        for (int b0 = 0; b0 < ngroups; b0 += 32) {
+            const int g = b0 + lane;
+            const unsigned c = g < ngroups ? cnt[g] : 0u;
+            unsigned incl = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            if (g < ngroups) off[g] = carry + incl - c;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) off[ngroups] = carry;
+    }
+    __syncthreads();
+    for (int g = threadIdx.x; g < ngroups; g += blockDim.x)
+        gbase[g] = cnt[g] ? atomicAdd(&gcursor[g], cnt[g]) : 0u;
+#pragma unroll
+    for (int k = 0; k < PYR_STAGE_ITEMS; ++k) {
+        if (gv[k] < 0) continue;
+        const unsigned j = off[gv[k]] + rk[k];
+        sx[j] = xv[k];
+        sy[j] = yv[k];
+        sv[j] = vv[k];
+        sg[j] = gv[k];
+    }
+    __syncthreads();
+    const int staged = (int)off[ngroups];
+    for (int j = threadIdx.x; j < staged; j += blockDim.x) {
+        const int g = sg[j];
+        const unsigned pos = gbase[g] + (unsigned)j - off[g];
+        ox[pos] = sx[j];
+        oy[pos] = sy[j];
+        if (ov) ov[pos] = sv[j];
+    }
+}
+
+__host__ __device__ __forceinline__ size_t stage_smem_bytes(int ngroups) {
+    return (size_t)(3 * ngroups + 1) * 4 + (size_t)PYR_STAGE_ROWS * 16;
+}
+
+// First pass: rows grouped by band (PYR_BAND_ROWS bucket rows).
+__global__ void __launch_bounds__(PYR_STAGE_THREADS, 1) pyr_band(const PyrParams p) {
+    extern __shared__ __align__(16) unsigned char smb[];
     const PyrEntry dx = p.tab_x[0], dy = p.tab_y[0];
-    const int64_t r0 = (int64_t)blockIdx.x * PYR_SCATTER_ROWS;
-    const int64_t r1 = r0 + PYR_SCATTER_ROWS < p.n ? r0 + PYR_SCATTER_ROWS : p.n;
-    // pass 1: the block's count per bucket
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const int bk = bucket_of(p, dx, dy, __ldcs(p.xs + i), __ldcs(p.ys + i));
-        if (bk >= 0) atomicAdd(&h[bk], 1u);
-    }
-    __syncthreads();
-    // reserve each bucket's range: one global atomic per non-empty bucket
-    for (int i = threadIdx.x; i < p.nbuckets; i += blockDim.x) {
-        const unsigned c = h[i];
-        if (c) h[i] = atomicAdd(&p.cursor[i], c);
-    }
-    __syncthreads();
-    // pass 2: place the rows (x/y again, mostly from L2)
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const float x = p.xs[i], y = p.ys[i];
+    const int nbands = (p.nbk + PYR_BAND_ROWS - 1) / PYR_BAND_ROWS;
+    const int band_div = p.nbk * PYR_BAND_ROWS;
+    StageIn in;
+    in.x = p.xs; in.y = p.ys; in.v = p.sv ? p.vs : nullptr;
+    in.r0 = (int64_t)blockIdx.x * PYR_STAGE_ROWS;
+    in.r1 = in.r0 + PYR_STAGE_ROWS < p.n ? in.r0 + PYR_STAGE_ROWS : p.n;
+    stage_and_write(in, nbands, [&](float x, float y) {
         const int bk = bucket_of(p, dx, dy, x, y);
-        if (bk < 0) continue;
-        const unsigned pos = atomicAdd(&h[bk], 1u);
-        p.sx[pos] = x;
-        p.sy[pos] = y;
-        if (p.sv) p.sv[pos] = p.vs[i];
+        return bk < 0 ? -1 : bk / band_div;
+    }, p.band_cursor, p.bx_, p.by_, p.sv ? p.bv_ : nullptr, smb);
+}
+
+// Second pass: the banded copy grouped by bucket.  A block's rows come from
+// a few consecutive bands, so its groups are only their buckets.
+__global__ void __launch_bounds__(PYR_STAGE_THREADS, 1) pyr_scatter(const PyrParams p) {
+    extern __shared__ __align__(16) unsigned char smb[];
+    __shared__ int s_lo, s_hi;
+    const PyrEntry dx = p.tab_x[0], dy = p.tab_y[0];
+    const int64_t total = p.bstart[p.nbuckets];
+    StageIn in;
+    in.x = p.bx_; in.y = p.by_; in.v = p.sv ? p.bv_ : nullptr;
+    in.r0 = (int64_t)blockIdx.x * PYR_STAGE_ROWS;
+    in.r1 = in.r0 + PYR_STAGE_ROWS < total ? in.r0 + PYR_STAGE_ROWS : total;
+    if (in.r0 >= in.r1) return;
+    if (threadIdx.x == 0) {
+        // the banded copy is ordered by band only: cover whole bands
+        const int band_div = p.nbk * PYR_BAND_ROWS;
+        s_lo = bucket_of(p, dx, dy, p.bx_[in.r0], p.by_[in.r0]) / band_div * band_div;
+        const int hi = (bucket_of(p, dx, dy, p.bx_[in.r1 - 1], p.by_[in.r1 - 1]) / band_div + 1) * band_div;
+        s_hi = hi < p.nbuckets ? hi : p.nbuckets;
     }
+    __syncthreads();
+    const int lo = s_lo;
+    if (s_hi - s_lo > PYR_STAGE_MAX_GROUPS) {
+        // a block spanning many sparse bands: place row by row
+        for (int64_t i = in.r0 + threadIdx.x; i < in.r1; i += blockDim.x) {
+            const float x = p.bx_[i], y = p.by_[i];
+            const int bk = bucket_of(p, dx, dy, x, y);
+            if (bk < 0) continue;
+            const unsigned pos = atomicAdd(&p.cursor[bk], 1u);
+            p.sx[pos] = x;
+            p.sy[pos] = y;
+            if (p.sv) p.sv[pos] = p.bv_[i];
+        }
+        return;
+    }
+    stage_and_write(in, s_hi - s_lo, [&](float x, float y) {
+        const int bk = bucket_of(p, dx, dy, x, y);
+        return bk < 0 ? -1 : bk - lo;
+    }, p.cursor + lo, p.sx, p.sy, p.sv, smb);
 }
 
 // ---------------------------------------------------------------- render
@@ -330,7 +483,7 @@ __global__ void __launch_bounds__(PYR_SCATTER_THREADS, 1) pyr_scatter(const PyrP
 struct PyrLevel {                 // per item and level, in shared memory
     PyrEntry hx, hy;              // home tiles of the item at this level
     int htx, hty;                 // their indices
-    int f;                        // footprint side
+    int f, lf;                    // footprint side and its log2
     int gx0, gy0;                 // footprint origin (global pixels of the level)
     int cf, cgx0, cgy0;           // the whole bucket's footprint (split > 0)
 };
@@ -363,6 +516,37 @@ __device__ __forceinline__ int tiles_of(float c, const PyrEntry &home, int ht, c
         if (c >= e.lo_f && c <= e.hi_f) g[k++] = u * ts + pyr_bin(c, e.ax);
     }
     return k;
+}
+
+__device__ __forceinline__ void pyr_queue(const PyrParams &p, int z, int gx, int gy, float v) {
+    const unsigned si = atomicAdd(&p.ctr->n_spill, 1u);
+    if ((int64_t)si < p.spill_cap) {
+        PyrSpill s;
+        s.z = (unsigned)z; s.gx = (unsigned)gx; s.gy = (unsigned)gy; s.v = v;
+        p.spill[si] = s;
+    } else {
+        atomicOr(&p.ctr->flags, 1u);
+    }
+}
+
+// Dyadic squares: a point on a tile edge (or outside its item's bucket)
+// runs the per-level binning; every contribution other than the floor
+// pixel already counted at zmax (gxp, gyp shifted to the level) is queued.
+static __device__ __noinline__ void pyr_dyadic_edges(const PyrParams &p, const PyrLevel *L, int nlev, float x,
+                                                     float y, float v, int gxp, int gyp, bool counted, float x0f,
+                                                     float y0f, float span_inv_x, float span_inv_y) {
+    for (int lz = 0; lz < nlev; ++lz) {
+        const PyrLevel &l = L[lz];
+        const int z = p.zmin + lz, k = p.zmax - z;
+        int gx[2], gy[2];
+        const int kx = tiles_of(x, l.hx, l.htx, p.tab_x, z, p.ts, x0f, span_inv_x, gx);
+        const int ky = kx ? tiles_of(y, l.hy, l.hty, p.tab_y, z, p.ts, y0f, span_inv_y, gy) : 0;
+        for (int a = 0; a < kx; ++a)
+            for (int c = 0; c < ky; ++c) {
+                if (counted && gx[a] == (gxp >> k) && gy[c] == (gyp >> k)) continue;
+                pyr_queue(p, z, gx[a], gy[c], v);
+            }
+    }
 }
 
 __global__ void pyr_render(const PyrParams p) {
@@ -399,6 +583,7 @@ __global__ void pyr_render(const PyrParams p) {
             const int z = p.zmin + threadIdx.x;
             PyrLevel &l = L[threadIdx.x];
             l.f = p.ts >> (bl - z);
+            l.lf = __ffs(l.f) - 1;
             l.gx0 = bx * l.f;
             l.gy0 = by * l.f;
             l.cf = l.f << p.split;
@@ -409,15 +594,54 @@ __global__ void pyr_render(const PyrParams p) {
             l.hx = p.tab_x[(1 << z) - 1 + l.htx];
             l.hy = p.tab_y[(1 << z) - 1 + l.hty];
         }
-        for (int i = threadIdx.x; i < 2 * p.footprint; i += blockDim.x) scnt[i] = 0u;
+        {
+            const int n4 = (2 * p.footprint) >> 2;
+            for (int i = threadIdx.x; i < n4; i += blockDim.x) ((uint4 *)scnt)[i] = make_uint4(0u, 0u, 0u, 0u);
+            for (int i = 4 * n4 + threadIdx.x; i < 2 * p.footprint; i += blockDim.x) scnt[i] = 0u;
+        }
         __syncthreads();
         const unsigned s0 = p.bstart[b] + j * (unsigned)p.chunk;
         const unsigned s1 = s0 + (unsigned)p.chunk < p.bstart[b + 1] ? s0 + (unsigned)p.chunk : p.bstart[b + 1];
-        for (unsigned i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-            const float x = p.sx[i], y = p.sy[i];
-            const float v = p.sv ? p.sv[i] : __int_as_float(0x7fc00000);
+        constexpr int RI = 4;                 // rows per thread and iteration, loaded up front
+        for (unsigned i0 = s0 + threadIdx.x; i0 < s1; i0 += RI * blockDim.x) {
+          float xv[RI], yv[RI], vv[RI];
+#pragma unroll
+          for (int r = 0; r < RI; ++r) {
+              const unsigned i = i0 + r * blockDim.x;
+              const bool live = i < s1;
+              xv[r] = live ? p.sx[i] : __int_as_float(0x7fc00000);
+              yv[r] = live ? p.sy[i] : 0.f;
+              vv[r] = (live && p.sv) ? p.sv[i] : __int_as_float(0x7fc00000);
+          }
+#pragma unroll 1
+          for (int r = 0; r < RI; ++r) {
+            if (i0 + r * blockDim.x >= s1) break;
+            const float x = xv[r], y = yv[r];
+            const float v = vv[r];
             const bool hasv = !(v != v);
             const unsigned key = hasv ? fkey(v) : 0u;
+            if (p.dyadic) {
+                // bin at zmax only; the coarser footprints are derived below
+                const PyrLevel &l = L[nlev - 1];
+                int gx[2], gy[2];
+                const int kx = tiles_of(x, l.hx, l.htx, p.tab_x, p.zmax, p.ts, x0f, span_inv_x, gx);
+                const int ky = kx ? tiles_of(y, l.hy, l.hty, p.tab_y, p.zmax, p.ts, y0f, span_inv_y, gy) : 0;
+                if (!kx || !ky) continue;
+                // the floor pixel: on a tile edge the right / upper tile's first pixel
+                const int gxp = kx == 2 ? max(gx[0], gx[1]) : gx[0];
+                const int gyp = ky == 2 ? max(gy[0], gy[1]) : gy[0];
+                const unsigned lx = (unsigned)(gxp - l.gx0), ly = (unsigned)(gyp - l.gy0);
+                if (lx < (unsigned)l.f && ly < (unsigned)l.f) {
+                    const int off = p.fp_off[nlev - 1] + (int)ly * l.f + (int)lx;
+                    atomicAdd(&scnt[off], 1u);
+                    if (hasv) atomicMax(&skey[off], key);
+                }
+                const bool in_bucket = (unsigned)(gxp - l.cgx0) < (unsigned)l.cf &&
+                                       (unsigned)(gyp - l.cgy0) < (unsigned)l.cf;
+                if (q == 0 && (!in_bucket || kx == 2 || ky == 2))
+                    pyr_dyadic_edges(p, L, nlev, x, y, v, gxp, gyp, in_bucket, x0f, y0f, span_inv_x, span_inv_y);
+                continue;
+            }
             for (int lz = 0; lz < nlev; ++lz) {
                 const PyrLevel &l = L[lz];
                 const int z = p.zmin + lz;
@@ -440,67 +664,109 @@ __global__ void pyr_render(const PyrParams p) {
                             if (cx < (unsigned)l.cf && cy < (unsigned)l.cf) continue;
                             if (q != 0) continue;     // one sibling queues what leaves the bucket
                         }
-                        const unsigned si = atomicAdd(&p.ctr->n_spill, 1u);
-                        if ((int64_t)si < p.spill_cap) {
-                            PyrSpill s;
-                            s.z = (unsigned)z; s.gx = (unsigned)gx[a]; s.gy = (unsigned)gy[c]; s.v = v;
-                            p.spill[si] = s;
-                        } else {
-                            atomicOr(&p.ctr->flags, 1u);
-                        }
+                        pyr_queue(p, z, gx[a], gy[c], v);
                     }
                 }
             }
+          }
         }
         __syncthreads();
+        if (p.dyadic) {
+            // level z from level z + 1: 2x2 sums of the counts, maxima of the keys
+            for (int lz = nlev - 2; lz >= 0; --lz) {
+                const int f = L[lz].f, fc = L[lz + 1].f;
+                const int o = p.fp_off[lz], oc = p.fp_off[lz + 1];
+                const int lf = L[lz].lf;
+                for (int i = threadIdx.x; i < f * f; i += blockDim.x) {
+                    const int r = i >> lf, c = i & (f - 1);
+                    const int a = oc + 2 * r * fc + 2 * c;
+                    scnt[o + i] = scnt[a] + scnt[a + 1] + scnt[a + fc] + scnt[a + fc + 1];
+                    skey[o + i] = max(max(skey[a], skey[a + 1]), max(skey[a + fc], skey[a + fc + 1]));
+                }
+                __syncthreads();
+            }
+        }
         const unsigned *rc = scnt, *rk = skey;
         bool write = true;
         if (nch > 1) {
-            const int64_t slot = (int64_t)p.slot_base[b] + (int64_t)j * nsub + q;
+            // A bucket split into chunks: every chunk adds its footprint into the
+            // bucket's zeroed slot with bulk reductions (add for counts, max for
+            // keys); the chunk that finishes last reads the slot back and writes it.
+            const int64_t slot = (int64_t)p.slot_base[b] + q;
             if (slot >= p.slot_cap) {
                 write = false;                              // flagged by the plan (cannot happen)
             } else {
                 unsigned *dst = p.partials + slot * 2 * p.footprint;
-                for (int i = threadIdx.x; i < 2 * p.footprint; i += blockDim.x) dst[i] = scnt[i];
-                __threadfence();
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncthreads();
-                if (threadIdx.x == 0)
+                if (threadIdx.x == 0) {
+                    const unsigned bytes = (unsigned)p.footprint * 4u;
+                    const unsigned sa = (unsigned)__cvta_generic_to_shared(scnt);
+                    const unsigned sk = (unsigned)__cvta_generic_to_shared(skey);
+                    for (unsigned o = 0; o < bytes; o += 16384u) {
+                        const unsigned sz = bytes - o < 16384u ? bytes - o : 16384u;
+                        asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.u32 [%0], [%1], %2;"
+                                     :: "l"((char *)dst + o), "r"(sa + o), "r"(sz) : "memory");
+                        asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.max.u32 [%0], [%1], %2;"
+                                     :: "l"((char *)(dst + p.footprint) + o), "r"(sk + o), "r"(sz) : "memory");
+                    }
+                    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+                    asm volatile("fence.proxy.async.global;" ::: "memory");
+                    __threadfence();
                     s_last = atomicAdd(&p.done[(int64_t)b * nsub + q], 1u) == nch - 1;
+                }
                 __syncthreads();
                 write = s_last;
                 if (write) {
                     __threadfence();
-                    // every chunk's partial is in its slot: fold them into shared memory
-                    for (int i = threadIdx.x; i < p.footprint; i += blockDim.x) {
-                        unsigned c = 0, k = 0;
-                        for (unsigned jj = 0; jj < nch; ++jj) {
-                            const unsigned *src = p.partials +
-                                ((int64_t)p.slot_base[b] + (int64_t)jj * nsub + q) * 2 * p.footprint;
-                            c += __ldcg(src + i);
-                            k = max(k, __ldcg(src + p.footprint + i));
-                        }
-                        scnt[i] = c;
-                        skey[i] = k;
-                    }
+                    const int n4 = (2 * p.footprint) >> 2;
+                    for (int i = threadIdx.x; i < n4; i += blockDim.x)
+                        ((uint4 *)scnt)[i] = __ldcg((const uint4 *)dst + i);
                     __syncthreads();
                 }
             }
         }
         if (write) {
+            const double qnan = __longlong_as_double(0x7ff8000000000000ll);
             for (int lz = 0; lz < nlev; ++lz) {
                 const PyrLevel &l = L[lz];
                 const int z = p.zmin + lz;
                 const int row0 = l.gy0 - l.hty * p.ts, col0 = l.gx0 - l.htx * p.ts;
                 const int64_t base = p.level_off[lz] +
                                      ((int64_t)((l.hty << z) + l.htx) * p.ts + row0) * p.ts + col0;
-                for (int i = threadIdx.x; i < l.f * l.f; i += blockDim.x) {
-                    const int r = i / l.f, c = i - r * l.f;
-                    const int off = p.fp_off[lz] + i;
-                    const int64_t o = base + (int64_t)r * p.ts + c;
-                    p.count_out[o] = rc[off];
-                    if (p.max_out) {
-                        const unsigned k = rk[off];
-                        p.max_out[o] = k ? (double)fkey_value(k) : __longlong_as_double(0x7ff8000000000000ll);
+                const unsigned *cs = rc + p.fp_off[lz];
+                const unsigned *ks = rk + p.fp_off[lz];
+                if (l.f >= 4 && p.vec_out) {
+                    // four consecutive pixels of a row per thread: one 16-byte count store,
+                    // two 16-byte max stores (the offsets are multiples of 4 pixels)
+                    const int q4 = (l.f * l.f) >> 2, lq = l.lf - 2;
+                    for (int i = threadIdx.x; i < q4; i += blockDim.x) {
+                        const int r = i >> lq, c = (i & ((l.f >> 2) - 1)) << 2;
+                        const int off = (r << l.lf) + c;
+                        const int64_t o = base + (int64_t)r * p.ts + c;
+                        const uint4 cv = *(const uint4 *)(cs + off);
+                        *(uint4 *)(p.count_out + o) = cv;
+                        if (p.max_out) {
+                            const uint4 kv = *(const uint4 *)(ks + off);
+                            double2 m0, m1;
+                            m0.x = kv.x ? (double)fkey_value(kv.x) : qnan;
+                            m0.y = kv.y ? (double)fkey_value(kv.y) : qnan;
+                            m1.x = kv.z ? (double)fkey_value(kv.z) : qnan;
+                            m1.y = kv.w ? (double)fkey_value(kv.w) : qnan;
+                            *(double2 *)(p.max_out + o) = m0;
+                            *(double2 *)(p.max_out + o + 2) = m1;
+                        }
+                    }
+                } else {
+                    for (int i = threadIdx.x; i < l.f * l.f; i += blockDim.x) {
+                        const int r = i >> l.lf, c = i & (l.f - 1);
+                        const int64_t o = base + (int64_t)r * p.ts + c;
+                        p.count_out[o] = cs[i];
+                        if (p.max_out) {
+                            const unsigned k = ks[i];
+                            p.max_out[o] = k ? (double)fkey_value(k) : qnan;
+                        }
                     }
                 }
             }
@@ -543,7 +809,7 @@ struct PyrLayout {
     int bls, nbk, nbuckets, nsub, footprint, ntab;
     int64_t fp_bytes, slot_cap, spill_cap;
     size_t off_tab_x, off_tab_y, off_bcount, off_bstart, off_cursor, off_item_base, off_slot_base, off_done,
-        off_ctr, off_sx, off_sy, off_sv, off_partials, off_spill, total;
+        off_ctr, off_sx, off_sy, off_sv, off_bx, off_by, off_bv, off_band, off_partials, off_spill, total;
 };
 
 static size_t pyr_align(size_t v) { return (v + 255) / 256 * 256; }
@@ -564,12 +830,12 @@ static int pyr_layout(int64_t n, bool has_v, const dsgb_pyramid_config *c, PyrLa
     int64_t fp = 0;
     for (int z = c->zmin; z <= c->zmax; ++z) {
         const int64_t f = c->tile_size >> (bl - z);
-        fp += f * f;
+        fp += (f * f + 3) & ~(int64_t)3;          // every level starts on a 16-byte boundary
     }
     if (fp * 8 > PYR_SMEM_LIMIT) return DSGB_E_UNSUPPORTED;
     L.footprint = (int)fp;
     L.fp_bytes = fp * 8;
-    L.slot_cap = (2 * (n / c->chunk) + 2) * L.nsub;
+    L.slot_cap = (n / c->chunk + 1) * L.nsub;       // a bucket is split only if it holds > chunk rows
     L.spill_cap = n / 64 + (1 << 20);
     size_t o = 0;
     L.off_tab_x = o; o = pyr_align(o + (size_t)L.ntab * sizeof(PyrEntry));
@@ -584,6 +850,10 @@ static int pyr_layout(int64_t n, bool has_v, const dsgb_pyramid_config *c, PyrLa
     L.off_sx = o; o = pyr_align(o + (size_t)n * 4);
     L.off_sy = o; o = pyr_align(o + (size_t)n * 4);
     L.off_sv = o; o = pyr_align(o + (has_v ? (size_t)n * 4 : 0));
+    L.off_bx = o; o = pyr_align(o + (size_t)n * 4);
+    L.off_by = o; o = pyr_align(o + (size_t)n * 4);
+    L.off_bv = o; o = pyr_align(o + (has_v ? (size_t)n * 4 : 0));
+    L.off_band = o; o = pyr_align(o + (size_t)L.nbk * 4);
     L.off_partials = o; o = pyr_align(o + (size_t)L.slot_cap * L.fp_bytes);
     L.off_spill = o; o = pyr_align(o + (size_t)L.spill_cap * sizeof(PyrSpill));
     L.total = o;
@@ -609,7 +879,11 @@ static int pyr_device_setup(int &sms) {
     if (!d.ready) {
         e = cudaFuncSetAttribute(pyr_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(pyr_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+            e = cudaFuncSetAttribute(pyr_band, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)stage_smem_bytes(1 << (PYR_MAX_Z + 1)));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(pyr_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)stage_smem_bytes(PYR_STAGE_MAX_GROUPS));
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(pyr_render, cudaFuncAttributeMaxDynamicSharedMemorySize, PYR_SMEM_LIMIT);
         if (e != cudaSuccess) return cuda_status(e, "dsgb_pyramid: cudaFuncSetAttribute");
@@ -695,6 +969,16 @@ extern "C" int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n, i
     p.sx = (float *)(w + L.off_sx);
     p.sy = (float *)(w + L.off_sy);
     p.sv = v_col >= 0 ? (float *)(w + L.off_sv) : nullptr;
+    p.bx_ = (float *)(w + L.off_bx);
+    p.by_ = (float *)(w + L.off_by);
+    p.bv_ = v_col >= 0 ? (float *)(w + L.off_bv) : nullptr;
+    p.band_cursor = (unsigned *)(w + L.off_band);
+    {
+        int ex = 0, ey = 0;
+        const double mx = frexp(config->x1 - config->x0, &ex), my = frexp(config->y1 - config->y0, &ey);
+        p.dyadic = config->x0 == 0.0 && config->y0 == 0.0 && mx == 0.5 && my == 0.5 &&
+                   ex > -100 && ex < 100 && ey > -100 && ey < 100;
+    }
     p.partials = (unsigned *)(w + L.off_partials);
     p.slot_cap = L.slot_cap;
     p.spill = (PyrSpill *)(w + L.off_spill);
@@ -705,11 +989,12 @@ extern "C" int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n, i
     for (int z = p.zmin; z <= p.zmax; ++z) {
         p.fp_off[z - p.zmin] = fo;
         const int f = p.ts >> (bl - z);
-        fo += f * f;
+        fo += (f * f + 3) & ~3;
         p.level_off[z - p.zmin] = dsgb_pyramid_tile_offset(p.zmin, z, p.ts);
     }
     p.count_out = counts;
     p.max_out = v_col >= 0 ? max_out : nullptr;
+    p.vec_out = ((uintptr_t)counts & 15u) == 0 && ((uintptr_t)p.max_out & 15u) == 0;
 
     cudaStream_t st = as_stream(stream);
     cudaError_t e = cudaMemsetAsync(p.bcount, 0, (size_t)L.nbuckets * 4, st);
@@ -720,9 +1005,15 @@ extern "C" int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n, i
     DSGB_CHECK_LAUNCH("pyr_hist");
     pyr_plan<<<1, 1024, 0, st>>>(p);
     DSGB_CHECK_LAUNCH("pyr_plan");
-    const int64_t sblocks = (n + PYR_SCATTER_ROWS - 1) / PYR_SCATTER_ROWS;
+    pyr_zero_slots<<<sms * 4, 256, 0, st>>>(p);
+    DSGB_CHECK_LAUNCH("pyr_zero_slots");
+    const int64_t sblocks = (n + PYR_STAGE_ROWS - 1) / PYR_STAGE_ROWS;
     if (sblocks > 0) {
-        pyr_scatter<<<(unsigned)sblocks, PYR_SCATTER_THREADS, (size_t)L.nbuckets * 4, st>>>(p);
+        const int nbands = (L.nbk + PYR_BAND_ROWS - 1) / PYR_BAND_ROWS;
+        pyr_band<<<(unsigned)sblocks, PYR_STAGE_THREADS, stage_smem_bytes(nbands), st>>>(p);
+        DSGB_CHECK_LAUNCH("pyr_band");
+        const int ng = L.nbuckets < PYR_STAGE_MAX_GROUPS ? L.nbuckets : PYR_STAGE_MAX_GROUPS;
+        pyr_scatter<<<(unsigned)sblocks, PYR_STAGE_THREADS, stage_smem_bytes(ng), st>>>(p);
         DSGB_CHECK_LAUNCH("pyr_scatter");
     }
     int per_sm = 0;
