@@ -234,7 +234,13 @@ def bench_pyramid(args, dev, peak, peak_kind):
     g.manual_seed(1)
     v = torch.randn(n, generator=g, device=dev, dtype=torch.float32)
     pyr = P.TilePyramid(x, y, v, zmin=0, zmax=6, tile_size=256)
-    best, results = P.autotune(pyr, repeats=2)
+    if args.pyramid_config:
+        sp, th, ch = (int(t) for t in args.pyramid_config.split(","))
+        best = dict(split=sp, threads=th, chunk=ch)
+        pyr.set_config(best)
+        results = []
+    else:
+        best, results = P.autotune(pyr, repeats=2)
     pyr.render()
     torch.cuda.synchronize()
     status = pyr.status()
@@ -271,6 +277,71 @@ def bench_pyramid(args, dev, peak, peak_kind):
                         "algorithmic_bytes": alg, "note": "12 B/point read + count/max tiles written once"},
            "gpu_launches_per_pyramid": 8}
     del pyr, x, y, v, frame
+    torch.cuda.empty_cache()
+    return res
+
+
+def bench_line(args, dev):
+    """The differentiation workload: Canvas.line (LineAxis0, line_width 1.5,
+    antialiased) of 1000 series x 10,000 float64 vertices (NaN separators,
+    10,010,000 rows) on 1024x512, sum('v'); y autoranged.  Forward alone, and
+    forward + backward of the MSE against the same series with y + N(0, 0.005)
+    through the hand-written adjoint (gradients w.r.t. v and y)."""
+    import torch
+    import datashader_gb300 as ds
+    from datashader_gb300 import autograd as ag
+    from datashader_gb300 import synthetic
+    nseries, length = args.line_series, 10_000
+    x, y, v, _ = synthetic.time_series_np(nseries, length, seed=0)
+    rng = np.random.default_rng(1)
+    y_t = y + rng.normal(0.0, 0.005, y.shape)
+    X, Y, V = (torch.from_numpy(a).to(dev) for a in (x, y, v))
+    YT = torch.from_numpy(y_t).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    frame = ds.TensorFrame({"x": X, "y": Y, "v": V})
+    cvs = ds.Canvas(plot_width=1024, plot_height=512, x_range=(0.0, 1.0))
+
+    def fwd():
+        return cvs.line(frame, "x", "y", agg=ds.sum("v"), line_width=1.5)
+
+    agg = fwd()
+    y_range = tuple(agg.attrs["y_range"])
+    fixed = ds.Canvas(plot_width=1024, plot_height=512, x_range=(0.0, 1.0), y_range=y_range)
+    target = torch.nan_to_num(ag.line_sum(X, YT, V, fixed)).detach()
+    for _ in range(2):
+        fwd()
+    f_ms = _events_time(fwd, max(3, args.steps // 2), stream)
+    f_ms = sum(f_ms) / len(f_ms)
+    Yg = Y.clone().requires_grad_(True)
+    Vg = V.clone().requires_grad_(True)
+
+    def step():
+        Yg.grad = None
+        Vg.grad = None
+        loss = torch.mean((torch.nan_to_num(ag.line_sum(X, Yg, Vg, fixed)) - target) ** 2)
+        loss.backward()
+
+    for _ in range(2):
+        step()
+    fb_ms = _events_time(step, max(3, args.steps // 2), stream)
+    fb_ms = sum(fb_ms) / len(fb_ms)
+    nseg = nseries * (length - 1)
+    # the oracle (the reference's CPU line loop) on a bounded sample of the series, one thread
+    import oracle
+    ns = max(1, min(nseries, args.line_cpu_series))
+    rows = ns * (length + 1)
+    t0 = time.perf_counter()
+    oracle.line_axis0({"x": x[:rows], "y": y[:rows], "v": v[:rows]}, "x", "y", 1024, 512, (0.0, 1.0), y_range,
+                      [oracle.spec("sum", "v")], line_width=1.5)
+    cpu_s = time.perf_counter() - t0
+    res = {"workload": f"Canvas.line LineAxis0 AA lw=1.5, {nseries} series x {length} float64 vertices, "
+                       "1024x512, sum('v')",
+           "forward_ms": f_ms, "forward_gsegments_per_s": nseg / (f_ms / 1e3) / 1e9,
+           "forward_backward_ms": fb_ms,
+           "cpu_baseline": {"value": ns * (length - 1) / cpu_s / 1e9, "unit": "Gsegments/s", "cores": 1,
+                            "kind": "port", "sample": f"{ns} series, one thread, {cpu_s:.2f} s"},
+           "gpu_launches_forward": 3, "gpu_launches_forward_backward": 4}
+    del X, Y, V, YT, frame, Yg, Vg, target
     torch.cuda.empty_cache()
     return res
 
@@ -464,6 +535,8 @@ def run_gpu(args):
     extras = {}
     if world == 1 and args.pyramid_n > 0:
         extras["pyramid"] = bench_pyramid(args, dev, peak, peak_kind)
+    if world == 1 and args.line_series > 0:
+        extras["line"] = bench_line(args, dev)
     if world == 1 and args.serving_n > 0 and args.serving_requests > 0:
         extras["serving"] = bench_serving(args, dev)
 
@@ -515,14 +588,38 @@ def main():
     ap.add_argument("--pyramid-n", type=int, default=200_000_000, help="0 skips the tile-pyramid workload")
     ap.add_argument("--serving-n", type=int, default=500_000_000, help="0 skips the viewport workload")
     ap.add_argument("--serving-requests", type=int, default=1000)
+    ap.add_argument("--line-series", type=int, default=1000, help="0 skips the line workload")
+    ap.add_argument("--line-cpu-series", type=int, default=20)
     ap.add_argument("--serving-slots", type=int, default=8)
     ap.add_argument("--serving-mem-gb", type=int, default=8)
+    ap.add_argument("--only", default="all", choices=["all", "pyramid", "line", "serving"],
+                    help="run one secondary workload alone (for profiling); prints its JSON object")
+    ap.add_argument("--pyramid-config", default=None,
+                    help="split,threads,chunk: skip the autotuner (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.only != "all":
+        return run_only(args)
     return run_gpu(args)
+
+
+def run_only(args):
+    """One secondary workload alone, e.g. under ncu."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    peak, peak_kind = measured_peak()
+    if args.only == "pyramid":
+        out = bench_pyramid(args, dev, peak, peak_kind)
+    elif args.only == "line":
+        out = bench_line(args, dev)
+    else:
+        out = bench_serving(args, dev)
+    print(json.dumps({args.only: out}))
+    return 0
 
 
 if __name__ == "__main__":

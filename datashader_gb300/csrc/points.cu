@@ -276,6 +276,18 @@ size_t cached_workspace_size(int64_t n, int width, int height);
 int launch_points_cached(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
                          const BinAxis &ax, const BinAxis &ay, const BinBounds &bb,
                          uint32_t *out, bool accumulate, void *ws, size_t ws_bytes, cudaStream_t st);
+int launch_points_cached_mean(const ColumnRef &xc, const ColumnRef &yc, const ColumnRef &vc, int64_t n,
+                              const dsgb_canvas *cv, const BinAxis &ax, const BinAxis &ay, const BinBounds &bb,
+                              double *sum, uint32_t *count, bool accumulate, void *ws, size_t ws_bytes,
+                              cudaStream_t st);
+
+// mean(v): bases[0] = SUM(v), bases[1] = COUNT(v), nothing else.
+static bool cached_mean_eligible(const PointsParams &p, uint32_t flags) {
+    return p.nbases == 2 && p.bases[0].op == DSGB_BASE_SUM && p.bases[1].op == DSGB_BASE_COUNT &&
+           p.bases[0].col >= 0 && p.bases[0].col == p.bases[1].col && p.bases[0].cat_col < 0 &&
+           p.bases[1].cat_col < 0 && !(flags & (DSGB_FLAG_EXACT_BIN | DSGB_FLAG_WARP_AGG | DSGB_FLAG_DETERMINISTIC)) &&
+           !p.x_log && !p.y_log && fast_path_ok(p.ax, p.ay);
+}
 
 // The hot-tile path (points_cached.cu) serves a plain count() of every row
 // on a canvas that the float32 fast path may bin.
@@ -341,6 +353,14 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
                                   workspace, ws_bytes, st);
         if (rc != DSGB_E_UNSUPPORTED) return rc;
     }
+    if (workspace && cached_mean_eligible(p, flags)) {
+        rc = launch_points_cached_mean(p.cols[x_col], p.cols[y_col], p.cols[p.bases[0].col], n, canvas, p.ax, p.ay,
+                                       p.bb, (double *)p.bases[0].agg, (uint32_t *)p.bases[1].agg,
+                                       (flags & DSGB_FLAG_NO_INIT) != 0, workspace, ws_bytes, st);
+        if (rc == DSGB_OK && !(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+        if (rc != DSGB_E_UNSUPPORTED) return rc;
+    }
     if (!(flags & DSGB_FLAG_NO_INIT)) {
         rc = bases_init(bases, nbases, ncells, st);
         if (rc) return rc;
@@ -363,9 +383,12 @@ extern "C" int dsgb_points(const dsgb_column *cols, int32_t ncols, int64_t n, in
 
 extern "C" size_t dsgb_points_workspace_size(int64_t n, const dsgb_canvas *canvas,
                                              const dsgb_base *bases, int32_t nbases) {
-    if (!canvas || n < 0 || nbases != 1 || !bases || bases[0].op != DSGB_BASE_COUNT ||
-        bases[0].col >= 0 || bases[0].cat_col >= 0)
-        return 0;
+    if (!canvas || n < 0 || !bases) return 0;
+    const bool count = nbases == 1 && bases[0].op == DSGB_BASE_COUNT && bases[0].col < 0 && bases[0].cat_col < 0;
+    const bool mean = nbases == 2 && bases[0].op == DSGB_BASE_SUM && bases[1].op == DSGB_BASE_COUNT &&
+                      bases[0].col >= 0 && bases[0].col == bases[1].col && bases[0].cat_col < 0 &&
+                      bases[1].cat_col < 0;
+    if (!count && !mean) return 0;
     return cached_workspace_size(n, canvas->width, canvas->height);
 }
 

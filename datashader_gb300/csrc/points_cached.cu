@@ -47,6 +47,8 @@ struct CachedParams {
     short *slot;                // ntiles
     int *slot_tile;             // K
     int32_t bulk_flush;         // canvas rows 16-byte aligned: flush with bulk reductions
+    const double *vs;           // mean: the value column (float64, 16-byte aligned)
+    double *sum_out;            // mean: the float64 sum base (out is the count base)
 };
 
 __device__ __forceinline__ int tile_cells(const CachedParams &p) { return 1 << (2 * p.ts); }
@@ -247,6 +249,122 @@ __global__ void __launch_bounds__(1024, 1) cached_main(const CachedParams p) {
     }
 }
 
+// ---- mean(v): float64 sums and uint32 counts of the hottest tiles in shared
+// memory (12 bytes a pixel, so about a third of the tiles of count()).
+// Rows whose value is NaN add nothing (reductions.py:1280-1297 with
+// _sum_zero and _count_ignore_antialiasing).
+__device__ __forceinline__ void mean_emit(const CachedParams &p, const short *tab, double *ssum, unsigned *scnt,
+                                          int xi, int yi, double v) {
+    const int s = tab[(yi >> p.ts) * p.tiles_x + (xi >> p.ts)];
+    if (s >= 0) {
+        const int tm = (1 << p.ts) - 1;
+        const unsigned c = ((unsigned)s << (2 * p.ts)) + ((unsigned)(yi & tm) << p.ts) + (unsigned)(xi & tm);
+        atomicAdd(&ssum[c], v);
+        atomicAdd(&scnt[c], 1u);
+    } else {
+        const int64_t pix = (int64_t)yi * p.width + xi;
+        atomicAdd(&p.sum_out[pix], v);
+        atomicAdd(&p.out[pix], 1u);
+    }
+}
+
+__global__ void __launch_bounds__(1024, 1) cached_mean_main(const CachedParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    short *tab = (short *)smem;
+    const int tab_bytes = ((p.ntiles * 2) + 15) & ~15;
+    const int tc = tile_cells(p);
+    const int cells = p.K * tc;
+    double *ssum = (double *)(smem + tab_bytes);
+    unsigned *scnt = (unsigned *)(ssum + cells);
+    for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x) tab[i] = p.slot[i];
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) { ssum[i] = 0.0; scnt[i] = 0u; }
+    __syncthreads();
+    const float4 *x4 = (const float4 *)p.xs;
+    const float4 *y4 = (const float4 *)p.ys;
+    const double2 *v2 = (const double2 *)p.vs;
+    const int64_t n4 = p.n >> 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n4; v += stride) {
+        const float4 a = __ldcs(x4 + v), b = __ldcs(y4 + v);
+        const double2 w0 = __ldcs(v2 + 2 * v), w1 = __ldcs(v2 + 2 * v + 1);
+        const float xs[4] = {a.x, a.y, a.z, a.w};
+        const float ys[4] = {b.x, b.y, b.z, b.w};
+        const double vs[4] = {w0.x, w0.y, w1.x, w1.y};
+        int xi[4], yi[4];
+        unsigned in = 0, need = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int r = isnull(vs[k]) ? 0 : bin_try_f32(xs[k], ys[k], p.bb, p.ax, p.ay, xi[k], yi[k]);
+            in |= (unsigned)(r != 0) << k;
+            need |= (unsigned)(r == 2) << k;
+        }
+        if (need) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if ((need >> k) & 1u) bin_exact_f32(xs[k], ys[k], p.ax, p.ay, xi[k], yi[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if ((in >> k) & 1u) mean_emit(p, tab, ssum, scnt, xi[k], yi[k], vs[k]);
+    }
+    for (int64_t i = 4 * n4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += stride) {
+        const double vv = p.vs[i];
+        if (isnull(vv)) continue;
+        int xi, yi;
+        const int r = bin_try_f32(p.xs[i], p.ys[i], p.bb, p.ax, p.ay, xi, yi);
+        if (r == 2) bin_exact_f32(p.xs[i], p.ys[i], p.ax, p.ay, xi, yi);
+        if (r) mean_emit(p, tab, ssum, scnt, xi, yi, vv);
+    }
+    __syncthreads();
+    if (p.bulk_flush) {
+        // one bulk reduction per cached tile row and array (add.f64 sums, add.u32 counts)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        const int side = 1 << p.ts;
+        bool issued = false;
+        for (int r = threadIdx.x; r < p.K * side; r += blockDim.x) {
+            const int slot = r >> p.ts, ry = r & (side - 1);
+            const int t = p.slot_tile[slot];
+            if (t < 0) continue;
+            const int yi = (t / p.tiles_x) * side + ry;
+            const int x0 = (t % p.tiles_x) * side;
+            if (yi >= p.height) continue;
+            const int ncols = p.width - x0 < side ? p.width - x0 : side;   // a multiple of 4
+            const unsigned off = ((unsigned)slot << (2 * p.ts)) + ((unsigned)ry << p.ts);
+            unsigned any = 0;
+            for (int c = 0; c < ncols; c += 4) {
+                const uint4 q = *(const uint4 *)(scnt + off + c);
+                any |= q.x | q.y | q.z | q.w;
+            }
+            if (!any) continue;
+            const int64_t g = (int64_t)yi * p.width + x0;
+            asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.u32 [%0], [%1], %2;"
+                         :: "l"(p.out + g), "r"((unsigned)__cvta_generic_to_shared(scnt + off)), "r"(ncols * 4)
+                         : "memory");
+            asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f64 [%0], [%1], %2;"
+                         :: "l"(p.sum_out + g), "r"((unsigned)__cvta_generic_to_shared(ssum + off)), "r"(ncols * 8)
+                         : "memory");
+            issued = true;
+        }
+        if (issued) {
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+        return;
+    }
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+        const unsigned c = scnt[i];
+        if (!c) continue;
+        const int t = p.slot_tile[i >> (2 * p.ts)];
+        const int within = i & (tc - 1);
+        const int yi = (t / p.tiles_x) * (1 << p.ts) + (within >> p.ts);
+        const int xi = (t % p.tiles_x) * (1 << p.ts) + (within & ((1 << p.ts) - 1));
+        const int64_t pix = (int64_t)yi * p.width + xi;
+        atomicAdd(&p.out[pix], c);
+        atomicAdd(&p.sum_out[pix], ssum[i]);
+    }
+}
+
 // ------------------------------------------------------------- host side
 
 struct CachedLayout {
@@ -256,7 +374,7 @@ struct CachedLayout {
 
 static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
-static bool cached_layout(int64_t n, int width, int height, CachedLayout &L) {
+static bool cached_layout(int64_t n, int width, int height, CachedLayout &L, int px_bytes = 4) {
     if (n < MIN_ROWS || width <= 0 || height <= 0) return false;
     int ts = 4;
     while (ts <= 6) {
@@ -269,7 +387,7 @@ static bool cached_layout(int64_t n, int width, int height, CachedLayout &L) {
     L.tiles_x = (width + (1 << ts) - 1) >> ts;
     L.ntiles = L.tiles_x * ((height + (1 << ts) - 1) >> ts);
     const int tab = ((L.ntiles * 2) + 15) & ~15;
-    const int tile_bytes = (1 << (2 * ts)) * 4;
+    const int tile_bytes = (1 << (2 * ts)) * px_bytes;
     L.K = (SMEM_BUDGET - tab) / tile_bytes;
     if (L.K > L.ntiles) L.K = L.ntiles;
     if (L.K < 1) return false;
@@ -319,6 +437,51 @@ int launch_points_cached(const ColumnRef &xc, const ColumnRef &yc, int64_t n, co
     if (e != cudaSuccess) return cuda_status(e, "cached count smem attribute");
     cached_main<<<L.grid, 1024, smem, st>>>(p);
     DSGB_CHECK_LAUNCH("cached count launch");
+    return DSGB_OK;
+}
+
+}  // namespace dsgb
+
+namespace dsgb {
+
+// mean('v') of float32 coordinates and a float64 value column, all 16-byte
+// aligned; `sum` and `count` are the SUM and COUNT bases.  The workspace of
+// the count path is large enough (it keeps more tiles).
+int launch_points_cached_mean(const ColumnRef &xc, const ColumnRef &yc, const ColumnRef &vc, int64_t n,
+                              const dsgb_canvas *cv, const BinAxis &ax, const BinAxis &ay, const BinBounds &bb,
+                              double *sum, uint32_t *count, bool accumulate, void *ws, size_t ws_bytes,
+                              cudaStream_t st) {
+    if (xc.dtype != DSGB_F32 || yc.dtype != DSGB_F32 || vc.dtype != DSGB_F64) return DSGB_E_UNSUPPORTED;
+    if (((uintptr_t)xc.data | (uintptr_t)yc.data | (uintptr_t)vc.data) & 15u) return DSGB_E_UNSUPPORTED;
+    if (!ws || ((uintptr_t)ws & 255u)) return DSGB_E_UNSUPPORTED;
+    CachedLayout Lc, L;
+    if (!cached_layout(n, cv->width, cv->height, Lc) || ws_bytes < Lc.total) return DSGB_E_UNSUPPORTED;
+    if (!cached_layout(n, cv->width, cv->height, L, 12)) return DSGB_E_UNSUPPORTED;
+    CachedParams p;
+    memset(&p, 0, sizeof(p));
+    p.xs = (const float *)xc.data; p.ys = (const float *)yc.data; p.vs = (const double *)vc.data; p.n = n;
+    p.width = cv->width; p.height = cv->height;
+    p.ts = L.ts; p.tiles_x = L.tiles_x; p.ntiles = L.ntiles; p.K = L.K;
+    p.ax = ax; p.ay = ay; p.bb = bb;
+    p.out = count;
+    p.sum_out = sum;
+    char *w = (char *)ws;
+    p.hist = (unsigned *)(w + Lc.off_hist);
+    p.slot = (short *)(w + Lc.off_slot);
+    p.slot_tile = (int *)(w + Lc.off_slot_tile);
+    p.bulk_flush = (cv->width % 4 == 0) && ((((uintptr_t)count | (uintptr_t)sum) & 15u) == 0);
+    const size_t cells = (size_t)cv->width * cv->height;
+    cudaError_t e = cudaMemsetAsync(p.hist, 0, (size_t)L.ntiles * 4 + 4, st);
+    if (e == cudaSuccess && !accumulate) e = cudaMemsetAsync(count, 0, cells * 4, st);
+    if (e == cudaSuccess && !accumulate) e = cudaMemsetAsync(sum, 0, cells * 8, st);
+    if (e != cudaSuccess) return cuda_status(e, "cached mean memset");
+    const int64_t chunk = SAMPLE_CHUNK < n / SAMPLE_BLOCKS ? SAMPLE_CHUNK : n / SAMPLE_BLOCKS;
+    cached_sample<<<SAMPLE_BLOCKS, SAMPLE_THREADS, (size_t)L.ntiles * 4, st>>>(p, chunk);
+    const size_t smem = (((size_t)L.ntiles * 2 + 15) & ~(size_t)15) + (size_t)L.K * (1 << (2 * L.ts)) * 12;
+    e = cudaFuncSetAttribute(cached_mean_main, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "cached mean smem attribute");
+    cached_mean_main<<<L.grid, 1024, smem, st>>>(p);
+    DSGB_CHECK_LAUNCH("cached mean launch");
     return DSGB_OK;
 }
 

@@ -305,3 +305,37 @@ def test_cached_count_single_hot_pixel():
     ref = run_points({"x": x, "y": y}, {}, ds.count(), CANVAS2)
     assert_same(got, ref)
     assert int(got.astype(np.int64).sum()) == n
+
+
+# ----------------------------------------- hot-tile mean path (workspace path)
+
+@pytest.mark.parametrize("shape", [(1024, 1024), (1000, 999), (4096, 2160), (6, 4)])
+def test_cached_mean_vs_oracle(shape):
+    """mean('v') through the shared-memory tile cache: float64 sums in another
+    order than the reference's row order, 1e-12 relative; NaN values skipped."""
+    w, h = shape
+    n = 1_400_003
+    rng = np.random.default_rng(w)
+    x, y = synthetic.gaussian_mixture_np(n, seed=w + 1, dtype=np.float32)
+    v = rng.lognormal(0.0, 1.0, n)
+    v[rng.random(n) < 0.03] = np.nan
+    cols = {"x": x, "y": y, "v": v}
+    canvas = dict(plot_width=w, plot_height=h, x_range=(-4, 4), y_range=(-3, 3))
+    agg = ds.summary(m=ds.mean("v"), c=ds.count("v"))
+    got = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", ds.mean("v")))
+    ref = run_points(cols, {}, ds.mean("v"), canvas)
+    assert_same(got, ref, rtol=1e-12)
+    both = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", agg))
+    assert_same(both["m"], ref, rtol=1e-12)
+
+
+def test_cached_mean_single_hot_pixel():
+    n = 6_000_000
+    x = np.full(n, 0.1, dtype=np.float32)
+    y = np.full(n, -0.2, dtype=np.float32)
+    x[::5] = 2.5
+    v = np.linspace(0.5, 1.5, n)
+    cols = {"x": x, "y": y, "v": v}
+    got = to_numpy(ds.Canvas(**CANVAS2).points(frame_from_numpy(cols), "x", "y", ds.mean("v")))
+    ref = run_points(cols, {}, ds.mean("v"), CANVAS2)
+    assert_same(got, ref, rtol=1e-12)
