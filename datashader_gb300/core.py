@@ -116,8 +116,59 @@ class TensorFrame:
         return tuple((k, str(v.dtype), tuple(self._cats.get(k, ()))) for k, v in self._cols.items())
 
 
+class PartitionedFrame:
+    """Row partitions of one frame (the reference's dask DataFrame, dask.py:53-219):
+    each partition is aggregated into its own partial bases (rows numbered
+    from the partition's ``row_offset``), the partials are combined
+    elementwise (``dsgb_combine``) and finalized once.  Partitions may live in
+    separate tensors (out-of-core chunks, or shards gathered from elsewhere)."""
+
+    def __init__(self, partitions):
+        parts = [as_frame(p) for p in partitions]
+        if not parts:
+            raise ValueError("PartitionedFrame needs at least one partition")
+        sig = parts[0].signature()
+        offset = 0
+        fixed = []
+        for p in parts:
+            if p.signature() != sig:
+                raise ValueError("partitions must have the same columns, dtypes and categories")
+            cats = {c: p.categories(c) for c in p.columns if p.is_categorical(c)}
+            fixed.append(TensorFrame({c: p[c] for c in p.columns}, categories=cats, device=p.device,
+                                     row_offset=offset))
+            offset += len(p)
+        self.partitions = fixed
+        self.device = fixed[0].device
+
+    def __len__(self):
+        return sum(len(p) for p in self.partitions)
+
+    # schema interface (the partitions share it)
+    def __contains__(self, name):
+        return name in self.partitions[0]
+
+    def __getitem__(self, name):
+        return self.partitions[0][name]
+
+    @property
+    def columns(self):
+        return self.partitions[0].columns
+
+    def dtype_kind(self, name):
+        return self.partitions[0].dtype_kind(name)
+
+    def is_categorical(self, name):
+        return self.partitions[0].is_categorical(name)
+
+    def categories(self, name):
+        return self.partitions[0].categories(name)
+
+    def signature(self):
+        return self.partitions[0].signature()
+
+
 def as_frame(source):
-    if isinstance(source, TensorFrame):
+    if isinstance(source, (TensorFrame, PartitionedFrame)):
         return source
     if isinstance(source, dict):
         return TensorFrame(source)
@@ -315,22 +366,31 @@ def bypixel(source, canvas, glyph, agg, *, antialias=False, flags=0):
     glyph.validate(frame)
     agg.validate(frame)
     canvas.validate()
+    if isinstance(frame, PartitionedFrame):
+        return partitioned_pipeline(frame, canvas, glyph, agg, flags=flags)
     return gpu_pipeline(frame, canvas, glyph, agg, antialias=antialias, flags=flags)
 
 
-def _column_bounds(frame, name, stream):
-    """Glyph._compute_bounds (glyph.py:51-78) on the device, then
-    maybe_expand_bounds (glyph.py:42-49)."""
+def _column_raw_bounds(frame, name, stream):
+    """Glyph._compute_bounds (glyph.py:51-78) on the device: NaN-skipping (min, max)."""
     t = frame[name]
     col = N.Column(t.data_ptr(), dsgb_dtype(t), 0)
     out = torch.empty(2, dtype=torch.float64, device=t.device)
     N.check(N.lib().dsgb_bounds(ctypes.byref(col), t.numel(), out.data_ptr(), stream), "dsgb_bounds")
-    mn, mx = out.cpu().tolist()
+    return tuple(out.cpu().tolist())
+
+
+def _expand_bounds(mn, mx):
+    """maybe_expand_bounds (glyph.py:42-49)."""
     if not (np.isfinite(mn) and np.isfinite(mx)):
         mn, mx = -1.0, 1.0
     elif mn == mx:
         mn, mx = mn - 1, mn + 1
     return mn, mx
+
+
+def _column_bounds(frame, name, stream):
+    return _expand_bounds(*_column_raw_bounds(frame, name, stream))
 
 
 def _derived_columns(frame, plan):
@@ -448,3 +508,57 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
     coords = {glyph.x_label: x_axis, glyph.y_label: y_axis}
     dims = [glyph.y_label, glyph.x_label]
     return _results(plan, ex, coords, dims, dict(x_range=x_range, y_range=y_range))
+
+
+def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
+    """dask.py:86-219 on one GPU: every partition into its own partial bases,
+    an elementwise combine, one finalize."""
+    if isinstance(glyph, LineAxis0):
+        raise NotImplementedError("partitioned sources are supported for Canvas.points")
+    if flags & N.FLAG_DETERMINISTIC:
+        raise NotImplementedError("the deterministic mode sums one frame in row order; concatenate the partitions")
+    parts = pframe.partitions
+    dev = pframe.device
+    if stream is None:
+        stream = torch.cuda.current_stream(dev).cuda_stream
+    plan = compile_plan(agg, parts[0])
+    if any(o.fin == N.FIN_GATHER for _, o in plan.outputs):
+        raise NotImplementedError("first/last/where with a lookup column gather values by global row; "
+                                  "they are not supported on partitioned sources")
+    if canvas.x_range is not None and canvas.y_range is not None:
+        x_range, y_range = canvas.x_range, canvas.y_range
+    else:
+        bx = [_column_raw_bounds(p, glyph.x, stream) for p in parts] or [(np.inf, -np.inf)]
+        by = [_column_raw_bounds(p, glyph.y, stream) for p in parts] or [(np.inf, -np.inf)]
+        x_range = canvas.x_range or _expand_bounds(min(b[0] for b in bx), max(b[1] for b in bx))
+        y_range = canvas.y_range or _expand_bounds(min(b[0] for b in by), max(b[1] for b in by))
+    canvas.validate_ranges(x_range, y_range)
+    width, height = canvas.plot_width, canvas.plot_height
+    x_st = canvas.x_axis.compute_scale_and_translate(x_range, width)
+    y_st = canvas.y_axis.compute_scale_and_translate(y_range, height)
+    cv = N.CanvasDesc(width, height, int(canvas.x_axis.is_log), int(canvas.y_axis.is_log),
+                      x_st[0], x_st[1], y_st[0], y_st[1],
+                      float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]))
+    L = N.lib()
+    execs = []
+    for part in parts:
+        ex = Executor(part, plan, glyph)
+        ex.allocate(height, width, dev)
+        wsz = int(L.dsgb_points_workspace_size_flags(len(part), ctypes.byref(cv), ex.bases, len(plan.bases),
+                                                     flags))
+        ws = workspace(dev, stream, wsz) if wsz else None
+        N.check(L.dsgb_points_ws(ex.cols, len(ex.names), len(part), part.row_offset, 0, 1, ctypes.byref(cv),
+                                 ex.bases, len(plan.bases), ex.outs, ex.nouts,
+                                 ws.data_ptr() if ws is not None else None, wsz, flags | N.FLAG_NO_FINALIZE,
+                                 stream), "dsgb_points_ws (partition)")
+        execs.append(ex)
+    head = execs[0]
+    for ex in execs[1:]:
+        N.check(L.dsgb_combine(head.bases, ex.bases, len(plan.bases), width * height, stream), "dsgb_combine")
+    if head.nouts:
+        N.check(L.dsgb_finalize(head.cols, len(head.names), parts[0].row_offset, head.bases, len(plan.bases),
+                                head.outs, head.nouts, width * height, stream), "dsgb_finalize")
+    coords = {glyph.x_label: canvas.x_axis.compute_index(x_st, width),
+              glyph.y_label: canvas.y_axis.compute_index(y_st, height)}
+    dims = [glyph.y_label, glyph.x_label]
+    return _results(plan, head, coords, dims, dict(x_range=x_range, y_range=y_range))

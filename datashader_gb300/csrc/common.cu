@@ -297,6 +297,70 @@ extern "C" int dsgb_device_sm_count(void) {
     return n;
 }
 
+// ---- combine: partial bases of two row partitions (datashader's dask
+// combine, dask.py:86-219 with each reduction's _combine).  Rows carry
+// their global index (row_offset), so row-index bases combine by min / max
+// and {key,row} pairs by the same order as the append.
+__global__ void combine_kernel(int op, void *dst, const void *src, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        switch (op) {
+        case DSGB_BASE_COUNT: ((unsigned *)dst)[i] += ((const unsigned *)src)[i]; break;
+        case DSGB_BASE_ANY: ((uint8_t *)dst)[i] |= ((const uint8_t *)src)[i]; break;
+        case DSGB_BASE_SUM: ((double *)dst)[i] += ((const double *)src)[i]; break;
+        case DSGB_BASE_MAX: case DSGB_BASE_MAX_ROW: {
+            long long *d = (long long *)dst;
+            const long long v = ((const long long *)src)[i];
+            if (v > d[i]) d[i] = v;
+            break;
+        }
+        case DSGB_BASE_MIN: case DSGB_BASE_MIN_ROW: {
+            long long *d = (long long *)dst;
+            const long long v = ((const long long *)src)[i];
+            if (v < d[i]) d[i] = v;
+            break;
+        }
+        case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: {
+            long long *d = (long long *)dst + 2 * i;
+            const long long *q = (const long long *)src + 2 * i;
+            const bool better = op == DSGB_BASE_ARGMAX ? pair_better<true>(q[0], q[1], d[0], d[1])
+                                                       : pair_better<false>(q[0], q[1], d[0], d[1]);
+            if (better) { d[0] = q[0]; d[1] = q[1]; }
+            break;
+        }
+        default: break;
+        }
+    }
+}
+
+extern "C" int dsgb_combine(const dsgb_base *dst, const dsgb_base *src, int32_t nbases, int64_t ncells,
+                            void *stream) {
+    if ((nbases > 0 && (!dst || !src)) || nbases < 0 || ncells < 0) {
+        set_error("dsgb_combine: bad arguments");
+        return DSGB_E_INVALID;
+    }
+    cudaStream_t st = as_stream(stream);
+    for (int b = 0; b < nbases; ++b) {
+        const dsgb_base &D = dst[b], &S = src[b];
+        if (D.op != S.op || D.ncat != S.ncat || !D.agg || !S.agg) {
+            set_error("dsgb_combine: base %d differs between the partials", b);
+            return DSGB_E_INVALID;
+        }
+        if (D.op >= DSGB_BASE_AA_SUM) {
+            set_error("dsgb_combine: antialiased line bases do not combine elementwise (base %d)", b);
+            return DSGB_E_UNSUPPORTED;
+        }
+        if (D.op < DSGB_BASE_COUNT) {
+            set_error("dsgb_combine: unknown base op %d", D.op);
+            return DSGB_E_INVALID;
+        }
+        const int64_t n = ncells * (D.ncat > 0 ? D.ncat : 1);
+        if (n == 0) continue;
+        combine_kernel<<<grid_for(n), 256, 0, st>>>(D.op, D.agg, S.agg, n);
+        DSGB_CHECK_LAUNCH("dsgb_combine");
+    }
+    return DSGB_OK;
+}
+
 extern "C" int dsgb_bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, void *stream) {
     if ((nbases > 0 && !bases) || nbases < 0 || ncells < 0) { set_error("dsgb_bases_init: bad args"); return DSGB_E_INVALID; }
     return bases_init(bases, nbases, ncells, as_stream(stream));

@@ -206,6 +206,14 @@ int dsgb_bucket_sort(const dsgb_column *cols, int32_t ncols, int64_t n, int32_t 
                      const double *domain, int32_t grid, void *const *out_data, int64_t *bucket_start,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+/* Combine the partial bases `src` of one row partition into `dst` (same
+ * plan, same canvas): counts and sums add, any ORs, min/max keys and row
+ * indexes take the min/max, {key,row} pairs keep the better pair (ties: the
+ * smaller global row).  Replaces the per-reduction _combine of datashader's
+ * partitioned (dask) path, dask.py:86-219 / compiler.py:478-507.
+ * Antialiased line bases are rejected (DSGB_E_UNSUPPORTED). */
+int dsgb_combine(const dsgb_base *dst, const dsgb_base *src, int32_t nbases, int64_t ncells, void *stream);
+
 /* ---- Canvas.line, LineAxis0 glyph ----------------------------------------
  * Replaces line.py:59-103 + 1033-1149.  line_width == 0 draws Bresenham
  * lines, > 0 antialiased lines; overwrite / use_2_stage_agg follow

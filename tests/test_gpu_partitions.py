@@ -1,0 +1,66 @@
+"""Partitioned sources: every row partition aggregated into its own partial
+bases, combined elementwise (dsgb_combine), finalized once, must equal the
+same rows as one frame (datashader's dask path, dask.py:86-219).  Bit-exact
+except float64 sums (1e-12 relative: another addition order)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import datashader_gb300 as ds
+from datashader_gb300 import synthetic
+from gpu_helpers import assert_same, to_numpy
+
+pytestmark = pytest.mark.gpu
+
+
+def _cols(n, seed):
+    rng = np.random.default_rng(seed)
+    x, y = synthetic.gaussian_mixture_np(n, seed=seed, dtype=np.float32)
+    v = rng.lognormal(0.0, 1.0, n)
+    v[rng.random(n) < 0.05] = np.nan
+    cat = rng.integers(0, 6, n).astype(np.int8)
+    return {"x": x, "y": y, "v": v, "cat": cat}
+
+
+def _frame(cols, lo=0, hi=None, offset=0):
+    t = {k: torch.from_numpy(np.ascontiguousarray(v[lo:hi])).cuda() for k, v in cols.items()}
+    return ds.TensorFrame(t, categories={"cat": list(range(6))}, row_offset=offset)
+
+
+AGG = ds.summary(count=ds.count(), s=ds.sum("v"), m=ds.mean("v"), mx=ds.max("v"), mn=ds.min("v"),
+                 w=ds.where(ds.max("v")), wmin=ds.where(ds.min("v")), by=ds.by("cat", ds.count()),
+                 any=ds.any("v"))
+
+
+@pytest.mark.parametrize("cuts", [(0, 1_200_000), (0, 37, 400_001, 1_999_999, 2_000_000)])
+def test_partitions_equal_one_frame(cuts):
+    n = 2_000_000
+    cols = _cols(n, seed=21)
+    whole = to_numpy(ds.Canvas(600, 400, (-4, 4), (-3, 3)).points(_frame(cols), "x", "y", AGG))
+    bounds = list(cuts) + [n] if cuts[-1] != n else list(cuts)
+    parts = [_frame(cols, a, b) for a, b in zip(bounds[:-1], bounds[1:])]
+    got = to_numpy(ds.Canvas(600, 400, (-4, 4), (-3, 3)).points(ds.PartitionedFrame(parts), "x", "y", AGG))
+    for k in whole:
+        if k in ("s", "m"):
+            assert_same(got[k], whole[k], rtol=1e-12, what=k)
+        else:
+            assert_same(got[k], whole[k], what=k)
+
+
+def test_partitions_autorange_and_count_path():
+    cols = _cols(3_000_000, seed=22)
+    cvs = ds.Canvas(1024, 1024)
+    whole = cvs.points(_frame(cols), "x", "y", ds.count())
+    parts = ds.PartitionedFrame([_frame(cols, 0, 1_500_000), _frame(cols, 1_500_000)])
+    got = cvs.points(parts, "x", "y", ds.count())
+    assert got.attrs["x_range"] == whole.attrs["x_range"] and got.attrs["y_range"] == whole.attrs["y_range"]
+    assert_same(to_numpy(got), to_numpy(whole))
+
+
+def test_partitions_reject_gathered_lookups():
+    cols = _cols(1000, seed=23)
+    parts = ds.PartitionedFrame([_frame(cols, 0, 500), _frame(cols, 500)])
+    with pytest.raises(NotImplementedError):
+        ds.Canvas(16, 16, (-4, 4), (-4, 4)).points(parts, "x", "y", ds.first("v"))
