@@ -139,7 +139,7 @@ EXPORTED = (
     "dsgb_points_ws", "dsgb_points_segments",
     "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_axis0_backward",
     "dsgb_points_backward", "dsgb_bounds", "dsgb_eq_hist_workspace_size", "dsgb_eq_hist_u32",
-    "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_pyramid_tile_offset", "dsgb_pyramid_workspace_size", "dsgb_pyramid", "dsgb_pyramid_status",
+    "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_shade_workspace_size", "dsgb_shade_u32", "dsgb_shade_f64", "dsgb_pyramid_tile_offset", "dsgb_pyramid_workspace_size", "dsgb_pyramid", "dsgb_pyramid_status",
 )
 
 _lock = threading.Lock()
@@ -182,6 +182,10 @@ def _declare(L):
     L.dsgb_eq_hist_workspace_size.restype = ctypes.c_size_t
     for nm in ("dsgb_eq_hist_u32", "dsgb_eq_hist_f64"):
         getattr(L, nm).argtypes = [P, i64, i32, P, P, P, P, i32, i32, i32, P, ctypes.c_size_t, P]
+    L.dsgb_shade_workspace_size.argtypes = []
+    L.dsgb_shade_workspace_size.restype = ctypes.c_size_t
+    for nm in ("dsgb_shade_u32", "dsgb_shade_f64"):
+        getattr(L, nm).argtypes = [P, i64, i32, P, P, i32, P, i32, i32, P, P, ctypes.c_size_t, P]
     L.dsgb_eq_hist_u32_static.argtypes = [P, i64, i32, P, P, P, P, i32, i32, i32, P]
     L.dsgb_pyramid_tile_offset.argtypes = [i32, i32, i32]
     L.dsgb_pyramid_tile_offset.restype = i64
@@ -192,7 +196,7 @@ def _declare(L):
     L.dsgb_pyramid_status.argtypes = [P, i64, i32, ctypes.POINTER(PyramidConfig), P, P]
     non_int = ("dsgb_last_error", "dsgb_eq_hist_workspace_size", "dsgb_pyramid_tile_offset",
                "dsgb_points_workspace_size", "dsgb_pyramid_workspace_size", "dsgb_bucket_sort_workspace_size",
-               "dsgb_points_workspace_size_flags")
+               "dsgb_points_workspace_size_flags", "dsgb_shade_workspace_size")
     for nm in EXPORTED:
         if nm not in non_int:
             getattr(L, nm).restype = ctypes.c_int

@@ -18,6 +18,7 @@
 // Four launches: min/max, histogram (shared-memory privatised low bins),
 // one-block scan (cdf, levels, span), apply (cdf lookup / interp + RGBA).
 #include "dsgb_internal.cuh"
+#include "shade_common.cuh"
 
 #include <cmath>
 #include <mutex>
@@ -64,15 +65,7 @@ static EqLayout layout(void *ws, int nbins) {
     return L;
 }
 
-__device__ __forceinline__ unsigned long long ord64(double v) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double unord64(unsigned long long u) {
-    unsigned long long b = (u >> 63) ? (u & 0x7fffffffffffffffull) : ~u;
-    return __longlong_as_double((long long)b);
-}
-__device__ __forceinline__ double dnan() { return __longlong_as_double(0x7ff8000000000000ll); }
+
 
 template <typename T> __device__ __forceinline__ bool masked(T v);
 template <> __device__ __forceinline__ bool masked<unsigned int>(unsigned int v) { return v == 0u; }
@@ -187,30 +180,6 @@ __global__ void __launch_bounds__(512) eqh_hist(const T *data, int64_t n, const 
     const int lim = nbins < SMEM_BINS ? nbins : SMEM_BINS;
     for (int j = threadIdx.x; j < lim; j += blockDim.x)
         if (sh[j]) atomicAdd(&hist[j], sh[j]);
-}
-
-// np.interp(x, xp, fp) for sorted xp (left = fp[0], right = fp[-1]).
-__device__ __forceinline__ double np_interp(double x, const double *xp, const double *fp, int len,
-                                            double left, double right) {
-    if (x != x) return x;
-    if (x > xp[len - 1]) return right;
-    if (x < xp[0]) return left;
-    int lo = 0, hi = len - 1;          // invariant xp[lo] <= x, and x < xp[hi] or hi = len-1
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (xp[mid] <= x) lo = mid; else hi = mid;
-    }
-    int j = lo;
-    if (x >= xp[len - 1]) j = len - 1;
-    if (j == len - 1) return fp[j];
-    if (xp[j] == x) return fp[j];
-    double slope = __ddiv_rn(__dsub_rn(fp[j + 1], fp[j]), __dsub_rn(xp[j + 1], xp[j]));
-    double r = __dadd_rn(__dmul_rn(slope, __dsub_rn(x, xp[j])), fp[j]);
-    if (r != r) {
-        r = __dadd_rn(__dmul_rn(slope, __dsub_rn(x, xp[j + 1])), fp[j + 1]);
-        if (r != r && fp[j] == fp[j + 1]) r = fp[j];
-    }
-    return r;
 }
 
 // One block: cumulative sums, cdf, levels, the float-path compaction and the span.

@@ -1,11 +1,11 @@
-"""tf.shade(how='eq_hist') and eq_hist on the GPU.
+"""tf.shade (how='eq_hist' | 'linear' | 'log' | 'cbrt') and eq_hist on the GPU.
 
 Mirrors datashader/transfer_functions/__init__.py: shade (616-745) for 2-D
-aggregates with a list colormap, the _interpolate prologue (251-297),
-eq_hist (148-223), _rescale_discrete_levels (234-248) and the list-colormap
-RGBA branch (317-351).  The histogram, CDF, lookup and colouring run in one
-libdsgb call (eq_hist.cu); other ``how`` values and colormap kinds are
-outside the GPU path.
+aggregates, the _interpolate prologue (251-297), eq_hist (148-223),
+_rescale_discrete_levels (234-248), the linear / log / cbrt interpolators
+(220-223) and the list-colormap and single-colour RGBA branches (317-351).
+Each shade is one libdsgb call (eq_hist.cu, shade.cu); matplotlib colormap
+callables and categorical (3-D) shading are outside the GPU path.
 """
 from __future__ import annotations
 
@@ -115,9 +115,49 @@ def eq_hist_agg(agg, nbins=256 * 256):
     return out, int(levels.item())
 
 
+_HOW_CODE = {"linear": 0, "log": 1, "cbrt": 2}
+
+
+def _run_shade(data, how, cmap, alpha, min_alpha, span, stream=None):
+    """One libdsgb shade call (how in linear / log / cbrt).  Returns the RGBA tensor."""
+    if data.dtype == torch.uint32:
+        fn = N.lib().dsgb_shade_u32
+    elif data.dtype == torch.float64:
+        fn = N.lib().dsgb_shade_f64
+    else:
+        raise NotImplementedError(f"shade on the GPU path takes uint32 or float64 aggregates, not {data.dtype}")
+    data = data.contiguous()
+    dev = data.device
+    if stream is None:
+        stream = torch.cuda.current_stream(dev).cuda_stream
+    single = isinstance(cmap, str) or (isinstance(cmap, tuple) and len(cmap) == 3 and
+                                       not isinstance(cmap[0], str))
+    cmap_buf, ncol, single_buf = None, 0, None
+    if single:
+        single_buf = (ctypes.c_uint8 * 3)(*rgb(cmap))
+    else:
+        cols = [rgb(c) for c in cmap]
+        if not 1 <= len(cols) <= 16:
+            raise ValueError("colormap must have 1..16 colours")
+        ncol = len(cols)
+        cmap_buf = (ctypes.c_uint8 * (3 * ncol))(*[v for c in cols for v in c])
+    span_buf = (ctypes.c_double * 2)(float(span[0]), float(span[1])) if span is not None else None
+    rgba = torch.empty(data.shape, dtype=torch.uint32, device=dev)
+    size = int(N.lib().dsgb_shade_workspace_size())
+    ws = _WS.get(("shade", dev))
+    if ws is None:
+        ws = torch.empty(size, dtype=torch.uint8, device=dev)
+        _WS[("shade", dev)] = ws
+    N.check(fn(data.data_ptr(), data.numel(), _HOW_CODE[how], span_buf, cmap_buf, ncol, single_buf, int(alpha),
+               int(min_alpha), rgba.data_ptr(), ws.data_ptr(), ws.numel(), stream), "dsgb_shade")
+    return rgba
+
+
 def shade(agg, cmap=("lightblue", "darkblue"), color_key=None, how="eq_hist", alpha=255,
           min_alpha=40, span=None, name=None, color_baseline=None, rescale_discrete_levels=False):
-    """tf.shade for a 2-D aggregate, how='eq_hist', list colormap."""
+    """tf.shade for a 2-D aggregate (transfer_functions/__init__.py:616-745):
+    how in eq_hist / linear / log / cbrt; a list colormap, or one colour with
+    an alpha ramp (linear / log / cbrt)."""
     if not isinstance(agg, Aggregate):
         raise TypeError("agg must be instance of DataArray")
     name = agg.name if name is None else name
@@ -125,8 +165,13 @@ def shade(agg, cmap=("lightblue", "darkblue"), color_key=None, how="eq_hist", al
         raise ValueError(f"min_alpha ({min_alpha}) and alpha ({alpha}) must be between 0 and 255")
     if agg.ndim != 2:
         raise NotImplementedError("only 2-D aggregates are shaded on the GPU path")
+    if how in _HOW_CODE:
+        if span is not None and not span[0] <= span[1]:
+            raise ValueError("span must be (low, high)")
+        rgba = _run_shade(agg.data, how, cmap, alpha, min_alpha, span)
+        return Image(rgba, agg.dims, agg.coords, agg.attrs, name=name)
     if how != "eq_hist":
-        raise NotImplementedError("only how='eq_hist' is on the GPU path")
+        raise ValueError(f"Unknown interpolation method: {how}")
     if span is not None:
         raise ValueError("span is not (yet) valid to use with eq_hist")
     if isinstance(cmap, str) or not isinstance(cmap, (list, tuple)):

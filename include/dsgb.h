@@ -284,6 +284,22 @@ int dsgb_eq_hist_u32_static(const uint32_t *data, int64_t n, int32_t nbins,
                             const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
                             int32_t rescale_discrete_levels, void *stream);
 
+/* tf.shade(how='linear' | 'log' | 'cbrt') of a 2-D aggregate
+ * (transfer_functions/__init__.py:220-356): how 0 = linear, 1 = log,
+ * 2 = cbrt; span (host, 2 doubles) or NULL; a list colormap (cmap_rgb,
+ * ncolors <= 16) or, when single_rgb != NULL, one colour with an alpha
+ * ramp from min_alpha to alpha.  rgba: uint32 per pixel.  The workspace is
+ * dsgb_shade_workspace_size() bytes, 256-byte aligned. */
+size_t dsgb_shade_workspace_size(void);
+int dsgb_shade_u32(const uint32_t *data, int64_t n, int32_t how, const double *span,
+                   const uint8_t *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb,
+                   int32_t alpha, int32_t min_alpha, uint32_t *rgba,
+                   void *workspace, size_t workspace_bytes, void *stream);
+int dsgb_shade_f64(const double *data, int64_t n, int32_t how, const double *span,
+                   const uint8_t *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb,
+                   int32_t alpha, int32_t min_alpha, uint32_t *rgba,
+                   void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- batched tile pyramid --------------------------------------------------
  * Every tile (z, tx, ty), zmin <= z <= zmax, of the square [x0,x1]x[y0,y1]
  * in one pass: tile (z, tx, ty) equals

@@ -291,4 +291,4 @@ def line_axis0(cols, x, y, width, height, x_range, y_range, specs, line_width=0.
     return _finalize(specs, keep)
 
 
-from .eq_hist import eq_hist, shade_eq_hist, interpolate_prologue  # noqa: E402,F401
+from .eq_hist import eq_hist, shade_eq_hist, shade_interp, interpolate_prologue  # noqa: E402,F401

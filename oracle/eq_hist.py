@@ -106,3 +106,50 @@ def shade_eq_hist(agg, cmap=("lightblue", "darkblue"), alpha=255, rescale_discre
     b = np.nan_to_num(np.interp(data, span, chans[2], left=255), copy=False).astype(np.uint8)
     a = np.where(np.isnan(data), 0, alpha).astype(np.uint8)
     return np.dstack([r, g, b, a]).view(np.uint32).reshape(data.shape)
+
+
+_HOW = {"log": lambda d, m: np.log1p(np.where(m, np.nan, d)),          # transfer_functions/__init__.py:220-223
+        "cbrt": lambda d, m: np.where(m, np.nan, d) ** (1 / 3.),
+        "linear": lambda d, m: np.where(m, np.nan, d)}
+
+
+def shade_interp(agg, how="linear", cmap=("lightblue", "darkblue"), alpha=255, min_alpha=40, span=None):
+    """tf.shade(agg, cmap, how in {linear, log, cbrt}, span) for a 2-D uint32 or float64
+    aggregate -> uint32 RGBA (transfer_functions/__init__.py:251-356).  ``cmap`` is a list
+    of colours, or one colour (str or RGB tuple) for the alpha-ramp branch."""
+    f = _HOW[how]
+    data = agg.copy()
+    mask = data == 0 if data.dtype.kind == "u" else np.isnan(data)
+    if mask.all():
+        return np.zeros(agg.shape, dtype=np.uint32)
+    if span is None:
+        offset = np.nanmin(data[~mask])
+    else:
+        offset = np.array(span, dtype=data.dtype)[0]
+        lo, hi = np.array(span, dtype=data.dtype)
+        data = np.where(mask, data, np.clip(data, lo, hi))              # masked_clip_2d
+    data -= offset
+    with np.errstate(invalid="ignore", divide="ignore"):
+        data = f(data, mask)
+        if span is None:
+            masked = np.where(~mask, data, np.nan)
+            span = np.nanmin(masked), np.nanmax(masked)
+        else:
+            span = f(np.array([0, span[1] - span[0]], dtype=np.float64), 0)
+    single = isinstance(cmap, str) or (isinstance(cmap, tuple) and not isinstance(cmap[0], str))
+    if not single:
+        chans = np.array([rgb(c) for c in cmap], dtype=np.float64).T
+        sp = np.linspace(span[0], span[1], len(cmap))
+        r = np.nan_to_num(np.interp(data, sp, chans[0], left=255), copy=False).astype(np.uint8)
+        g = np.nan_to_num(np.interp(data, sp, chans[1], left=255), copy=False).astype(np.uint8)
+        b = np.nan_to_num(np.interp(data, sp, chans[2], left=255), copy=False).astype(np.uint8)
+        a = np.where(np.isnan(data), 0, alpha).astype(np.uint8)
+    else:
+        color = rgb(cmap)
+        aspan = np.arange(min_alpha, alpha + 1)
+        sp = np.linspace(span[0], span[1], len(aspan))
+        r = np.full(data.shape, color[0], dtype=np.uint8)
+        g = np.full(data.shape, color[1], dtype=np.uint8)
+        b = np.full(data.shape, color[2], dtype=np.uint8)
+        a = np.nan_to_num(np.interp(data, sp, aspan, left=0, right=255), copy=False).astype(np.uint8)
+    return np.dstack([r, g, b, a]).view(np.uint32).reshape(data.shape)

@@ -7,7 +7,9 @@ Reads (as text, via ``ast``; nothing from the reference is imported or run):
   ``line_antialias_df`` input frame and the LineAxis0 entry of
   ``line_antialias_nan_params``;
 * ``datashader/tests/test_transfer_functions.py`` -- ``eq_hist_sol`` and
-  ``eq_hist_sol_rescale_discrete_levels`` (uint32 RGBA images).
+  ``eq_hist_sol_rescale_discrete_levels`` (uint32 RGBA images), the
+  linear / log / cbrt ``solution_lists`` and the ``sol`` arrays of
+  ``test_span_cmap_single`` and ``test_shade_cmap``.
 
 Usage::
 
@@ -108,7 +110,31 @@ def main(ref_root):
             eq[name] = dict(_jsonable(val), source=src)
     with open(os.path.join(HERE, "eq_hist.json"), "w") as f:
         json.dump(eq, f, indent=0)
-    print("wrote", sorted(goldens), sorted(eq))
+
+    shade = {}
+    for name, (val, line) in _literal_assignments(tf_path, ("solution_lists",)).items():
+        src = f"datashader/tests/test_transfer_functions.py:{line}"
+        shade[name] = {how: dict(_jsonable(np.array(v, dtype="u4")), source=src) for how, v in val.items()}
+    for fn, (val, line) in _function_sols(tf_path, ("test_span_cmap_single", "test_shade_cmap")).items():
+        shade[fn] = dict(_jsonable(np.array(val, dtype="u4")), source=f"datashader/tests/test_transfer_functions.py:{line}")
+    with open(os.path.join(HERE, "shade.json"), "w") as f:
+        json.dump(shade, f, indent=0)
+    print("wrote", sorted(goldens), sorted(eq), sorted(shade))
+
+
+def _function_sols(path, names):
+    """The first literal ``sol = np.array(...)`` inside each named test function."""
+    tree = ast.parse(open(path).read())
+    out = {}
+    for node in tree.body:
+        if isinstance(node, ast.FunctionDef) and node.name in names:
+            for st in node.body:
+                if (isinstance(st, ast.Assign) and isinstance(st.targets[0], ast.Name) and st.targets[0].id == "sol"
+                        and isinstance(st.value, ast.Call)):
+                    code = compile(ast.Expression(st.value), path, "eval")
+                    out[node.name] = (eval(code, {"np": np}), st.lineno)
+                    break
+    return out
 
 
 if __name__ == "__main__":

@@ -268,3 +268,22 @@ def eq_hist_agg_a():
     c = np.arange(10, 19, dtype="f8").reshape((3, 3))
     c[[0, 1, 2], [0, 1, 2]] = np.nan
     return a, c
+
+
+def shade_golden(key, how=None):
+    """test_transfer_functions.py solution images (uint32 RGBA) from tests/golden/shade.json."""
+    g = load_golden("shade.json", key)
+    return golden_array(g[how] if how is not None else g)
+
+
+def span_variants(x, sol):
+    """check_span (test_transfer_functions.py:130-149): mask one pixel, then also
+    the largest value; the masked pixels become transparent."""
+    x = x.copy()
+    sol = sol.copy()
+    x[0, 1] = 0 if x.dtype.kind in "iu" else np.nan
+    sol[0, 1] = sol[0, 0]
+    yield x.copy(), sol.copy()
+    x[2, 1] = 0 if x.dtype.kind in "iu" else np.nan
+    sol[2, 1] = sol[0, 0]
+    yield x.copy(), sol.copy()

@@ -10,6 +10,7 @@ accumulates them in float32, the GPU in float64).
 from __future__ import annotations
 
 import numpy as np
+import torch
 import pytest
 
 import datashader_gb300 as ds
@@ -87,3 +88,72 @@ def test_gpu_eq_hist_rgba_golden():
         got = img.data.view(torch.int32).cpu().numpy().view(np.uint32)
         np.testing.assert_array_equal(got, sol)
         np.testing.assert_array_equal(got, oracle.shade_eq_hist(data, ["pink", "red"]))
+
+
+# ---- tf.shade(how='linear' | 'log' | 'cbrt') on the GPU ------------------
+
+def _shade_gpu(data, how, cmap, span=None):
+    if data.dtype == np.uint32:
+        t = torch.from_numpy(data.view(np.int32)).cuda().view(torch.uint32)
+    else:
+        t = torch.from_numpy(data).cuda()
+    agg = ds.Aggregate(t, ["y", "x"], {}, {})
+    img = ds.tf.shade(agg, cmap=cmap, how=how, span=span)
+    return img.data.view(torch.int32).cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("how", ["linear", "log", "cbrt"])
+@pytest.mark.parametrize("span", [None, [11, 17], [11.0, 17.0]])
+def test_gpu_shade_interp_golden(how, span):
+    """test_transfer_functions.py:175-193 for the u4 and f8 aggregates, and the
+    check_span variants (:130-149)."""
+    a, c = refcases.eq_hist_agg_a()
+    sol = refcases.shade_golden("solution_lists", how)
+    for agg in (a, c):
+        np.testing.assert_array_equal(_shade_gpu(agg, how, ["pink", "red"], span), sol)
+        if span is not None:
+            for x, s in refcases.span_variants(agg, sol):
+                np.testing.assert_array_equal(_shade_gpu(x, how, ("#FFC0CB", "#FF0000"), span), s)
+
+
+@pytest.mark.parametrize("cmap", ["black", (0, 0, 0), "#000000"])
+def test_gpu_shade_single_colour_and_three_colours(cmap):
+    a, _ = refcases.eq_hist_agg_a()
+    sol = refcases.shade_golden("test_span_cmap_single")
+    np.testing.assert_array_equal(_shade_gpu(a, "log", cmap), sol)
+    for x, s in refcases.span_variants(a, sol):
+        np.testing.assert_array_equal(_shade_gpu(x, "log", cmap, [11.0, 17.0]), s)
+    np.testing.assert_array_equal(_shade_gpu(a, "log", ["red", (0, 255, 0), "#0000FF"]),
+                                  refcases.shade_golden("test_shade_cmap"))
+
+
+@pytest.mark.parametrize("how", ["linear", "log", "cbrt"])
+def test_gpu_shade_large_vs_oracle(how):
+    """Count and float64 aggregates of real size against the numpy restatement:
+    linear bit-identical; log / cbrt call CUDA's log1p / pow and numpy the C
+    library's, so a channel may differ by one step on a colour boundary."""
+    rng = np.random.default_rng(3)
+    cnt = rng.poisson(rng.gamma(0.5, 30.0, (700, 900))).astype(np.uint32)
+    val = rng.lognormal(0.0, 2.0, (700, 900))
+    val[rng.random(val.shape) < 0.3] = np.nan
+    for data in (cnt, val):
+        for cmap in (["lightblue", "darkblue"], ["red", (0, 255, 0), "#0000FF", "white"], "black"):
+            got = _shade_gpu(data, how, cmap)
+            ref = oracle.shade_interp(data, how, cmap)
+            g = got.view(np.uint8).astype(int)
+            r = ref.view(np.uint8).astype(int)
+            if how == "linear":
+                np.testing.assert_array_equal(got, ref)
+            else:
+                assert np.abs(g - r).max() <= 1
+                assert (g != r).mean() < 1e-3
+            span = (float(np.nanpercentile(data[data > 0] if data.dtype.kind == "u" else data, 20)),
+                    float(np.nanpercentile(data[data > 0] if data.dtype.kind == "u" else data, 80)))
+            if data.dtype.kind == "u":
+                span = (int(span[0]), int(span[1]))
+            got = _shade_gpu(data, how, cmap, span)
+            ref = oracle.shade_interp(data, how, cmap, span=span)
+            if how == "linear":
+                np.testing.assert_array_equal(got, ref)
+            else:
+                assert np.abs(got.view(np.uint8).astype(int) - ref.view(np.uint8).astype(int)).max() <= 1

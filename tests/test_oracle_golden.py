@@ -115,3 +115,42 @@ def test_oracle_mutation_is_caught():
     cols["x"][0] = 1.0           # move one row to the other column of pixels
     got = run_points(cols, cats, ds.count(), refcases.C2)
     assert not np.array_equal(got, np.array([[5, 5], [5, 5]]))
+
+
+# ---- tf.shade(how='linear' | 'log' | 'cbrt') -----------------------------
+
+@pytest.mark.parametrize("how", ["linear", "log", "cbrt"])
+@pytest.mark.parametrize("span", [None, [11, 17], [11.0, 17.0]])
+def test_oracle_shade_interp_golden(how, span):
+    """test_transfer_functions.py:175-193 (test_shade) for the u4 and f8 aggregates."""
+    a, c = refcases.eq_hist_agg_a()
+    sol = refcases.shade_golden("solution_lists", how)
+    for agg in (a, c):
+        np.testing.assert_array_equal(oracle.shade_interp(agg, how, ["pink", "red"], span=span), sol)
+
+
+@pytest.mark.parametrize("how", ["linear", "log", "cbrt"])
+@pytest.mark.parametrize("cmap", [["pink", "red"], ("#FFC0CB", "#FF0000")])
+def test_oracle_shade_span_cmap_list(how, cmap):
+    """test_span_cmap_list / check_span (test_transfer_functions.py:130-149, 214-222)."""
+    a, c = refcases.eq_hist_agg_a()
+    for agg in (a, c):
+        for x, sol in refcases.span_variants(agg, refcases.shade_golden("solution_lists", how)):
+            np.testing.assert_array_equal(oracle.shade_interp(x, how, cmap, span=[11.0, 17.0]), sol)
+
+
+@pytest.mark.parametrize("cmap", ["black", (0, 0, 0), "#000000"])
+def test_oracle_shade_single_colour(cmap):
+    """test_span_cmap_single and test_shade_cmap_non_categorical_alpha (:225-239, 282-290)."""
+    a, _ = refcases.eq_hist_agg_a()
+    sol = refcases.shade_golden("test_span_cmap_single")
+    np.testing.assert_array_equal(oracle.shade_interp(a, "log", cmap), sol)
+    for x, s in refcases.span_variants(a, sol):
+        np.testing.assert_array_equal(oracle.shade_interp(x, "log", cmap, span=[11.0, 17.0]), s)
+
+
+def test_oracle_shade_three_colours():
+    """test_shade_cmap (:272-279)."""
+    a, _ = refcases.eq_hist_agg_a()
+    np.testing.assert_array_equal(oracle.shade_interp(a, "log", ["red", (0, 255, 0), "#0000FF"]),
+                                  refcases.shade_golden("test_shade_cmap"))
