@@ -21,7 +21,8 @@ import torch
 from . import _native as N
 from . import reductions as rd
 from .compiler import compile_plan
-from .glyphs import Point, LineAxis0
+from .glyphs import (Point, LineAxis0, LineAxis0Multi, LinesAxis1, LinesAxis1XConstant,
+                     LinesAxis1YConstant, _MultiLine)
 
 
 # ----------------------------------------------------------------- sources
@@ -333,10 +334,7 @@ class Canvas:
                              "antialias keyword arguments; use line_width instead.")
         if antialias:
             line_width = 1.0
-        if axis != 0 or not (isinstance(x, (Number, str)) and isinstance(y, (Number, str))):
-            raise NotImplementedError("only the LineAxis0 glyph (axis=0, one x and one y column) "
-                                      "is on the GPU path")
-        glyph = LineAxis0(x, y)
+        glyph = _line_glyph(x, y, axis)
         glyph.set_line_width(line_width)
         if glyph.antialiased:
             non_cat = agg.reduction if isinstance(agg, rd.by) else agg
@@ -345,6 +343,11 @@ class Canvas:
                                         rd._max_or_min_row_index, rd.where)):
                 raise NotImplementedError(
                     f"{type(non_cat)} reduction not implemented for antialiased lines")
+        if glyph.antialiased and isinstance(glyph, _MultiLine):
+            from .compiler import compile_plan as _cp
+            if _cp(agg, as_frame(source), antialias=True).use_2_stage:
+                raise NotImplementedError("two-stage antialiased reductions over several lines are not on the "
+                                          "GPU path")
         return bypixel(source, self, glyph, agg, antialias=glyph.antialiased)
 
     def validate_ranges(self, x_range, y_range):
@@ -358,6 +361,57 @@ class Canvas:
     def validate(self):
         self.validate_ranges(self.x_range, self.y_range)
         self.validate_size(self.plot_width, self.plot_height)
+
+
+def _broadcast_columns(x, y):
+    """core.py:1433-1443: a single column name against a list becomes a list."""
+    lengths = {len(a) for a in (x, y) if isinstance(a, (list, tuple))}
+    if len(lengths) != 1:
+        return x, y
+    n = lengths.pop()
+    return tuple((a,) * n if isinstance(a, (Number, str)) else a for a in (x, y))
+
+
+def _line_glyph(x, y, axis):
+    """core.py:412-456: the glyph for the x / y / axis combination."""
+    ox, oy = x, y
+    x, y = _broadcast_columns(x, y)
+    if axis == 0:
+        if isinstance(x, (Number, str)) and isinstance(y, (Number, str)):
+            return LineAxis0(x, y)
+        if isinstance(x, (list, tuple)) and isinstance(y, (list, tuple)):
+            return LineAxis0Multi(tuple(x), tuple(y))
+        raise ValueError(f"Invalid combination of x and y arguments to Canvas.line when axis=0.\n"
+                         f"    Received:\n        x: {ox!r}\n        y: {oy!r}")
+    if axis == 1:
+        if isinstance(x, (list, tuple)) and isinstance(y, (list, tuple)):
+            return LinesAxis1(tuple(x), tuple(y))
+        if isinstance(x, np.ndarray) and isinstance(y, (list, tuple)):
+            return LinesAxis1XConstant(x, tuple(y))
+        if isinstance(x, (list, tuple)) and isinstance(y, np.ndarray):
+            return LinesAxis1YConstant(tuple(x), y)
+        if isinstance(x, (Number, str)) and isinstance(y, (Number, str)):
+            raise NotImplementedError("ragged-array lines (LinesAxis1Ragged) are not on the GPU path")
+        raise ValueError(f"Invalid combination of x and y arguments to Canvas.line when axis=1.\n"
+                         f"    Received:\n        x: {ox!r}\n        y: {oy!r}")
+    raise ValueError(f"The axis argument to Canvas.line must be 0 or 1\n    Received: {axis}")
+
+
+def _vertex_array(frame, spec, nrows):
+    """float64 vertex array of a multi-line glyph: [nrows][len(spec)] from the
+    columns, or the constant numpy array itself (1-D)."""
+    if isinstance(spec, np.ndarray):
+        return torch.as_tensor(np.ascontiguousarray(spec, dtype=np.float64), device=frame.device)
+    cols = [frame[c].to(torch.float64) for c in spec]
+    return torch.stack(cols, dim=1).contiguous() if cols else torch.empty((nrows, 0), dtype=torch.float64,
+                                                                         device=frame.device)
+
+
+def _array_bounds(t, stream):
+    col = N.Column(t.data_ptr(), N.F64, 0)
+    out = torch.empty(2, dtype=torch.float64, device=t.device)
+    N.check(N.lib().dsgb_bounds(ctypes.byref(col), t.numel(), out.data_ptr(), stream), "dsgb_bounds")
+    return _expand_bounds(*out.cpu().tolist())
 
 
 def bypixel(source, canvas, glyph, agg, *, antialias=False, flags=0):
@@ -408,7 +462,11 @@ class Executor:
         self.plan = plan
         self.glyph = glyph
         derived = _derived_columns(frame, plan)
-        names = [glyph.x, glyph.y] + [c for c in plan.columns if c not in (glyph.x, glyph.y)]
+        if isinstance(glyph, _MultiLine):
+            # vertices travel separately (dsgb_lines); the columns are the appends' fields
+            names = list(plan.columns)
+        else:
+            names = [glyph.x, glyph.y] + [c for c in plan.columns if c not in (glyph.x, glyph.y)]
         self.names = names
         self.tensors = [derived[n] if n in derived else frame[n] for n in names]
         self.col_index = {n: i for i, n in enumerate(names)}
@@ -478,8 +536,14 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
     if stream is None:
         stream = torch.cuda.current_stream(frame.device).cuda_stream
     plan = compile_plan(agg, frame, antialias=antialias)
-    x_range = canvas.x_range or _column_bounds(frame, glyph.x, stream)
-    y_range = canvas.y_range or _column_bounds(frame, glyph.y, stream)
+    if isinstance(glyph, _MultiLine):
+        xs = _vertex_array(frame, glyph.x, len(frame))
+        ys = _vertex_array(frame, glyph.y, len(frame))
+        x_range = canvas.x_range or _array_bounds(xs, stream)
+        y_range = canvas.y_range or _array_bounds(ys, stream)
+    else:
+        x_range = canvas.x_range or _column_bounds(frame, glyph.x, stream)
+        y_range = canvas.y_range or _column_bounds(frame, glyph.y, stream)
     canvas.validate_ranges(x_range, y_range)
     width, height = canvas.plot_width, canvas.plot_height
     x_st = canvas.x_axis.compute_scale_and_translate(x_range, width)
@@ -497,6 +561,26 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
                                float(glyph.line_width), 1, int(plan.overwrite), int(plan.use_2_stage),
                                ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
         N.check(rc, "dsgb_line_axis0")
+    elif isinstance(glyph, _MultiLine):
+        if glyph.layout == 1 and len(glyph.x) > 1 and any(
+                b.op in (N.BASE_MIN_ROW, N.BASE_MAX_ROW, N.BASE_ARGMAX, N.BASE_ARGMIN) for b in plan.bases):
+            # the reference visits line j outer, row i inner (line.py:1190-1194), so first / last /
+            # where follow (line, row) order, not the row order that row-index bases keep
+            raise NotImplementedError("first / last / where over several axis=0 lines are not on the GPU path")
+        if glyph.layout == 1:
+            nv, xrow, yrow = xs.shape[1], xs.shape[1], ys.shape[1]
+        else:
+            nv = xs.shape[-1] if xs.dim() == 2 else ys.shape[-1]
+            xrow = nv if xs.dim() == 2 else 0
+            yrow = nv if ys.dim() == 2 else 0
+        cols, ncols = ex.cols, len(ex.names)
+        if ncols == 0:                       # count() / any(): no field column, any valid pointer
+            cols = (N.Column * 1)(N.Column(ys.data_ptr(), N.F64, 0))
+            ncols = 1
+        rc = L.dsgb_lines(cols, ncols, len(frame), frame.row_offset, glyph.layout, xs.data_ptr(), ys.data_ptr(),
+                          nv, xrow, yrow, ctypes.byref(cv), float(glyph.line_width), 1, int(plan.overwrite),
+                          ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
+        N.check(rc, "dsgb_lines")
     else:
         wsz = int(L.dsgb_points_workspace_size_flags(len(frame), ctypes.byref(cv), ex.bases, len(plan.bases),
                                                      flags))

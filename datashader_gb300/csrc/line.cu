@@ -300,40 +300,94 @@ __device__ __forceinline__ void map_snap(const LineParams &p, double x, double y
 }
 
 // line.py:1104-1124 + 1045-1095, one segment.
+// One segment of a line (rows' vertices (x0, y0) -> (x1, y1), previous
+// vertex (xm, ym)): clip, map, antialiased coverage or Bresenham
+// (line.py:1033-1097 _build_draw_segment).  `row` is the row whose fields
+// the appends use.
+__device__ void draw_segment(const LineParams &p, int64_t row, double x0, double y0, double x1, double y1,
+                             bool segment_start, bool segment_end, double xm, double ym) {
+    const bool antialias = p.line_width > 0.0;
+    bool skip = isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1);
+    bool cs = false, ce = false;
+    liang_barsky(p.xmin, p.xmax, p.ymin, p.ymax, x0, x1, y0, y1, skip, cs, ce);
+    if (skip) return;
+    const bool clipped = cs || ce;
+    segment_start = segment_start || cs;
+    if (antialias) {
+        // line.py:723-726 map_onto_pixel_no_snap
+        const double px0 = x0 * p.sx + p.tx - 0.5, py0 = y0 * p.sy + p.ty - 0.5;
+        const double px1 = x1 * p.sx + p.tx - 0.5, py1 = y1 * p.sy + p.ty - 0.5;
+        double pxm = 0.0, pym = 0.0;
+        if (!segment_start) { pxm = xm * p.sx + p.tx - 0.5; pym = ym * p.sy + p.ty - 0.5; }
+        const long long nx = pyround((p.xmax - p.xmin) * p.sx);
+        const long long ny = pyround((p.ymax - p.ymin) * p.sy);
+        full_antialias(p, p.line_width, p.overwrite != 0, row, px0, px1, py0, py1,
+                       segment_start, segment_end, pxm, pym, nx, ny);
+    } else {
+        long long ix0, iy0, ix1, iy1;
+        map_snap(p, x0, y0, ix0, iy0);
+        map_snap(p, x1, y1, ix1, iy1);
+        bresenham(p, row, segment_start, ix0, ix1, iy0, iy1, clipped);
+    }
+}
+
 __global__ void __launch_bounds__(256) line_axis0_kernel(const LineParams p) {
     const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
-    const bool antialias = p.line_width > 0.0;
     for (int64_t i = gtid(); i + 1 < p.n; i += gstride()) {
-        double x0 = load_f64(X, i), y0 = load_f64(Y, i);
-        double x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
+        const double x0 = load_f64(X, i), y0 = load_f64(Y, i);
+        const double x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
         // the previous row, with numba's wrap of index -1 onto the last row
         const int64_t im = i > 0 ? i - 1 : p.n - 1;
-        bool segment_start = (i == 0) ? (p.plot_start != 0)
-                                      : (isnull(load_f64(X, im)) || isnull(load_f64(Y, im)));
-        bool segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
+        const bool segment_start = (i == 0) ? (p.plot_start != 0)
+                                            : (isnull(load_f64(X, im)) || isnull(load_f64(Y, im)));
+        const bool segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
         double xm = 0.0, ym = 0.0;
         if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, im); ym = load_f64(Y, im); }
-        bool skip = isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1);
-        bool cs = false, ce = false;
-        liang_barsky(p.xmin, p.xmax, p.ymin, p.ymax, x0, x1, y0, y1, skip, cs, ce);
-        if (skip) continue;
-        const bool clipped = cs || ce;
-        segment_start = segment_start || cs;
-        if (antialias) {
-            // line.py:723-726 map_onto_pixel_no_snap
-            const double px0 = x0 * p.sx + p.tx - 0.5, py0 = y0 * p.sy + p.ty - 0.5;
-            const double px1 = x1 * p.sx + p.tx - 0.5, py1 = y1 * p.sy + p.ty - 0.5;
-            double pxm = 0.0, pym = 0.0;
-            if (!segment_start) { pxm = xm * p.sx + p.tx - 0.5; pym = ym * p.sy + p.ty - 0.5; }
-            const long long nx = pyround((p.xmax - p.xmin) * p.sx);
-            const long long ny = pyround((p.ymax - p.ymin) * p.sy);
-            full_antialias(p, p.line_width, p.overwrite != 0, i, px0, px1, py0, py1,
-                           segment_start, segment_end, pxm, pym, nx, ny);
+        draw_segment(p, i, x0, y0, x1, y1, segment_start, segment_end, xm, ym);
+    }
+}
+
+// Multi-line layouts over float64 vertex arrays.
+//   LAYOUT 1, LineAxis0Multi (line.py:1152-1242): xs, ys [nrows][nlines];
+//       line j runs down the rows; segment (i, j) appends row i; the
+//       segment start and the previous vertex follow LineAxis0.
+//   LAYOUT 2, the LinesAxis1 family (line.py:1244-1437): line i runs along
+//       the nv columns of row i, vertex (i, j) = (xs[i * xrow + j],
+//       ys[i * yrow + j]); xrow = 0 is LinesAxis1XConstant (one x array for
+//       every line), yrow = 0 LinesAxis1YConstant, both nv LinesAxis1;
+//       segment (i, j) appends row i; a segment starts at j == 0 or after a
+//       NaN.
+// Consecutive threads take consecutive array elements (coalesced loads).
+struct LinesGeom {
+    const double *xs, *ys;
+    int64_t nrows, nv;      // LAYOUT 1: nv = lines; LAYOUT 2: nv = vertices per line
+    int64_t xrow, yrow;     // LAYOUT 2: row strides of xs and ys (0 = shared by all rows)
+};
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(256) lines_kernel(const LineParams p, const LinesGeom g) {
+    const int64_t nseg = LAYOUT == 1 ? (g.nrows - 1) * g.nv : g.nrows * (g.nv - 1);
+    for (int64_t s = gtid(); s < nseg; s += gstride()) {
+        if (LAYOUT == 1) {
+            const int64_t i = s / g.nv, j = s - i * g.nv;
+            const double *X = g.xs + j, *Y = g.ys + j;
+            const int64_t st = g.nv;
+            const double x0 = X[i * st], y0 = Y[i * st], x1 = X[(i + 1) * st], y1 = Y[(i + 1) * st];
+            const int64_t im = i > 0 ? i - 1 : g.nrows - 1;
+            const bool segment_start = (i == 0) ? (p.plot_start != 0) : (isnull(X[im * st]) || isnull(Y[im * st]));
+            const bool segment_end = (i == g.nrows - 2) || isnull(X[(i + 2) * st]) || isnull(Y[(i + 2) * st]);
+            double xm = 0.0, ym = 0.0;
+            if (!(segment_start || p.use_2_stage)) { xm = X[im * st]; ym = Y[im * st]; }
+            draw_segment(p, i, x0, y0, x1, y1, segment_start, segment_end, xm, ym);
         } else {
-            long long ix0, iy0, ix1, iy1;
-            map_snap(p, x0, y0, ix0, iy0);
-            map_snap(p, x1, y1, ix1, iy1);
-            bresenham(p, i, segment_start, ix0, ix1, iy0, iy1, clipped);
+            const int64_t i = s / (g.nv - 1), j = s - i * (g.nv - 1);
+            const double *X = g.xs + i * g.xrow, *Y = g.ys + i * g.yrow;
+            const double x0 = X[j], x1 = X[j + 1], y0 = Y[j], y1 = Y[j + 1];
+            const bool segment_start = (j == 0) || isnull(X[j - 1]) || isnull(Y[j - 1]);
+            const bool segment_end = (j == g.nv - 2) || isnull(X[j + 2]) || isnull(Y[j + 2]);
+            double xm = 0.0, ym = 0.0;
+            if (!(segment_start || p.use_2_stage)) { xm = X[j - 1]; ym = Y[j - 1]; }
+            draw_segment(p, i, x0, y0, x1, y1, segment_start, segment_end, xm, ym);
         }
     }
 }
@@ -413,6 +467,58 @@ extern "C" int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n
         if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
         line_axis0_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
         DSGB_CHECK_LAUNCH("line_axis0 kernel");
+    }
+    if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+        rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+    return rc;
+}
+
+extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
+                          int32_t layout, const double *xs, const double *ys, int64_t nv, int64_t x_row_stride,
+                          int64_t y_row_stride, const dsgb_canvas *canvas, double line_width, int32_t plot_start,
+                          int32_t overwrite,
+                          const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                          uint32_t flags, void *stream) {
+    if (layout != 1 && layout != 2) {
+        set_error("dsgb_lines: layout must be 1 (LineAxis0Multi) or 2 (LinesAxis1 family)");
+        return DSGB_E_INVALID;
+    }
+    if (layout == 2 && ((x_row_stride != 0 && x_row_stride != nv) || (y_row_stride != 0 && y_row_stride != nv))) {
+        set_error("dsgb_lines: row strides must be 0 (shared) or nv");
+        return DSGB_E_INVALID;
+    }
+    if (nrows < 0 || nv < 1 || (nrows > 0 && (!xs || !ys))) {
+        set_error("dsgb_lines: invalid vertex arrays");
+        return DSGB_E_INVALID;
+    }
+    LineParams p;
+    // the field columns are indexed by row; x/y come from xs / ys
+    int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
+    if (rc) return rc;
+    if (!(line_width >= 0.0)) { set_error("dsgb_lines: line_width must be >= 0"); return DSGB_E_INVALID; }
+    p.line_width = line_width;
+    p.plot_start = plot_start;
+    p.overwrite = overwrite;
+    p.use_2_stage = 0;
+    LinesGeom g;
+    g.xs = xs; g.ys = ys; g.nrows = nrows; g.nv = nv;
+    g.xrow = layout == 1 ? nv : x_row_stride;
+    g.yrow = layout == 1 ? nv : y_row_stride;
+    cudaStream_t st = as_stream(stream);
+    const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    if (!(flags & DSGB_FLAG_NO_INIT)) {
+        rc = bases_init(bases, nbases, ncells, st);
+        if (rc) return rc;
+    }
+    const int64_t nseg = layout == 1 ? (nrows > 0 ? (nrows - 1) * nv : 0) : nrows * (nv - 1);
+    if (nseg > 0 && nbases > 0) {
+        int sms = sm_count();
+        if (sms <= 0) sms = 148;
+        int64_t blocks = (nseg + 255) / 256;
+        if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+        if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(p, g);
+        else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(p, g);
+        DSGB_CHECK_LAUNCH("lines kernel");
     }
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
         rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);

@@ -226,6 +226,20 @@ int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t r
                     const dsgb_output *outs, int32_t nouts,
                     uint32_t flags, void *stream);
 
+/* Canvas.line with the multi-line glyphs (line.py:106-430, 1152-1437):
+ * layout 1 = LineAxis0Multi (xs, ys float64 [nrows][nv], nv lines running
+ * down the rows); layout 2 = LinesAxis1 family (one line per row through nv
+ * vertices: vertex (i, j) = (xs[i*x_row_stride + j], ys[i*y_row_stride + j]),
+ * a stride of 0 shares one array across the rows: XConstant / YConstant).
+ * Segment (i, j) appends row i's fields (cols).  Reductions as
+ * dsgb_line_axis0; two-stage antialiased plans are not supported. */
+int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
+               int32_t layout, const double *xs, const double *ys, int64_t nv,
+               int64_t x_row_stride, int64_t y_row_stride, const dsgb_canvas *canvas,
+               double line_width, int32_t plot_start, int32_t overwrite,
+               const dsgb_base *bases, int32_t nbases,
+               const dsgb_output *outs, int32_t nouts, uint32_t flags, void *stream);
+
 /* Adjoint of the antialiased LineAxis0 sum('v') aggregate (self-intersecting
  * form): given dL/dagg (f64, height*width), accumulate dL/dv (f64, n) and
  * dL/dy (f64, n, y in data units) with coverage recomputed, not stored.

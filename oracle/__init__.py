@@ -78,6 +78,11 @@ def lib():
                 ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                 ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 9 + [
                 ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
+            L.oracle_lines.argtypes = [
+                ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 9 + [
+                ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
             L.oracle_bounds.argtypes = [ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             _lib = L
@@ -288,6 +293,46 @@ def line_axis0(cols, x, y, width, height, x_range, y_range, specs, line_width=0.
                         float(y_range[0]), float(y_range[1]), float(line_width),
                         1 if plot_start else 0, 1 if overwrite else 0, 1 if use_2_stage else 0,
                         reds, len(specs))
+    return _finalize(specs, keep)
+
+
+def lines(cols, layout, xs, ys, width, height, x_range, y_range, specs, line_width=0.0, plot_start=True,
+          row_offset=0):
+    """Canvas.line with a multi-line glyph (line.py:1152-1437).
+
+    layout 1 (LineAxis0Multi): xs, ys float64 [nrows][nlines].
+    layout 2 (LinesAxis1 family): xs [nrows][nv] or [nv] (XConstant), ys [nrows][nv]
+    or [nv] (YConstant).  ``cols`` holds the field columns, indexed by row."""
+    xs = np.ascontiguousarray(xs, dtype=np.float64)
+    ys = np.ascontiguousarray(ys, dtype=np.float64)
+    if layout == 1:
+        nrows, nv = xs.shape
+        xrow = yrow = nv
+    else:
+        nv = xs.shape[-1] if xs.ndim == 2 else ys.shape[-1]
+        nrows = ys.shape[0] if ys.ndim == 2 else xs.shape[0]
+        xrow = nv if xs.ndim == 2 else 0
+        yrow = nv if ys.ndim == 2 else 0
+    if x_range is None:
+        x_range = maybe_expand_bounds(compute_bounds(xs.ravel()))
+    if y_range is None:
+        y_range = maybe_expand_bounds(compute_bounds(ys.ravel()))
+    sx, tx = scale_translate(x_range, width)
+    sy, ty = scale_translate(y_range, height)
+    antialias = line_width > 0
+    if antialias:
+        self_intersect, overwrite, use_2_stage = aa_flags(specs)
+        if use_2_stage:
+            raise NotImplementedError("two-stage antialiased reductions over several lines")
+        specs = [dict(s, self_intersect=self_intersect) for s in specs]
+    else:
+        overwrite = False
+    reds, keep, colarrs, ptrs = _prepare(cols, specs, (height, width), antialias)
+    L = lib()
+    L.oracle_init(reds, len(specs), height * width, 1 if antialias else 0)
+    L.oracle_lines(layout, nrows, nv, xs.ctypes.data, ys.ctypes.data, xrow, yrow, ptrs, row_offset, width, height,
+                   sx, tx, sy, ty, float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]),
+                   float(line_width), 1 if plot_start else 0, 1 if overwrite else 0, reds, len(specs))
     return _finalize(specs, keep)
 
 

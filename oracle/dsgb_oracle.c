@@ -571,6 +571,42 @@ static void map_no_snap(double sx, double tx, double sy, double ty, double x, do
 
 /* line.py:1033-1097 (draw_segment) driven by line.py:1099-1136
  * (_build_extend_line_axis0: perform_extend_line + extend_cpu). */
+/* line.py:1033-1097 -- _build_draw_segment: clip, map, AA or Bresenham for
+ * one segment whose appends use row i. */
+static void draw_segment(int64_t i, int64_t row_offset, double x0, double y0, double x1, double y1,
+                         int segment_start, int segment_end, double xm, double ym,
+                         const double *const *cols, int32_t width,
+                         double sx, double tx, double sy, double ty,
+                         double xmin, double xmax, double ymin, double ymax,
+                         double line_width, int32_t overwrite, oracle_red *reds, int nreds) {
+    int antialias = line_width > 0.0;
+    int skip = 0;
+    if (isnull_d(x0) || isnull_d(y0) || isnull_d(x1) || isnull_d(y1)) skip = 1;
+    int clipped_start = 0, clipped_end = 0;
+    liang_barsky(xmin, xmax, ymin, ymax, &x0, &x1, &y0, &y1, &skip, &clipped_start, &clipped_end);
+    if (skip) return;
+    int clipped = clipped_start || clipped_end;
+    segment_start = segment_start || clipped_start;
+    if (antialias) {
+        double px0, py0, px1, py1, pxm, pym;
+        map_no_snap(sx, tx, sy, ty, x0, y0, &px0, &py0);
+        map_no_snap(sx, tx, sy, ty, x1, y1, &px1, &py1);
+        if (segment_start) { pxm = 0.0; pym = 0.0; }
+        else map_no_snap(sx, tx, sy, ty, xm, ym, &pxm, &pym);
+        double gx = (xmax - xmin) * sx, gy = (ymax - ymin) * sy;
+        int64_t nx = (int64_t)pyround(gx), ny = (int64_t)pyround(gy);
+        full_antialias(line_width, overwrite, i, i + row_offset, px0, px1, py0, py1,
+                       segment_start, segment_end, pxm, pym, nx, ny, width,
+                       reds, nreds, cols);
+    } else {
+        int64_t ix0, iy0, ix1, iy1;
+        map_snap(sx, tx, sy, ty, xmax, ymax, x0, y0, &ix0, &iy0);
+        map_snap(sx, tx, sy, ty, xmax, ymax, x1, y1, &ix1, &iy1);
+        bresenham(i, i + row_offset, segment_start, ix0, ix1, iy0, iy1, clipped, width,
+                  reds, nreds, cols);
+    }
+}
+
 int oracle_line_axis0(int64_t n, const double *xs, const double *ys,
                       const double *const *cols, int64_t row_offset,
                       int32_t width, int32_t height,
@@ -579,9 +615,7 @@ int oracle_line_axis0(int64_t n, const double *xs, const double *ys,
                       double line_width, int32_t plot_start,
                       int32_t overwrite, int32_t use_2_stage_agg,
                       oracle_red *reds, int nreds) {
-    int antialias = line_width > 0.0;
     for (int64_t i = 0; i + 1 < n; ++i) {
-        double x0 = xs[i], y0 = ys[i], x1 = xs[i + 1], y1 = ys[i + 1];
         /* xs[i - 1] with numba's wrap of index -1 onto the last row */
         const int64_t im = i > 0 ? i - 1 : n - 1;
         int segment_start = (i == 0) ? plot_start : (isnull_d(xs[im]) || isnull_d(ys[im]));
@@ -589,30 +623,52 @@ int oracle_line_axis0(int64_t n, const double *xs, const double *ys,
         double xm, ym;
         if (segment_start || use_2_stage_agg) { xm = 0.0; ym = 0.0; }
         else { xm = xs[im]; ym = ys[im]; }
-        int skip = 0;
-        if (isnull_d(x0) || isnull_d(y0) || isnull_d(x1) || isnull_d(y1)) skip = 1;
-        int clipped_start = 0, clipped_end = 0;
-        liang_barsky(xmin, xmax, ymin, ymax, &x0, &x1, &y0, &y1, &skip, &clipped_start, &clipped_end);
-        if (skip) continue;
-        int clipped = clipped_start || clipped_end;
-        segment_start = segment_start || clipped_start;
-        if (antialias) {
-            double px0, py0, px1, py1, pxm, pym;
-            map_no_snap(sx, tx, sy, ty, x0, y0, &px0, &py0);
-            map_no_snap(sx, tx, sy, ty, x1, y1, &px1, &py1);
-            if (segment_start) { pxm = 0.0; pym = 0.0; }
-            else map_no_snap(sx, tx, sy, ty, xm, ym, &pxm, &pym);
-            double gx = (xmax - xmin) * sx, gy = (ymax - ymin) * sy;
-            int64_t nx = (int64_t)pyround(gx), ny = (int64_t)pyround(gy);
-            full_antialias(line_width, overwrite, i, i + row_offset, px0, px1, py0, py1,
-                           segment_start, segment_end, pxm, pym, nx, ny, width,
-                           reds, nreds, cols);
-        } else {
-            int64_t ix0, iy0, ix1, iy1;
-            map_snap(sx, tx, sy, ty, xmax, ymax, x0, y0, &ix0, &iy0);
-            map_snap(sx, tx, sy, ty, xmax, ymax, x1, y1, &ix1, &iy1);
-            bresenham(i, i + row_offset, segment_start, ix0, ix1, iy0, iy1, clipped, width,
-                      reds, nreds, cols);
+        draw_segment(i, row_offset, xs[i], ys[i], xs[i + 1], ys[i + 1], segment_start, segment_end, xm, ym,
+                     cols, width, sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite, reds, nreds);
+    }
+    (void)height;
+    return 0;
+}
+
+/* Multi-line layouts, in the reference's iteration order:
+ *   layout 1, LineAxis0Multi (line.py:1152-1200): xs, ys [nrows][nv], column
+ *       j outer, row i inner;
+ *   layout 2, LinesAxis1 / XConstant / YConstant (line.py:1244-1437): row i
+ *       outer, column j inner, vertex (xs[i*xrow + j], ys[i*yrow + j]). */
+int oracle_lines(int32_t layout, int64_t nrows, int64_t nv, const double *xs, const double *ys,
+                 int64_t xrow, int64_t yrow, const double *const *cols, int64_t row_offset,
+                 int32_t width, int32_t height, double sx, double tx, double sy, double ty,
+                 double xmin, double xmax, double ymin, double ymax,
+                 double line_width, int32_t plot_start, int32_t overwrite, oracle_red *reds, int nreds) {
+    if (layout == 1) {
+        for (int64_t j = 0; j < nv; ++j) {
+            for (int64_t i = 0; i + 1 < nrows; ++i) {
+                const int64_t im = i > 0 ? i - 1 : nrows - 1;
+#define XA(r) xs[(r) * nv + j]
+#define YA(r) ys[(r) * nv + j]
+                int segment_start = (i == 0) ? plot_start : (isnull_d(XA(im)) || isnull_d(YA(im)));
+                int segment_end = (i == nrows - 2) || isnull_d(XA(i + 2)) || isnull_d(YA(i + 2));
+                double xm = 0.0, ym = 0.0;
+                if (!segment_start) { xm = XA(im); ym = YA(im); }
+                draw_segment(i, row_offset, XA(i), YA(i), XA(i + 1), YA(i + 1), segment_start, segment_end,
+                             xm, ym, cols, width, sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite,
+                             reds, nreds);
+#undef XA
+#undef YA
+            }
+        }
+    } else {
+        for (int64_t i = 0; i < nrows; ++i) {
+            const double *X = xs + i * xrow, *Y = ys + i * yrow;
+            for (int64_t j = 0; j + 1 < nv; ++j) {
+                int segment_start = (j == 0) || isnull_d(X[j - 1]) || isnull_d(Y[j - 1]);
+                int segment_end = (j == nv - 2) || isnull_d(X[j + 2]) || isnull_d(Y[j + 2]);
+                double xm = 0.0, ym = 0.0;
+                if (!segment_start) { xm = X[j - 1]; ym = Y[j - 1]; }
+                draw_segment(i, row_offset, X[j], Y[j], X[j + 1], Y[j + 1], segment_start, segment_end, xm, ym,
+                             cols, width, sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite,
+                             reds, nreds);
+            }
         }
     }
     (void)height;

@@ -6,6 +6,11 @@ Reads (as text, via ``ast``; nothing from the reference is imported or run):
   arrays (``line_antialias_sol_*``, ``line_antialias_nan_sol_*``), the
   ``line_antialias_df`` input frame and the LineAxis0 entry of
   ``line_antialias_nan_params``;
+* ``datashader/tests/test_pandas.py`` -- the multi-line cases of
+  ``line_manual_range_params`` / ``line_autorange_params`` (ragged-array
+  entries skipped) and the ``sol`` arrays of ``test_line_manual_range``,
+  ``test_line_autorange``, ``test_line_autorange_axis1_x_constant`` and
+  ``test_line_agg_sum_axis1_none_constant`` (with its frame);
 * ``datashader/tests/test_transfer_functions.py`` -- ``eq_hist_sol`` and
   ``eq_hist_sol_rescale_discrete_levels`` (uint32 RGBA images), the
   linear / log / cbrt ``solution_lists`` and the ``sol`` arrays of
@@ -111,6 +116,25 @@ def main(ref_root):
     with open(os.path.join(HERE, "eq_hist.json"), "w") as f:
         json.dump(eq, f, indent=0)
 
+    lines = {}
+    for name, (val, line) in _literal_assignments(pandas_path, ("line_manual_range_params",
+                                                                "line_autorange_params")).items():
+        cases = []
+        for df_args, kw in val:
+            if isinstance(kw.get("x"), str) and isinstance(kw.get("y"), str):
+                continue                                           # ragged arrays
+            cols = {k: [float(v) for v in vals] for k, vals in df_args[0].items()}
+            kwj = {k: ({"array": [float(v) for v in np.ravel(v)]} if isinstance(v, np.ndarray) else v)
+                   for k, v in kw.items()}
+            cases.append({"columns": cols, "kwargs": kwj})
+        lines[name] = {"source": f"datashader/tests/test_pandas.py:{line}", "cases": cases}
+    for fn, sols in _function_all_sols(pandas_path, ("test_line_manual_range", "test_line_autorange",
+                                                     "test_line_autorange_axis1_x_constant",
+                                                     "test_line_agg_sum_axis1_none_constant")).items():
+        lines[fn] = [dict(_jsonable(np.asarray(v)), source=f"datashader/tests/test_pandas.py:{ln}") for v, ln in sols]
+    with open(os.path.join(HERE, "lines_multi.json"), "w") as f:
+        json.dump(lines, f, indent=0)
+
     shade = {}
     for name, (val, line) in _literal_assignments(tf_path, ("solution_lists",)).items():
         src = f"datashader/tests/test_transfer_functions.py:{line}"
@@ -119,7 +143,23 @@ def main(ref_root):
         shade[fn] = dict(_jsonable(np.array(val, dtype="u4")), source=f"datashader/tests/test_transfer_functions.py:{line}")
     with open(os.path.join(HERE, "shade.json"), "w") as f:
         json.dump(shade, f, indent=0)
-    print("wrote", sorted(goldens), sorted(eq), sorted(shade))
+    print("wrote", sorted(goldens), sorted(eq), sorted(shade), sorted(lines))
+
+
+def _function_all_sols(path, names):
+    """Every literal ``sol = np.array(...)`` inside each named test function, in source order."""
+    tree = ast.parse(open(path).read())
+    out = {}
+    for node in tree.body:
+        if isinstance(node, ast.FunctionDef) and node.name in names:
+            found = []
+            for st in ast.walk(node):
+                if (isinstance(st, ast.Assign) and isinstance(st.targets[0], ast.Name) and st.targets[0].id == "sol"
+                        and isinstance(st.value, ast.Call)):
+                    code = compile(ast.Expression(st.value), path, "eval")
+                    found.append((eval(code, {"np": np, "nan": np.nan}), st.lineno))
+            out[node.name] = sorted(found, key=lambda t: t[1])
+    return out
 
 
 def _function_sols(path, names):

@@ -287,3 +287,34 @@ def span_variants(x, sol):
     x[2, 1] = 0 if x.dtype.kind in "iu" else np.nan
     sol[2, 1] = sol[0, 0]
     yield x.copy(), sol.copy()
+
+
+def lines_golden(key):
+    return load_golden("lines_multi.json", key)
+
+
+def line_kwargs(kw):
+    """The Canvas.line keyword arguments of a golden case (constant arrays as numpy)."""
+    out = {}
+    for k, v in kw.items():
+        out[k] = np.array(v["array"]) if isinstance(v, dict) else v
+    return out
+
+
+def multi_line_arrays(columns, kw):
+    """(layout, xs, ys) float64 arrays of a multi-line case, as the glyphs see them
+    (core.py:412-456 dispatch with the column broadcast of :1433-1443)."""
+    x, y, axis = kw["x"], kw["y"], kw.get("axis", 0)
+    if isinstance(x, str) and isinstance(y, (list, tuple)):
+        x = [x] * len(y)
+    if isinstance(y, str) and isinstance(x, (list, tuple)):
+        y = [y] * len(x)
+
+    def arr(spec):
+        if isinstance(spec, dict):
+            return np.array(spec["array"], dtype=np.float64)
+        if isinstance(spec, np.ndarray):
+            return spec.astype(np.float64)
+        return np.stack([np.asarray(columns[c], dtype=np.float64) for c in spec], axis=1)
+
+    return (1 if axis == 0 else 2), arr(x), arr(y)

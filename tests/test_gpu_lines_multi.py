@@ -1,0 +1,115 @@
+"""Multi-line glyphs on the GPU (LineAxis0Multi, LinesAxis1, LinesAxis1XConstant,
+LinesAxis1YConstant): the reference's golden images, then larger random
+cases against the oracle.  Integer reductions bit-exact; float64 sums 1e-12
+relative; antialiased float32 aggregates 3e-7 relative (the reference
+accumulates them in float32)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import datashader_gb300 as ds
+import oracle
+import refcases
+from gpu_helpers import assert_same, to_numpy
+
+pytestmark = pytest.mark.gpu
+
+
+def _frame(cols):
+    return ds.TensorFrame({k: torch.from_numpy(np.asarray(v, dtype=np.float64)).cuda() for k, v in cols.items()})
+
+
+def test_manual_range_golden():
+    sol = refcases.golden_array(refcases.lines_golden("test_line_manual_range")[0])
+    for case in refcases.lines_golden("line_manual_range_params")["cases"]:
+        cvs = ds.Canvas(plot_width=7, plot_height=7, x_range=(-3, 3), y_range=(-3, 3))
+        agg = cvs.line(_frame(case["columns"]), agg=ds.count(), **refcases.line_kwargs(case["kwargs"]))
+        np.testing.assert_array_equal(to_numpy(agg), sol, err_msg=str(case["kwargs"]))
+
+
+@pytest.mark.parametrize("line_width", [0, 1])
+def test_autorange_golden(line_width):
+    sols = refcases.lines_golden("test_line_autorange")
+    sol = refcases.golden_array(sols[0] if line_width else sols[1])
+    for case in refcases.lines_golden("line_autorange_params")["cases"]:
+        cvs = ds.Canvas(plot_width=9, plot_height=9)
+        agg = cvs.line(_frame(case["columns"]), agg=ds.count(), line_width=line_width,
+                       **refcases.line_kwargs(case["kwargs"]))
+        assert agg.attrs["x_range"] == (-4.0, 4.0) and agg.attrs["y_range"] == (-4.0, 4.0)
+        if line_width:
+            np.testing.assert_allclose(to_numpy(agg), sol, rtol=1e-6, atol=1e-6, equal_nan=True)
+        else:
+            np.testing.assert_array_equal(to_numpy(agg), sol)
+
+
+def test_axis1_x_constant_and_sum_golden():
+    sol = refcases.golden_array(refcases.lines_golden("test_line_autorange_axis1_x_constant")[0])
+    frame = _frame({"y0": [0.0, 0.0], "y1": [-4.0, 4.0], "y2": [0.0, 0.0]})
+    agg = ds.Canvas(plot_width=9, plot_height=9).line(frame, np.array([-4, 0, 4]), ["y0", "y1", "y2"], ds.count(),
+                                                      axis=1)
+    np.testing.assert_array_equal(to_numpy(agg), sol)
+    case = refcases.lines_golden("line_manual_range_params")["cases"][0]
+    frame = _frame(dict(case["columns"], v=[7.0, 9.0]))
+    agg = ds.Canvas(plot_width=7, plot_height=7, x_range=(-3, 3), y_range=(-3, 3)).line(
+        frame, ["x0", "x1", "x2"], ["y0", "y1", "y2"], ds.sum("v"), axis=1)
+    sol = refcases.golden_array(refcases.lines_golden("test_line_agg_sum_axis1_none_constant")[0])
+    np.testing.assert_array_equal(to_numpy(agg), sol)
+
+
+def _random_case(kind, nrows, nv, seed):
+    rng = np.random.default_rng(seed)
+    cols = {}
+    if kind == "axis0multi":
+        for j in range(nv):
+            cols[f"x{j}"] = np.linspace(0, 1, nrows) + 0.01 * j
+            cols[f"y{j}"] = np.cumsum(rng.normal(0, 0.05, nrows))
+            cols[f"y{j}"][rng.random(nrows) < 0.02] = np.nan
+        kw = dict(x=[f"x{j}" for j in range(nv)], y=[f"y{j}" for j in range(nv)], axis=0)
+    else:
+        ys = np.cumsum(rng.normal(0, 0.05, (nrows, nv)), axis=1)
+        ys[rng.random(ys.shape) < 0.02] = np.nan
+        for j in range(nv):
+            cols[f"y{j}"] = ys[:, j]
+        if kind == "xconst":
+            kw = dict(x=np.linspace(0, 1, nv), y=[f"y{j}" for j in range(nv)], axis=1)
+        else:
+            xs = np.linspace(0, 1, nv)[None, :] + rng.normal(0, 0.002, (nrows, nv))
+            for j in range(nv):
+                cols[f"x{j}"] = xs[:, j]
+            kw = dict(x=[f"x{j}" for j in range(nv)], y=[f"y{j}" for j in range(nv)], axis=1)
+    cols["v"] = rng.uniform(0, 1, nrows)
+    cols["v"][rng.random(nrows) < 0.05] = np.nan
+    return cols, kw
+
+
+REDS = [("count", ds.count(), oracle.spec("count"), 0.0),
+        ("sum", ds.sum("v"), oracle.spec("sum", "v"), 1e-12),
+        ("max", ds.max("v"), oracle.spec("max", "v"), 0.0),
+        ("first", ds.first("v"), oracle.spec("first", "v"), 0.0),
+        ("any", ds.any(), oracle.spec("any"), 0.0)]
+
+
+@pytest.mark.parametrize("kind", ["axis0multi", "xconst", "axis1"])
+@pytest.mark.parametrize("line_width", [0, 1.5])
+def test_random_multi_lines_vs_oracle(kind, line_width):
+    cols, kw = _random_case(kind, 600 if kind == "axis0multi" else 120, 6 if kind == "axis0multi" else 250, 7)
+    frame = _frame(cols)
+    layout, xs, ys = refcases.multi_line_arrays(cols, kw)
+    xr, yr = (0.0, 1.0), (float(np.nanmin(ys)), float(np.nanmax(ys)))
+    for name, red, spec, rtol in REDS:
+        if line_width and name in ("max", "first"):
+            continue          # two-stage antialiased plans stay off the multi-line GPU path
+        if kind == "axis0multi" and name == "first":
+            # (line, row) visiting order of the reference: not served on the GPU path
+            with pytest.raises(NotImplementedError):
+                ds.Canvas(plot_width=30, plot_height=20, x_range=xr, y_range=yr).line(frame, agg=red, **kw)
+            continue
+        cvs = ds.Canvas(plot_width=300, plot_height=200, x_range=xr, y_range=yr)
+        got = to_numpy(cvs.line(frame, agg=red, line_width=line_width, **kw))
+        ref = oracle.lines({"v": cols["v"]}, layout, xs, ys, 300, 200, xr, yr, [spec], line_width=line_width)[0]
+        if line_width and name in ("count", "any"):
+            assert_same(got, ref, rtol=3e-7, atol=1e-7, what=f"{kind} {name}")
+        else:
+            assert_same(got, ref, rtol=rtol, what=f"{kind} {name}")

@@ -154,3 +154,48 @@ def test_oracle_shade_three_colours():
     a, _ = refcases.eq_hist_agg_a()
     np.testing.assert_array_equal(oracle.shade_interp(a, "log", ["red", (0, 255, 0), "#0000FF"]),
                                   refcases.shade_golden("test_shade_cmap"))
+
+
+# ---- multi-line glyphs (LineAxis0Multi, LinesAxis1 / XConstant / YConstant) ----
+
+def test_oracle_multi_line_manual_range_golden():
+    """test_pandas.py:1654-1749 (test_line_manual_range), non-ragged cases: count on 7x7."""
+    sol = refcases.golden_array(refcases.lines_golden("test_line_manual_range")[0])
+    for case in refcases.lines_golden("line_manual_range_params")["cases"]:
+        layout, xs, ys = refcases.multi_line_arrays(case["columns"], case["kwargs"])
+        got = oracle.lines({}, layout, xs, ys, 7, 7, (-3, 3), (-3, 3), [oracle.spec("count")])[0]
+        np.testing.assert_array_equal(got, sol, err_msg=str(case["kwargs"]))
+
+
+@pytest.mark.parametrize("line_width", [0, 1])
+def test_oracle_multi_line_autorange_golden(line_width):
+    """test_pandas.py:1752-1860 (test_line_autorange): count, autoranged 9x9, lw 0 and 1."""
+    sols = refcases.lines_golden("test_line_autorange")
+    sol = refcases.golden_array(sols[0] if line_width else sols[1])
+    for case in refcases.lines_golden("line_autorange_params")["cases"]:
+        layout, xs, ys = refcases.multi_line_arrays(case["columns"], case["kwargs"])
+        got = oracle.lines({}, layout, xs, ys, 9, 9, None, None, [oracle.spec("count")],
+                           line_width=line_width)[0]
+        if line_width:
+            np.testing.assert_allclose(got, sol, rtol=1e-6, atol=1e-6, equal_nan=True)
+        else:
+            np.testing.assert_array_equal(got, sol)
+
+
+def test_oracle_axis1_x_constant_and_sum_golden():
+    """test_pandas.py:1863-1932: LinesAxis1XConstant autorange count; LinesAxis1 sum('v')
+    (the frame of test_line_agg_sum_axis1_none_constant is the axis1 manual-range case plus
+    v = [7, 9])."""
+    sol = refcases.golden_array(refcases.lines_golden("test_line_autorange_axis1_x_constant")[0])
+    cols = {"y0": [0.0, 0.0], "y1": [-4.0, 4.0], "y2": [0.0, 0.0]}
+    layout, xs, ys = refcases.multi_line_arrays(cols, {"x": {"array": [-4, 0, 4]}, "y": ["y0", "y1", "y2"],
+                                                       "axis": 1})
+    got = oracle.lines({}, layout, xs, ys, 9, 9, None, None, [oracle.spec("count")])[0]
+    np.testing.assert_array_equal(got, sol)
+    case = refcases.lines_golden("line_manual_range_params")["cases"][0]
+    cols = dict(case["columns"], v=[7.0, 9.0])
+    layout, xs, ys = refcases.multi_line_arrays(cols, case["kwargs"])
+    got = oracle.lines({"v": np.array([7.0, 9.0])}, layout, xs, ys, 7, 7, (-3, 3), (-3, 3),
+                       [oracle.spec("sum", "v")])[0]
+    sol = refcases.golden_array(refcases.lines_golden("test_line_agg_sum_axis1_none_constant")[0])
+    np.testing.assert_array_equal(got, sol)
