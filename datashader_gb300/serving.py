@@ -138,6 +138,7 @@ class Request:
     done: float = math.nan
     rows: int = 0
     result: object = None
+    segments: object = None
 
     @property
     def latency(self):
@@ -187,6 +188,15 @@ class SegmentExecutor:
             self._plans[kind] = p
         return p
 
+    def work_bytes(self, req):
+        """Device bytes a request touches: its rows (13 B each on the store) and
+        its aggregate buffers.  Caches the request's segments."""
+        if getattr(req, "segments", None) is None:
+            req.segments = self.store.segments(req.x_range, req.y_range)
+            req.rows = sum(e - b for b, e in req.segments)
+        bytes_per_row = sum(t.element_size() for t in (self.store.frame[c] for c in self.store.frame.columns))
+        return req.rows * bytes_per_row + self.agg_bytes(req)
+
     def agg_bytes(self, req):
         """Device bytes of the request's aggregate buffers (bases + outputs)."""
         _, plan = self.plan(req.kind)
@@ -203,6 +213,8 @@ class SegmentExecutor:
     def launch(self, req, stream, segments=None):
         agg, plan = self.plan(req.kind)
         frame = self.store.frame
+        if segments is None:
+            segments = getattr(req, "segments", None)
         if segments is None:
             segments = self.store.segments(req.x_range, req.y_range)
         req.rows = sum(e - b for b, e in segments)
@@ -243,12 +255,27 @@ class SegmentExecutor:
 
 class ViewportServer:
     """Continuous batching of viewport requests over ``slots`` CUDA streams
-    under a ``mem_budget`` of aggregate-buffer bytes."""
+    under a ``mem_budget`` of aggregate-buffer bytes.
 
-    def __init__(self, executor, slots=8, mem_budget=8 << 30, device=None, streams=None):
+    Admission: arrived requests are taken in arrival order while a slot is
+    free and their aggregate buffers fit in the budget (the first request
+    that does not fit waits, and so does everything behind it).  A heavy
+    request (more than ``heavy_bytes`` of rows and buffers) runs only while
+    fewer than ``max_heavy`` other heavy ones do (``max_heavy_backlogged``
+    once more requests wait than there are slots); lighter requests behind
+    it may go first, so a large viewport does not hold up small ones, and at
+    light load large ones do not slow each other down by sharing the GPU."""
+
+    def __init__(self, executor, slots=8, mem_budget=8 << 30, device=None, streams=None,
+                 heavy_bytes=256 << 20, max_heavy=1, max_heavy_backlogged=None):
         self.ex = executor
         self.slots = slots
         self.mem_budget = mem_budget
+        self.heavy_bytes = heavy_bytes
+        self.max_heavy = max_heavy
+        # with more arrived requests waiting than there are slots, throughput
+        # matters more than one request's latency: let heavy ones overlap
+        self.max_heavy_backlogged = slots if max_heavy_backlogged is None else max_heavy_backlogged
         if streams is None:
             dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
             streams = [torch.cuda.Stream(dev) for _ in range(slots)]
@@ -256,6 +283,7 @@ class ViewportServer:
         self.peak_mem = 0
         self.peak_mem_shared = 0          # peak bytes while more than one request was in flight
         self.peak_inflight = 0
+        self.peak_heavy = 0
 
     def run(self, requests, mode="batched", keep_results=False, clock=time.perf_counter, idle=None):
         """Serve ``requests`` (sorted by arrival) in real time.
@@ -273,7 +301,7 @@ class ViewportServer:
             now = clock() - t0
             progressed = False
             for slot in list(inflight):
-                req, ev, nbytes = inflight[slot]
+                req, ev, nbytes, _ = inflight[slot]
                 if ev.query():
                     req.done = clock() - t0
                     if not keep_results:
@@ -282,12 +310,22 @@ class ViewportServer:
                     free.append(slot)
                     mem -= nbytes
                     progressed = True
-            while pending and free and pending[0].arrival <= now:
-                req = pending[0]
+            heavy_now = sum(1 for _, _, _, h in inflight.values() if h)
+            backlog = 0
+            while backlog < len(pending) and pending[backlog].arrival <= now:
+                backlog += 1
+            heavy_cap = self.max_heavy if backlog <= self.slots else self.max_heavy_backlogged
+            k = 0
+            while k < len(pending) and free and pending[k].arrival <= now:
+                req = pending[k]
                 nbytes = self.ex.agg_bytes(req)
                 if inflight and mem + nbytes > self.mem_budget:
-                    break                      # head of line waits for memory to free up
-                pending.popleft()
+                    break                      # waits for memory to free up, and so does the rest
+                heavy = mode == "batched" and self.ex.work_bytes(req) > self.heavy_bytes
+                if heavy and heavy_now >= heavy_cap:
+                    k += 1                     # lighter requests behind it may go first
+                    continue
+                del pending[k]
                 slot = free.pop()
                 req.admitted = clock() - t0
                 if mode == "plain":
@@ -295,12 +333,14 @@ class ViewportServer:
                 else:
                     ev, result = self.ex.launch(req, self.streams[slot])
                 req.result = result
-                inflight[slot] = (req, ev, nbytes)
+                inflight[slot] = (req, ev, nbytes, heavy)
+                heavy_now += heavy
                 mem += nbytes
                 self.peak_mem = max(self.peak_mem, mem)
                 if len(inflight) > 1:
                     self.peak_mem_shared = max(self.peak_mem_shared, mem)
                 self.peak_inflight = max(self.peak_inflight, len(inflight))
+                self.peak_heavy = max(self.peak_heavy, heavy_now)
                 progressed = True
             if not progressed:
                 if idle is not None:

@@ -57,8 +57,12 @@ class _FakeExecutor:
     def agg_bytes(self, req):
         return req.width * req.height * 4
 
+    def work_bytes(self, req):
+        return self.agg_bytes(req) * 10
+
     def _ev(self, req):
         dur = 1e-3 + req.width * req.height * 1e-9
+        self.running_heavy = getattr(self, "running_heavy", [])
         return _Event(self.clock, self.clock.t + dur), ("result", req.rid)
 
     def launch(self, req, stream, segments=None):
@@ -81,8 +85,9 @@ def test_scheduler_admits_by_memory_and_slots_fifo():
     assert server.peak_inflight <= 6
     assert server.peak_mem <= budget and server.peak_mem_shared <= budget
     order = sorted(reqs, key=lambda r: r.arrival)
-    adm = [r.admitted for r in order]
-    assert adm == sorted(adm)                          # FIFO admission
+    for heavy in (False, True):                        # FIFO within each class (lights may overtake heavies)
+        adm = [r.admitted for r in order if (ex.work_bytes(r) > server.heavy_bytes) == heavy]
+        assert adm == sorted(adm)
     assert all(r.result == ("result", r.rid) for r in reqs)
     stats = S.summarize(reqs)
     assert stats["requests"] == 300 and stats["p99_ms"] >= stats["p50_ms"] > 0
@@ -106,3 +111,29 @@ def test_oversized_request_runs_alone():
     server = S.ViewportServer(ex, slots=4, mem_budget=1000, streams=[None] * 4)
     server.run(reqs, clock=clock, idle=clock.idle)
     assert server.peak_inflight == 1 and all(np.isfinite(r.done) for r in reqs)
+
+
+def test_heavy_requests_run_one_at_a_time_and_lights_overtake():
+    clock = _Clock()
+    ex = _FakeExecutor(clock)
+    big = [S.Request(i, 0.0, (0, 1), (0, 1), 4096, 2160, "by") for i in range(4)]
+    small = [S.Request(100 + i, 0.0, (0, 0.01), (0, 0.01), 256, 256, "count") for i in range(20)]
+    reqs = big + small                       # all arrive together, the heavy ones first
+    server = S.ViewportServer(ex, slots=4, mem_budget=1 << 40, streams=[None] * 4,
+                              heavy_bytes=4096 * 2160 * 4 * 5, max_heavy=1, max_heavy_backlogged=1)
+    server.run(reqs, clock=clock, idle=clock.idle)
+    assert server.peak_heavy == 1
+    assert all(np.isfinite(r.done) for r in reqs)
+    spans = sorted((r.admitted, r.done) for r in big)
+    assert all(spans[i][1] <= spans[i + 1][0] for i in range(len(spans) - 1))   # heavy ones in turn
+    assert max(r.done for r in small) < max(r.done for r in big)                # small ones did not wait
+
+
+def test_heavy_requests_overlap_when_backlogged():
+    clock = _Clock()
+    ex = _FakeExecutor(clock)
+    reqs = [S.Request(i, 0.0, (0, 1), (0, 1), 4096, 2160, "by") for i in range(12)]
+    server = S.ViewportServer(ex, slots=4, mem_budget=1 << 40, streams=[None] * 4,
+                              heavy_bytes=1, max_heavy=1)
+    server.run(reqs, clock=clock, idle=clock.idle)
+    assert server.peak_heavy > 1 and all(np.isfinite(r.done) for r in reqs)
