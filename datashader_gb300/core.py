@@ -557,10 +557,13 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
                       float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]))
     L = N.lib()
     if isinstance(glyph, LineAxis0):
-        rc = L.dsgb_line_axis0(ex.cols, len(ex.names), len(frame), frame.row_offset, 0, 1, ctypes.byref(cv),
-                               float(glyph.line_width), 1, int(plan.overwrite), int(plan.use_2_stage),
-                               ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
-        N.check(rc, "dsgb_line_axis0")
+        wsz = int(L.dsgb_line_workspace_size(len(frame))) if glyph.line_width > 0 else 0
+        ws = workspace(frame.device, stream, wsz) if wsz else None
+        rc = L.dsgb_line_axis0_ws(ex.cols, len(ex.names), len(frame), frame.row_offset, 0, 1, ctypes.byref(cv),
+                                  float(glyph.line_width), 1, int(plan.overwrite), int(plan.use_2_stage),
+                                  ex.bases, len(plan.bases), ex.outs, ex.nouts,
+                                  ws.data_ptr() if ws is not None else None, wsz, flags, stream)
+        N.check(rc, "dsgb_line_axis0_ws")
     elif isinstance(glyph, _MultiLine):
         if glyph.layout == 1 and len(glyph.x) > 1 and any(
                 b.op in (N.BASE_MIN_ROW, N.BASE_MAX_ROW, N.BASE_ARGMAX, N.BASE_ARGMIN) for b in plan.bases):

@@ -347,6 +347,71 @@ __global__ void __launch_bounds__(256) line_axis0_kernel(const LineParams p) {
     }
 }
 
+// ---- antialiased LineAxis0 in work order.  One thread per segment leaves
+// most lanes idle when the segments of a warp cover different numbers of
+// pixels (the float64 pipe issues each instruction for the whole warp).
+// Segments are first bucketed by an estimate of their pixel work (the area
+// of their padded bounding box in pixels), counting-sorted by bucket, and
+// drawn in that order, so the lanes of a warp do similar work.
+constexpr int LINE_WORK_BUCKETS = 64;
+constexpr int LINE_ORDER_TILE = 4096;
+
+__device__ __forceinline__ int line_work_bucket(const LineParams &p, int64_t i) {
+    const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
+    const double x0 = load_f64(X, i), y0 = load_f64(Y, i), x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
+    if (isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1)) return 0;
+    const double pad = p.line_width + 2.0;
+    const double w = (fabs((x1 - x0) * p.sx) + pad) * (fabs((y1 - y0) * p.sy) + pad);
+    if (!(w < 2.0 * (LINE_WORK_BUCKETS - 1))) return LINE_WORK_BUCKETS - 1;
+    return (int)(w * 0.5);
+}
+
+__global__ void __launch_bounds__(256) line_work_hist(const LineParams p, unsigned *hist) {
+    __shared__ unsigned h[LINE_WORK_BUCKETS];
+    if (threadIdx.x < LINE_WORK_BUCKETS) h[threadIdx.x] = 0;
+    __syncthreads();
+    for (int64_t i = gtid(); i + 1 < p.n; i += gstride()) atomicAdd(&h[line_work_bucket(p, i)], 1u);
+    __syncthreads();
+    if (threadIdx.x < LINE_WORK_BUCKETS && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void line_work_scan(const unsigned *hist, unsigned *cursor) {
+    if (threadIdx.x != 0) return;
+    unsigned o = 0;
+    for (int b = 0; b < LINE_WORK_BUCKETS; ++b) { cursor[b] = o; o += hist[b]; }
+}
+
+__global__ void __launch_bounds__(256) line_work_order(const LineParams p, unsigned *cursor, unsigned *order) {
+    __shared__ unsigned h[LINE_WORK_BUCKETS];
+    if (threadIdx.x < LINE_WORK_BUCKETS) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t s0 = (int64_t)blockIdx.x * LINE_ORDER_TILE;
+    const int64_t s1 = s0 + LINE_ORDER_TILE < p.n - 1 ? s0 + LINE_ORDER_TILE : p.n - 1;
+    for (int64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) atomicAdd(&h[line_work_bucket(p, i)], 1u);
+    __syncthreads();
+    if (threadIdx.x < LINE_WORK_BUCKETS && h[threadIdx.x])
+        h[threadIdx.x] = atomicAdd(&cursor[threadIdx.x], h[threadIdx.x]);
+    __syncthreads();
+    for (int64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x)
+        order[atomicAdd(&h[line_work_bucket(p, i)], 1u)] = (unsigned)i;
+}
+
+__global__ void __launch_bounds__(256) line_axis0_ordered_kernel(const LineParams p, const unsigned *order) {
+    const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
+    for (int64_t k = gtid(); k + 1 < p.n; k += gstride()) {
+        const int64_t i = order[k];
+        const double x0 = load_f64(X, i), y0 = load_f64(Y, i);
+        const double x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
+        const int64_t im = i > 0 ? i - 1 : p.n - 1;
+        const bool segment_start = (i == 0) ? (p.plot_start != 0)
+                                            : (isnull(load_f64(X, im)) || isnull(load_f64(Y, im)));
+        const bool segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
+        double xm = 0.0, ym = 0.0;
+        if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, im); ym = load_f64(Y, im); }
+        draw_segment(p, i, x0, y0, x1, y1, segment_start, segment_end, xm, ym);
+    }
+}
+
 // Multi-line layouts over float64 vertex arrays.
 //   LAYOUT 1, LineAxis0Multi (line.py:1152-1242): xs, ys [nrows][nlines];
 //       line j runs down the rows; segment (i, j) appends row i; the
@@ -439,6 +504,32 @@ int build_line_params(LineParams &p, const dsgb_column *cols, int32_t ncols, int
 
 using namespace dsgb;
 
+static size_t line_ws_align(size_t v) { return (v + 255) / 256 * 256; }
+
+extern "C" size_t dsgb_line_workspace_size(int64_t n) {
+    if (n < 2) return 0;
+    return line_ws_align((size_t)LINE_WORK_BUCKETS * 8) + line_ws_align((size_t)(n - 1) * 4);
+}
+
+static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                           int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                           double line_width, int32_t plot_start, int32_t overwrite,
+                           int32_t use_2_stage_agg,
+                           const dsgb_base *bases, int32_t nbases,
+                           const dsgb_output *outs, int32_t nouts,
+                           void *workspace, size_t ws_bytes, uint32_t flags, void *stream);
+
+extern "C" int dsgb_line_axis0_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                                  int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                                  double line_width, int32_t plot_start, int32_t overwrite,
+                                  int32_t use_2_stage_agg,
+                                  const dsgb_base *bases, int32_t nbases,
+                                  const dsgb_output *outs, int32_t nouts,
+                                  void *workspace, size_t workspace_bytes, uint32_t flags, void *stream) {
+    return line_axis0_impl(cols, ncols, n, row_offset, x_col, y_col, canvas, line_width, plot_start, overwrite,
+                           use_2_stage_agg, bases, nbases, outs, nouts, workspace, workspace_bytes, flags, stream);
+}
+
 extern "C" int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
                                int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
                                double line_width, int32_t plot_start, int32_t overwrite,
@@ -446,6 +537,17 @@ extern "C" int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n
                                const dsgb_base *bases, int32_t nbases,
                                const dsgb_output *outs, int32_t nouts,
                                uint32_t flags, void *stream) {
+    return line_axis0_impl(cols, ncols, n, row_offset, x_col, y_col, canvas, line_width, plot_start, overwrite,
+                           use_2_stage_agg, bases, nbases, outs, nouts, nullptr, 0, flags, stream);
+}
+
+static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                           int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                           double line_width, int32_t plot_start, int32_t overwrite,
+                           int32_t use_2_stage_agg,
+                           const dsgb_base *bases, int32_t nbases,
+                           const dsgb_output *outs, int32_t nouts,
+                           void *workspace, size_t ws_bytes, uint32_t flags, void *stream) {
     LineParams p;
     int rc = build_line_params(p, cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases);
     if (rc) return rc;
@@ -465,7 +567,21 @@ extern "C" int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n
         if (sms <= 0) sms = 148;
         int64_t blocks = (n + 255) / 256;
         if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
-        line_axis0_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
+        const size_t need = dsgb_line_workspace_size(n);
+        if (line_width > 0.0 && workspace && ws_bytes >= need && !((uintptr_t)workspace & 255u)) {
+            unsigned *hist = (unsigned *)workspace;
+            unsigned *cursor = hist + LINE_WORK_BUCKETS;
+            unsigned *order = (unsigned *)((char *)workspace + line_ws_align((size_t)LINE_WORK_BUCKETS * 8));
+            cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)LINE_WORK_BUCKETS * 4, st);
+            if (e != cudaSuccess) return cuda_status(e, "line workspace memset");
+            line_work_hist<<<(unsigned)blocks, 256, 0, st>>>(p, hist);
+            line_work_scan<<<1, 32, 0, st>>>(hist, cursor);
+            const int64_t tiles = (n - 1 + LINE_ORDER_TILE - 1) / LINE_ORDER_TILE;
+            line_work_order<<<(unsigned)tiles, 256, 0, st>>>(p, cursor, order);
+            line_axis0_ordered_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, order);
+        } else {
+            line_axis0_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
+        }
         DSGB_CHECK_LAUNCH("line_axis0 kernel");
     }
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)

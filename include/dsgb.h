@@ -226,6 +226,19 @@ int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t r
                     const dsgb_output *outs, int32_t nouts,
                     uint32_t flags, void *stream);
 
+/* dsgb_line_axis0 with a workspace of dsgb_line_workspace_size(n) bytes
+ * (256-byte aligned): antialiased segments are then drawn in order of
+ * their estimated pixel work, so that the lanes of a warp do similar work.
+ * Same results. */
+size_t dsgb_line_workspace_size(int64_t n);
+int dsgb_line_axis0_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
+                       int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
+                       double line_width, int32_t plot_start, int32_t overwrite,
+                       int32_t use_2_stage_agg,
+                       const dsgb_base *bases, int32_t nbases,
+                       const dsgb_output *outs, int32_t nouts,
+                       void *workspace, size_t workspace_bytes, uint32_t flags, void *stream);
+
 /* Canvas.line with the multi-line glyphs (line.py:106-430, 1152-1437):
  * layout 1 = LineAxis0Multi (xs, ys float64 [nrows][nv], nv lines running
  * down the rows); layout 2 = LinesAxis1 family (one line per row through nv
