@@ -49,11 +49,11 @@ def workload(n):
 
 
 # DRAM bytes (read + write) of one hot-tile count launch, from an ncu capture
-# of cached_main at 2e7 rows (164.54 MB read, 3.08 MB written; profiles/
+# of cached_main at 2e7 rows (163.31 MB read, 3.09 MB written; profiles/
 # cached_main_count_2e7_1024_full.md): reads scale with rows, writes with the
 # touched pixels of the 1024x1024 canvas.
 def count_traffic(n):
-    return 164.54e6 / 2e7 * n + 3.08e6
+    return 163.31e6 / 2e7 * n + 3.09e6
 
 
 def measured_peak():
