@@ -95,6 +95,7 @@ struct PyrParams {
     unsigned *cursor;                         // nbuckets
     unsigned *band_cursor;                    // nbk (bucket rows)
     unsigned *item_base;                      // nbuckets + 1 (items before bucket b)
+    unsigned *item_bucket;                    // n_items: the bucket of each work item
     unsigned *slot_base;                      // nbuckets (accumulation slot of b, when split in chunks)
     unsigned *done;                           // nbuckets << (2 * split)
     PyrCounters *ctr;
@@ -291,6 +292,7 @@ __global__ void __launch_bounds__(1024) pyr_plan(const PyrParams p) {
         if (b % (p.nbk * PYR_BAND_ROWS) == 0) p.band_cursor[b / (p.nbk * PYR_BAND_ROWS)] = o_cnt;
         p.item_base[b] = o_items;
         p.slot_base[b] = o_slots;
+        for (unsigned i = 0; i < ch * nsub; ++i) p.item_bucket[o_items + i] = (unsigned)b;
         o_cnt += c;
         o_items += ch * nsub;
         o_slots += ch > 1 ? (unsigned)nsub : 0u;
@@ -335,10 +337,10 @@ __device__ __forceinline__ unsigned warp_reserve(unsigned *h, unsigned key, bool
 // reserves each group's range with one global atomic, stages the rows in
 // shared memory in group order and writes them out as contiguous runs, so
 // that global stores are coalesced instead of one sector per row.
-constexpr int PYR_STAGE_THREADS = 1024;
+constexpr int PYR_STAGE_THREADS = 512;
 constexpr int PYR_STAGE_ITEMS = 8;
 constexpr int PYR_STAGE_ROWS = PYR_STAGE_THREADS * PYR_STAGE_ITEMS;
-constexpr int PYR_STAGE_MAX_GROUPS = 4096;    // 48 KB of counters + 128 KB of staged rows
+constexpr int PYR_STAGE_MAX_GROUPS = 4096;    // 48 KB of counters + 64 KB of staged rows: two blocks an SM
 
 struct StageIn {
     const float *x, *y, *v;       // v may be null
@@ -379,21 +381,42 @@ __device__ void stage_and_write(const StageIn in, int ngroups, G group_of, unsig
         rk[k] = warp_reserve(cnt, gv[k] >= 0 ? (unsigned)gv[k] : 0u, gv[k] >= 0);
     }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        // exclusive scan of the group counts by one warp
-        unsigned carry = 0;
-        for (int b0 = 0; b0 < ngroups; b0 += 32) {
-            const int g = b0 + lane;
-            const unsigned c = g < ngroups ? cnt[g] : 0u;
-            unsigned incl = c;
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += u;
-            }
-            if (g < ngroups) off[g] = carry + incl - c;
-            carry += __shfl_sync(0xffffffffu, incl, 31);
+    {
+        // exclusive scan of the group counts by the whole block: each thread
+        // sums a run of consecutive groups, the runs are scanned across the
+        // block (warp shuffles, then the warp totals), and each thread writes
+        // its run's offsets
+        __shared__ unsigned wsum[32];
+        const int per = (ngroups + (int)blockDim.x - 1) / (int)blockDim.x;
+        const int g0 = threadIdx.x * per;
+        const int g1 = g0 + per < ngroups ? g0 + per : ngroups;
+        unsigned own = 0;
+        for (int g = g0; g < g1; ++g) own += cnt[g];
+        unsigned incl = own;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
         }
-        if (lane == 0) off[ngroups] = carry;
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const int nw = (int)blockDim.x >> 5;
+            const unsigned w = lane < nw ? wsum[lane] : 0u;
+            unsigned wi = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned u = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += u;
+            }
+            __syncwarp();
+            if (lane < nw) wsum[lane] = wi - w;
+            if (lane == nw - 1) off[ngroups] = wi;
+        }
+        __syncthreads();
+        unsigned run = wsum[warp] + incl - own;
+        for (int g = g0; g < g1; ++g) {
+            off[g] = run;
+            run += cnt[g];
+        }
     }
     __syncthreads();
     for (int g = threadIdx.x; g < ngroups; g += blockDim.x)
@@ -423,7 +446,7 @@ __host__ __device__ __forceinline__ size_t stage_smem_bytes(int ngroups) {
 }
 
 // First pass: rows grouped by band (PYR_BAND_ROWS bucket rows).
-__global__ void __launch_bounds__(PYR_STAGE_THREADS, 1) pyr_band(const PyrParams p) {
+__global__ void __launch_bounds__(PYR_STAGE_THREADS, 2) pyr_band(const PyrParams p) {
     extern __shared__ __align__(16) unsigned char smb[];
     const PyrEntry dx = p.tab_x[0], dy = p.tab_y[0];
     const int nbands = (p.nbk + PYR_BAND_ROWS - 1) / PYR_BAND_ROWS;
@@ -440,7 +463,7 @@ __global__ void __launch_bounds__(PYR_STAGE_THREADS, 1) pyr_band(const PyrParams
 
 // Second pass: the banded copy grouped by bucket.  A block's rows come from
 // a few consecutive bands, so its groups are only their buckets.
-__global__ void __launch_bounds__(PYR_STAGE_THREADS, 1) pyr_scatter(const PyrParams p) {
+__global__ void __launch_bounds__(PYR_STAGE_THREADS, 2) pyr_scatter(const PyrParams p) {
     extern __shared__ __align__(16) unsigned char smb[];
     __shared__ int s_lo, s_hi;
     const PyrEntry dx = p.tab_x[0], dy = p.tab_y[0];
@@ -507,13 +530,19 @@ __device__ __forceinline__ int tiles_of(float c, const PyrEntry &home, int ht, c
         return k;
     }
     // not in the home tile (the bucket estimate was off): search around a new estimate
+    // (g written with constant indices only, so that it stays in registers)
     int t = (int)((c - c0f) * span_inv_f * (float)nt);
     int k = 0;
-    for (int d = -2; d <= 2 && k < 2; ++d) {
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
         const int u = t + d;
-        if (u < 0 || u >= nt) continue;
+        if (k >= 2 || u < 0 || u >= nt) continue;
         const PyrEntry e = lvl[u];
-        if (c >= e.lo_f && c <= e.hi_f) g[k++] = u * ts + pyr_bin(c, e.ax);
+        if (c >= e.lo_f && c <= e.hi_f) {
+            const int gv = u * ts + pyr_bin(c, e.ax);
+            if (k == 0) g[0] = gv; else g[1] = gv;
+            ++k;
+        }
     }
     return k;
 }
@@ -541,39 +570,41 @@ static __device__ __noinline__ void pyr_dyadic_edges(const PyrParams &p, const P
         int gx[2], gy[2];
         const int kx = tiles_of(x, l.hx, l.htx, p.tab_x, z, p.ts, x0f, span_inv_x, gx);
         const int ky = kx ? tiles_of(y, l.hy, l.hty, p.tab_y, z, p.ts, y0f, span_inv_y, gy) : 0;
-        for (int a = 0; a < kx; ++a)
-            for (int c = 0; c < ky; ++c) {
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                if (a >= kx || c >= ky) continue;
                 if (counted && gx[a] == (gxp >> k) && gy[c] == (gyp >> k)) continue;
                 pyr_queue(p, z, gx[a], gy[c], v);
             }
     }
 }
 
-__global__ void pyr_render(const PyrParams p) {
+__global__ void __launch_bounds__(1024, 1) pyr_render(const PyrParams p) {
     extern __shared__ __align__(16) unsigned char sm[];
     unsigned *scnt = (unsigned *)sm;
     unsigned *skey = scnt + p.footprint;
     __shared__ PyrLevel L[PYR_MAX_Z + 1];
-    __shared__ unsigned s_item;
+    __shared__ unsigned s_q[2];                // this item and the next (ping-pong)
     __shared__ bool s_last;
     const int nlev = p.zmax - p.zmin + 1;
     const int nsub = 1 << (2 * p.split), sside = 1 << p.split;
     const int bl = p.bls + p.split;
     const float span_inv_x = 1.0f / (float)(p.x1 - p.x0), span_inv_y = 1.0f / (float)(p.y1 - p.y0);
     const float x0f = (float)p.x0, y0f = (float)p.y0;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&p.ctr->queue, 1u);
-        __syncthreads();
-        const unsigned item = s_item;
-        if (item >= p.ctr->n_items) break;
-        // bucket of the item: the last b with item_base[b] <= item
-        int lo = 0, hi = p.nbuckets - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(&p.item_base[mid]) <= item) lo = mid; else hi = mid - 1;
-        }
-        const int b = lo;
-        const unsigned rel = item - p.item_base[b];
+    const unsigned n_items = p.ctr->n_items;
+    if (threadIdx.x == 0) s_q[0] = atomicAdd(&p.ctr->queue, 1u);
+    __syncthreads();
+    for (unsigned it = 0;; ++it) {
+        const unsigned item = s_q[it & 1];
+        if (item >= n_items) break;
+        // the next item is taken now (its slot was last read before the
+        // previous iteration's final barrier); the atomic's latency hides
+        // behind this item
+        if (threadIdx.x == 0) s_q[(it + 1) & 1] = atomicAdd(&p.ctr->queue, 1u);
+        const int b = (int)__ldg(&p.item_bucket[item]);
+        const unsigned rel = item - __ldg(&p.item_base[b]);
         const unsigned j = rel / nsub, q = rel % nsub;
         const unsigned bcnt = p.bstart[b + 1] - p.bstart[b];
         const unsigned nch = chunks_of(bcnt, p.chunk);
@@ -594,10 +625,16 @@ __global__ void pyr_render(const PyrParams p) {
             l.hx = p.tab_x[(1 << z) - 1 + l.htx];
             l.hy = p.tab_y[(1 << z) - 1 + l.hty];
         }
-        {
+        if (p.dyadic) {
+            // only the finest level accumulates; the coarser ones are derived
+            const int o4 = p.fp_off[nlev - 1] >> 2, k4 = (p.footprint >> 2) - o4;
+            for (int i = threadIdx.x; i < 2 * k4; i += blockDim.x) {
+                const int j = i < k4 ? o4 + i : (p.footprint >> 2) + o4 + (i - k4);
+                ((uint4 *)scnt)[j] = make_uint4(0u, 0u, 0u, 0u);
+            }
+        } else {
             const int n4 = (2 * p.footprint) >> 2;
             for (int i = threadIdx.x; i < n4; i += blockDim.x) ((uint4 *)scnt)[i] = make_uint4(0u, 0u, 0u, 0u);
-            for (int i = 4 * n4 + threadIdx.x; i < 2 * p.footprint; i += blockDim.x) scnt[i] = 0u;
         }
         __syncthreads();
         const unsigned s0 = p.bstart[b] + j * (unsigned)p.chunk;
@@ -616,8 +653,12 @@ __global__ void pyr_render(const PyrParams p) {
 #pragma unroll 1
           for (int r = 0; r < RI; ++r) {
             if (i0 + r * blockDim.x >= s1) break;
-            const float x = xv[r], y = yv[r];
-            const float v = vv[r];
+            // take the front row and shift the rest down: constant indices
+            // keep the rows in registers in this rolled loop
+            const float x = xv[0], y = yv[0];
+            const float v = vv[0];
+#pragma unroll
+            for (int u = 0; u + 1 < RI; ++u) { xv[u] = xv[u + 1]; yv[u] = yv[u + 1]; vv[u] = vv[u + 1]; }
             const bool hasv = !(v != v);
             const unsigned key = hasv ? fkey(v) : 0u;
             if (p.dyadic) {
@@ -649,8 +690,11 @@ __global__ void pyr_render(const PyrParams p) {
                 const int kx = tiles_of(x, l.hx, l.htx, p.tab_x, z, p.ts, x0f, span_inv_x, gx);
                 if (!kx) continue;
                 const int ky = tiles_of(y, l.hy, l.hty, p.tab_y, z, p.ts, y0f, span_inv_y, gy);
-                for (int a = 0; a < kx; ++a) {
-                    for (int c = 0; c < ky; ++c) {
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        if (a >= kx || c >= ky) continue;
                         const unsigned lx = (unsigned)(gx[a] - l.gx0), ly = (unsigned)(gy[c] - l.gy0);
                         if (lx < (unsigned)l.f && ly < (unsigned)l.f) {
                             const int off = p.fp_off[lz] + (int)ly * l.f + (int)lx;
@@ -808,7 +852,8 @@ __global__ void pyr_spill(const PyrParams p) {
 struct PyrLayout {
     int bls, nbk, nbuckets, nsub, footprint, ntab;
     int64_t fp_bytes, slot_cap, spill_cap;
-    size_t off_tab_x, off_tab_y, off_bcount, off_bstart, off_cursor, off_item_base, off_slot_base, off_done,
+    size_t off_tab_x, off_tab_y, off_bcount, off_bstart, off_cursor, off_item_base, off_item_bucket, off_slot_base,
+        off_done,
         off_ctr, off_sx, off_sy, off_sv, off_bx, off_by, off_bv, off_band, off_partials, off_spill, total;
 };
 
@@ -844,6 +889,8 @@ static int pyr_layout(int64_t n, bool has_v, const dsgb_pyramid_config *c, PyrLa
     L.off_bstart = o; o = pyr_align(o + (size_t)(L.nbuckets + 1) * 4);
     L.off_cursor = o; o = pyr_align(o + (size_t)L.nbuckets * 4);
     L.off_item_base = o; o = pyr_align(o + (size_t)(L.nbuckets + 1) * 4);
+    // items = sum over buckets of max(1, ceil(count / chunk)) * nsub <= (n / chunk + nbuckets) * nsub
+    L.off_item_bucket = o; o = pyr_align(o + ((size_t)(n / c->chunk) + (size_t)L.nbuckets) * L.nsub * 4);
     L.off_slot_base = o; o = pyr_align(o + (size_t)L.nbuckets * 4);
     L.off_done = o; o = pyr_align(o + (size_t)L.nbuckets * L.nsub * 4);
     L.off_ctr = o; o = pyr_align(o + sizeof(PyrCounters));
@@ -963,6 +1010,7 @@ extern "C" int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n, i
     p.bstart = (unsigned *)(w + L.off_bstart);
     p.cursor = (unsigned *)(w + L.off_cursor);
     p.item_base = (unsigned *)(w + L.off_item_base);
+    p.item_bucket = (unsigned *)(w + L.off_item_bucket);
     p.slot_base = (unsigned *)(w + L.off_slot_base);
     p.done = (unsigned *)(w + L.off_done);
     p.ctr = (PyrCounters *)(w + L.off_ctr);
