@@ -339,3 +339,46 @@ def test_cached_mean_single_hot_pixel():
     got = to_numpy(ds.Canvas(**CANVAS2).points(frame_from_numpy(cols), "x", "y", ds.mean("v")))
     ref = run_points(cols, {}, ds.mean("v"), CANVAS2)
     assert_same(got, ref, rtol=1e-12)
+
+
+def _edge_coords(lo, hi, npx, rng, m):
+    """float32 coordinates that probe every decision of the binning: each
+    pixel edge and its float neighbours, the bounds and the floats just
+    beyond them, half-pixel bands inside and outside, non-finite and huge
+    values; the rest Gaussian."""
+    lo32, hi32 = np.float32(lo), np.float32(hi)
+    px = (hi - lo) / npx
+    edges = (lo + np.arange(npx + 1) * px).astype(np.float32)
+    specials = [lo32, hi32, np.nextafter(lo32, np.float32(-np.inf)), np.nextafter(lo32, np.float32(np.inf)),
+                np.nextafter(hi32, np.float32(-np.inf)), np.nextafter(hi32, np.float32(np.inf))]
+    for f in (-2.0, -1.5, -1.0, -0.75, -0.5, -0.25, 0.25, 0.5, 0.75):
+        specials += [np.float32(lo + f * px), np.float32(hi - f * px)]
+    specials += [np.nan, np.inf, -np.inf, 1e30, -1e30, 3e38, -3e38, 1e7, -1e7, 0.0, -0.0, 1e-40]
+    probe = np.concatenate([edges, np.nextafter(edges, np.float32(np.inf)),
+                            np.nextafter(edges, np.float32(-np.inf)), np.asarray(specials, np.float32)])
+    out = rng.normal((lo + hi) / 2, (hi - lo) / 5, m).astype(np.float32)
+    idx = rng.choice(m, size=min(m // 3, 40 * probe.size), replace=False)
+    out[idx] = probe[rng.integers(0, probe.size, idx.size)]
+    return out
+
+
+@pytest.mark.parametrize("w,h,xr,yr", [(1024, 1024, (-4.0, 4.0), (-4.0, 4.0)),
+                                       (1000, 999, (-3.3, 2.7), (0.1, 0.7)),
+                                       (333, 4096, (1e3, 1e3 + 17.0), (-1e-3, 2e-3))])
+def test_cached_paths_adversarial_coordinates(w, h, xr, yr):
+    """The cached count / mean kernels classify rows by the float32 image
+    alone (no bounds compares): bit-exact counts and 1e-12 means against the
+    oracle on coordinates at every pixel edge, at and beyond the bounds, and
+    non-finite or huge."""
+    n = 1_300_000
+    rng = np.random.default_rng(w + h)
+    x = _edge_coords(xr[0], xr[1], w, rng, n)
+    y = _edge_coords(yr[0], yr[1], h, rng, n)
+    v = rng.lognormal(0.0, 1.0, n)
+    v[rng.random(n) < 0.02] = np.nan
+    canvas = dict(plot_width=w, plot_height=h, x_range=xr, y_range=yr)
+    cols = {"x": x, "y": y, "v": v}
+    got = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", ds.count()))
+    assert_same(got, run_points(cols, {}, ds.count(), canvas))
+    got = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", ds.mean("v")))
+    assert_same(got, run_points(cols, {}, ds.mean("v"), canvas), rtol=1e-12)
