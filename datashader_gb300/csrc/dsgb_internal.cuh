@@ -169,6 +169,34 @@ __device__ __forceinline__ void atomic_min_key(long long *slot, long long key) {
     if (*(volatile long long *)slot > key) atomicMin(slot, key);
 }
 
+// Exact float32 -> float64 widening with integer operations only.  GB300
+// runs the float conversion instruction on its narrow float64 pipe; this
+// form keeps bulk conversions on the integer ALU.  A normal float keeps its
+// sign and mantissa (shifted up by 29 bits) and its exponent is rebiased by
+// 1023 - 127 = 896; zero, subnormals (normalised by their leading bit),
+// infinities and NaNs take the rare branch.
+__device__ __forceinline__ double f32_to_f64_exact(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu, m = b & 0x7fffffu, sign = b & 0x80000000u;
+    unsigned hi, lo;
+    if (e - 1u < 254u) {                       // normal: 1 <= e <= 254
+        hi = sign | (((b & 0x7fffffffu) >> 3) + (896u << 20));
+        lo = b << 29;
+    } else if (e == 0xffu) {                   // inf / NaN: exponent all ones, payload shifted
+        hi = sign | 0x7ff00000u | (m >> 3);
+        lo = m << 29;
+    } else if (m == 0u) {                      // +-0
+        hi = sign;
+        lo = 0u;
+    } else {                                   // subnormal: m * 2^-149, leading bit at p
+        const int p = 31 - __clz((int)m);
+        const unsigned long long frac = ((unsigned long long)m << (52 - p)) & 0xfffffffffffffull;
+        hi = sign | ((unsigned)(p - 149 + 1023) << 20) | (unsigned)(frac >> 32);
+        lo = (unsigned)frac;
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 // Grid-stride helpers.
 __device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }

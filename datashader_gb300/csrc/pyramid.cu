@@ -794,10 +794,10 @@ __global__ void __launch_bounds__(1024, 1) pyr_render(const PyrParams p) {
                         if (p.max_out) {
                             const uint4 kv = *(const uint4 *)(ks + off);
                             double2 m0, m1;
-                            m0.x = kv.x ? (double)fkey_value(kv.x) : qnan;
-                            m0.y = kv.y ? (double)fkey_value(kv.y) : qnan;
-                            m1.x = kv.z ? (double)fkey_value(kv.z) : qnan;
-                            m1.y = kv.w ? (double)fkey_value(kv.w) : qnan;
+                            m0.x = kv.x ? f32_to_f64_exact(fkey_value(kv.x)) : qnan;
+                            m0.y = kv.y ? f32_to_f64_exact(fkey_value(kv.y)) : qnan;
+                            m1.x = kv.z ? f32_to_f64_exact(fkey_value(kv.z)) : qnan;
+                            m1.y = kv.w ? f32_to_f64_exact(fkey_value(kv.w)) : qnan;
                             *(double2 *)(p.max_out + o) = m0;
                             *(double2 *)(p.max_out + o + 2) = m1;
                         }
@@ -809,7 +809,7 @@ __global__ void __launch_bounds__(1024, 1) pyr_render(const PyrParams p) {
                         p.count_out[o] = cs[i];
                         if (p.max_out) {
                             const unsigned k = ks[i];
-                            p.max_out[o] = k ? (double)fkey_value(k) : qnan;
+                            p.max_out[o] = k ? f32_to_f64_exact(fkey_value(k)) : qnan;
                         }
                     }
                 }

@@ -43,6 +43,10 @@ def _data(n, seed, x_range=(0.0, 1.0), y_range=(0.0, 1.0), zmax=6):
     ey = np.array(extra_y, dtype=np.float32)
     ev = rng.standard_normal(ex.size).astype(np.float32)
     ev[::7] = np.nan
+    # values whose float64 widening takes every branch: subnormals, infinities, extremes
+    special = np.array([1e-40, -1e-42, 1.4e-45, -1.4e-45, np.inf, -np.inf, 3.4e38, -3.4e38, 1.17549435e-38,
+                        -0.0, 0.0], dtype=np.float32)
+    ev[3::11][:special.size] = special[:ev[3::11].size]
     x = np.concatenate([x, ex, ex])      # edge points twice: counts of 2 on edges
     y = np.concatenate([y, ey, ey])
     v = np.concatenate([v, ev, ev[::-1]])
