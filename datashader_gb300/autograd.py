@@ -102,10 +102,13 @@ class _LineSum(torch.autograd.Function):
         gy = torch.empty(n, dtype=torch.float64, device=v.device)
         cols = (N.Column * 3)(N.Column(x.data_ptr(), dsgb_dtype(x), 0), N.Column(y.data_ptr(), dsgb_dtype(y), 0),
                               N.Column(v.data_ptr(), dsgb_dtype(v), 0))
-        N.check(N.lib().dsgb_line_axis0_backward(cols, 3, n, 0, 1, 2, ctypes.byref(cv), float(ctx.line_width), 1,
-                                                 grad.data_ptr(), None, gv.data_ptr(), gy.data_ptr(),
-                                                 torch.cuda.current_stream(v.device).cuda_stream),
-                "dsgb_line_axis0_backward")
+        L = N.lib()
+        wsz = int(L.dsgb_line_workspace_size(n))
+        ws = torch.empty(max(wsz, 1), dtype=torch.uint8, device=v.device)
+        N.check(L.dsgb_line_axis0_backward_ws(cols, 3, n, 0, 1, 2, ctypes.byref(cv), float(ctx.line_width), 1,
+                                              grad.data_ptr(), None, gv.data_ptr(), gy.data_ptr(),
+                                              ws.data_ptr(), wsz, torch.cuda.current_stream(v.device).cuda_stream),
+                "dsgb_line_axis0_backward_ws")
         return gv.to(v.dtype), gy.to(y.dtype), None, None, None
 
 

@@ -57,6 +57,20 @@ struct BaseDev {
     void *agg;
 };
 
+// Work order of the antialiased LineAxis0 segments (line.cu): segment
+// indices counting-sorted by an estimate of their pixel work, so that the
+// lanes of a warp draw segments of similar size.  Shared by the forward and
+// the adjoint.  Returns the order (n - 1 entries inside the workspace) or
+// null when the workspace is missing or too small (callers then draw in
+// row order).
+struct LineWorkArgs {
+    ColumnRef X, Y;
+    int64_t n;
+    double sx, sy, line_width;
+};
+size_t line_work_order_bytes(int64_t n);
+const unsigned *build_line_work_order(const LineWorkArgs &a, void *workspace, size_t ws_bytes, cudaStream_t st);
+
 // Load element i of a column as float64 (the promotion numba applies when a
 // column meets a float64 scale or aggregate).  Integers never read as NaN.
 __device__ __forceinline__ double load_f64(const ColumnRef &c, int64_t i) {

@@ -356,9 +356,10 @@ __global__ void __launch_bounds__(256) line_axis0_kernel(const LineParams p) {
 constexpr int LINE_WORK_BUCKETS = 64;
 constexpr int LINE_ORDER_TILE = 4096;
 
-__device__ __forceinline__ int line_work_bucket(const LineParams &p, int64_t i) {
-    const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
-    const double x0 = load_f64(X, i), y0 = load_f64(Y, i), x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
+static size_t line_ws_align(size_t v) { return (v + 255) / 256 * 256; }
+
+__device__ __forceinline__ int line_work_bucket(const LineWorkArgs &p, int64_t i) {
+    const double x0 = load_f64(p.X, i), y0 = load_f64(p.Y, i), x1 = load_f64(p.X, i + 1), y1 = load_f64(p.Y, i + 1);
     if (isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1)) return 0;
     const double pad = p.line_width + 2.0;
     const double w = (fabs((x1 - x0) * p.sx) + pad) * (fabs((y1 - y0) * p.sy) + pad);
@@ -366,7 +367,7 @@ __device__ __forceinline__ int line_work_bucket(const LineParams &p, int64_t i) 
     return (int)(w * 0.5);
 }
 
-__global__ void __launch_bounds__(256) line_work_hist(const LineParams p, unsigned *hist) {
+__global__ void __launch_bounds__(256) line_work_hist(const LineWorkArgs p, unsigned *hist) {
     __shared__ unsigned h[LINE_WORK_BUCKETS];
     if (threadIdx.x < LINE_WORK_BUCKETS) h[threadIdx.x] = 0;
     __syncthreads();
@@ -381,7 +382,7 @@ __global__ void line_work_scan(const unsigned *hist, unsigned *cursor) {
     for (int b = 0; b < LINE_WORK_BUCKETS; ++b) { cursor[b] = o; o += hist[b]; }
 }
 
-__global__ void __launch_bounds__(256) line_work_order(const LineParams p, unsigned *cursor, unsigned *order) {
+__global__ void __launch_bounds__(256) line_work_order(const LineWorkArgs p, unsigned *cursor, unsigned *order) {
     __shared__ unsigned h[LINE_WORK_BUCKETS];
     if (threadIdx.x < LINE_WORK_BUCKETS) h[threadIdx.x] = 0;
     __syncthreads();
@@ -394,6 +395,25 @@ __global__ void __launch_bounds__(256) line_work_order(const LineParams p, unsig
     __syncthreads();
     for (int64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x)
         order[atomicAdd(&h[line_work_bucket(p, i)], 1u)] = (unsigned)i;
+}
+
+size_t line_work_order_bytes(int64_t n) {
+    if (n < 2) return 0;
+    return line_ws_align((size_t)LINE_WORK_BUCKETS * 8) + line_ws_align((size_t)(n - 1) * 4);
+}
+
+const unsigned *build_line_work_order(const LineWorkArgs &a, void *workspace, size_t ws_bytes, cudaStream_t st) {
+    if (a.n < 2 || !workspace || ws_bytes < line_work_order_bytes(a.n) || ((uintptr_t)workspace & 255u))
+        return nullptr;
+    unsigned *hist = (unsigned *)workspace;
+    unsigned *cursor = hist + LINE_WORK_BUCKETS;
+    unsigned *order = (unsigned *)((char *)workspace + line_ws_align((size_t)LINE_WORK_BUCKETS * 8));
+    if (cudaMemsetAsync(hist, 0, (size_t)LINE_WORK_BUCKETS * 4, st) != cudaSuccess) return nullptr;
+    line_work_hist<<<grid_of(a.n - 1), 256, 0, st>>>(a, hist);
+    line_work_scan<<<1, 32, 0, st>>>(hist, cursor);
+    const int64_t tiles = (a.n - 1 + LINE_ORDER_TILE - 1) / LINE_ORDER_TILE;
+    line_work_order<<<(unsigned)tiles, 256, 0, st>>>(a, cursor, order);
+    return order;
 }
 
 __global__ void __launch_bounds__(256) line_axis0_ordered_kernel(const LineParams p, const unsigned *order) {
@@ -504,12 +524,7 @@ int build_line_params(LineParams &p, const dsgb_column *cols, int32_t ncols, int
 
 using namespace dsgb;
 
-static size_t line_ws_align(size_t v) { return (v + 255) / 256 * 256; }
-
-extern "C" size_t dsgb_line_workspace_size(int64_t n) {
-    if (n < 2) return 0;
-    return line_ws_align((size_t)LINE_WORK_BUCKETS * 8) + line_ws_align((size_t)(n - 1) * 4);
-}
+extern "C" size_t dsgb_line_workspace_size(int64_t n) { return line_work_order_bytes(n); }
 
 static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
                            int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
@@ -567,17 +582,14 @@ static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, in
         if (sms <= 0) sms = 148;
         int64_t blocks = (n + 255) / 256;
         if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
-        const size_t need = dsgb_line_workspace_size(n);
-        if (line_width > 0.0 && workspace && ws_bytes >= need && !((uintptr_t)workspace & 255u)) {
-            unsigned *hist = (unsigned *)workspace;
-            unsigned *cursor = hist + LINE_WORK_BUCKETS;
-            unsigned *order = (unsigned *)((char *)workspace + line_ws_align((size_t)LINE_WORK_BUCKETS * 8));
-            cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)LINE_WORK_BUCKETS * 4, st);
-            if (e != cudaSuccess) return cuda_status(e, "line workspace memset");
-            line_work_hist<<<(unsigned)blocks, 256, 0, st>>>(p, hist);
-            line_work_scan<<<1, 32, 0, st>>>(hist, cursor);
-            const int64_t tiles = (n - 1 + LINE_ORDER_TILE - 1) / LINE_ORDER_TILE;
-            line_work_order<<<(unsigned)tiles, 256, 0, st>>>(p, cursor, order);
+        const unsigned *order = nullptr;
+        if (line_width > 0.0) {
+            LineWorkArgs a;
+            a.X = p.cols[p.x_col]; a.Y = p.cols[p.y_col]; a.n = n;
+            a.sx = p.sx; a.sy = p.sy; a.line_width = line_width;
+            order = build_line_work_order(a, workspace, ws_bytes, st);
+        }
+        if (order) {
             line_axis0_ordered_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, order);
         } else {
             line_axis0_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);

@@ -219,8 +219,13 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
     }
 }
 
-__global__ void __launch_bounds__(256) line_backward_kernel(const BwdParams p) {
-    for (int64_t i = gtid(); i + 1 < p.n; i += gstride()) {
+// `order` (may be null) lists the segments in work order (see
+// build_line_work_order): the lanes of a warp then recompute segments of
+// similar pixel counts.  Each segment's results go to its own rows, so the
+// order changes only the order of the grad_y atomics.
+__global__ void __launch_bounds__(256) line_backward_kernel(const BwdParams p, const unsigned *order) {
+    for (int64_t k = gtid(); k + 1 < p.n; k += gstride()) {
+        const int64_t i = order ? (int64_t)order[k] : k;
         const double field = load_f64(p.V, i);
         const double xv0 = load_f64(p.X, i), yv0 = load_f64(p.Y, i);
         const double xv1 = load_f64(p.X, i + 1), yv1 = load_f64(p.Y, i + 1);
@@ -305,12 +310,12 @@ __global__ void __launch_bounds__(256) points_backward_kernel(const PBwdParams p
 
 using namespace dsgb;
 
-extern "C" int dsgb_line_axis0_backward(const dsgb_column *cols, int32_t ncols, int64_t n,
-                                        int32_t x_col, int32_t y_col, int32_t v_col,
-                                        const dsgb_canvas *canvas, double line_width,
-                                        int32_t plot_start, const double *grad_agg,
-                                        const uint8_t *agg_any, double *grad_v, double *grad_y,
-                                        void *stream) {
+extern "C" int dsgb_line_axis0_backward_ws(const dsgb_column *cols, int32_t ncols, int64_t n,
+                                           int32_t x_col, int32_t y_col, int32_t v_col,
+                                           const dsgb_canvas *canvas, double line_width,
+                                           int32_t plot_start, const double *grad_agg,
+                                           const uint8_t *agg_any, double *grad_v, double *grad_y,
+                                           void *workspace, size_t workspace_bytes, void *stream) {
     if (!cols || !canvas || !grad_agg || !grad_v || !grad_y || n < 0 || x_col < 0 || y_col < 0 || v_col < 0 ||
         x_col >= ncols || y_col >= ncols || v_col >= ncols || canvas->width <= 0 || canvas->height <= 0) {
         set_error("dsgb_line_axis0_backward: invalid arguments");
@@ -334,9 +339,24 @@ extern "C" int dsgb_line_axis0_backward(const dsgb_column *cols, int32_t ncols, 
     cudaError_t e = cudaMemsetAsync(grad_y, 0, (size_t)n * 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(grad_v, 0, (size_t)n * 8, st);
     if (e != cudaSuccess) return cuda_status(e, "dsgb_line_axis0_backward memset");
-    if (n > 1) line_backward_kernel<<<grid_of(n), 256, 0, st>>>(p);
+    if (n > 1) {
+        LineWorkArgs a;
+        a.X = p.X; a.Y = p.Y; a.n = n; a.sx = p.sx; a.sy = p.sy; a.line_width = line_width;
+        const unsigned *order = build_line_work_order(a, workspace, workspace_bytes, st);
+        line_backward_kernel<<<grid_of(n), 256, 0, st>>>(p, order);
+    }
     DSGB_CHECK_LAUNCH("dsgb_line_axis0_backward");
     return DSGB_OK;
+}
+
+extern "C" int dsgb_line_axis0_backward(const dsgb_column *cols, int32_t ncols, int64_t n,
+                                        int32_t x_col, int32_t y_col, int32_t v_col,
+                                        const dsgb_canvas *canvas, double line_width,
+                                        int32_t plot_start, const double *grad_agg,
+                                        const uint8_t *agg_any, double *grad_v, double *grad_y,
+                                        void *stream) {
+    return dsgb_line_axis0_backward_ws(cols, ncols, n, x_col, y_col, v_col, canvas, line_width, plot_start,
+                                       grad_agg, agg_any, grad_v, grad_y, nullptr, 0, stream);
 }
 
 extern "C" int dsgb_points_backward(const dsgb_column *cols, int32_t ncols, int64_t n,

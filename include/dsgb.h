@@ -264,6 +264,18 @@ int dsgb_line_axis0_backward(const dsgb_column *cols, int32_t ncols, int64_t n,
                              const uint8_t *agg_any, double *grad_v, double *grad_y,
                              void *stream);
 
+/* dsgb_line_axis0_backward with a workspace of dsgb_line_workspace_size(n)
+ * bytes (256-byte aligned): the segments are recomputed in the forward's
+ * work order (bucketed by estimated pixel count), so the lanes of a warp do
+ * similar work.  Same results up to the order of the float64 atomics that
+ * accumulate dL/dy; a missing or short workspace runs in row order. */
+int dsgb_line_axis0_backward_ws(const dsgb_column *cols, int32_t ncols, int64_t n,
+                                int32_t x_col, int32_t y_col, int32_t v_col,
+                                const dsgb_canvas *canvas, double line_width,
+                                int32_t plot_start, const double *grad_agg,
+                                const uint8_t *agg_any, double *grad_v, double *grad_y,
+                                void *workspace, size_t workspace_bytes, void *stream);
+
 /* Adjoint of points sum / mean w.r.t. the value column (gather):
  * grad_v[i] = grad_agg[p(i)] (sum) or grad_agg[p(i)]/count[p(i)] (mean when
  * counts != NULL); rows that are NaN or out of bounds get 0. */

@@ -137,3 +137,43 @@ def test_points_adjoint_vs_finite_differences(mean):
         lp = float((torch.nan_to_num(f(X, Y, torch.from_numpy(vp).cuda(), cvs)) * w).sum())
         lm = float((torch.nan_to_num(f(X, Y, torch.from_numpy(vm).cuda(), cvs)) * w).sum())
         assert abs((lp - lm) / (2 * h) - float(V.grad[i])) <= 1e-7 * max(1.0, abs(float(V.grad[i])))
+
+
+def test_line_adjoint_work_order_matches_row_order():
+    """The adjoint with a workspace recomputes segments in work order; without
+    one, in row order.  dL/dv is a plain store per segment (bit-identical);
+    dL/dy sums float64 atomics in another order (1e-12 relative)."""
+    import ctypes
+    from datashader_gb300 import _native as N
+    from datashader_gb300.autograd import _canvas_desc
+    from datashader_gb300.core import dsgb_dtype
+    x, y, v = _series(nseries=40, length=400, seed=5)
+    cvs = _canvas(y)
+    dev = torch.device("cuda")
+    xt, yt, vt = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (x, y, v))
+    rng = np.random.default_rng(5)
+    grad = torch.from_numpy(rng.standard_normal((cvs.plot_height, cvs.plot_width))).to(dev)
+    n = vt.numel()
+    cv = _canvas_desc(cvs, cvs.x_range, cvs.y_range)
+    cols = (N.Column * 3)(N.Column(xt.data_ptr(), dsgb_dtype(xt), 0), N.Column(yt.data_ptr(), dsgb_dtype(yt), 0),
+                          N.Column(vt.data_ptr(), dsgb_dtype(vt), 0))
+    L = N.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    out = []
+    for ordered in (False, True):
+        gv = torch.empty(n, dtype=torch.float64, device=dev)
+        gy = torch.empty(n, dtype=torch.float64, device=dev)
+        if ordered:
+            wsz = int(L.dsgb_line_workspace_size(n))
+            ws = torch.empty(wsz, dtype=torch.uint8, device=dev)
+            N.check(L.dsgb_line_axis0_backward_ws(cols, 3, n, 0, 1, 2, ctypes.byref(cv), 1.5, 1, grad.data_ptr(),
+                                                  None, gv.data_ptr(), gy.data_ptr(), ws.data_ptr(), wsz, st),
+                    "dsgb_line_axis0_backward_ws")
+        else:
+            N.check(L.dsgb_line_axis0_backward(cols, 3, n, 0, 1, 2, ctypes.byref(cv), 1.5, 1, grad.data_ptr(),
+                                               None, gv.data_ptr(), gy.data_ptr(), st), "dsgb_line_axis0_backward")
+        out.append((gv.cpu().numpy(), gy.cpu().numpy()))
+    (gv0, gy0), (gv1, gy1) = out
+    assert np.array_equal(gv0, gv1)
+    np.testing.assert_allclose(gy1, gy0, rtol=1e-12, atol=1e-12 * np.abs(gy0).max())
+    assert np.abs(gv0).max() > 0 and np.abs(gy0).max() > 0
