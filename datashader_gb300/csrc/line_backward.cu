@@ -30,24 +30,35 @@
 namespace dsgb {
 
 // ---------------------------------------------------------------- duals
+//
+// The value is float64 and computed with exactly the forward kernel's
+// operations (it decides every pixel and branch).  The three tangents are
+// float32: they only feed dL/dy, whose contract is agreement with float64
+// finite differences to 1e-4 relative, and GB300 issues float64 at a small
+// fraction of its float32 rate, so each dual operation costs one float64
+// operation instead of seven.
 
 struct D3 {
-    double v, g0, g1, g2;
+    double v;
+    float g0, g1, g2;
 };
-__device__ __forceinline__ D3 dc(double v) { return D3{v, 0.0, 0.0, 0.0}; }
+__device__ __forceinline__ float f32(double v) { return __double2float_rn(v); }
+__device__ __forceinline__ D3 dc(double v) { return D3{v, 0.0f, 0.0f, 0.0f}; }
 __device__ __forceinline__ D3 operator+(D3 a, D3 b) { return D3{a.v + b.v, a.g0 + b.g0, a.g1 + b.g1, a.g2 + b.g2}; }
 __device__ __forceinline__ D3 operator-(D3 a, D3 b) { return D3{a.v - b.v, a.g0 - b.g0, a.g1 - b.g1, a.g2 - b.g2}; }
 __device__ __forceinline__ D3 operator-(D3 a) { return D3{-a.v, -a.g0, -a.g1, -a.g2}; }
 __device__ __forceinline__ D3 operator*(D3 a, D3 b) {
-    return D3{a.v * b.v, a.g0 * b.v + a.v * b.g0, a.g1 * b.v + a.v * b.g1, a.g2 * b.v + a.v * b.g2};
+    const float af = f32(a.v), bf = f32(b.v);
+    return D3{a.v * b.v, a.g0 * bf + af * b.g0, a.g1 * bf + af * b.g1, a.g2 * bf + af * b.g2};
 }
 __device__ __forceinline__ D3 operator/(D3 a, D3 b) {
     const double q = a.v / b.v;
-    return D3{q, (a.g0 - q * b.g0) / b.v, (a.g1 - q * b.g1) / b.v, (a.g2 - q * b.g2) / b.v};
+    const float qf = f32(q), rb = 1.0f / f32(b.v);
+    return D3{q, (a.g0 - qf * b.g0) * rb, (a.g1 - qf * b.g1) * rb, (a.g2 - qf * b.g2) * rb};
 }
 __device__ __forceinline__ D3 dsqrt(D3 a) {
     const double r = sqrt(a.v);
-    const double k = r > 0.0 ? 0.5 / r : 0.0;
+    const float k = r > 0.0 ? 0.5f / f32(r) : 0.0f;
     return D3{r, a.g0 * k, a.g1 * k, a.g2 * k};
 }
 __device__ __forceinline__ D3 dabs(D3 a) { return a.v < 0.0 ? -a : a; }
@@ -167,6 +178,7 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
     const long long yend = clampi_b((long long)floor(b[4 + (lowindex + 2) % 4].v), 0, ymaxi);
     int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
     const double lw_lo = 0.5 * (line_width - aa);
+    float ty0 = 0.0f, ty1 = 0.0f, ty2 = 0.0f;     // the y tangents of this segment, in float32
     for (long long y = ystart; y <= yend; ++y) {
         const double yd = (double)y;
         if (ll == lowindex && yd > b[4 + lu].v) { ll = lu; lu = (ll + 1) % 4; }
@@ -211,12 +223,16 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
                 const double g = p.grad[pix];
                 const D3 d = value - prev_value;
                 gv += g * d.v;
-                gy0 += g * field * d.g0;
-                gy1 += g * field * d.g1;
-                gy2 += g * field * d.g2;
+                const float gf = f32(g * field);
+                ty0 += gf * d.g0;
+                ty1 += gf * d.g1;
+                ty2 += gf * d.g2;
             }
         }
     }
+    gy0 += (double)ty0;
+    gy1 += (double)ty1;
+    gy2 += (double)ty2;
 }
 
 // `order` (may be null) lists the segments in work order (see
@@ -239,7 +255,7 @@ __global__ void __launch_bounds__(256) line_backward_kernel(const BwdParams p, c
         if (isnull(field) || isnull(xv0) || isnull(yv0) || isnull(xv1) || isnull(yv1)) continue;
         // tangents: g0 = d/dy_{i-1}, g1 = d/dy_i, g2 = d/dy_{i+1}
         D3 x0 = dc(xv0), x1 = dc(xv1);
-        D3 y0 = D3{yv0, 0.0, 1.0, 0.0}, y1 = D3{yv1, 0.0, 0.0, 1.0};
+        D3 y0 = D3{yv0, 0.0f, 1.0f, 0.0f}, y1 = D3{yv1, 0.0f, 0.0f, 1.0f};
         // line.py:734-780 (Liang-Barsky) in duals
         bool skip = false;
         if (x0.v < p.xmin && x1.v < p.xmin) skip = true;
@@ -265,7 +281,7 @@ __global__ void __launch_bounds__(256) line_backward_kernel(const BwdParams p, c
         D3 pxm = dc(0.0), pym = dc(0.0);
         if (!segment_start) {
             pxm = dc(xmv) * sxd + txd - half;
-            pym = D3{ymv, 1.0, 0.0, 0.0} * syd + tyd - half;
+            pym = D3{ymv, 1.0f, 0.0f, 0.0f} * syd + tyd - half;
         }
         const long long nx = (long long)rint((p.xmax - p.xmin) * p.sx);
         const long long ny = (long long)rint((p.ymax - p.ymin) * p.sy);
