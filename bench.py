@@ -383,9 +383,9 @@ def bench_serving(args, dev):
     out = {"workload": f"{n:,} resident points (13 B/point), {args.serving_requests} requests per rate",
            "store_sort_ms": sort_s * 1e3, "slots": args.serving_slots, "mem_budget_gb": args.serving_mem_gb,
            "rates": {}}
-    for rate in (200, 1000, 5000):
+    for rate in (int(r) for r in args.serving_rates.split(",")):
         per = {}
-        for mode in ("batched", "sequential", "plain"):
+        for mode in args.serving_modes.split(","):
             reqs = S.generate_requests(args.serving_requests, rate=rate, seed=rate)
             server.peak_inflight = 0
             server.run(reqs, mode=mode)
@@ -592,6 +592,8 @@ def main():
     ap.add_argument("--line-series", type=int, default=1000, help="0 skips the line workload")
     ap.add_argument("--line-cpu-series", type=int, default=20)
     ap.add_argument("--serving-slots", type=int, default=8)
+    ap.add_argument("--serving-rates", default="200,1000,5000", help="Poisson arrival rates (req/s)")
+    ap.add_argument("--serving-modes", default="batched,sequential,plain")
     ap.add_argument("--serving-mem-gb", type=int, default=8)
     ap.add_argument("--only", default="all", choices=["all", "pyramid", "line", "serving"],
                     help="run one secondary workload alone (for profiling); prints its JSON object")
