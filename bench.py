@@ -56,6 +56,13 @@ def count_traffic(n):
     return 163.31e6 / 2e7 * n + 3.09e6
 
 
+# The same for the hot-tile mean('v') launch (x/y float32 + v float64), from
+# an ncu capture of cached_mean_main at 2e7 rows (329.75 MB read, 3.51 MB
+# written; profiles/cached_mean_main_mean_2e7_1024_full.md).
+def mean_traffic(n):
+    return 329.75e6 / 2e7 * n + 3.51e6
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -485,7 +492,7 @@ def run_gpu(args):
     _probe.allocate(1024, 1024, dev)
     _cv = N.CanvasDesc(1024, 1024, 0, 0, 128.0, 512.0, 128.0, 512.0, -4.0, 4.0, -4.0, 4.0)
     kernels_per_count = 2 if N.lib().dsgb_points_workspace_size(n, ctypes.byref(_cv), _probe.bases, 1) else 1
-    rl_mean = roofline(ds.mean("v"), 16, 12, args.steps)
+    rl_mean = roofline(ds.mean("v"), 16, 12, args.steps, traffic=mean_traffic(n))
 
     # mean through the public API
     for _ in range(2):
