@@ -139,7 +139,7 @@ EXPORTED = (
     "dsgb_points_ws", "dsgb_points_segments",
     "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_workspace_size", "dsgb_line_axis0_ws", "dsgb_lines", "dsgb_line_axis0_backward", "dsgb_line_axis0_backward_ws",
     "dsgb_points_backward", "dsgb_bounds", "dsgb_eq_hist_workspace_size", "dsgb_eq_hist_u32",
-    "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_shade_workspace_size", "dsgb_shade_u32", "dsgb_shade_f64", "dsgb_pyramid_tile_offset", "dsgb_pyramid_workspace_size", "dsgb_pyramid", "dsgb_pyramid_status",
+    "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_shade_workspace_size", "dsgb_shade_u32", "dsgb_shade_f64", "dsgb_composite", "dsgb_pyramid_tile_offset", "dsgb_pyramid_workspace_size", "dsgb_pyramid", "dsgb_pyramid_status",
 )
 
 _lock = threading.Lock()
@@ -192,6 +192,7 @@ def _declare(L):
         getattr(L, nm).argtypes = [P, i64, i32, P, P, P, P, i32, i32, i32, P, ctypes.c_size_t, P]
     L.dsgb_shade_workspace_size.argtypes = []
     L.dsgb_shade_workspace_size.restype = ctypes.c_size_t
+    L.dsgb_composite.argtypes = [P, P, u32, i64, i32, P, P]
     for nm in ("dsgb_shade_u32", "dsgb_shade_f64"):
         getattr(L, nm).argtypes = [P, i64, i32, P, P, i32, P, i32, i32, P, P, ctypes.c_size_t, P]
     L.dsgb_eq_hist_u32_static.argtypes = [P, i64, i32, P, P, P, P, i32, i32, i32, P]

@@ -179,3 +179,64 @@ def shade(agg, cmap=("lightblue", "darkblue"), color_key=None, how="eq_hist", al
     _, _, rgba = _run_eq_hist(agg.data, cmap=list(cmap), alpha=alpha,
                               rescale_discrete_levels=rescale_discrete_levels)
     return Image(rgba, agg.dims, agg.coords, agg.attrs, name=name)
+
+
+# ---------------------------------------------------------------- compositing
+
+_COMPOSITE = {"source": 0, "over": 1, "add": 2, "saturate": 3}
+
+
+def _composite(src, dst, how):
+    """op(src, dst) per pixel on the GPU (dsgb_composite): dst is a tensor of
+    src's shape or one uint32 pixel value."""
+    if how not in _COMPOSITE:
+        ops = ", ".join(repr(k) for k in _COMPOSITE)
+        raise ValueError(f"Operator {how!r} not one of the supported image operators: {ops}")
+    src = src.contiguous()
+    out = torch.empty_like(src)
+    if isinstance(dst, torch.Tensor):
+        dst = dst.contiguous()
+        dptr, dval = dst.data_ptr(), 0
+    else:
+        dptr, dval = None, int(dst) & 0xFFFFFFFF
+    N.check(N.lib().dsgb_composite(src.data_ptr(), dptr, dval, src.numel(), _COMPOSITE[how], out.data_ptr(),
+                                   torch.cuda.current_stream(src.device).cuda_stream), "dsgb_composite")
+    return out
+
+
+def stack(*imgs, **kwargs):
+    """tf.stack (transfer_functions/__init__.py:115-145): later images are
+    composited onto earlier ones with ``how`` (default 'over')."""
+    if not imgs:
+        raise ValueError("No images passed in")
+    shapes = []
+    for i in imgs:
+        if not isinstance(i, Image):
+            raise TypeError(f"Expected `Image`, got: `{type(i)}`")
+        if not shapes:
+            shapes.append(i.shape)
+        elif i.shape not in shapes:
+            raise ValueError("The stacked images must have the same shape.")
+    name = kwargs.get("name", None)
+    how = kwargs.get("how", "over")
+    if how not in _COMPOSITE:
+        _composite(imgs[0].data, 0, how)            # raises the reference's message
+    if len(imgs) == 1:
+        return imgs[0]
+    acc = imgs[0].data
+    for img in imgs[1:]:
+        acc = _composite(img.data, acc, how)
+    return Image(acc, imgs[0].dims, imgs[0].coords, imgs[0].attrs, name=name)
+
+
+def set_background(img, color=None, name=None):
+    """tf.set_background (transfer_functions/__init__.py:748-767): the image
+    composited 'over' an opaque background colour."""
+    if not isinstance(img, Image):
+        raise TypeError(f"Expected `Image`, got: `{type(img)}`")
+    name = img.name if name is None else name
+    if color is None:
+        return img
+    r, g, b = rgb(color)
+    background = r | (g << 8) | (b << 16) | (255 << 24)
+    return Image(_composite(img.data, background, "over"), img.dims, img.coords, img.attrs, name=name)

@@ -339,6 +339,14 @@ int dsgb_shade_f64(const double *data, int64_t n, int32_t how, const double *spa
                    int32_t alpha, int32_t min_alpha, uint32_t *rgba,
                    void *workspace, size_t workspace_bytes, void *stream);
 
+/* Image compositing (datashader/composite.py:31-127; tf.stack
+ * transfer_functions/__init__.py:115-145 and tf.set_background :748-767):
+ * out[i] = op(src[i], dst ? dst[i] : dst_value) on uint32 RGBA pixels, op
+ * 0 = source, 1 = over, 2 = add, 3 = saturate, bit-identical to the
+ * reference's float64 arithmetic.  out may alias src or dst. */
+int dsgb_composite(const uint32_t *src, const uint32_t *dst, uint32_t dst_value, int64_t n, int32_t op,
+                   uint32_t *out, void *stream);
+
 /* ---- batched tile pyramid --------------------------------------------------
  * Every tile (z, tx, ty), zmin <= z <= zmax, of the square [x0,x1]x[y0,y1]
  * in one pass: tile (z, tx, ty) equals

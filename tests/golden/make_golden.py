@@ -14,7 +14,14 @@ Reads (as text, via ``ast``; nothing from the reference is imported or run):
 * ``datashader/tests/test_transfer_functions.py`` -- ``eq_hist_sol`` and
   ``eq_hist_sol_rescale_discrete_levels`` (uint32 RGBA images), the
   linear / log / cbrt ``solution_lists`` and the ``sol`` arrays of
-  ``test_span_cmap_single`` and ``test_shade_cmap``.
+  ``test_span_cmap_single`` and ``test_shade_cmap``;
+* ``datashader/tests/test_composite.py`` -- every ``assert_equal(op(src,
+  dst), o)`` of the source / over / add / saturate tests: the module's
+  literal ``src`` and colours, each test body's numpy statements on ``o``
+  replayed in order (they are plain numpy on literals), the operator under
+  test never called;
+* ``datashader/tests/test_tiles.py`` -- the extent, zoom and expected tile
+  of ``test_meters_to_tile``.
 
 Usage::
 
@@ -143,7 +150,64 @@ def main(ref_root):
         shade[fn] = dict(_jsonable(np.array(val, dtype="u4")), source=f"datashader/tests/test_transfer_functions.py:{line}")
     with open(os.path.join(HERE, "shade.json"), "w") as f:
         json.dump(shade, f, indent=0)
-    print("wrote", sorted(goldens), sorted(eq), sorted(shade), sorted(lines))
+    comp = _composite_cases(os.path.join(tests, "test_composite.py"))
+    with open(os.path.join(HERE, "composite.json"), "w") as f:
+        json.dump(comp, f, indent=0)
+    tiles = _meters_to_tile_case(os.path.join(tests, "test_tiles.py"))
+    with open(os.path.join(HERE, "tiles.json"), "w") as f:
+        json.dump(tiles, f, indent=0)
+    print("wrote", sorted(goldens), sorted(eq), sorted(shade), sorted(lines), len(comp["cases"]), "composite cases",
+          sorted(tiles))
+
+
+def _meters_to_tile_case(path):
+    """Literal extent, zoom and asserted tile of test_meters_to_tile."""
+    tree = ast.parse(open(path).read())
+    for node in tree.body:
+        if isinstance(node, ast.FunctionDef) and node.name == "test_meters_to_tile":
+            env = {}
+            for st in node.body:
+                if (isinstance(st, ast.Assign) and isinstance(st.targets[0], ast.Name)
+                        and st.targets[0].id in ("full_extent_of_data", "zoom")):
+                    env[st.targets[0].id] = ast.literal_eval(st.value)
+                elif isinstance(st, ast.Assert) and isinstance(st.test, ast.Compare):
+                    env["expected"] = ast.literal_eval(st.test.comparators[0])
+                    env["source"] = f"datashader/tests/test_tiles.py:{st.lineno}"
+            return {"meters_to_tile": {"extent": list(env["full_extent_of_data"]), "zoom": env["zoom"],
+                                       "expected": list(env["expected"]), "source": env["source"]}}
+    raise ValueError("test_meters_to_tile not found")
+
+
+def _composite_cases(path):
+    """(operator, src, dst, expected) of each assertion in test_composite.py."""
+    tree = ast.parse(open(path).read())
+    ns = {"np": np}
+    for node in tree.body:                       # module literals: src and the colours
+        if isinstance(node, ast.Assign) and isinstance(node.targets[0], ast.Name):
+            exec(compile(ast.Module([node], type_ignores=[]), path, "exec"), ns)
+    cases = []
+    for node in tree.body:
+        if not (isinstance(node, ast.FunctionDef) and node.name.startswith("test_")):
+            continue
+        env = dict(ns)
+        for st in node.body:
+            if isinstance(st, ast.Assign):         # o = ..., o[...] = ...: numpy on literals
+                exec(compile(ast.Module([st], type_ignores=[]), path, "exec"), env)
+            elif isinstance(st, ast.Expr) and isinstance(st.value, ast.Call):
+                call = st.value
+                fn = ast.unparse(call.func)
+                if fn != "np.testing.assert_equal":
+                    continue
+                op_call, want = call.args
+                op = op_call.func.id
+                src = eval(compile(ast.Expression(op_call.args[0]), path, "eval"), env)
+                dst = eval(compile(ast.Expression(op_call.args[1]), path, "eval"), env)
+                exp = eval(compile(ast.Expression(want), path, "eval"), env)
+                cases.append({"op": op, "src": np.asarray(src, dtype=np.uint32).ravel().tolist(),
+                              "shape": list(np.shape(src)), "dst": int(np.uint32(dst)),
+                              "expected": np.asarray(exp, dtype=np.uint32).ravel().tolist(),
+                              "source": f"datashader/tests/test_composite.py:{st.lineno}"})
+    return {"cases": cases}
 
 
 def _function_all_sols(path, names):
