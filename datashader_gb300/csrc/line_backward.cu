@@ -68,8 +68,12 @@ __device__ __forceinline__ D3 dclamp(D3 x, double lo, double hi) {
     D3 m = x.v < hi ? x : dc(hi);
     return lo > m.v ? dc(lo) : m;
 }
-__device__ __forceinline__ D3 dlinearstep(double e0, double e1, D3 x) {
-    return dclamp((x - dc(e0)) / dc(e1 - e0), 0.0, 1.0);
+// den = edge1 - edge0, computed once per segment; exactly 1.0 skips the
+// division (x / 1.0 == x, and the constant divisor has no tangents), as in
+// the forward kernel.
+__device__ __forceinline__ D3 dlinearstep(double e0, double den, bool unit_den, D3 x) {
+    const D3 d = x - dc(e0);
+    return dclamp(unit_den ? d : d / dc(den), 0.0, 1.0);
 }
 __device__ __forceinline__ D3 dx_intercept(double y, D3 cx0, D3 cy0, D3 cx1, D3 cy1) {
     if (cy0.v == cy1.v) return cx1;
@@ -178,6 +182,8 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
     const long long yend = clampi_b((long long)floor(b[4 + (lowindex + 2) % 4].v), 0, ymaxi);
     int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
     const double lw_lo = 0.5 * (line_width - aa);
+    const double ls_den = halfwidth - lw_lo;
+    const bool unit_den = ls_den == 1.0;
     float ty0 = 0.0f, ty1 = 0.0f, ty2 = 0.0f;     // the y tangents of this segment, in float32
     for (long long y = ystart; y <= yend; ++y) {
         const double yd = (double)y;
@@ -206,12 +212,12 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
                         prev_correction = true;
                 }
             }
-            D3 value = dc(1.0) - dlinearstep(lw_lo, halfwidth, distance);
+            D3 value = dc(1.0) - dlinearstep(lw_lo, ls_den, unit_den, distance);
             value = value * dc(scale);
             D3 prev_value = dc(0.0);
             if (prev_correction) {
                 const D3 prev_distance = dabs((xd - x0) * prev_rightx + (ydd - y0) * prev_righty);
-                prev_value = dc(1.0) - dlinearstep(lw_lo, halfwidth, prev_distance);
+                prev_value = dc(1.0) - dlinearstep(lw_lo, ls_den, unit_den, prev_distance);
                 prev_value = prev_value * dc(scale);
                 if (value.v <= prev_value.v) value = dc(0.0);
             }
