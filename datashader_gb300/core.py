@@ -168,6 +168,29 @@ class PartitionedFrame:
         return self.partitions[0].signature()
 
 
+class HostFrame(TensorFrame):
+    """Named columns held in pinned host memory (numpy arrays or CPU tensors
+    are pinned once, on construction).  Canvas.points streams them to the
+    GPU in chunks of ``chunk_rows`` rows through two device buffers: the copy
+    of one chunk (its own CUDA stream) overlaps the aggregation of the
+    previous one, every chunk accumulates into the same bases with its row
+    offset, and one finalize at the end reads the lookup column of first /
+    last / where straight from the pinned host memory.  The data never has
+    to fit in device memory.  ``device`` is the GPU that aggregates."""
+
+    def __init__(self, columns, categories=None, device=None, row_offset=0, chunk_rows=1 << 24):
+        self.gpu = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if int(chunk_rows) < 1:
+            raise ValueError("chunk_rows must be positive")
+        self.chunk_rows = int(chunk_rows)
+        super().__init__(columns, categories=categories, device="cpu", row_offset=row_offset)
+
+    def _to_device(self, v):
+        t = v if isinstance(v, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(v))
+        t = t.cpu().contiguous()
+        return t if t.is_pinned() else t.pin_memory()
+
+
 def as_frame(source):
     if isinstance(source, (TensorFrame, PartitionedFrame)):
         return source
@@ -422,6 +445,8 @@ def bypixel(source, canvas, glyph, agg, *, antialias=False, flags=0):
     canvas.validate()
     if isinstance(frame, PartitionedFrame):
         return partitioned_pipeline(frame, canvas, glyph, agg, flags=flags)
+    if isinstance(frame, HostFrame):
+        return streamed_pipeline(frame, canvas, glyph, agg, flags=flags)
     return gpu_pipeline(frame, canvas, glyph, agg, antialias=antialias, flags=flags)
 
 
@@ -645,6 +670,132 @@ def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
     if head.nouts:
         N.check(L.dsgb_finalize(head.cols, len(head.names), parts[0].row_offset, head.bases, len(plan.bases),
                                 head.outs, head.nouts, width * height, stream), "dsgb_finalize")
+    coords = {glyph.x_label: canvas.x_axis.compute_index(x_st, width),
+              glyph.y_label: canvas.y_axis.compute_index(y_st, height)}
+    dims = [glyph.y_label, glyph.x_label]
+    return _results(plan, head, coords, dims, dict(x_range=x_range, y_range=y_range))
+
+
+_COPY_STREAMS = {}
+
+
+def _chunks(n, size):
+    return [(c0, min(n, c0 + size)) for c0 in range(0, n, size)] or [(0, 0)]
+
+
+class _Staging:
+    """Two device buffers per column and the events that order a chunk's
+    copy (on a copy stream) against the kernels that read it."""
+
+    def __init__(self, hframe, names, dev):
+        self.hf, self.names, self.dev = hframe, names, dev
+        self.rows = min(hframe.chunk_rows, max(len(hframe), 1))
+        self.bufs = {k: [torch.empty(self.rows, dtype=hframe[k].dtype, device=dev) for _ in range(2)]
+                     for k in names}
+        key = str(dev)
+        if key not in _COPY_STREAMS:
+            _COPY_STREAMS[key] = torch.cuda.Stream(dev)
+        self.copy = _COPY_STREAMS[key]
+        self.ready = [torch.cuda.Event() for _ in range(2)]
+        self.free = [torch.cuda.Event() for _ in range(2)]
+
+    def stage(self, i, c0, c1, compute):
+        """Copy rows [c0, c1) into slot i % 2 and make ``compute`` wait for them."""
+        s = i % 2
+        with torch.cuda.stream(self.copy):
+            if i >= 2:
+                self.copy.wait_event(self.free[s])       # the kernels of chunk i - 2 are done with the slot
+            for k in self.names:
+                self.bufs[k][s][:c1 - c0].copy_(self.hf[k][c0:c1], non_blocking=True)
+            self.ready[s].record(self.copy)
+        compute.wait_event(self.ready[s])
+        return {k: self.bufs[k][s][:c1 - c0] for k in self.names}
+
+    def release(self, i, compute):
+        self.free[i % 2].record(compute)
+
+
+def _streamed_bounds(hf, staging, names, compute):
+    lo = {k: np.inf for k in names}
+    hi = {k: -np.inf for k in names}
+    stream = compute.cuda_stream
+    for i, (c0, c1) in enumerate(_chunks(len(hf), staging.rows)):
+        if c1 == c0:
+            continue
+        cols = staging.stage(i, c0, c1, compute)
+        for k in names:
+            t = cols[k]
+            out = torch.empty(2, dtype=torch.float64, device=staging.dev)
+            N.check(N.lib().dsgb_bounds(ctypes.byref(N.Column(t.data_ptr(), dsgb_dtype(t), 0)), t.numel(),
+                                        out.data_ptr(), stream), "dsgb_bounds")
+            mn, mx = out.cpu().tolist()
+            lo[k], hi[k] = min(lo[k], mn), max(hi[k], mx)
+        staging.release(i, compute)
+    return {k: _expand_bounds(lo[k], hi[k]) for k in names}
+
+
+def streamed_pipeline(hf, canvas, glyph, agg, *, flags=0):
+    """Canvas.points over a HostFrame: chunks copied on a copy stream while
+    the previous chunk aggregates; bases initialised by the first chunk,
+    accumulated by the rest (each with its global row offset), finalized
+    once (first / last / where gather from the pinned host column)."""
+    if not isinstance(glyph, Point):
+        raise NotImplementedError("host-resident frames are streamed for Canvas.points")
+    if flags & N.FLAG_DETERMINISTIC:
+        raise NotImplementedError("the deterministic mode sums one device frame in row order")
+    dev = hf.gpu
+    compute = torch.cuda.current_stream(dev)
+    stream = compute.cuda_stream
+    plan = compile_plan(agg, hf)
+    needed = [glyph.x, glyph.y]
+    for c in list(plan.columns) + [src for src, _, _ in plan.derived.values()]:
+        if c in hf and c not in needed:
+            needed.append(c)
+    staging = _Staging(hf, needed, dev)
+    if canvas.x_range is None or canvas.y_range is None:
+        b = _streamed_bounds(hf, staging, [k for k, r in ((glyph.x, canvas.x_range), (glyph.y, canvas.y_range))
+                                           if r is None], compute)
+        x_range = canvas.x_range or b[glyph.x]
+        y_range = canvas.y_range or b[glyph.y]
+    else:
+        x_range, y_range = canvas.x_range, canvas.y_range
+    canvas.validate_ranges(x_range, y_range)
+    width, height = canvas.plot_width, canvas.plot_height
+    x_st = canvas.x_axis.compute_scale_and_translate(x_range, width)
+    y_st = canvas.y_axis.compute_scale_and_translate(y_range, height)
+    cv = N.CanvasDesc(width, height, int(canvas.x_axis.is_log), int(canvas.y_axis.is_log),
+                      x_st[0], x_st[1], y_st[0], y_st[1],
+                      float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]))
+    L = N.lib()
+    head = ex = None
+    for i, (c0, c1) in enumerate(_chunks(len(hf), staging.rows)):
+        cols = staging.stage(i, c0, c1, compute)
+        chunk = TensorFrame(cols, categories={k: v for k, v in hf._cats.items() if k in cols}, device=dev,
+                            row_offset=hf.row_offset + c0)
+        ex = Executor(chunk, plan, glyph)
+        if head is None:
+            ex.allocate(height, width, dev)
+            head = ex
+        else:
+            ex.base_tensors, ex.bases, ex.out_tensors, ex.outs, ex.nouts = (
+                head.base_tensors, head.bases, head.out_tensors, head.outs, head.nouts)
+        m = c1 - c0
+        wsz = int(L.dsgb_points_workspace_size_flags(m, ctypes.byref(cv), head.bases, len(plan.bases), flags))
+        ws = workspace(dev, stream, wsz) if wsz else None
+        f = flags | N.FLAG_NO_FINALIZE | (N.FLAG_NO_INIT if i > 0 else 0)
+        N.check(L.dsgb_points_ws(ex.cols, len(ex.names), m, hf.row_offset + c0, 0, 1, ctypes.byref(cv),
+                                 head.bases, len(plan.bases), head.outs, head.nouts,
+                                 ws.data_ptr() if ws is not None else None, wsz, f, stream),
+                "dsgb_points_ws (chunk)")
+        staging.release(i, compute)
+    if head.nouts:
+        # the finalize's gathers index global rows: give it the whole pinned host columns
+        # (mapped into the device's address space); derived columns are not gathered
+        fin = (N.Column * len(ex.names))(*[
+            N.Column(hf[k].data_ptr() if k in hf else t.data_ptr(), dsgb_dtype(hf[k] if k in hf else t), 0)
+            for k, t in zip(ex.names, ex.tensors)])
+        N.check(L.dsgb_finalize(fin, len(ex.names), hf.row_offset, head.bases, len(plan.bases), head.outs,
+                                head.nouts, width * height, stream), "dsgb_finalize")
     coords = {glyph.x_label: canvas.x_axis.compute_index(x_st, width),
               glyph.y_label: canvas.y_axis.compute_index(y_st, height)}
     dims = [glyph.y_label, glyph.x_label]
