@@ -420,7 +420,7 @@ __device__ void stage_and_write(const StageIn in, int ngroups, G group_of, unsig
     }
     __syncthreads();
     for (int g = threadIdx.x; g < ngroups; g += blockDim.x)
-        gbase[g] = cnt[g] ? atomicAdd(&gcursor[g], cnt[g]) : 0u;
+        gbase[g] = (cnt[g] ? atomicAdd(&gcursor[g], cnt[g]) : 0u) - off[g];   // global base minus staged base
 #pragma unroll
     for (int k = 0; k < PYR_STAGE_ITEMS; ++k) {
         if (gv[k] < 0) continue;
@@ -434,7 +434,7 @@ __device__ void stage_and_write(const StageIn in, int ngroups, G group_of, unsig
     const int staged = (int)off[ngroups];
     for (int j = threadIdx.x; j < staged; j += blockDim.x) {
         const int g = sg[j];
-        const unsigned pos = gbase[g] + (unsigned)j - off[g];
+        const unsigned pos = gbase[g] + (unsigned)j;
         ox[pos] = sx[j];
         oy[pos] = sy[j];
         if (ov) ov[pos] = sv[j];
