@@ -634,9 +634,8 @@ def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
     if stream is None:
         stream = torch.cuda.current_stream(dev).cuda_stream
     plan = compile_plan(agg, parts[0])
-    if any(o.fin == N.FIN_GATHER for _, o in plan.outputs):
-        raise NotImplementedError("first/last/where with a lookup column gather values by global row; "
-                                  "they are not supported on partitioned sources")
+    if any(o.fin == N.FIN_GATHER for _, o in plan.outputs) and len(parts) > 64:
+        raise NotImplementedError("first/last/where with a lookup column gather from at most 64 partitions")
     if canvas.x_range is not None and canvas.y_range is not None:
         x_range, y_range = canvas.x_range, canvas.y_range
     else:
@@ -668,8 +667,15 @@ def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
     for ex in execs[1:]:
         N.check(L.dsgb_combine(head.bases, ex.bases, len(plan.bases), width * height, stream), "dsgb_combine")
     if head.nouts:
-        N.check(L.dsgb_finalize(head.cols, len(head.names), parts[0].row_offset, head.bases, len(plan.bases),
-                                head.outs, head.nouts, width * height, stream), "dsgb_finalize")
+        # gathers (first / last / where with a lookup column) read the selected global row
+        # from the partition that holds it
+        ncols = len(head.names)
+        pcols = (N.Column * max(1, ncols * len(execs)))(*[c for ex in execs for c in ex.cols])
+        first = (ctypes.c_int64 * len(parts))(*[p.row_offset for p in parts])
+        rows = (ctypes.c_int64 * len(parts))(*[len(p) for p in parts])
+        N.check(L.dsgb_finalize_partitioned(pcols, ncols, len(parts), first, rows, head.bases, len(plan.bases),
+                                            head.outs, head.nouts, width * height, stream),
+                "dsgb_finalize_partitioned")
     coords = {glyph.x_label: canvas.x_axis.compute_index(x_st, width),
               glyph.y_label: canvas.y_axis.compute_index(y_st, height)}
     dims = [glyph.y_label, glyph.x_label]

@@ -185,6 +185,33 @@ __global__ void finalize_kernel(const FinArgs a) {
     }
 }
 
+// Gather over row partitions (dask.py:102-117 numbers each partition's rows
+// from its own offset): the row that the combined row-index base selected
+// is looked up in the partition that holds it.
+constexpr int FIN_MAX_PARTS = 64;
+struct GatherParts {
+    int32_t nparts, b0op;
+    const void *b0;
+    void *out;
+    int64_t n;
+    ColumnRef col[FIN_MAX_PARTS];
+    int64_t first[FIN_MAX_PARTS], rows[FIN_MAX_PARTS];
+};
+
+__global__ void gather_parts_kernel(const __grid_constant__ GatherParts g) {
+    for (int64_t i = gtid(); i < g.n; i += gstride()) {
+        const long long r = base_row(g.b0op, g.b0, i);
+        double v = nan_d();
+        if (r >= 0) {
+            for (int p = 0; p < g.nparts; ++p) {
+                const long long j = r - g.first[p];
+                if (j >= 0 && j < g.rows[p]) { v = load_f64(g.col[p], j); break; }
+            }
+        }
+        ((double *)g.out)[i] = v;
+    }
+}
+
 static int base_elem_bytes(int op) {
     switch (op) {
     case DSGB_BASE_COUNT: case DSGB_BASE_AA_CNT0: return 4;
@@ -371,6 +398,53 @@ extern "C" int dsgb_finalize(const dsgb_column *cols, int32_t ncols, int64_t row
                              const dsgb_output *outs, int32_t nouts, int64_t ncells, void *stream) {
     if ((nbases > 0 && !bases) || (nouts > 0 && !outs) || ncells < 0) { set_error("dsgb_finalize: bad args"); return DSGB_E_INVALID; }
     return finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, as_stream(stream));
+}
+
+// dsgb_finalize for bases combined from row partitions: every output but the
+// gathers as dsgb_finalize with partition 0's columns; a gather reads its row
+// from the partition [first, first + rows) that holds it (NaN if none).
+extern "C" int dsgb_finalize_partitioned(const dsgb_column *part_cols, int32_t ncols, int32_t nparts,
+                                         const int64_t *part_first, const int64_t *part_rows,
+                                         const dsgb_base *bases, int32_t nbases, const dsgb_output *outs,
+                                         int32_t nouts, int64_t ncells, void *stream) {
+    if ((nbases > 0 && !bases) || (nouts > 0 && !outs) || ncells < 0 || nparts < 1 || ncols < 0 ||
+        (ncols > 0 && !part_cols) || !part_first || !part_rows) {
+        set_error("dsgb_finalize_partitioned: bad args");
+        return DSGB_E_INVALID;
+    }
+    if (nparts > FIN_MAX_PARTS) {
+        set_error("dsgb_finalize_partitioned: at most %d partitions", FIN_MAX_PARTS);
+        return DSGB_E_UNSUPPORTED;
+    }
+    cudaStream_t st = as_stream(stream);
+    for (int o = 0; o < nouts; ++o) {
+        const dsgb_output &O = outs[o];
+        if (O.op != DSGB_FIN_GATHER) {
+            const int rc = finalize_outputs(part_cols, ncols, part_first[0], bases, nbases, &O, 1, ncells, st);
+            if (rc) return rc;
+            continue;
+        }
+        if (!O.out || O.base0 < 0 || O.base0 >= nbases || O.col < 0 || O.col >= ncols) {
+            set_error("dsgb_finalize_partitioned: output %d invalid", o);
+            return DSGB_E_INVALID;
+        }
+        GatherParts g;
+        memset(&g, 0, sizeof(g));
+        g.nparts = nparts;
+        g.b0op = bases[O.base0].op;
+        g.b0 = bases[O.base0].agg;
+        g.out = O.out;
+        g.n = ncells * (bases[O.base0].ncat < 1 ? 1 : bases[O.base0].ncat);
+        for (int p = 0; p < nparts; ++p) {
+            const dsgb_column &c = part_cols[(int64_t)p * ncols + O.col];
+            g.col[p] = ColumnRef{c.data, c.dtype};
+            g.first[p] = part_first[p];
+            g.rows[p] = part_rows[p];
+        }
+        if (g.n > 0) gather_parts_kernel<<<grid_for(g.n), 256, 0, st>>>(g);
+        DSGB_CHECK_LAUNCH("dsgb_finalize_partitioned gather");
+    }
+    return DSGB_OK;
 }
 
 // The min/max travel as order-preserving uint64 in the first 16 bytes of

@@ -149,6 +149,17 @@ int dsgb_bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, void
 int dsgb_finalize(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
                   const dsgb_base *bases, int32_t nbases,
                   const dsgb_output *outs, int32_t nouts, int64_t ncells, void *stream);
+/* dsgb_finalize for bases combined (dsgb_combine) from row partitions
+ * (dask.py:86-219, each partition numbering its rows from its own offset,
+ * :102-117): part_cols[p * ncols + c] is column c of partition p, whose
+ * rows are the global rows [part_first[p], part_first[p] + part_rows[p])
+ * (host arrays, nparts <= 64).  A gather output (first / last / where with
+ * a lookup column) reads the selected row from the partition that holds it;
+ * every other output is finalized as by dsgb_finalize. */
+int dsgb_finalize_partitioned(const dsgb_column *part_cols, int32_t ncols, int32_t nparts,
+                              const int64_t *part_first, const int64_t *part_rows,
+                              const dsgb_base *bases, int32_t nbases, const dsgb_output *outs,
+                              int32_t nouts, int64_t ncells, void *stream);
 
 /* ---- Canvas.points ------------------------------------------------------
  * Replaces points.py:182-242 (+ compiler.py create/append/finalize).

@@ -59,8 +59,27 @@ def test_partitions_autorange_and_count_path():
     assert_same(to_numpy(got), to_numpy(whole))
 
 
-def test_partitions_reject_gathered_lookups():
-    cols = _cols(1000, seed=23)
-    parts = ds.PartitionedFrame([_frame(cols, 0, 500), _frame(cols, 500)])
+GATHER = ds.summary(f=ds.first("v"), l=ds.last("v"), wy=ds.where(ds.max("v"), "y"),
+                    wx=ds.where(ds.min("v"), "x"), byf=ds.by("cat", ds.first("v")))
+
+
+@pytest.mark.parametrize("cuts", [(0, 1_000_000), (0, 1, 250_000, 250_001, 1_500_000)])
+def test_partitions_gather_lookups_from_the_holding_partition(cuts):
+    """first / last / where with a lookup column: the combined row-index base
+    picks a global row, the finalize reads it from the partition holding it."""
+    n = 1_800_000
+    cols = _cols(n, seed=23)
+    cvs = ds.Canvas(500, 300, (-4, 4), (-3, 3))
+    whole = to_numpy(cvs.points(_frame(cols), "x", "y", GATHER))
+    bounds = list(cuts) + [n]
+    parts = [_frame(cols, a, b, offset=a) for a, b in zip(bounds[:-1], bounds[1:])]
+    got = to_numpy(cvs.points(ds.PartitionedFrame(parts), "x", "y", GATHER))
+    for k in whole:
+        assert_same(got[k], whole[k], what=k)
+
+
+def test_partitions_reject_gathered_lookups_beyond_64():
+    cols = _cols(6500, seed=24)
+    parts = ds.PartitionedFrame([_frame(cols, a, a + 100, offset=a) for a in range(0, 6500, 100)])
     with pytest.raises(NotImplementedError):
         ds.Canvas(16, 16, (-4, 4), (-4, 4)).points(parts, "x", "y", ds.first("v"))
