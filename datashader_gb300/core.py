@@ -622,18 +622,38 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
     return _results(plan, ex, coords, dims, dict(x_range=x_range, y_range=y_range))
 
 
+def _line_chunks(parts):
+    """dask.py:222-266: partition 0 alone with plot_start; every later
+    partition behind the last row of the previous one, with plot_start False
+    (the segment across the boundary is drawn with the later partition)."""
+    out = []
+    for i, part in enumerate(parts):
+        if i == 0 or len(parts[i - 1]) == 0:
+            out.append((part, 1))
+            continue
+        prev = parts[i - 1]
+        cols = {c: torch.cat([prev[c][-1:], part[c]]) for c in part.columns}
+        cats = {c: part.categories(c) for c in part.columns if part.is_categorical(c)}
+        out.append((TensorFrame(cols, categories=cats, device=part.device, row_offset=part.row_offset - 1), 0))
+    return out
+
+
 def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
     """dask.py:86-219 on one GPU: every partition into its own partial bases,
-    an elementwise combine, one finalize."""
-    if isinstance(glyph, LineAxis0):
-        raise NotImplementedError("partitioned sources are supported for Canvas.points")
+    an elementwise combine, one finalize.  LineAxis0 partitions are drawn as
+    the reference's dask line path draws them (dask.py:222-266)."""
+    is_line = isinstance(glyph, LineAxis0)
+    if isinstance(glyph, _MultiLine):
+        raise NotImplementedError("partitioned sources are supported for Canvas.points and LineAxis0 lines")
     if flags & N.FLAG_DETERMINISTIC:
         raise NotImplementedError("the deterministic mode sums one frame in row order; concatenate the partitions")
     parts = pframe.partitions
     dev = pframe.device
     if stream is None:
         stream = torch.cuda.current_stream(dev).cuda_stream
-    plan = compile_plan(agg, parts[0])
+    plan = compile_plan(agg, parts[0], antialias=is_line and glyph.antialiased)
+    if is_line and plan.use_2_stage:
+        raise NotImplementedError("two-stage antialiased plans are not supported on partitioned sources")
     if any(o.fin == N.FIN_GATHER for _, o in plan.outputs) and len(parts) > 64:
         raise NotImplementedError("first/last/where with a lookup column gather from at most 64 partitions")
     if canvas.x_range is not None and canvas.y_range is not None:
@@ -652,16 +672,26 @@ def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
                       float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]))
     L = N.lib()
     execs = []
-    for part in parts:
+    chunks = _line_chunks(parts) if is_line else [(p, 1) for p in parts]
+    for part, plot_start in chunks:
         ex = Executor(part, plan, glyph)
         ex.allocate(height, width, dev)
-        wsz = int(L.dsgb_points_workspace_size_flags(len(part), ctypes.byref(cv), ex.bases, len(plan.bases),
-                                                     flags))
-        ws = workspace(dev, stream, wsz) if wsz else None
-        N.check(L.dsgb_points_ws(ex.cols, len(ex.names), len(part), part.row_offset, 0, 1, ctypes.byref(cv),
-                                 ex.bases, len(plan.bases), ex.outs, ex.nouts,
-                                 ws.data_ptr() if ws is not None else None, wsz, flags | N.FLAG_NO_FINALIZE,
-                                 stream), "dsgb_points_ws (partition)")
+        if is_line:
+            wsz = int(L.dsgb_line_workspace_size(len(part))) if glyph.line_width > 0 else 0
+            ws = workspace(dev, stream, wsz) if wsz else None
+            N.check(L.dsgb_line_axis0_ws(ex.cols, len(ex.names), len(part), part.row_offset, 0, 1, ctypes.byref(cv),
+                                         float(glyph.line_width), plot_start, int(plan.overwrite), 0,
+                                         ex.bases, len(plan.bases), ex.outs, ex.nouts,
+                                         ws.data_ptr() if ws is not None else None, wsz,
+                                         flags | N.FLAG_NO_FINALIZE, stream), "dsgb_line_axis0_ws (partition)")
+        else:
+            wsz = int(L.dsgb_points_workspace_size_flags(len(part), ctypes.byref(cv), ex.bases, len(plan.bases),
+                                                         flags))
+            ws = workspace(dev, stream, wsz) if wsz else None
+            N.check(L.dsgb_points_ws(ex.cols, len(ex.names), len(part), part.row_offset, 0, 1, ctypes.byref(cv),
+                                     ex.bases, len(plan.bases), ex.outs, ex.nouts,
+                                     ws.data_ptr() if ws is not None else None, wsz, flags | N.FLAG_NO_FINALIZE,
+                                     stream), "dsgb_points_ws (partition)")
         execs.append(ex)
     head = execs[0]
     for ex in execs[1:]:
@@ -671,9 +701,9 @@ def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
         # from the partition that holds it
         ncols = len(head.names)
         pcols = (N.Column * max(1, ncols * len(execs)))(*[c for ex in execs for c in ex.cols])
-        first = (ctypes.c_int64 * len(parts))(*[p.row_offset for p in parts])
-        rows = (ctypes.c_int64 * len(parts))(*[len(p) for p in parts])
-        N.check(L.dsgb_finalize_partitioned(pcols, ncols, len(parts), first, rows, head.bases, len(plan.bases),
+        first = (ctypes.c_int64 * len(chunks))(*[c.row_offset for c, _ in chunks])
+        rows = (ctypes.c_int64 * len(chunks))(*[len(c) for c, _ in chunks])
+        N.check(L.dsgb_finalize_partitioned(pcols, ncols, len(chunks), first, rows, head.bases, len(plan.bases),
                                             head.outs, head.nouts, width * height, stream),
                 "dsgb_finalize_partitioned")
     coords = {glyph.x_label: canvas.x_axis.compute_index(x_st, width),

@@ -331,10 +331,10 @@ extern "C" int dsgb_device_sm_count(void) {
 __global__ void combine_kernel(int op, void *dst, const void *src, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         switch (op) {
-        case DSGB_BASE_COUNT: ((unsigned *)dst)[i] += ((const unsigned *)src)[i]; break;
+        case DSGB_BASE_COUNT: case DSGB_BASE_AA_CNT0: ((unsigned *)dst)[i] += ((const unsigned *)src)[i]; break;
         case DSGB_BASE_ANY: ((uint8_t *)dst)[i] |= ((const uint8_t *)src)[i]; break;
-        case DSGB_BASE_SUM: ((double *)dst)[i] += ((const double *)src)[i]; break;
-        case DSGB_BASE_MAX: case DSGB_BASE_MAX_ROW: {
+        case DSGB_BASE_SUM: case DSGB_BASE_AA_SUM: ((double *)dst)[i] += ((const double *)src)[i]; break;
+        case DSGB_BASE_MAX: case DSGB_BASE_MAX_ROW: case DSGB_BASE_AA_MAX: {
             long long *d = (long long *)dst;
             const long long v = ((const long long *)src)[i];
             if (v > d[i]) d[i] = v;
@@ -346,10 +346,10 @@ __global__ void combine_kernel(int op, void *dst, const void *src, int64_t n) {
             if (v < d[i]) d[i] = v;
             break;
         }
-        case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: {
+        case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: case DSGB_BASE_AA_ARGMAX: {
             long long *d = (long long *)dst + 2 * i;
             const long long *q = (const long long *)src + 2 * i;
-            const bool better = op == DSGB_BASE_ARGMAX ? pair_better<true>(q[0], q[1], d[0], d[1])
+            const bool better = op != DSGB_BASE_ARGMIN ? pair_better<true>(q[0], q[1], d[0], d[1])
                                                        : pair_better<false>(q[0], q[1], d[0], d[1]);
             if (better) { d[0] = q[0]; d[1] = q[1]; }
             break;
@@ -372,11 +372,7 @@ extern "C" int dsgb_combine(const dsgb_base *dst, const dsgb_base *src, int32_t 
             set_error("dsgb_combine: base %d differs between the partials", b);
             return DSGB_E_INVALID;
         }
-        if (D.op >= DSGB_BASE_AA_SUM) {
-            set_error("dsgb_combine: antialiased line bases do not combine elementwise (base %d)", b);
-            return DSGB_E_UNSUPPORTED;
-        }
-        if (D.op < DSGB_BASE_COUNT) {
+        if (D.op < DSGB_BASE_COUNT || D.op > DSGB_BASE_AA_ARGMAX) {
             set_error("dsgb_combine: unknown base op %d", D.op);
             return DSGB_E_INVALID;
         }

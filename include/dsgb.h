@@ -222,7 +222,9 @@ int dsgb_bucket_sort(const dsgb_column *cols, int32_t ncols, int64_t n, int32_t 
  * indexes take the min/max, {key,row} pairs keep the better pair (ties: the
  * smaller global row).  Replaces the per-reduction _combine of datashader's
  * partitioned (dask) path, dask.py:86-219 / compiler.py:478-507.
- * Antialiased line bases are rejected (DSGB_E_UNSUPPORTED). */
+ * Antialiased line bases of single-stage plans (dsgb_line_axis0 with
+ * use_2_stage_agg = 0) combine like their plain forms: coverage sums and
+ * counts add, maxima and {key,row} maxima keep the larger. */
 int dsgb_combine(const dsgb_base *dst, const dsgb_base *src, int32_t nbases, int64_t ncells, void *stream);
 
 /* ---- Canvas.line, LineAxis0 glyph ----------------------------------------

@@ -83,3 +83,46 @@ def test_partitions_reject_gathered_lookups_beyond_64():
     parts = ds.PartitionedFrame([_frame(cols, a, a + 100, offset=a) for a in range(0, 6500, 100)])
     with pytest.raises(NotImplementedError):
         ds.Canvas(16, 16, (-4, 4), (-4, 4)).points(parts, "x", "y", ds.first("v"))
+
+
+def _line_frame(cols, lo, hi):
+    return ds.TensorFrame({k: torch.from_numpy(np.ascontiguousarray(v[lo:hi])).cuda() for k, v in cols.items()})
+
+
+@pytest.mark.parametrize("lw", [0.0, 1.5])
+@pytest.mark.parametrize("red", ["count", "sum", "max"])
+def test_partitioned_lines_follow_the_reference_dask_path(lw, red):
+    """LineAxis0 over row partitions (dask.py:222-266): partition 0 drawn with
+    plot_start, every later one behind the previous partition's last row with
+    plot_start False; partials combined, finalized once.  Against the oracle
+    run on the same chunks and combined the reference's way (sum / nansum /
+    nanmax)."""
+    from datashader_gb300 import synthetic as S
+    import oracle
+    x, y, v, _ = S.time_series_np(8, 500, seed=4)
+    cols = {"x": x, "y": y, "v": v}
+    n = len(x)
+    cuts = [0, 700, 701, 2004, 3006, n]               # inside a series, next to it, on NaN separators
+    parts = [_line_frame(cols, a, b) for a, b in zip(cuts[:-1], cuts[1:])]
+    yr = (float(np.nanmin(y)) - 0.01, float(np.nanmax(y)) + 0.01)
+    cvs = ds.Canvas(plot_width=300, plot_height=200, x_range=(0.0, 1.0), y_range=yr)
+    agg = {"count": ds.count(), "sum": ds.sum("v"), "max": ds.max("v")}[red]
+    got = to_numpy(cvs.line(ds.PartitionedFrame(parts), "x", "y", agg=agg, line_width=lw))
+    spec = oracle.spec(red, None if red == "count" else "v")
+    partials = []
+    for i, (a, b) in enumerate(zip(cuts[:-1], cuts[1:])):
+        lo = a if i == 0 else a - 1
+        chunk = {k: val[lo:b] for k, val in cols.items()}
+        partials.append(oracle.line_axis0(chunk, "x", "y", 300, 200, (0.0, 1.0), yr, [spec], line_width=lw,
+                                          plot_start=(i == 0), row_offset=lo)[0])
+    stack = np.stack([np.asarray(p, dtype=np.float64) for p in partials])
+    if red == "max":
+        want = np.fmax.reduce(stack, axis=0)
+    elif np.issubdtype(partials[0].dtype, np.integer):
+        want = stack.sum(axis=0)
+    else:
+        with np.errstate(invalid="ignore"):
+            want = np.where(np.isnan(stack).all(axis=0), np.nan, np.nansum(stack, axis=0))
+    want = want.astype(partials[0].dtype)
+    rtol = 0.0 if red == "max" or (red == "count" and lw == 0) else (3e-7 if partials[0].dtype == np.float32 else 1e-12)
+    assert_same(got, want, rtol=rtol, what=f"{red} lw={lw}")
