@@ -33,15 +33,29 @@ struct BsParams {
     int64_t n;
     int32_t grid, nb;                         // nb = grid * grid + 1
     double x0, x1, y0, y1, sx, sy;
+    int32_t f32;                              // x and y float32: the estimate in float32
+    float x0f, x1f, y0f, y1f, sxf, syf;
     unsigned *count;                          // nb
     unsigned *cursor;                         // nb
     int64_t *start;                           // nb + 1
 };
 
+// The bucket is an estimate (readers widen by one bucket and always read the
+// outside bucket), so float32 columns are bucketed in float32: GB300 issues
+// float64 at a small fraction of the float32 rate.
 __device__ __forceinline__ int bs_bucket(const BsParams &p, int64_t i) {
-    const double x = load_f64(p.in[p.x_col], i), y = load_f64(p.in[p.y_col], i);
-    if (!(x >= p.x0 && x <= p.x1 && y >= p.y0 && y <= p.y1)) return p.nb - 1;
-    int bx = (int)((x - p.x0) * p.sx), by = (int)((y - p.y0) * p.sy);
+    int bx, by;
+    if (p.f32) {
+        const float x = __ldg((const float *)p.in[p.x_col].data + i), y = __ldg((const float *)p.in[p.y_col].data + i);
+        if (!(x >= p.x0f && x <= p.x1f && y >= p.y0f && y <= p.y1f)) return p.nb - 1;
+        bx = (int)((x - p.x0f) * p.sxf);
+        by = (int)((y - p.y0f) * p.syf);
+    } else {
+        const double x = load_f64(p.in[p.x_col], i), y = load_f64(p.in[p.y_col], i);
+        if (!(x >= p.x0 && x <= p.x1 && y >= p.y0 && y <= p.y1)) return p.nb - 1;
+        bx = (int)((x - p.x0) * p.sx);
+        by = (int)((y - p.y0) * p.sy);
+    }
     bx = bx < 0 ? 0 : (bx >= p.grid ? p.grid - 1 : bx);
     by = by < 0 ? 0 : (by >= p.grid ? p.grid - 1 : by);
     return by * p.grid + bx;
@@ -164,6 +178,9 @@ extern "C" int dsgb_bucket_sort(const dsgb_column *cols, int32_t ncols, int64_t 
     p.x0 = domain[0]; p.x1 = domain[1]; p.y0 = domain[2]; p.y1 = domain[3];
     p.sx = grid / (p.x1 - p.x0);
     p.sy = grid / (p.y1 - p.y0);
+    p.f32 = cols[x_col].dtype == DSGB_F32 && cols[y_col].dtype == DSGB_F32;
+    p.x0f = (float)p.x0; p.x1f = (float)p.x1; p.y0f = (float)p.y0; p.y1f = (float)p.y1;
+    p.sxf = (float)p.sx; p.syf = (float)p.sy;
     const size_t half = need / 2;
     p.count = (unsigned *)workspace;
     p.cursor = (unsigned *)((char *)workspace + half);
