@@ -146,6 +146,11 @@ __device__ __forceinline__ double x_intercept(double y, double cx0, double cy0, 
     return cx0 + frac * (cx1 - cx0);
 }
 __device__ __forceinline__ double sq(double v) { return v * v; }
+// element i (0..3) of four scalars, by selects
+__device__ __forceinline__ double pick4(int i, double a0, double a1, double a2, double a3) {
+    const double lo = (i & 1) ? a1 : a0, hi = (i & 1) ? a3 : a2;
+    return (i & 2) ? hi : lo;
+}
 
 // line.py:826-981 -- _full_antialias.
 __device__ void full_antialias(const LineParams &p, double line_width, bool overwrite, int64_t i,
@@ -172,25 +177,27 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
     alongy /= length;
     const double rightx = alongy;
     const double righty = -alongx;
-    double b[8];
+    // the four corners (bx[k], by[k]) as scalars: they are picked by a run-time
+    // index per scanline, which an array would leave in local memory
+    double bx0, bx1, bx2, bx3, by0, by1, by2, by3;
     if (flip_order) {
-        b[0] = x1 - halfwidth * (rightx - alongx);
-        b[1] = x1 - halfwidth * (-rightx - alongx);
-        b[2] = x0 - halfwidth * (-rightx + alongx);
-        b[3] = x0 - halfwidth * (rightx + alongx);
-        b[4] = y1 - halfwidth * (righty - alongy);
-        b[5] = y1 - halfwidth * (-righty - alongy);
-        b[6] = y0 - halfwidth * (-righty + alongy);
-        b[7] = y0 - halfwidth * (righty + alongy);
+        bx0 = x1 - halfwidth * (rightx - alongx);
+        bx1 = x1 - halfwidth * (-rightx - alongx);
+        bx2 = x0 - halfwidth * (-rightx + alongx);
+        bx3 = x0 - halfwidth * (rightx + alongx);
+        by0 = y1 - halfwidth * (righty - alongy);
+        by1 = y1 - halfwidth * (-righty - alongy);
+        by2 = y0 - halfwidth * (-righty + alongy);
+        by3 = y0 - halfwidth * (righty + alongy);
     } else {
-        b[0] = x0 + halfwidth * (rightx - alongx);
-        b[1] = x0 + halfwidth * (-rightx - alongx);
-        b[2] = x1 + halfwidth * (-rightx + alongx);
-        b[3] = x1 + halfwidth * (rightx + alongx);
-        b[4] = y0 + halfwidth * (righty - alongy);
-        b[5] = y0 + halfwidth * (-righty - alongy);
-        b[6] = y1 + halfwidth * (-righty + alongy);
-        b[7] = y1 + halfwidth * (righty + alongy);
+        bx0 = x0 + halfwidth * (rightx - alongx);
+        bx1 = x0 + halfwidth * (-rightx - alongx);
+        bx2 = x1 + halfwidth * (-rightx + alongx);
+        bx3 = x1 + halfwidth * (rightx + alongx);
+        by0 = y0 + halfwidth * (righty - alongy);
+        by1 = y0 + halfwidth * (-righty - alongy);
+        by2 = y1 + halfwidth * (-righty + alongy);
+        by3 = y1 + halfwidth * (righty + alongy);
     }
     long long xmaxi = nx - 1, ymaxi = ny - 1;
     if (flip_xy) { long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
@@ -209,16 +216,18 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
             overwrite = true;
         }
     }
-    const long long ystart = clampi((long long)ceil(b[4 + lowindex]), 0, ymaxi);
-    const long long yend = clampi((long long)floor(b[4 + (lowindex + 2) % 4]), 0, ymaxi);
+    const long long ystart = clampi((long long)ceil(pick4(lowindex, by0, by1, by2, by3)), 0, ymaxi);
+    const long long yend = clampi((long long)floor(pick4((lowindex + 2) % 4, by0, by1, by2, by3)), 0, ymaxi);
     int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
     const double lw_lo = 0.5 * (line_width - aa);
     for (long long y = ystart; y <= yend; ++y) {
         const double yd = (double)y;
-        if (ll == lowindex && yd > b[4 + lu]) { ll = lu; lu = (ll + 1) % 4; }
-        if (rl == lowindex && yd > b[4 + ru]) { rl = ru; ru = (rl + 3) % 4; }
-        const long long xleft = clampi((long long)ceil(x_intercept(yd, b[ll], b[4 + ll], b[lu], b[4 + lu])), 0, xmaxi);
-        const long long xright = clampi((long long)floor(x_intercept(yd, b[rl], b[4 + rl], b[ru], b[4 + ru])), 0, xmaxi);
+        if (ll == lowindex && yd > pick4(lu, by0, by1, by2, by3)) { ll = lu; lu = (ll + 1) % 4; }
+        if (rl == lowindex && yd > pick4(ru, by0, by1, by2, by3)) { rl = ru; ru = (rl + 3) % 4; }
+        const long long xleft = clampi((long long)ceil(x_intercept(yd, pick4(ll, bx0, bx1, bx2, bx3),
+            pick4(ll, by0, by1, by2, by3), pick4(lu, bx0, bx1, bx2, bx3), pick4(lu, by0, by1, by2, by3))), 0, xmaxi);
+        const long long xright = clampi((long long)floor(x_intercept(yd, pick4(rl, bx0, bx1, bx2, bx3),
+            pick4(rl, by0, by1, by2, by3), pick4(ru, bx0, bx1, bx2, bx3), pick4(ru, by0, by1, by2, by3))), 0, xmaxi);
         for (long long x = xleft; x <= xright; ++x) {
             const double xd = (double)x;
             const double along = (xd - x0) * alongx + (yd - y0) * alongy;
@@ -331,7 +340,7 @@ __device__ void draw_segment(const LineParams &p, int64_t row, double x0, double
     }
 }
 
-__global__ void __launch_bounds__(256) line_axis0_kernel(const LineParams p) {
+__global__ void __launch_bounds__(256, 1) line_axis0_kernel(const LineParams p) {
     const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
     for (int64_t i = gtid(); i + 1 < p.n; i += gstride()) {
         const double x0 = load_f64(X, i), y0 = load_f64(Y, i);
@@ -416,7 +425,7 @@ const unsigned *build_line_work_order(const LineWorkArgs &a, void *workspace, si
     return order;
 }
 
-__global__ void __launch_bounds__(256) line_axis0_ordered_kernel(const LineParams p, const unsigned *order) {
+__global__ void __launch_bounds__(256, 1) line_axis0_ordered_kernel(const LineParams p, const unsigned *order) {
     const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
     for (int64_t k = gtid(); k + 1 < p.n; k += gstride()) {
         const int64_t i = order[k];
@@ -450,7 +459,7 @@ struct LinesGeom {
 };
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(256) lines_kernel(const LineParams p, const LinesGeom g) {
+__global__ void __launch_bounds__(256, 1) lines_kernel(const LineParams p, const LinesGeom g) {
     const int64_t nseg = LAYOUT == 1 ? (g.nrows - 1) * g.nv : g.nrows * (g.nv - 1);
     for (int64_t s = gtid(); s < nseg; s += gstride()) {
         if (LAYOUT == 1) {

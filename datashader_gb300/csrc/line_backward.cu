@@ -80,6 +80,12 @@ __device__ __forceinline__ D3 dx_intercept(double y, D3 cx0, D3 cy0, D3 cx1, D3 
     const D3 frac = (dc(y) - cy0) / (cy1 - cy0);
     return cx0 + frac * (cx1 - cx0);
 }
+// element i (0..3) of four duals, by selects
+__device__ __forceinline__ D3 dpick4(int i, const D3 &a0, const D3 &a1, const D3 &a2, const D3 &a3) {
+    const D3 &lo = (i & 1) ? a1 : a0;
+    const D3 &hi = (i & 1) ? a3 : a2;
+    return (i & 2) ? hi : lo;
+}
 __device__ __forceinline__ long long clampi_b(long long x, long long lo, long long hi) {
     long long m = x < hi ? x : hi;
     return lo > m ? lo : m;
@@ -141,25 +147,27 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
     alongy = alongy / length;
     const D3 rightx = alongy, righty = -alongx;
     const D3 hw = dc(halfwidth);
-    D3 b[8];
+    // corners as scalars (picked per scanline by a run-time index: an array
+    // would live in local memory)
+    D3 bx0, bx1, bx2, bx3, by0, by1, by2, by3;
     if (flip_order) {
-        b[0] = x1 - hw * (rightx - alongx);
-        b[1] = x1 - hw * (-rightx - alongx);
-        b[2] = x0 - hw * (-rightx + alongx);
-        b[3] = x0 - hw * (rightx + alongx);
-        b[4] = y1 - hw * (righty - alongy);
-        b[5] = y1 - hw * (-righty - alongy);
-        b[6] = y0 - hw * (-righty + alongy);
-        b[7] = y0 - hw * (righty + alongy);
+        bx0 = x1 - hw * (rightx - alongx);
+        bx1 = x1 - hw * (-rightx - alongx);
+        bx2 = x0 - hw * (-rightx + alongx);
+        bx3 = x0 - hw * (rightx + alongx);
+        by0 = y1 - hw * (righty - alongy);
+        by1 = y1 - hw * (-righty - alongy);
+        by2 = y0 - hw * (-righty + alongy);
+        by3 = y0 - hw * (righty + alongy);
     } else {
-        b[0] = x0 + hw * (rightx - alongx);
-        b[1] = x0 + hw * (-rightx - alongx);
-        b[2] = x1 + hw * (-rightx + alongx);
-        b[3] = x1 + hw * (rightx + alongx);
-        b[4] = y0 + hw * (righty - alongy);
-        b[5] = y0 + hw * (-righty - alongy);
-        b[6] = y1 + hw * (-righty + alongy);
-        b[7] = y1 + hw * (righty + alongy);
+        bx0 = x0 + hw * (rightx - alongx);
+        bx1 = x0 + hw * (-rightx - alongx);
+        bx2 = x1 + hw * (-rightx + alongx);
+        bx3 = x1 + hw * (rightx + alongx);
+        by0 = y0 + hw * (righty - alongy);
+        by1 = y0 + hw * (-righty - alongy);
+        by2 = y1 + hw * (-righty + alongy);
+        by3 = y1 + hw * (righty + alongy);
     }
     long long xmaxi = nx - 1, ymaxi = ny - 1;
     if (flip_xy) { long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
@@ -178,8 +186,8 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
             overwrite = true;
         }
     }
-    const long long ystart = clampi_b((long long)ceil(b[4 + lowindex].v), 0, ymaxi);
-    const long long yend = clampi_b((long long)floor(b[4 + (lowindex + 2) % 4].v), 0, ymaxi);
+    const long long ystart = clampi_b((long long)ceil(dpick4(lowindex, by0, by1, by2, by3).v), 0, ymaxi);
+    const long long yend = clampi_b((long long)floor(dpick4((lowindex + 2) % 4, by0, by1, by2, by3).v), 0, ymaxi);
     int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
     const double lw_lo = 0.5 * (line_width - aa);
     const double ls_den = halfwidth - lw_lo;
@@ -187,10 +195,12 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
     float ty0 = 0.0f, ty1 = 0.0f, ty2 = 0.0f;     // the y tangents of this segment, in float32
     for (long long y = ystart; y <= yend; ++y) {
         const double yd = (double)y;
-        if (ll == lowindex && yd > b[4 + lu].v) { ll = lu; lu = (ll + 1) % 4; }
-        if (rl == lowindex && yd > b[4 + ru].v) { rl = ru; ru = (rl + 3) % 4; }
-        const long long xleft = clampi_b((long long)ceil(dx_intercept(yd, b[ll], b[4 + ll], b[lu], b[4 + lu]).v), 0, xmaxi);
-        const long long xright = clampi_b((long long)floor(dx_intercept(yd, b[rl], b[4 + rl], b[ru], b[4 + ru]).v), 0, xmaxi);
+        if (ll == lowindex && yd > dpick4(lu, by0, by1, by2, by3).v) { ll = lu; lu = (ll + 1) % 4; }
+        if (rl == lowindex && yd > dpick4(ru, by0, by1, by2, by3).v) { rl = ru; ru = (rl + 3) % 4; }
+        const long long xleft = clampi_b((long long)ceil(dx_intercept(yd, dpick4(ll, bx0, bx1, bx2, bx3),
+            dpick4(ll, by0, by1, by2, by3), dpick4(lu, bx0, bx1, bx2, bx3), dpick4(lu, by0, by1, by2, by3)).v), 0, xmaxi);
+        const long long xright = clampi_b((long long)floor(dx_intercept(yd, dpick4(rl, bx0, bx1, bx2, bx3),
+            dpick4(rl, by0, by1, by2, by3), dpick4(ru, bx0, bx1, bx2, bx3), dpick4(ru, by0, by1, by2, by3)).v), 0, xmaxi);
         for (long long x = xleft; x <= xright; ++x) {
             const D3 xd = dc((double)x), ydd = dc(yd);
             const D3 along = (xd - x0) * alongx + (ydd - y0) * alongy;
@@ -245,7 +255,7 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
 // build_line_work_order): the lanes of a warp then recompute segments of
 // similar pixel counts.  Each segment's results go to its own rows, so the
 // order changes only the order of the grad_y atomics.
-__global__ void __launch_bounds__(256) line_backward_kernel(const BwdParams p, const unsigned *order) {
+__global__ void __launch_bounds__(256, 1) line_backward_kernel(const BwdParams p, const unsigned *order) {
     for (int64_t k = gtid(); k + 1 < p.n; k += gstride()) {
         const int64_t i = order ? (int64_t)order[k] : k;
         const double field = load_f64(p.V, i);
