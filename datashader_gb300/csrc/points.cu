@@ -13,7 +13,7 @@ namespace dsgb {
 
 // float32 coordinates, 4 rows per thread per iteration (float4 streaming loads).
 template <int MODE, bool FAST, bool WARPAGG>
-__global__ void __launch_bounds__(256) points_f32_kernel(const PointsParams p) {
+__global__ void __launch_bounds__(256, 4) points_f32_kernel(const PointsParams p) {
     const float *xs = (const float *)p.cols[p.x_col].data;
     const float *ys = (const float *)p.cols[p.y_col].data;
     const int64_t n4 = p.n >> 2;
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(256) points_f32_kernel(const PointsParams p) {
 
 // float64 coordinates, 2 rows per thread per iteration (double2 streaming loads).
 template <int MODE, bool FAST>
-__global__ void __launch_bounds__(256) points_f64_kernel(const PointsParams p) {
+__global__ void __launch_bounds__(256, 4) points_f64_kernel(const PointsParams p) {
     const double *xs = (const double *)p.cols[p.x_col].data;
     const double *ys = (const double *)p.cols[p.y_col].data;
     const int64_t n2 = p.n >> 1;
