@@ -22,7 +22,7 @@ from . import _native as N
 from . import reductions as rd
 from .compiler import compile_plan
 from .glyphs import (Point, LineAxis0, LineAxis0Multi, LinesAxis1, LinesAxis1XConstant,
-                     LinesAxis1YConstant, _MultiLine)
+                     LinesAxis1YConstant, LinesAxis1Ragged, _MultiLine)
 
 
 # ----------------------------------------------------------------- sources
@@ -44,6 +44,41 @@ def dsgb_dtype(t: torch.Tensor) -> int:
         raise TypeError(f"unsupported column dtype {t.dtype}") from None
 
 
+class RaggedColumn:
+    """A ragged-array column (the reference's RaggedArray, datashader/
+    datatypes.py): row i holds ``flat[starts[i]:starts[i + 1]]``, the last
+    row running to the end of ``flat``.  Build it from a list of per-row
+    sequences, or from ``flat`` (float64) and ``starts`` (int64,
+    non-decreasing, within ``flat``)."""
+
+    def __init__(self, rows=None, *, flat=None, starts=None):
+        if rows is not None:
+            lens = [len(r) for r in rows]
+            flat = np.concatenate([np.asarray(r, dtype=np.float64) for r in rows]) if lens else np.zeros(0)
+            starts = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64) if lens else np.zeros(0, np.int64)
+        flat = flat if isinstance(flat, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(flat))
+        starts = starts if isinstance(starts, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(starts))
+        self.flat = flat.to(torch.float64).contiguous()
+        self.starts = starts.to(torch.int64).contiguous()
+        if self.flat.dim() != 1 or self.starts.dim() != 1:
+            raise ValueError("a ragged column needs a 1-D flat array and 1-D start indices")
+        if self.starts.numel():
+            st = self.starts
+            if bool((st[0] < 0) | (st[-1] > self.flat.numel())) or bool((st[1:] < st[:-1]).any()):
+                raise ValueError("ragged start indices must be non-decreasing and within the flat array")
+
+    def __len__(self):
+        return self.starts.numel()
+
+    @property
+    def device(self):
+        return self.flat.device
+
+    def to(self, device, non_blocking=False):
+        return RaggedColumn(flat=self.flat.to(device, non_blocking=non_blocking),
+                            starts=self.starts.to(device, non_blocking=non_blocking))
+
+
 class TensorFrame:
     """Named, equal-length 1-D columns on one CUDA device.
 
@@ -61,12 +96,17 @@ class TensorFrame:
         self._cols = {}
         n = None
         for k, v in dict(columns).items():
-            t = self._to_device(v)
-            if t.dim() != 1:
-                raise ValueError(f"column {k!r} must be 1-D")
+            if isinstance(v, RaggedColumn):
+                t = v if v.device == self.device else v.to(self.device)
+                rows = len(t)
+            else:
+                t = self._to_device(v)
+                if t.dim() != 1:
+                    raise ValueError(f"column {k!r} must be 1-D")
+                rows = t.shape[0]
             if n is None:
-                n = t.shape[0]
-            elif t.shape[0] != n:
+                n = rows
+            elif rows != n:
                 raise ValueError("columns must have equal length")
             self._cols[k] = t
         self._n = n or 0
@@ -105,6 +145,8 @@ class TensorFrame:
     def dtype_kind(self, name):
         if name in self._cats:
             return "c"
+        if isinstance(self._cols[name], RaggedColumn):
+            return "R"
         return _KIND.get(self._cols[name].dtype, "?")
 
     def is_categorical(self, name):
@@ -114,7 +156,8 @@ class TensorFrame:
         return self._cats[name]
 
     def signature(self):
-        return tuple((k, str(v.dtype), tuple(self._cats.get(k, ()))) for k, v in self._cols.items())
+        return tuple((k, "ragged" if isinstance(v, RaggedColumn) else str(v.dtype), tuple(self._cats.get(k, ())))
+                     for k, v in self._cols.items())
 
 
 class PartitionedFrame:
@@ -414,7 +457,7 @@ def _line_glyph(x, y, axis):
         if isinstance(x, (list, tuple)) and isinstance(y, np.ndarray):
             return LinesAxis1YConstant(tuple(x), y)
         if isinstance(x, (Number, str)) and isinstance(y, (Number, str)):
-            raise NotImplementedError("ragged-array lines (LinesAxis1Ragged) are not on the GPU path")
+            return LinesAxis1Ragged(x, y)
         raise ValueError(f"Invalid combination of x and y arguments to Canvas.line when axis=1.\n"
                          f"    Received:\n        x: {ox!r}\n        y: {oy!r}")
     raise ValueError(f"The axis argument to Canvas.line must be 0 or 1\n    Received: {axis}")
@@ -561,7 +604,11 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
     if stream is None:
         stream = torch.cuda.current_stream(frame.device).cuda_stream
     plan = compile_plan(agg, frame, antialias=antialias)
-    if isinstance(glyph, _MultiLine):
+    if isinstance(glyph, LinesAxis1Ragged):
+        xr, yr = frame[glyph.x], frame[glyph.y]
+        x_range = canvas.x_range or _array_bounds(xr.flat, stream)
+        y_range = canvas.y_range or _array_bounds(yr.flat, stream)
+    elif isinstance(glyph, _MultiLine):
         xs = _vertex_array(frame, glyph.x, len(frame))
         ys = _vertex_array(frame, glyph.y, len(frame))
         x_range = canvas.x_range or _array_bounds(xs, stream)
@@ -589,6 +636,16 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
                                   ex.bases, len(plan.bases), ex.outs, ex.nouts,
                                   ws.data_ptr() if ws is not None else None, wsz, flags, stream)
         N.check(rc, "dsgb_line_axis0_ws")
+    elif isinstance(glyph, LinesAxis1Ragged):
+        cols, ncols = ex.cols, len(ex.names)
+        if ncols == 0:                       # count() / any(): no field column, any valid pointer
+            cols = (N.Column * 1)(N.Column(xr.flat.data_ptr(), N.F64, 0))
+            ncols = 1
+        rc = L.dsgb_lines_ragged(cols, ncols, len(frame), frame.row_offset, xr.flat.data_ptr(), xr.flat.numel(),
+                                 xr.starts.data_ptr(), yr.flat.data_ptr(), yr.flat.numel(), yr.starts.data_ptr(),
+                                 ctypes.byref(cv), float(glyph.line_width), int(plan.overwrite),
+                                 ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
+        N.check(rc, "dsgb_lines_ragged")
     elif isinstance(glyph, _MultiLine):
         if glyph.layout == 1 and len(glyph.x) > 1 and any(
                 b.op in (N.BASE_MIN_ROW, N.BASE_MAX_ROW, N.BASE_ARGMAX, N.BASE_ARGMIN) for b in plan.bases):

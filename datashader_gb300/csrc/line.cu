@@ -486,6 +486,43 @@ __global__ void __launch_bounds__(256, 1) lines_kernel(const LineParams p, const
     }
 }
 
+// LinesAxis1Ragged (line.py:457-523, 1538-1612): row i runs over its own
+// slices of the flat x and y arrays, [xs[i], xs[i+1]) and [ys[i], ys[i+1])
+// (the last row to the flat lengths), through the shorter of the two.  One
+// thread per flat x vertex finds its row by bisection over the starts (non-
+// decreasing); the slices are clamped to the arrays, so malformed starts
+// cannot read outside them.
+struct RaggedGeom {
+    const double *xf, *yf;
+    const int64_t *xs, *ys;
+    int64_t nrows, nx, ny;
+};
+
+__global__ void __launch_bounds__(256, 1) lines_ragged_kernel(const LineParams p, const RaggedGeom g) {
+    for (int64_t k = gtid(); k < g.nx; k += gstride()) {
+        int64_t lo = 0, hi = g.nrows - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (g.xs[mid] <= k) lo = mid; else hi = mid - 1;
+        }
+        const int64_t i = lo;
+        const bool last = i == g.nrows - 1;
+        const int64_t xa = min(max(g.xs[i], (int64_t)0), g.nx);
+        const int64_t xb = max(min(last ? g.nx : g.xs[i + 1], g.nx), xa);
+        const int64_t ya = min(max(g.ys[i], (int64_t)0), g.ny);
+        const int64_t yb = max(min(last ? g.ny : g.ys[i + 1], g.ny), ya);
+        const int64_t len = min(xb - xa, yb - ya);
+        const int64_t j = k - xa;
+        if (j < 0 || j + 1 >= len) continue;
+        const double *X = g.xf + xa, *Y = g.yf + ya;
+        const bool segment_start = (j == 0) || isnull(X[j - 1]) || isnull(Y[j - 1]);
+        const bool segment_end = (j == len - 2) || isnull(X[j + 2]) || isnull(Y[j + 2]);
+        double xm = 0.0, ym = 0.0;
+        if (!(segment_start || p.use_2_stage)) { xm = X[j - 1]; ym = Y[j - 1]; }
+        draw_segment(p, i, X[j], Y[j], X[j + 1], Y[j + 1], segment_start, segment_end, xm, ym);
+    }
+}
+
 int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st);
 int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
                      const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
@@ -656,6 +693,42 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
         if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(p, g);
         else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(p, g);
         DSGB_CHECK_LAUNCH("lines kernel");
+    }
+    if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+        rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+    return rc;
+}
+
+extern "C" int dsgb_lines_ragged(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
+                                 const double *x_flat, int64_t nx, const int64_t *x_start,
+                                 const double *y_flat, int64_t ny, const int64_t *y_start,
+                                 const dsgb_canvas *canvas, double line_width, int32_t overwrite,
+                                 const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                                 uint32_t flags, void *stream) {
+    if (nrows < 0 || nx < 0 || ny < 0 || (nrows > 0 && (!x_start || !y_start)) || (nx > 0 && !x_flat) ||
+        (ny > 0 && !y_flat)) {
+        set_error("dsgb_lines_ragged: invalid vertex arrays");
+        return DSGB_E_INVALID;
+    }
+    LineParams p;
+    int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
+    if (rc) return rc;
+    if (!(line_width >= 0.0)) { set_error("dsgb_lines_ragged: line_width must be >= 0"); return DSGB_E_INVALID; }
+    p.line_width = line_width;
+    p.plot_start = 1;
+    p.overwrite = overwrite;
+    p.use_2_stage = 0;
+    RaggedGeom g;
+    g.xf = x_flat; g.yf = y_flat; g.xs = x_start; g.ys = y_start; g.nrows = nrows; g.nx = nx; g.ny = ny;
+    cudaStream_t st = as_stream(stream);
+    const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    if (!(flags & DSGB_FLAG_NO_INIT)) {
+        rc = bases_init(bases, nbases, ncells, st);
+        if (rc) return rc;
+    }
+    if (nrows > 0 && nx > 1 && nbases > 0) {
+        lines_ragged_kernel<<<grid_of(nx), 256, 0, st>>>(p, g);
+        DSGB_CHECK_LAUNCH("lines ragged kernel");
     }
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
         rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);

@@ -125,3 +125,24 @@ class LinesAxis1XConstant(LinesAxis1):
 
 class LinesAxis1YConstant(LinesAxis1):
     """One line per row; ``y`` is one numpy array shared by every line (line.py:383-430)."""
+
+
+class LinesAxis1Ragged(_MultiLine):
+    """One line per row through ragged x and y columns (RaggedColumn; line.py:457-523)."""
+    layout = 3
+
+    def required_columns(self):
+        return [self.x, self.y]
+
+    def validate(self, schema):
+        for c, name in ((self.x, "x"), (self.y, "y")):
+            if c not in schema:
+                raise ValueError(f"column {c!r} not found")
+            if schema.dtype_kind(c) != "R":
+                raise ValueError(f"{name} must be a RaggedArray")
+
+    def __hash__(self):
+        return hash((type(self), self.x, self.y))
+
+    def __eq__(self, other):
+        return type(self) is type(other) and self.x == other.x and self.y == other.y

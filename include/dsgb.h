@@ -266,6 +266,19 @@ int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t ro
                const dsgb_base *bases, int32_t nbases,
                const dsgb_output *outs, int32_t nouts, uint32_t flags, void *stream);
 
+/* Canvas.line(axis=1) over ragged x / y columns (LinesAxis1Ragged,
+ * line.py:457-523 and 1538-1612): row i's vertices are x_flat[x_start[i] ..
+ * x_start[i+1]) and y_flat[y_start[i] .. y_start[i+1]) (the last row to nx /
+ * ny; starts are device int64, non-decreasing), drawn through the shorter of
+ * the two; segment j appends row i's fields (cols).  Reductions as
+ * dsgb_lines; two-stage antialiased plans are not supported. */
+int dsgb_lines_ragged(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
+                      const double *x_flat, int64_t nx, const int64_t *x_start,
+                      const double *y_flat, int64_t ny, const int64_t *y_start,
+                      const dsgb_canvas *canvas, double line_width, int32_t overwrite,
+                      const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                      uint32_t flags, void *stream);
+
 /* Adjoint of the antialiased LineAxis0 sum('v') aggregate (self-intersecting
  * form): given dL/dagg (f64, height*width), accumulate dL/dv (f64, n) and
  * dL/dy (f64, n, y in data units) with coverage recomputed, not stored.

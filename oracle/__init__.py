@@ -83,6 +83,11 @@ def lib():
                 ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                 ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 9 + [
                 ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
+            L.oracle_lines_ragged.argtypes = [
+                ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 9 + [
+                ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
             L.oracle_bounds.argtypes = [ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             _lib = L
@@ -333,6 +338,40 @@ def lines(cols, layout, xs, ys, width, height, x_range, y_range, specs, line_wid
     L.oracle_lines(layout, nrows, nv, xs.ctypes.data, ys.ctypes.data, xrow, yrow, ptrs, row_offset, width, height,
                    sx, tx, sy, ty, float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]),
                    float(line_width), 1 if plot_start else 0, 1 if overwrite else 0, reds, len(specs))
+    return _finalize(specs, keep)
+
+
+def lines_ragged(cols, x_rows, y_rows, width, height, x_range, y_range, specs, line_width=0.0, row_offset=0):
+    """Canvas.line(axis=1) over ragged x / y columns (LinesAxis1Ragged,
+    line.py:457-523, 1538-1612): ``x_rows`` / ``y_rows`` are lists of
+    per-row vertex lists; ``cols`` holds the field columns, indexed by row."""
+    nrows = len(x_rows)
+    xf = np.ascontiguousarray(np.concatenate([np.asarray(r, dtype=np.float64) for r in x_rows])
+                              if nrows else np.zeros(0), dtype=np.float64)
+    yf = np.ascontiguousarray(np.concatenate([np.asarray(r, dtype=np.float64) for r in y_rows])
+                              if nrows else np.zeros(0), dtype=np.float64)
+    xstart = np.ascontiguousarray(np.concatenate([[0], np.cumsum([len(r) for r in x_rows])[:-1]]), dtype=np.int64)
+    ystart = np.ascontiguousarray(np.concatenate([[0], np.cumsum([len(r) for r in y_rows])[:-1]]), dtype=np.int64)
+    if x_range is None:
+        x_range = maybe_expand_bounds(compute_bounds(xf))
+    if y_range is None:
+        y_range = maybe_expand_bounds(compute_bounds(yf))
+    sx, tx = scale_translate(x_range, width)
+    sy, ty = scale_translate(y_range, height)
+    antialias = line_width > 0
+    overwrite = False
+    if antialias:
+        self_intersect, overwrite, use_2_stage = aa_flags(specs)
+        if use_2_stage:
+            raise NotImplementedError("two-stage antialiased reductions over several lines")
+        specs = [dict(s, self_intersect=self_intersect) for s in specs]
+    reds, keep, colarrs, ptrs = _prepare(cols, specs, (height, width), antialias)
+    L = lib()
+    L.oracle_init(reds, len(specs), height * width, 1 if antialias else 0)
+    L.oracle_lines_ragged(nrows, xf.ctypes.data, xf.size, xstart.ctypes.data, yf.ctypes.data, yf.size,
+                          ystart.ctypes.data, ptrs, row_offset, width, height, sx, tx, sy, ty,
+                          float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]),
+                          float(line_width), 1 if overwrite else 0, reds, len(specs))
     return _finalize(specs, keep)
 
 

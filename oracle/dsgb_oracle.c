@@ -675,6 +675,35 @@ int oracle_lines(int32_t layout, int64_t nrows, int64_t nv, const double *xs, co
     return 0;
 }
 
+/* line.py:1538-1612 -- LinesAxis1Ragged (_build_extend_line_axis1_ragged,
+ * single-stage form): row i runs over its own slices of the flat x and y
+ * arrays (start indices; the last row ends at the flat length), through
+ * the shorter of the two; segment j appends row i. */
+int oracle_lines_ragged(int64_t nrows, const double *xf, int64_t nx, const int64_t *xstart,
+                        const double *yf, int64_t ny, const int64_t *ystart,
+                        const double *const *cols, int64_t row_offset,
+                        int32_t width, int32_t height, double sx, double tx, double sy, double ty,
+                        double xmin, double xmax, double ymin, double ymax,
+                        double line_width, int32_t overwrite, oracle_red *reds, int nreds) {
+    for (int64_t i = 0; i < nrows; ++i) {
+        const int64_t x0i = xstart[i], x1i = i < nrows - 1 ? xstart[i + 1] : nx;
+        const int64_t y0i = ystart[i], y1i = i < nrows - 1 ? ystart[i + 1] : ny;
+        const int64_t len = (x1i - x0i) < (y1i - y0i) ? (x1i - x0i) : (y1i - y0i);
+        const double *X = xf + x0i, *Y = yf + y0i;
+        for (int64_t j = 0; j + 1 < len; ++j) {
+            int segment_start = (j == 0) || isnull_d(X[j - 1]) || isnull_d(Y[j - 1]);
+            int segment_end = (j == len - 2) || isnull_d(X[j + 2]) || isnull_d(Y[j + 2]);
+            double xm = 0.0, ym = 0.0;
+            if (!segment_start) { xm = X[j - 1]; ym = Y[j - 1]; }
+            draw_segment(i, row_offset, X[j], Y[j], X[j + 1], Y[j + 1], segment_start, segment_end, xm, ym,
+                         cols, width, sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite,
+                         reds, nreds);
+        }
+    }
+    (void)height;
+    return 0;
+}
+
 /* glyph.py:66-78 -- _compute_bounds_numba: NaN-skipping min/max. */
 void oracle_bounds(int64_t n, const double *v, double *out_min, double *out_max) {
     double mn = INFINITY, mx = -INFINITY;

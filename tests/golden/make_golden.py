@@ -128,8 +128,11 @@ def main(ref_root):
                                                                 "line_autorange_params")).items():
         cases = []
         for df_args, kw in val:
-            if isinstance(kw.get("x"), str) and isinstance(kw.get("y"), str):
-                continue                                           # ragged arrays
+            if isinstance(kw.get("x"), str) and isinstance(kw.get("y"), str) and kw.get("axis") == 1:
+                # ragged arrays: per-row vertex lists
+                cols = {k: [[float(v) for v in row] for row in vals] for k, vals in df_args[0].items()}
+                cases.append({"columns": cols, "kwargs": dict(kw), "ragged": True})
+                continue
             cols = {k: [float(v) for v in vals] for k, vals in df_args[0].items()}
             kwj = {k: ({"array": [float(v) for v in np.ravel(v)]} if isinstance(v, np.ndarray) else v)
                    for k, v in kw.items()}

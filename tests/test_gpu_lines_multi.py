@@ -17,7 +17,9 @@ from gpu_helpers import assert_same, to_numpy
 pytestmark = pytest.mark.gpu
 
 
-def _frame(cols):
+def _frame(cols, ragged=False):
+    if ragged:
+        return ds.TensorFrame({k: ds.RaggedColumn(v) for k, v in cols.items()})
     return ds.TensorFrame({k: torch.from_numpy(np.asarray(v, dtype=np.float64)).cuda() for k, v in cols.items()})
 
 
@@ -25,7 +27,8 @@ def test_manual_range_golden():
     sol = refcases.golden_array(refcases.lines_golden("test_line_manual_range")[0])
     for case in refcases.lines_golden("line_manual_range_params")["cases"]:
         cvs = ds.Canvas(plot_width=7, plot_height=7, x_range=(-3, 3), y_range=(-3, 3))
-        agg = cvs.line(_frame(case["columns"]), agg=ds.count(), **refcases.line_kwargs(case["kwargs"]))
+        agg = cvs.line(_frame(case["columns"], case.get("ragged", False)), agg=ds.count(),
+                       **refcases.line_kwargs(case["kwargs"]))
         np.testing.assert_array_equal(to_numpy(agg), sol, err_msg=str(case["kwargs"]))
 
 
@@ -35,7 +38,7 @@ def test_autorange_golden(line_width):
     sol = refcases.golden_array(sols[0] if line_width else sols[1])
     for case in refcases.lines_golden("line_autorange_params")["cases"]:
         cvs = ds.Canvas(plot_width=9, plot_height=9)
-        agg = cvs.line(_frame(case["columns"]), agg=ds.count(), line_width=line_width,
+        agg = cvs.line(_frame(case["columns"], case.get("ragged", False)), agg=ds.count(), line_width=line_width,
                        **refcases.line_kwargs(case["kwargs"]))
         assert agg.attrs["x_range"] == (-4.0, 4.0) and agg.attrs["y_range"] == (-4.0, 4.0)
         if line_width:
@@ -113,3 +116,36 @@ def test_random_multi_lines_vs_oracle(kind, line_width):
             assert_same(got, ref, rtol=3e-7, atol=1e-7, what=f"{kind} {name}")
         else:
             assert_same(got, ref, rtol=rtol, what=f"{kind} {name}")
+
+
+@pytest.mark.parametrize("lw", [0.0, 1.5])
+@pytest.mark.parametrize("red", ["count", "sum", "max", "mean"])
+def test_ragged_random_vs_oracle(lw, red):
+    """LinesAxis1Ragged on rows of every length (0, 1, 2, many; x and y of
+    different lengths, NaN breaks) against the oracle's restatement of
+    line.py:1538-1612."""
+    rng = np.random.default_rng(31)
+    nrows = 400
+    xr, yr = [], []
+    for i in range(nrows):
+        lx = int(rng.integers(0, 40)) if i % 7 else int(rng.integers(0, 3))
+        ly = lx if i % 5 else max(0, lx + int(rng.integers(-3, 4)))
+        x = np.cumsum(rng.uniform(0.0, 0.05, lx)) + rng.uniform(-1, 1)
+        y = np.cumsum(rng.normal(0.0, 0.08, ly)) + rng.uniform(-1, 1)
+        if lx > 4 and i % 3 == 0:
+            x[lx // 2] = np.nan
+        xr.append(x)
+        yr.append(y)
+    v = rng.uniform(0.5, 2.0, nrows)
+    frame = ds.TensorFrame({"x": ds.RaggedColumn(xr), "y": ds.RaggedColumn(yr),
+                            "v": torch.from_numpy(v).cuda()})
+    agg = {"count": ds.count(), "sum": ds.sum("v"), "max": ds.max("v"), "mean": ds.mean("v")}[red]
+    cvs = ds.Canvas(plot_width=200, plot_height=150, x_range=(-1.5, 2.5), y_range=(-2.5, 2.5))
+    got = to_numpy(cvs.line(frame, "x", "y", agg=agg, axis=1, line_width=lw))
+    spec = oracle.spec(red, None if red == "count" else "v")
+    ref = oracle.lines_ragged({"v": v}, xr, yr, 200, 150, (-1.5, 2.5), (-2.5, 2.5), [spec], line_width=lw)[0]
+    rtol = 0.0 if red in ("count", "max") and lw == 0 else (3e-7 if ref.dtype == np.float32 else 1e-12)
+    assert_same(got, ref, rtol=rtol, what=f"{red} lw={lw}")
+    auto = ds.Canvas(plot_width=64, plot_height=48).line(frame, "x", "y", agg=ds.count(), axis=1)
+    ref_auto = oracle.lines_ragged({}, xr, yr, 64, 48, None, None, [oracle.spec("count")])[0]
+    assert_same(to_numpy(auto), ref_auto)

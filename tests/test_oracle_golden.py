@@ -159,9 +159,14 @@ def test_oracle_shade_three_colours():
 # ---- multi-line glyphs (LineAxis0Multi, LinesAxis1 / XConstant / YConstant) ----
 
 def test_oracle_multi_line_manual_range_golden():
-    """test_pandas.py:1654-1749 (test_line_manual_range), non-ragged cases: count on 7x7."""
+    """test_pandas.py:1654-1749 (test_line_manual_range), every case incl. ragged arrays: count on 7x7."""
     sol = refcases.golden_array(refcases.lines_golden("test_line_manual_range")[0])
     for case in refcases.lines_golden("line_manual_range_params")["cases"]:
+        if case.get("ragged"):
+            c = case["columns"]
+            got = oracle.lines_ragged({}, c["x"], c["y"], 7, 7, (-3, 3), (-3, 3), [oracle.spec("count")])[0]
+            np.testing.assert_array_equal(got, sol, err_msg="ragged")
+            continue
         layout, xs, ys = refcases.multi_line_arrays(case["columns"], case["kwargs"])
         got = oracle.lines({}, layout, xs, ys, 7, 7, (-3, 3), (-3, 3), [oracle.spec("count")])[0]
         np.testing.assert_array_equal(got, sol, err_msg=str(case["kwargs"]))
@@ -173,9 +178,14 @@ def test_oracle_multi_line_autorange_golden(line_width):
     sols = refcases.lines_golden("test_line_autorange")
     sol = refcases.golden_array(sols[0] if line_width else sols[1])
     for case in refcases.lines_golden("line_autorange_params")["cases"]:
-        layout, xs, ys = refcases.multi_line_arrays(case["columns"], case["kwargs"])
-        got = oracle.lines({}, layout, xs, ys, 9, 9, None, None, [oracle.spec("count")],
-                           line_width=line_width)[0]
+        if case.get("ragged"):
+            c = case["columns"]
+            got = oracle.lines_ragged({}, c["x"], c["y"], 9, 9, None, None, [oracle.spec("count")],
+                                      line_width=line_width)[0]
+        else:
+            layout, xs, ys = refcases.multi_line_arrays(case["columns"], case["kwargs"])
+            got = oracle.lines({}, layout, xs, ys, 9, 9, None, None, [oracle.spec("count")],
+                               line_width=line_width)[0]
         if line_width:
             np.testing.assert_allclose(got, sol, rtol=1e-6, atol=1e-6, equal_nan=True)
         else:
