@@ -647,11 +647,6 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
                                  ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
         N.check(rc, "dsgb_lines_ragged")
     elif isinstance(glyph, _MultiLine):
-        if glyph.layout == 1 and len(glyph.x) > 1 and any(
-                b.op in (N.BASE_MIN_ROW, N.BASE_MAX_ROW, N.BASE_ARGMAX, N.BASE_ARGMIN) for b in plan.bases):
-            # the reference visits line j outer, row i inner (line.py:1190-1194), so first / last /
-            # where follow (line, row) order, not the row order that row-index bases keep
-            raise NotImplementedError("first / last / where over several axis=0 lines are not on the GPU path")
         if glyph.layout == 1:
             nv, xrow, yrow = xs.shape[1], xs.shape[1], ys.shape[1]
         else:

@@ -28,15 +28,20 @@ struct LineParams {
     double xmin, xmax, ymin, ymax;
     double line_width;
     int32_t plot_start, overwrite, use_2_stage;
+    int64_t field_mod;      // > 0: appends carry a visit key (row = key % field_mod); 0: the row itself
 };
 
 // One append of row i (field row = segment start) at pixel (x, y).
-// aa / pa are aa_factor / prev_aa_factor (1, 0 for Bresenham lines).
-__device__ void line_append(const LineParams &p, int64_t i, long long x, long long y,
+// aa / pa are aa_factor / prev_aa_factor (1, 0 for Bresenham lines).  With
+// p.field_mod > 0, i is a visit key (line j, row r: j * field_mod + r) that
+// orders the row-index bases as the reference visits the appends; the
+// fields are read at row r.
+__device__ void line_append(const LineParams &p, int64_t key, long long x, long long y,
                             double aa, double pa) {
     if (x < 0 || y < 0 || x >= p.width || y >= p.height) return;  // memory safety only
     const int64_t pix = (int64_t)y * p.width + x;
-    const long long row = (long long)(i + p.row_offset);
+    const int64_t i = p.field_mod > 0 ? key % p.field_mod : key;
+    const long long row = (long long)(key + p.row_offset);
 #pragma unroll 1
     for (int b = 0; b < p.nbases; ++b) {
         const BaseDev &B = p.bases[b];
@@ -472,7 +477,9 @@ __global__ void __launch_bounds__(256, 1) lines_kernel(const LineParams p, const
             const bool segment_end = (i == g.nrows - 2) || isnull(X[(i + 2) * st]) || isnull(Y[(i + 2) * st]);
             double xm = 0.0, ym = 0.0;
             if (!(segment_start || p.use_2_stage)) { xm = X[im * st]; ym = Y[im * st]; }
-            draw_segment(p, i, x0, y0, x1, y1, segment_start, segment_end, xm, ym);
+            // line j's appends come after every append of lines 0 .. j-1 (line.py:1190-1194)
+            draw_segment(p, p.field_mod > 0 ? j * p.field_mod + i : i, x0, y0, x1, y1, segment_start, segment_end,
+                         xm, ym);
         } else {
             const int64_t i = s / (g.nv - 1), j = s - i * (g.nv - 1);
             const double *X = g.xs + i * g.xrow, *Y = g.ys + i * g.yrow;
@@ -520,6 +527,18 @@ __global__ void __launch_bounds__(256, 1) lines_ragged_kernel(const LineParams p
         double xm = 0.0, ym = 0.0;
         if (!(segment_start || p.use_2_stage)) { xm = X[j - 1]; ym = Y[j - 1]; }
         draw_segment(p, i, X[j], Y[j], X[j + 1], Y[j + 1], segment_start, segment_end, xm, ym);
+    }
+}
+
+// Visit keys (j * nrows + r, plus the row offset) held by the row-index
+// bases back to rows (r plus the row offset); empty cells keep their marker.
+__global__ void unkey_rows_kernel(int op, void *agg, int64_t n, int64_t nrows, int64_t row_offset) {
+    for (int64_t c = gtid(); c < n; c += gstride()) {
+        long long *v = (long long *)agg;
+        long long *r = (op == DSGB_BASE_MIN_ROW || op == DSGB_BASE_MAX_ROW) ? v + c : v + 2 * c + 1;
+        const long long k = *r;
+        if (k == ROW_EMPTY_MIN || k < row_offset) continue;             // empty (max-row empty is -1)
+        *r = row_offset + (k - row_offset) % nrows;
     }
 }
 
@@ -674,6 +693,7 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
     p.plot_start = plot_start;
     p.overwrite = overwrite;
     p.use_2_stage = 0;
+    if (layout == 1 && nv > 1) p.field_mod = nrows;
     LinesGeom g;
     g.xs = xs; g.ys = ys; g.nrows = nrows; g.nv = nv;
     g.xrow = layout == 1 ? nv : x_row_stride;
@@ -693,6 +713,24 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
         if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(p, g);
         else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(p, g);
         DSGB_CHECK_LAUNCH("lines kernel");
+    }
+    if (p.field_mod > 0) {
+        // visit keys -> rows; a key of one call does not order against a row of another
+        for (int32_t b = 0; b < nbases; ++b) {
+            const int op = bases[b].op;
+            if (op != DSGB_BASE_MIN_ROW && op != DSGB_BASE_MAX_ROW && op != DSGB_BASE_ARGMAX && op != DSGB_BASE_ARGMIN)
+                continue;
+            if (flags & DSGB_FLAG_NO_INIT) {
+                set_error("dsgb_lines: row-index bases over several axis=0 lines cannot accumulate across calls");
+                return DSGB_E_INVALID;
+            }
+            const int64_t n = ncells * (bases[b].cat_col >= 0 ? bases[b].ncat : 1);
+            int64_t blocks = (n + 255) / 256;
+            if (blocks > 4096) blocks = 4096;
+            if (blocks > 0)
+                unkey_rows_kernel<<<(unsigned)blocks, 256, 0, st>>>(op, bases[b].agg, n, nrows, row_offset);
+            DSGB_CHECK_LAUNCH("unkey rows");
+        }
     }
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
         rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);

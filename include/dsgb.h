@@ -258,7 +258,10 @@ int dsgb_line_axis0_ws(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
  * vertices: vertex (i, j) = (xs[i*x_row_stride + j], ys[i*y_row_stride + j]),
  * a stride of 0 shares one array across the rows: XConstant / YConstant).
  * Segment (i, j) appends row i's fields (cols).  Reductions as
- * dsgb_line_axis0; two-stage antialiased plans are not supported. */
+ * dsgb_line_axis0; two-stage antialiased plans are not supported.  With
+ * layout 1 and nv > 1, first / last / where follow the reference's visit
+ * order (line j outer, row i inner: line.py:1190-1194), so their row-index
+ * bases cannot accumulate across calls (DSGB_FLAG_NO_INIT is rejected). */
 int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
                int32_t layout, const double *xs, const double *ys, int64_t nv,
                int64_t x_row_stride, int64_t y_row_stride, const dsgb_canvas *canvas,

@@ -104,11 +104,6 @@ def test_random_multi_lines_vs_oracle(kind, line_width):
     for name, red, spec, rtol in REDS:
         if line_width and name in ("max", "first"):
             continue          # two-stage antialiased plans stay off the multi-line GPU path
-        if kind == "axis0multi" and name == "first":
-            # (line, row) visiting order of the reference: not served on the GPU path
-            with pytest.raises(NotImplementedError):
-                ds.Canvas(plot_width=30, plot_height=20, x_range=xr, y_range=yr).line(frame, agg=red, **kw)
-            continue
         cvs = ds.Canvas(plot_width=300, plot_height=200, x_range=xr, y_range=yr)
         got = to_numpy(cvs.line(frame, agg=red, line_width=line_width, **kw))
         ref = oracle.lines({"v": cols["v"]}, layout, xs, ys, 300, 200, xr, yr, [spec], line_width=line_width)[0]
@@ -116,6 +111,30 @@ def test_random_multi_lines_vs_oracle(kind, line_width):
             assert_same(got, ref, rtol=3e-7, atol=1e-7, what=f"{kind} {name}")
         else:
             assert_same(got, ref, rtol=rtol, what=f"{kind} {name}")
+
+
+@pytest.mark.parametrize("nv", [2, 6])
+def test_axis0multi_row_index_reductions_follow_line_order(nv):
+    """first / last / where over several axis=0 lines: the reference visits line j
+    outer, row i inner (line.py:1190-1194), so on pixels that several lines cross the
+    first row of line 0 wins over an earlier row of line 1.  The lines overlap on
+    most pixels of a 40 x 30 canvas, so row order and (line, row) order disagree."""
+    cols, kw = _random_case("axis0multi", 900, nv, 11)
+    rng = np.random.default_rng(12)
+    cols["w"] = rng.normal(0, 1, 900)
+    frame = _frame(cols)
+    layout, xs, ys = refcases.multi_line_arrays(cols, kw)
+    xr, yr = (0.0, 1.0), (float(np.nanmin(ys)), float(np.nanmax(ys)))
+    cvs = ds.Canvas(plot_width=40, plot_height=30, x_range=xr, y_range=yr)
+    agg = ds.summary(f=ds.first("v"), l=ds.last("v"), wr=ds.where(ds.max("v")),
+                     wl=ds.where(ds.min("v"), "w"), c=ds.count())
+    got = cvs.line(frame, agg=agg, **kw)
+    specs = [oracle.spec("first", "v"), oracle.spec("last", "v"),
+             oracle.spec("where", selector=oracle.spec("max", "v")),
+             oracle.spec("where", selector=oracle.spec("min", "v"), lookup="w"), oracle.spec("count")]
+    ref = oracle.lines({"v": cols["v"], "w": cols["w"]}, layout, xs, ys, 40, 30, xr, yr, specs)
+    for k, r in zip(("f", "l", "wr", "wl", "c"), ref):
+        assert_same(to_numpy(got[k]), r, what=f"nv={nv} {k}")
 
 
 @pytest.mark.parametrize("lw", [0.0, 1.5])
