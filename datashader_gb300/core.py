@@ -639,7 +639,7 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
     elif isinstance(glyph, LinesAxis1Ragged):
         cols, ncols = ex.cols, len(ex.names)
         if ncols == 0:                       # count() / any(): no field column, any valid pointer
-            cols = (N.Column * 1)(N.Column(xr.flat.data_ptr(), N.F64, 0))
+            cols = (N.Column * 1)(N.Column(xr.starts.data_ptr(), N.I64, 0))   # one entry a row
             ncols = 1
         rc = L.dsgb_lines_ragged(cols, ncols, len(frame), frame.row_offset, xr.flat.data_ptr(), xr.flat.numel(),
                                  xr.starts.data_ptr(), yr.flat.data_ptr(), yr.flat.numel(), yr.starts.data_ptr(),
