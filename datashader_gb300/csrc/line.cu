@@ -32,15 +32,16 @@ struct LineParams {
 };
 
 // One append of row i (field row = segment start) at pixel (x, y).
-// aa / pa are aa_factor / prev_aa_factor (1, 0 for Bresenham lines).  With
-// p.field_mod > 0, i is a visit key (line j, row r: j * field_mod + r) that
-// orders the row-index bases as the reference visits the appends; the
-// fields are read at row r.
+// aa / pa are aa_factor / prev_aa_factor (1, 0 for Bresenham lines).  KEYED:
+// `key` is a visit key (line j, row r: j * p.field_mod + r) that orders the
+// row-index bases as the reference visits the appends, and the fields are
+// read at row r; otherwise `key` is the row.
+template <bool KEYED>
 __device__ void line_append(const LineParams &p, int64_t key, long long x, long long y,
                             double aa, double pa) {
     if (x < 0 || y < 0 || x >= p.width || y >= p.height) return;  // memory safety only
     const int64_t pix = (int64_t)y * p.width + x;
-    const int64_t i = p.field_mod > 0 ? key % p.field_mod : key;
+    const int64_t i = KEYED ? key % p.field_mod : key;
     const long long row = (long long)(key + p.row_offset);
 #pragma unroll 1
     for (int b = 0; b < p.nbases; ++b) {
@@ -158,6 +159,7 @@ __device__ __forceinline__ double pick4(int i, double a0, double a1, double a2, 
 }
 
 // line.py:826-981 -- _full_antialias.
+template <bool KEYED>
 __device__ void full_antialias(const LineParams &p, double line_width, bool overwrite, int64_t i,
                                double x0, double x1, double y0, double y1,
                                bool segment_start, bool segment_end, double xm, double ym,
@@ -264,14 +266,15 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
                 if (value <= prev_value) value = 0.0;
             }
             if (value > 0.0) {
-                if (flip_xy) line_append(p, i, y, x, value, prev_value);
-                else line_append(p, i, x, y, value, prev_value);
+                if (flip_xy) line_append<KEYED>(p, i, y, x, value, prev_value);
+                else line_append<KEYED>(p, i, x, y, value, prev_value);
             }
         }
     }
 }
 
 // line.py:986-1031 -- integer Bresenham.
+template <bool KEYED>
 __device__ void bresenham(const LineParams &p, int64_t i, bool segment_start, long long x0, long long x1,
                           long long y0, long long y1, bool clipped) {
     long long dx = x1 - x0;
@@ -280,15 +283,15 @@ __device__ void bresenham(const LineParams &p, int64_t i, bool segment_start, lo
     long long dy = y1 - y0;
     const long long iy = (dy > 0) - (dy < 0);
     dy = (dy < 0 ? -dy : dy) * 2;
-    if (!clipped && !(dx | dy)) { line_append(p, i, x0, y0, 1.0, 0.0); return; }
-    if (segment_start) line_append(p, i, x0, y0, 1.0, 0.0);
+    if (!clipped && !(dx | dy)) { line_append<KEYED>(p, i, x0, y0, 1.0, 0.0); return; }
+    if (segment_start) line_append<KEYED>(p, i, x0, y0, 1.0, 0.0);
     if (dx >= dy) {
         long long error = 2 * dy - dx;
         while (x0 != x1) {
             if (error >= 0 && (error || ix > 0)) { error -= 2 * dx; y0 += iy; }
             error += 2 * dy;
             x0 += ix;
-            line_append(p, i, x0, y0, 1.0, 0.0);
+            line_append<KEYED>(p, i, x0, y0, 1.0, 0.0);
         }
     } else {
         long long error = 2 * dx - dy;
@@ -296,7 +299,7 @@ __device__ void bresenham(const LineParams &p, int64_t i, bool segment_start, lo
             if (error >= 0 && (error || iy > 0)) { error -= 2 * dy; x0 += ix; }
             error += 2 * dx;
             y0 += iy;
-            line_append(p, i, x0, y0, 1.0, 0.0);
+            line_append<KEYED>(p, i, x0, y0, 1.0, 0.0);
         }
     }
 }
@@ -318,6 +321,7 @@ __device__ __forceinline__ void map_snap(const LineParams &p, double x, double y
 // vertex (xm, ym)): clip, map, antialiased coverage or Bresenham
 // (line.py:1033-1097 _build_draw_segment).  `row` is the row whose fields
 // the appends use.
+template <bool KEYED = false>
 __device__ void draw_segment(const LineParams &p, int64_t row, double x0, double y0, double x1, double y1,
                              bool segment_start, bool segment_end, double xm, double ym) {
     const bool antialias = p.line_width > 0.0;
@@ -335,13 +339,13 @@ __device__ void draw_segment(const LineParams &p, int64_t row, double x0, double
         if (!segment_start) { pxm = xm * p.sx + p.tx - 0.5; pym = ym * p.sy + p.ty - 0.5; }
         const long long nx = pyround((p.xmax - p.xmin) * p.sx);
         const long long ny = pyround((p.ymax - p.ymin) * p.sy);
-        full_antialias(p, p.line_width, p.overwrite != 0, row, px0, px1, py0, py1,
+        full_antialias<KEYED>(p, p.line_width, p.overwrite != 0, row, px0, px1, py0, py1,
                        segment_start, segment_end, pxm, pym, nx, ny);
     } else {
         long long ix0, iy0, ix1, iy1;
         map_snap(p, x0, y0, ix0, iy0);
         map_snap(p, x1, y1, ix1, iy1);
-        bresenham(p, row, segment_start, ix0, ix1, iy0, iy1, clipped);
+        bresenham<KEYED>(p, row, segment_start, ix0, ix1, iy0, iy1, clipped);
     }
 }
 
@@ -478,8 +482,10 @@ __global__ void __launch_bounds__(256, 1) lines_kernel(const LineParams p, const
             double xm = 0.0, ym = 0.0;
             if (!(segment_start || p.use_2_stage)) { xm = X[im * st]; ym = Y[im * st]; }
             // line j's appends come after every append of lines 0 .. j-1 (line.py:1190-1194)
-            draw_segment(p, p.field_mod > 0 ? j * p.field_mod + i : i, x0, y0, x1, y1, segment_start, segment_end,
-                         xm, ym);
+            if (p.field_mod > 0)
+                draw_segment<true>(p, j * p.field_mod + i, x0, y0, x1, y1, segment_start, segment_end, xm, ym);
+            else
+                draw_segment(p, i, x0, y0, x1, y1, segment_start, segment_end, xm, ym);
         } else {
             const int64_t i = s / (g.nv - 1), j = s - i * (g.nv - 1);
             const double *X = g.xs + i * g.xrow, *Y = g.ys + i * g.yrow;
