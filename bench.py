@@ -567,6 +567,11 @@ def run_gpu(args):
             base = {"value": gpts, "unit": "Gpoints/s", "cores": 1, "kind": "port",
                     "sample": f"{args.cpu_sample} rows of the same distribution, count, one thread, "
                               f"{dt:.2f} s"}
+            nth = os.cpu_count() or 1
+            if nth > 1:      # the same sample over one row partition per host thread
+                g_all, dt_all = cpu_baseline(args.cpu_sample, threads=nth)
+                base["all_threads"] = {"value": g_all, "unit": "Gpoints/s", "cores": nth,
+                                       "sample": f"the same rows, {nth} threads, {dt_all:.2f} s"}
         line = {
             "metric": METRIC, "value": value, "unit": "Gpoints/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
