@@ -36,6 +36,7 @@ class BaseSpec:
     cat: Optional[str]      # name of the category-code column
     ncat: int
     flags: int = 0
+    fold: int = 0           # two-stage plans over several lines: the stage-2 fold (DSGB_FOLD_*), 0 = none
 
     @property
     def elem_bytes(self):
@@ -127,6 +128,35 @@ def aa_stage_flags(agg):
     return si, overwrite, use_2
 
 
+def _stage2_fold(red):
+    """The stage-2 fold that a two-stage plan over several lines applies to the
+    single base of ``red`` (compiler.py:153-196 with the combinations of
+    reductions.py: count and sum SUM_2AGG, any and max MAX, min MIN, first
+    FIRST, last LAST, the row indexes MIN / MAX over -1); 0 where it has none
+    here (mean, _sum_zero, _count_ignore_antialiasing, where)."""
+    if isinstance(red, rd._count_ignore_antialiasing):
+        return 0
+    if isinstance(red, rd.count):
+        return N.FOLD_SUM_F32          # float32 aggregate (reductions.py:542-543)
+    if isinstance(red, rd.any):
+        return N.FOLD_MAX
+    if isinstance(red, rd.sum) and not isinstance(red, rd._sum_zero):
+        return N.FOLD_SUM
+    if isinstance(red, rd.max):
+        return N.FOLD_MAX
+    if isinstance(red, rd.min):
+        return N.FOLD_MIN
+    if isinstance(red, rd.first):
+        return N.FOLD_FIRST
+    if isinstance(red, rd.last):
+        return N.FOLD_LAST
+    if isinstance(red, rd._min_row_index):
+        return N.FOLD_ROW_MIN
+    if isinstance(red, rd._max_row_index):
+        return N.FOLD_MAX
+    return 0
+
+
 class _Builder:
     def __init__(self, schema, antialias, si):
         self.schema = schema
@@ -144,8 +174,8 @@ class _Builder:
             self.columns.append(name)
         return name
 
-    def base(self, op, col, cat, ncat, flags=0):
-        spec = BaseSpec(op, self.col(col), cat, ncat, flags)
+    def base(self, op, col, cat, ncat, flags=0, fold=0):
+        spec = BaseSpec(op, self.col(col), cat, ncat, flags, fold)
         if spec not in self.index:
             self.index[spec] = len(self.bases)
             self.bases.append(spec)
@@ -171,7 +201,8 @@ class _Builder:
             name, n, cats, dim = self.categorizer(red)
             return self.reduction(red.reduction, name, n, cats, dim)
         kw = dict(categories=categories, cat_dim=cat_dim)
-        B = lambda op, col, flags=0: self.base(op, col, cat, ncat, flags)  # noqa: E731
+        fold = _stage2_fold(red) if (self.antialias and not self.si) else 0
+        B = lambda op, col, flags=0: self.base(op, col, cat, ncat, flags, fold)  # noqa: E731
         c = red.column if not isinstance(red, rd._max_or_min_row_index) else None
         aa = self.antialias
         if isinstance(red, rd._count_ignore_antialiasing):

@@ -411,9 +411,12 @@ class Canvas:
                     f"{type(non_cat)} reduction not implemented for antialiased lines")
         if glyph.antialiased and isinstance(glyph, _MultiLine):
             from .compiler import compile_plan as _cp
-            if _cp(agg, as_frame(source), antialias=True).use_2_stage:
-                raise NotImplementedError("two-stage antialiased reductions over several lines are not on the "
-                                          "GPU path")
+            plan = _cp(agg, as_frame(source), antialias=True)
+            if plan.use_2_stage and (isinstance(glyph, LinesAxis1Ragged) or any(b.fold == 0 for b in plan.bases)):
+                # folded line by line for count / sum / any / max / min / first / last and the row
+                # indexes; mean, where and _count_ignore_antialiasing have no stage-2 fold here
+                raise NotImplementedError("this two-stage antialiased plan over several lines is not on the GPU "
+                                          "path (ragged lines, mean, where or _count_ignore_antialiasing)")
         return bypixel(source, self, glyph, agg, antialias=glyph.antialiased)
 
     def validate_ranges(self, x_range, y_range):
@@ -657,10 +660,21 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
         if ncols == 0:                       # count() / any(): no field column, any valid pointer
             cols = (N.Column * 1)(N.Column(ys.data_ptr(), N.F64, 0))
             ncols = 1
-        rc = L.dsgb_lines(cols, ncols, len(frame), frame.row_offset, glyph.layout, xs.data_ptr(), ys.data_ptr(),
-                          nv, xrow, yrow, ctypes.byref(cv), float(glyph.line_width), 1, int(plan.overwrite),
-                          ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
-        N.check(rc, "dsgb_lines")
+        if antialias and plan.use_2_stage:
+            # each line alone, folded line by line (line.py:1203-1226 and siblings)
+            line_aggs = [torch.empty_like(t) for t in ex.base_tensors]
+            folds = (ctypes.c_int32 * max(1, len(plan.bases)))(*[b.fold for b in plan.bases])
+            ptrs = (ctypes.c_void_p * max(1, len(plan.bases)))(*[t.data_ptr() for t in line_aggs])
+            rc = L.dsgb_lines_2stage(cols, ncols, len(frame), frame.row_offset, glyph.layout, xs.data_ptr(),
+                                     ys.data_ptr(), nv, xrow, yrow, ctypes.byref(cv), float(glyph.line_width),
+                                     int(plan.overwrite), ex.bases, len(plan.bases), folds, ptrs, ex.outs,
+                                     ex.nouts, flags, stream)
+            N.check(rc, "dsgb_lines_2stage")
+        else:
+            rc = L.dsgb_lines(cols, ncols, len(frame), frame.row_offset, glyph.layout, xs.data_ptr(),
+                              ys.data_ptr(), nv, xrow, yrow, ctypes.byref(cv), float(glyph.line_width), 1,
+                              int(plan.overwrite), ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
+            N.check(rc, "dsgb_lines")
     else:
         wsz = int(L.dsgb_points_workspace_size_flags(len(frame), ctypes.byref(cv), ex.bases, len(plan.bases),
                                                      flags))

@@ -465,14 +465,17 @@ struct LinesGeom {
     const double *xs, *ys;
     int64_t nrows, nv;      // LAYOUT 1: nv = lines; LAYOUT 2: nv = vertices per line
     int64_t xrow, yrow;     // LAYOUT 2: row strides of xs and ys (0 = shared by all rows)
+    int64_t only_line;      // >= 0: draw this line alone (two-stage plans); -1: every line
 };
 
 template <int LAYOUT>
 __global__ void __launch_bounds__(256, 1) lines_kernel(const LineParams p, const LinesGeom g) {
-    const int64_t nseg = LAYOUT == 1 ? (g.nrows - 1) * g.nv : g.nrows * (g.nv - 1);
+    const bool one = g.only_line >= 0;
+    const int64_t nseg = one ? (LAYOUT == 1 ? g.nrows - 1 : g.nv - 1)
+                             : (LAYOUT == 1 ? (g.nrows - 1) * g.nv : g.nrows * (g.nv - 1));
     for (int64_t s = gtid(); s < nseg; s += gstride()) {
         if (LAYOUT == 1) {
-            const int64_t i = s / g.nv, j = s - i * g.nv;
+            const int64_t i = one ? s : s / g.nv, j = one ? g.only_line : s - i * g.nv;
             const double *X = g.xs + j, *Y = g.ys + j;
             const int64_t st = g.nv;
             const double x0 = X[i * st], y0 = Y[i * st], x1 = X[(i + 1) * st], y1 = Y[(i + 1) * st];
@@ -487,7 +490,7 @@ __global__ void __launch_bounds__(256, 1) lines_kernel(const LineParams p, const
             else
                 draw_segment(p, i, x0, y0, x1, y1, segment_start, segment_end, xm, ym);
         } else {
-            const int64_t i = s / (g.nv - 1), j = s - i * (g.nv - 1);
+            const int64_t i = one ? g.only_line : s / (g.nv - 1), j = one ? s : s - i * (g.nv - 1);
             const double *X = g.xs + i * g.xrow, *Y = g.ys + i * g.yrow;
             const double x0 = X[j], x1 = X[j + 1], y0 = Y[j], y1 = Y[j + 1];
             const bool segment_start = (j == 0) || isnull(X[j - 1]) || isnull(Y[j - 1]);
@@ -704,6 +707,7 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
     g.xs = xs; g.ys = ys; g.nrows = nrows; g.nv = nv;
     g.xrow = layout == 1 ? nv : x_row_stride;
     g.yrow = layout == 1 ? nv : y_row_stride;
+    g.only_line = -1;
     cudaStream_t st = as_stream(stream);
     const int64_t ncells = (int64_t)canvas->width * canvas->height;
     if (!(flags & DSGB_FLAG_NO_INIT)) {
@@ -736,6 +740,131 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
             if (blocks > 0)
                 unkey_rows_kernel<<<(unsigned)blocks, 256, 0, st>>>(op, bases[b].agg, n, nrows, row_offset);
             DSGB_CHECK_LAUNCH("unkey rows");
+        }
+    }
+    if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+        rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+    return rc;
+}
+
+namespace dsgb {
+
+// Stage-2 fold of one line's aggregate into the accumulator (compiler.py:
+// 198-268 with utils.py:615-923), on the int64 storage of the bases:
+// AA_MAX keys (empty = KEY_EMPTY_MAX, below every key), MIN_ROW rows (empty
+// = ROW_EMPTY_MIN, above every row), MAX_ROW rows (empty = -1).
+__global__ void stage2_fold_kernel(int fold, long long *acc, const long long *part, int64_t n) {
+    for (int64_t c = gtid(); c < n; c += gstride()) {
+        long long a = acc[c];
+        const long long o = part[c];
+        switch (fold) {
+        case DSGB_FOLD_MAX: if (o > a) a = o; break;                 // nanmax_in_place / row_max_in_place
+        case DSGB_FOLD_ROW_MIN: if (o < a) a = o; break;             // row_min_in_place
+        case DSGB_FOLD_MIN:                                           // nanmin_in_place
+            if (o != KEY_EMPTY_MAX && (a == KEY_EMPTY_MAX || o < a)) a = o;
+            break;
+        case DSGB_FOLD_FIRST: if (a == KEY_EMPTY_MAX) a = o; break;  // nanfirst_in_place
+        case DSGB_FOLD_LAST: if (o != KEY_EMPTY_MAX) a = o; break;   // nanlast_in_place
+        case DSGB_FOLD_SUM:                                           // nansum_in_place, float64
+            if (o != KEY_EMPTY_MAX) a = a == KEY_EMPTY_MAX ? o : f64_key(__dadd_rn(key_f64(a), key_f64(o)));
+            break;
+        case DSGB_FOLD_SUM_F32:                                       // nansum_in_place on a float32 aggregate
+            if (o != KEY_EMPTY_MAX)
+                a = a == KEY_EMPTY_MAX ? o
+                    : f64_key((double)__fadd_rn((float)key_f64(a), (float)key_f64(o)));
+            break;
+        default: break;
+        }
+        acc[c] = a;
+    }
+}
+
+static bool fold_fits(int op, int fold) {
+    if (op == DSGB_BASE_AA_MAX)
+        return fold == DSGB_FOLD_MAX || fold == DSGB_FOLD_MIN || fold == DSGB_FOLD_FIRST || fold == DSGB_FOLD_LAST ||
+               fold == DSGB_FOLD_SUM || fold == DSGB_FOLD_SUM_F32;
+    if (op == DSGB_BASE_MIN_ROW) return fold == DSGB_FOLD_ROW_MIN;
+    if (op == DSGB_BASE_MAX_ROW) return fold == DSGB_FOLD_MAX;
+    return false;
+}
+
+}  // namespace dsgb
+
+extern "C" int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
+                                 int32_t layout, const double *xs, const double *ys, int64_t nv,
+                                 int64_t x_row_stride, int64_t y_row_stride, const dsgb_canvas *canvas,
+                                 double line_width, int32_t overwrite, const dsgb_base *bases, int32_t nbases,
+                                 const int32_t *folds, void *const *line_aggs, const dsgb_output *outs,
+                                 int32_t nouts, uint32_t flags, void *stream) {
+    if (layout != 1 && layout != 2) {
+        set_error("dsgb_lines_2stage: layout must be 1 (LineAxis0Multi) or 2 (LinesAxis1 family)");
+        return DSGB_E_INVALID;
+    }
+    if (layout == 2 && ((x_row_stride != 0 && x_row_stride != nv) || (y_row_stride != 0 && y_row_stride != nv))) {
+        set_error("dsgb_lines_2stage: row strides must be 0 (shared) or nv");
+        return DSGB_E_INVALID;
+    }
+    if (nrows < 0 || nv < 1 || (nrows > 0 && (!xs || !ys))) {
+        set_error("dsgb_lines_2stage: invalid vertex arrays");
+        return DSGB_E_INVALID;
+    }
+    if (!(line_width > 0.0)) { set_error("dsgb_lines_2stage: two-stage plans are antialiased (line_width > 0)"); return DSGB_E_INVALID; }
+    if (flags & DSGB_FLAG_NO_INIT) {
+        set_error("dsgb_lines_2stage: a two-stage plan cannot accumulate across calls");
+        return DSGB_E_INVALID;
+    }
+    if (nbases > 0 && (!folds || !line_aggs)) { set_error("dsgb_lines_2stage: folds / line_aggs missing"); return DSGB_E_INVALID; }
+    LineParams p;
+    int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
+    if (rc) return rc;
+    dsgb_base line_bases[MAX_BASES];
+    for (int32_t b = 0; b < nbases; ++b) {
+        if (!fold_fits(bases[b].op, folds[b]) || !line_aggs[b]) {
+            set_error("dsgb_lines_2stage: base %d (op %d) has no stage-2 fold %d", b, bases[b].op, folds[b]);
+            return DSGB_E_UNSUPPORTED;
+        }
+        line_bases[b] = bases[b];
+        line_bases[b].agg = line_aggs[b];
+    }
+    p.line_width = line_width;
+    p.plot_start = 1;
+    p.overwrite = overwrite;
+    p.use_2_stage = 1;                     // the previous vertex is not read (line.py:1170, 1266)
+    LineParams pl = p;                     // the same plan drawing into the per-line aggregates
+    for (int32_t b = 0; b < nbases; ++b) pl.bases[b].agg = line_aggs[b];
+    LinesGeom g;
+    g.xs = xs; g.ys = ys; g.nrows = nrows; g.nv = nv;
+    g.xrow = layout == 1 ? nv : x_row_stride;
+    g.yrow = layout == 1 ? nv : y_row_stride;
+    cudaStream_t st = as_stream(stream);
+    const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    rc = bases_init(bases, nbases, ncells, st);
+    if (rc) return rc;
+    const int64_t nlines = layout == 1 ? nv : nrows;
+    const int64_t nseg = layout == 1 ? nrows - 1 : nv - 1;   // segments of one line
+    int sms = sm_count();
+    if (sms <= 0) sms = 148;
+    int64_t blocks = (nseg + 255) / 256;
+    if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+    for (int64_t L = 0; L < nlines && nseg > 0 && nbases > 0; ++L) {
+        // line 0 draws straight into the accumulators (the first pass copies,
+        // compiler.py:218-222); every later line into freshly initialised
+        // per-line aggregates, folded in line order
+        g.only_line = L;
+        if (L > 0) {
+            rc = bases_init(line_bases, nbases, ncells, st);
+            if (rc) return rc;
+        }
+        if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(L > 0 ? pl : p, g);
+        else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(L > 0 ? pl : p, g);
+        DSGB_CHECK_LAUNCH("two-stage lines kernel");
+        for (int32_t b = 0; b < nbases && L > 0; ++b) {
+            const int64_t n = ncells * (bases[b].ncat < 1 ? 1 : bases[b].ncat);
+            const unsigned fb = (unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+            if (fb == 0) continue;
+            stage2_fold_kernel<<<fb, 256, 0, st>>>(folds[b], (long long *)bases[b].agg,
+                                                  (const long long *)line_aggs[b], n);
+            DSGB_CHECK_LAUNCH("stage-2 fold");
         }
     }
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)

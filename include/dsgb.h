@@ -269,6 +269,35 @@ int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t ro
                const dsgb_base *bases, int32_t nbases,
                const dsgb_output *outs, int32_t nouts, uint32_t flags, void *stream);
 
+/* Two-stage antialiased plans over several lines (the reference's
+ * cpu_antialias_2agg_impl, line.py:1203-1226 for LineAxis0Multi and
+ * :1300-1318 with its siblings for the LinesAxis1 family; compiler.py:198-268
+ * for the folds).  Each line is drawn alone: line 0 into the bases, every
+ * later line into `line_aggs[b]` (caller-owned device buffers of the same
+ * size as bases[b].agg, initialised here), which is then folded into
+ * bases[b].agg with folds[b], in line order.  Arguments otherwise as
+ * dsgb_lines; line_width > 0.  The previous vertex is never read (two-stage
+ * plans draw every segment as if it started a line, line.py:1170, 1266).
+ * Supported bases and folds: DSGB_BASE_AA_MAX with any value fold,
+ * DSGB_BASE_MIN_ROW with DSGB_FOLD_ROW_MIN, DSGB_BASE_MAX_ROW with
+ * DSGB_FOLD_MAX.  Cost: one launch per line plus one initialisation and one
+ * fold of each base over the canvas per line after the first. */
+enum {
+    DSGB_FOLD_SUM      = 1,  /* nansum_in_place, float64 (count / sum, self_intersect=False) */
+    DSGB_FOLD_SUM_F32  = 2,  /* nansum_in_place on a float32 aggregate (antialiased count)   */
+    DSGB_FOLD_MAX      = 3,  /* nanmax_in_place (any, max) / row_max_in_place (MAX_ROW)      */
+    DSGB_FOLD_MIN      = 4,  /* nanmin_in_place (min)                                       */
+    DSGB_FOLD_FIRST    = 5,  /* nanfirst_in_place (first)                                   */
+    DSGB_FOLD_LAST     = 6,  /* nanlast_in_place (last)                                     */
+    DSGB_FOLD_ROW_MIN  = 7   /* row_min_in_place (MIN_ROW)                                  */
+};
+int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
+                      int32_t layout, const double *xs, const double *ys, int64_t nv,
+                      int64_t x_row_stride, int64_t y_row_stride, const dsgb_canvas *canvas,
+                      double line_width, int32_t overwrite, const dsgb_base *bases, int32_t nbases,
+                      const int32_t *folds, void *const *line_aggs, const dsgb_output *outs,
+                      int32_t nouts, uint32_t flags, void *stream);
+
 /* Canvas.line(axis=1) over ragged x / y columns (LinesAxis1Ragged,
  * line.py:457-523 and 1538-1612): row i's vertices are x_flat[x_start[i] ..
  * x_start[i+1]) and y_flat[y_start[i] .. y_start[i+1]) (the last row to nx /

@@ -83,6 +83,7 @@ def lib():
                 ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                 ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 9 + [
                 ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
+            L.oracle_lines_2stage.argtypes = L.oracle_lines.argtypes
             L.oracle_lines_ragged.argtypes = [
                 ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
@@ -325,19 +326,21 @@ def lines(cols, layout, xs, ys, width, height, x_range, y_range, specs, line_wid
     sx, tx = scale_translate(x_range, width)
     sy, ty = scale_translate(y_range, height)
     antialias = line_width > 0
+    use_2_stage = False
     if antialias:
         self_intersect, overwrite, use_2_stage = aa_flags(specs)
-        if use_2_stage:
-            raise NotImplementedError("two-stage antialiased reductions over several lines")
         specs = [dict(s, self_intersect=self_intersect) for s in specs]
     else:
         overwrite = False
     reds, keep, colarrs, ptrs = _prepare(cols, specs, (height, width), antialias)
     L = lib()
     L.oracle_init(reds, len(specs), height * width, 1 if antialias else 0)
-    L.oracle_lines(layout, nrows, nv, xs.ctypes.data, ys.ctypes.data, xrow, yrow, ptrs, row_offset, width, height,
-                   sx, tx, sy, ty, float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]),
-                   float(line_width), 1 if plot_start else 0, 1 if overwrite else 0, reds, len(specs))
+    fn = L.oracle_lines_2stage if use_2_stage else L.oracle_lines
+    rc = fn(layout, nrows, nv, xs.ctypes.data, ys.ctypes.data, xrow, yrow, ptrs, row_offset, width, height,
+            sx, tx, sy, ty, float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]),
+            float(line_width), 1 if plot_start else 0, 1 if overwrite else 0, reds, len(specs))
+    if rc == -2:
+        raise NotImplementedError("a reduction of this two-stage antialiased plan has no stage-2 fold in the oracle")
     return _finalize(specs, keep)
 
 

@@ -675,6 +675,137 @@ int oracle_lines(int32_t layout, int64_t nrows, int64_t nv, const double *xs, co
     return 0;
 }
 
+/* ---------------------------------------------------------------------- */
+/* Two-stage antialiased plans over several lines (cpu_antialias_2agg_impl,  */
+/* line.py:1203-1226 for LineAxis0Multi, :1300-1318 and siblings for the     */
+/* LinesAxis1 family): each line is drawn alone into freshly initialised     */
+/* aggregates (every stage-2 zero equals the create() value), then folded   */
+/* into the accumulators with the reduction's stage-2 combination           */
+/* (compiler.py:198-268); a plan over one line keeps the drawn aggregates.  */
+/* ---------------------------------------------------------------------- */
+
+static void draw_one_line(int32_t layout, int64_t L, int64_t nrows, int64_t nv, const double *xs, const double *ys,
+                          int64_t xrow, int64_t yrow, const double *const *cols, int64_t row_offset, int32_t width,
+                          double sx, double tx, double sy, double ty, double xmin, double xmax, double ymin,
+                          double ymax, double line_width, int32_t plot_start, int32_t overwrite,
+                          oracle_red *reds, int nreds) {
+    if (layout == 1) {
+        const int64_t j = L;
+        for (int64_t i = 0; i + 1 < nrows; ++i) {
+            const int64_t im = i > 0 ? i - 1 : nrows - 1;
+#define XA(r) xs[(r) * nv + j]
+#define YA(r) ys[(r) * nv + j]
+            int segment_start = (i == 0) ? plot_start : (isnull_d(XA(im)) || isnull_d(YA(im)));
+            int segment_end = (i == nrows - 2) || isnull_d(XA(i + 2)) || isnull_d(YA(i + 2));
+            draw_segment(i, row_offset, XA(i), YA(i), XA(i + 1), YA(i + 1), segment_start, segment_end,
+                         0.0, 0.0, cols, width, sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite,
+                         reds, nreds);
+#undef XA
+#undef YA
+        }
+    } else {
+        const int64_t i = L;
+        const double *X = xs + i * xrow, *Y = ys + i * yrow;
+        for (int64_t j = 0; j + 1 < nv; ++j) {
+            int segment_start = (j == 0) || isnull_d(X[j - 1]) || isnull_d(Y[j - 1]);
+            int segment_end = (j == nv - 2) || isnull_d(X[j + 2]) || isnull_d(Y[j + 2]);
+            draw_segment(i, row_offset, X[j], Y[j], X[j + 1], Y[j + 1], segment_start, segment_end, 0.0, 0.0,
+                         cols, width, sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite, reds, nreds);
+        }
+    }
+}
+
+static size_t stage2_elem(int kind) {
+    switch (kind) {
+    case ORK_COUNT: case ORK_ANY: return 4;                 /* float32 when antialiased */
+    case ORK_SUM: case ORK_MIN: case ORK_MAX: case ORK_FIRST: case ORK_LAST:
+    case ORK_MIN_ROW: case ORK_MAX_ROW: return 8;
+    default: return 0;                                      /* no stage-2 fold restated here */
+    }
+}
+
+/* ret <- combine(ret, other): nansum_in_place (utils.py:885-897, float32 for the
+ * float32 count), nanmax_in_place / nanmin_in_place (:639-668),
+ * nanfirst_in_place / nanlast_in_place (:615-636), row_max_in_place /
+ * row_min_in_place (:901-923).  count and sum fold with SUM_2AGG, any and max
+ * with MAX, min with MIN, first / last with FIRST / LAST, the row indexes with
+ * MIN / MAX over -1 (reductions.py:545-549, 1040-1045, 837, 1173, 1218, 1396,
+ * 1434, 2257, 2311). */
+static void stage2_fold(int kind, void *ret, const void *other, int64_t n) {
+    if (kind == ORK_COUNT || kind == ORK_ANY) {
+        float *r = (float *)ret;
+        const float *o = (const float *)other;
+        for (int64_t k = 0; k < n; ++k) {
+            const float a = r[k], b = o[k];
+            const int an = !(a <= 0.0f || a > 0.0f), bn = !(b <= 0.0f || b > 0.0f);
+            if (kind == ORK_COUNT) {
+                if (an) { if (!bn) r[k] = b; }
+                else if (!bn) r[k] = a + b;
+            } else {
+                if (an) { if (!bn) r[k] = b; }
+                else if (!bn && b > a) r[k] = b;
+            }
+        }
+    } else if (kind == ORK_MIN_ROW || kind == ORK_MAX_ROW) {
+        int64_t *r = (int64_t *)ret;
+        const int64_t *o = (const int64_t *)other;
+        for (int64_t k = 0; k < n; ++k)
+            if (o[k] > -1 && (r[k] == -1 || (kind == ORK_MIN_ROW ? o[k] < r[k] : o[k] > r[k]))) r[k] = o[k];
+    } else {
+        double *r = (double *)ret;
+        const double *o = (const double *)other;
+        for (int64_t k = 0; k < n; ++k) {
+            const double a = r[k], b = o[k];
+            const int an = isnull_d(a), bn = isnull_d(b);
+            switch (kind) {
+            case ORK_SUM: if (an) { if (!bn) r[k] = b; } else if (!bn) r[k] = a + b; break;
+            case ORK_MAX: if (an) { if (!bn) r[k] = b; } else if (!bn && b > a) r[k] = b; break;
+            case ORK_MIN: if (an) { if (!bn) r[k] = b; } else if (!bn && b < a) r[k] = b; break;
+            case ORK_FIRST: if (an && !bn) r[k] = b; break;
+            case ORK_LAST: if (!bn) r[k] = b; break;
+            default: break;
+            }
+        }
+    }
+}
+
+/* Returns 0, or -2 when a reduction has no stage-2 fold restated here. */
+int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double *xs, const double *ys,
+                        int64_t xrow, int64_t yrow, const double *const *cols, int64_t row_offset,
+                        int32_t width, int32_t height, double sx, double tx, double sy, double ty,
+                        double xmin, double xmax, double ymin, double ymax,
+                        double line_width, int32_t plot_start, int32_t overwrite, oracle_red *reds, int nreds) {
+    const int64_t ncells = (int64_t)width * height;
+    const int64_t nlines = layout == 1 ? nv : nrows;
+    for (int r = 0; r < nreds; ++r)
+        if (stage2_elem(reds[r].kind) == 0) return -2;
+    void *acc[64];
+    if (nreds > 64) return -2;
+    for (int r = 0; r < nreds; ++r) acc[r] = NULL;
+    for (int64_t L = 0; L < nlines; ++L) {
+        if (L > 0) oracle_init(reds, nreds, ncells, 1);
+        draw_one_line(layout, L, nrows, nv, xs, ys, xrow, yrow, cols, row_offset, width, sx, tx, sy, ty,
+                      xmin, xmax, ymin, ymax, line_width, plot_start, overwrite, reds, nreds);
+        if (nlines == 1) return 0;
+        for (int r = 0; r < nreds; ++r) {
+            const int64_t n = red_cells(ncells, &reds[r]);
+            const size_t bytes = (size_t)n * stage2_elem(reds[r].kind);
+            if (L == 0) {
+                acc[r] = malloc(bytes ? bytes : 1);
+                memcpy(acc[r], reds[r].agg, bytes);
+            } else {
+                stage2_fold(reds[r].kind, acc[r], reds[r].agg, n);
+            }
+        }
+    }
+    for (int r = 0; r < nreds && nlines > 1; ++r) {
+        const int64_t n = red_cells(ncells, &reds[r]);
+        memcpy(reds[r].agg, acc[r], (size_t)n * stage2_elem(reds[r].kind));
+        free(acc[r]);
+    }
+    return 0;
+}
+
 /* line.py:1538-1612 -- LinesAxis1Ragged (_build_extend_line_axis1_ragged,
  * single-stage form): row i runs over its own slices of the flat x and y
  * arrays (start indices; the last row ends at the flat length), through

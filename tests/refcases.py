@@ -261,6 +261,66 @@ def line_cases():
     return cases
 
 
+def both_lines_cases():
+    """TestLineAntialias both_lines (test_pandas.py:2698-2785): the two lines of
+    line_antialias_df drawn together as LineAxis0Multi (x=["x0", "x1"],
+    y=["y0", "y1"], line_width=1), each expected image built from the single-line
+    solutions as the reference test builds it (nansum / nanmax / nanmin / rowmin /
+    rowmax, :2304-2331).  Returns (columns, canvas, cases); `two_stage` marks the
+    plans the reference runs line by line with a stage-2 fold."""
+    g = load_golden("line_antialias.json")
+    src = {k: golden_array(v) for k, v in g["line_antialias_df"]["columns"].items()}
+    A = {k: golden_array(v) for k, v in g.items() if k.startswith("line_antialias_sol")}
+    s0, s1, s0i = A["line_antialias_sol_0"], A["line_antialias_sol_1"], A["line_antialias_sol_0_intersect"]
+    c0, c1 = A["line_antialias_sol_count_ignore_aa_0"], A["line_antialias_sol_count_ignore_aa_1"]
+
+    def both_nan(a, b):
+        return np.isnan(a) & np.isnan(b)
+
+    def nansum(a, b):
+        r = np.nan_to_num(a) + np.nan_to_num(b)
+        r[both_nan(a, b)] = np.nan
+        return r
+
+    def nanmax(a, b):
+        r = np.maximum(np.nan_to_num(a), np.nan_to_num(b))
+        r[both_nan(a, b)] = np.nan
+        return r
+
+    def nanmin(a, b):
+        r = np.minimum(np.nan_to_num(a, nan=1e10), np.nan_to_num(b, nan=1e10))
+        r[both_nan(a, b)] = np.nan
+        return r
+
+    def rowmin(a, b):
+        big = max(a.max(), b.max()) + 1
+        r = np.minimum(np.where(a < 0, big, a), np.where(b < 0, big, b))
+        return np.where(r == big, -1, r)
+
+    with np.errstate(divide="ignore", invalid="ignore"):
+        mean = 3 * (np.nan_to_num(s0i) + np.nan_to_num(s1)) / (np.nan_to_num(c0) + np.nan_to_num(c1))
+    cases = [
+        ("any", ds.any(), nanmax(s0, s1), False),
+        ("count_no_intersect", ds.count(self_intersect=False), nansum(s0, s1), True),
+        ("count_intersect", ds.count(self_intersect=True), nansum(s0i, s1), False),
+        ("sum_no_intersect", ds.sum("value", self_intersect=False), 3 * nansum(s0, s1), True),
+        ("sum_intersect", ds.sum("value", self_intersect=True), 3 * nansum(s0i, s1), False),
+        ("max", ds.max("value"), 3 * nanmax(s0, s1), False),
+        ("min", ds.min("value"), 3 * nanmin(s0, s1), True),
+        ("first", ds.first("value"), 3 * np.where(np.isnan(s0), s1, s0), True),
+        ("last", ds.last("value"), 3 * np.where(np.isnan(s1), s0, s1), True),
+        ("count_ignore_aa", ds._count_ignore_antialiasing("value"), c0 + c1, False),
+        ("mean", ds.mean("value"), mean, False),
+        ("min_row_index", ds._min_row_index(),
+         rowmin(A["line_antialias_sol_min_index_0"], A["line_antialias_sol_min_index_1"]), True),
+        ("max_row_index", ds._max_row_index(),
+         np.maximum(A["line_antialias_sol_max_index_0"], A["line_antialias_sol_max_index_1"]), False),
+    ]
+    canvas = dict(plot_width=11, plot_height=11, x_range=(-0.1875, 1.1875), y_range=(-0.1875, 1.1875))
+    out = [dict(id=f"both_lines_{cid}", agg=agg, expected=exp, two_stage=two) for cid, agg, exp, two in cases]
+    return src, canvas, out
+
+
 def eq_hist_agg_a():
     """test_transfer_functions.py:23-37 build_agg 'a' (uint32, zero diagonal)."""
     a = np.arange(10, 19, dtype="u4").reshape((3, 3))

@@ -102,8 +102,6 @@ def test_random_multi_lines_vs_oracle(kind, line_width):
     layout, xs, ys = refcases.multi_line_arrays(cols, kw)
     xr, yr = (0.0, 1.0), (float(np.nanmin(ys)), float(np.nanmax(ys)))
     for name, red, spec, rtol in REDS:
-        if line_width and name in ("max", "first"):
-            continue          # two-stage antialiased plans stay off the multi-line GPU path
         cvs = ds.Canvas(plot_width=300, plot_height=200, x_range=xr, y_range=yr)
         got = to_numpy(cvs.line(frame, agg=red, line_width=line_width, **kw))
         ref = oracle.lines({"v": cols["v"]}, layout, xs, ys, 300, 200, xr, yr, [spec], line_width=line_width)[0]
@@ -111,6 +109,87 @@ def test_random_multi_lines_vs_oracle(kind, line_width):
             assert_same(got, ref, rtol=3e-7, atol=1e-7, what=f"{kind} {name}")
         else:
             assert_same(got, ref, rtol=rtol, what=f"{kind} {name}")
+
+
+BOTH_SRC, BOTH_CANVAS, BOTH_CASES = refcases.both_lines_cases()
+
+
+@pytest.mark.parametrize("case", BOTH_CASES, ids=[c["id"] for c in BOTH_CASES])
+def test_both_lines_golden(case):
+    """TestLineAntialias both_lines (test_pandas.py:2698-2785): two lines of
+    line_antialias_df as LineAxis0Multi at line_width 1, the two-stage plans
+    (count / sum with self_intersect=False, min, first, last, min row index)
+    folded line by line."""
+    frame = _frame(BOTH_SRC)
+    cvs = ds.Canvas(**BOTH_CANVAS)
+    got = to_numpy(cvs.line(frame, x=["x0", "x1"], y=["y0", "y1"], agg=case["agg"], line_width=1))
+    exp = case["expected"]
+    if got.dtype.kind == "f":
+        np.testing.assert_array_almost_equal(got, exp, decimal=5)      # the reference's close=True
+    else:
+        np.testing.assert_array_equal(got, exp)
+    from oracle_bridge import specs_of
+    _, specs, _ = specs_of(case["agg"], BOTH_SRC, {})
+    xs = np.stack([BOTH_SRC["x0"], BOTH_SRC["x1"]], axis=1)
+    ys = np.stack([BOTH_SRC["y0"], BOTH_SRC["y1"]], axis=1)
+    ref = oracle.lines({"value": BOTH_SRC["value"]}, 1, xs, ys, 11, 11, BOTH_CANVAS["x_range"],
+                       BOTH_CANVAS["y_range"], specs, line_width=1)[0]
+    if ref.dtype == np.float32:
+        assert_same(got, ref, rtol=3e-7, atol=1e-7)
+    else:
+        assert_same(got, ref, rtol=1e-12, atol=1e-15)
+
+
+TWO_STAGE = [("count", ds.count(self_intersect=False), oracle.spec("count", self_intersect=False)),
+             ("sum", ds.sum("v", self_intersect=False), oracle.spec("sum", "v", self_intersect=False)),
+             ("min", ds.min("v"), oracle.spec("min", "v")),
+             ("first", ds.first("v"), oracle.spec("first", "v")),
+             ("last", ds.last("v"), oracle.spec("last", "v")),
+             ("min_row", ds._min_row_index(), oracle.spec("min_row"))]
+
+
+@pytest.mark.parametrize("kind", ["axis0multi", "xconst", "axis1"])
+@pytest.mark.parametrize("name", [t[0] for t in TWO_STAGE])
+def test_two_stage_multi_lines_vs_oracle(kind, name):
+    """Two-stage antialiased plans over several lines, each line drawn alone and
+    folded in line order (line.py:1203-1226, 1300-1318 and siblings): float32 count
+    3e-7 relative, float64 sum in the reference's line order 1e-12, the rest exact."""
+    _, red, spec = next(t for t in TWO_STAGE if t[0] == name)
+    cols, kw = _random_case(kind, 400 if kind == "axis0multi" else 60, 5 if kind == "axis0multi" else 120, 19)
+    frame = _frame(cols)
+    layout, xs, ys = refcases.multi_line_arrays(cols, kw)
+    xr, yr = (0.0, 1.0), (float(np.nanmin(ys)), float(np.nanmax(ys)))
+    got = to_numpy(ds.Canvas(plot_width=160, plot_height=90, x_range=xr, y_range=yr).line(
+        frame, agg=red, line_width=1.5, **kw))
+    ref = oracle.lines({"v": cols["v"]}, layout, xs, ys, 160, 90, xr, yr, [spec], line_width=1.5)[0]
+    if ref.dtype == np.float32:
+        assert_same(got, ref, rtol=3e-7, atol=1e-7, what=f"{kind} {name}")
+    elif ref.dtype.kind == "f":
+        assert_same(got, ref, rtol=1e-12, what=f"{kind} {name}")
+    else:
+        assert_same(got, ref, what=f"{kind} {name}")
+
+
+def test_two_stage_summary_and_unserved_plans():
+    cols, kw = _random_case("axis0multi", 300, 4, 23)
+    frame = _frame(cols)
+    layout, xs, ys = refcases.multi_line_arrays(cols, kw)
+    xr, yr = (0.0, 1.0), (float(np.nanmin(ys)), float(np.nanmax(ys)))
+    cvs = ds.Canvas(plot_width=70, plot_height=50, x_range=xr, y_range=yr)
+    agg = ds.summary(c=ds.count(), mn=ds.min("v"), mx=ds.max("v"), f=ds.first("v"), a=ds.any())
+    got = cvs.line(frame, agg=agg, line_width=1.5, **kw)
+    specs = [oracle.spec("count"), oracle.spec("min", "v"), oracle.spec("max", "v"), oracle.spec("first", "v"),
+             oracle.spec("any")]
+    ref = oracle.lines({"v": cols["v"]}, layout, xs, ys, 70, 50, xr, yr, specs, line_width=1.5)
+    for k, r in zip(("c", "mn", "mx", "f", "a"), ref):
+        if r.dtype == np.float32:
+            assert_same(to_numpy(got[k]), r, rtol=3e-7, atol=1e-7, what=k)
+        else:
+            assert_same(to_numpy(got[k]), r, what=k)
+    with pytest.raises(NotImplementedError):
+        cvs.line(frame, agg=ds.summary(m=ds.mean("v"), f=ds.first("v")), line_width=1.5, **kw)
+    with pytest.raises(NotImplementedError):
+        cvs.line(frame, agg=ds.where(ds.min("v")), line_width=1.5, **kw)
 
 
 @pytest.mark.parametrize("nv", [2, 6])

@@ -209,3 +209,21 @@ def test_oracle_axis1_x_constant_and_sum_golden():
                        [oracle.spec("sum", "v")])[0]
     sol = refcases.golden_array(refcases.lines_golden("test_line_agg_sum_axis1_none_constant")[0])
     np.testing.assert_array_equal(got, sol)
+
+
+BOTH_SRC, BOTH_CANVAS, BOTH_CASES = refcases.both_lines_cases()
+
+
+@pytest.mark.parametrize("case", BOTH_CASES, ids=[c["id"] for c in BOTH_CASES])
+def test_oracle_both_lines_golden(case):
+    """Two lines as LineAxis0Multi at line_width 1, including the two-stage plans
+    (count / sum with self_intersect=False, min, first, last, min row index)."""
+    from oracle_bridge import specs_of
+    _, specs, _ = specs_of(case["agg"], BOTH_SRC, {})
+    xs = np.stack([BOTH_SRC["x0"], BOTH_SRC["x1"]], axis=1)
+    ys = np.stack([BOTH_SRC["y0"], BOTH_SRC["y1"]], axis=1)
+    cv = BOTH_CANVAS
+    got = oracle.lines({"value": BOTH_SRC["value"]}, 1, xs, ys, cv["plot_width"], cv["plot_height"],
+                       cv["x_range"], cv["y_range"], specs, line_width=1)[0]
+    assert oracle.aa_flags(specs)[2] == case["two_stage"]
+    _check(got, case["expected"], got.dtype.kind == "f")
