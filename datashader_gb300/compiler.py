@@ -132,10 +132,11 @@ def _stage2_fold(red):
     """The stage-2 fold that a two-stage plan over several lines applies to the
     single base of ``red`` (compiler.py:153-196 with the combinations of
     reductions.py: count and sum SUM_2AGG, any and max MAX, min MIN, first
-    FIRST, last LAST, the row indexes MIN / MAX over -1); 0 where it has none
-    here (mean, _sum_zero, _count_ignore_antialiasing, where)."""
-    if isinstance(red, rd._count_ignore_antialiasing):
-        return 0
+    FIRST, last LAST, the row indexes MIN / MAX over -1; mean, _sum_zero and
+    _count_ignore_antialiasing append additively in either mode and fold by
+    SUM_2AGG over zeros, a plain sum); 0 where it has none here (where)."""
+    if isinstance(red, (rd._count_ignore_antialiasing, rd._sum_zero, rd.mean)):
+        return N.FOLD_ADD
     if isinstance(red, rd.count):
         return N.FOLD_SUM_F32          # float32 aggregate (reductions.py:542-543)
     if isinstance(red, rd.any):

@@ -413,10 +413,9 @@ class Canvas:
             from .compiler import compile_plan as _cp
             plan = _cp(agg, as_frame(source), antialias=True)
             if plan.use_2_stage and (isinstance(glyph, LinesAxis1Ragged) or any(b.fold == 0 for b in plan.bases)):
-                # folded line by line for count / sum / any / max / min / first / last and the row
-                # indexes; mean, where and _count_ignore_antialiasing have no stage-2 fold here
+                # folded line by line for every reduction but where
                 raise NotImplementedError("this two-stage antialiased plan over several lines is not on the GPU "
-                                          "path (ragged lines, mean, where or _count_ignore_antialiasing)")
+                                          "path (ragged lines or where)")
         return bypixel(source, self, glyph, agg, antialias=glyph.antialiased)
 
     def validate_ranges(self, x_range, y_range):

@@ -780,6 +780,7 @@ __global__ void stage2_fold_kernel(int fold, long long *acc, const long long *pa
 }
 
 static bool fold_fits(int op, int fold) {
+    if (op == DSGB_BASE_AA_SUM || op == DSGB_BASE_AA_CNT0) return fold == DSGB_FOLD_ADD;
     if (op == DSGB_BASE_AA_MAX)
         return fold == DSGB_FOLD_MAX || fold == DSGB_FOLD_MIN || fold == DSGB_FOLD_FIRST || fold == DSGB_FOLD_LAST ||
                fold == DSGB_FOLD_SUM || fold == DSGB_FOLD_SUM_F32;
@@ -817,21 +818,29 @@ extern "C" int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t
     LineParams p;
     int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
     if (rc) return rc;
-    dsgb_base line_bases[MAX_BASES];
+    dsgb_base line_bases[MAX_BASES];      // the per-line aggregates to re-initialise for every line
+    int32_t nline_bases = 0;
     for (int32_t b = 0; b < nbases; ++b) {
-        if (!fold_fits(bases[b].op, folds[b]) || !line_aggs[b]) {
+        if (!fold_fits(bases[b].op, folds[b]) || (folds[b] != DSGB_FOLD_ADD && !line_aggs[b])) {
             set_error("dsgb_lines_2stage: base %d (op %d) has no stage-2 fold %d", b, bases[b].op, folds[b]);
             return DSGB_E_UNSUPPORTED;
         }
-        line_bases[b] = bases[b];
-        line_bases[b].agg = line_aggs[b];
+        if (folds[b] == DSGB_FOLD_ADD) continue;
+        line_bases[nline_bases] = bases[b];
+        line_bases[nline_bases].agg = line_aggs[b];
+        ++nline_bases;
     }
     p.line_width = line_width;
     p.plot_start = 1;
     p.overwrite = overwrite;
     p.use_2_stage = 1;                     // the previous vertex is not read (line.py:1170, 1266)
-    LineParams pl = p;                     // the same plan drawing into the per-line aggregates
-    for (int32_t b = 0; b < nbases; ++b) pl.bases[b].agg = line_aggs[b];
+    // the same plan drawing into the per-line aggregates; additive bases (the
+    // zero-initialised sums and counts of mean, _sum_zero and
+    // _count_ignore_antialiasing, whose stage-2 nansum is a plain sum) keep
+    // drawing into their accumulators
+    LineParams pl = p;
+    for (int32_t b = 0; b < nbases; ++b)
+        if (folds[b] != DSGB_FOLD_ADD) pl.bases[b].agg = line_aggs[b];
     LinesGeom g;
     g.xs = xs; g.ys = ys; g.nrows = nrows; g.nv = nv;
     g.xrow = layout == 1 ? nv : x_row_stride;
@@ -851,14 +860,15 @@ extern "C" int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t
         // compiler.py:218-222); every later line into freshly initialised
         // per-line aggregates, folded in line order
         g.only_line = L;
-        if (L > 0) {
-            rc = bases_init(line_bases, nbases, ncells, st);
+        if (L > 0 && nline_bases > 0) {
+            rc = bases_init(line_bases, nline_bases, ncells, st);
             if (rc) return rc;
         }
         if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(L > 0 ? pl : p, g);
         else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(L > 0 ? pl : p, g);
         DSGB_CHECK_LAUNCH("two-stage lines kernel");
         for (int32_t b = 0; b < nbases && L > 0; ++b) {
+            if (folds[b] == DSGB_FOLD_ADD) continue;
             const int64_t n = ncells * (bases[b].ncat < 1 ? 1 : bases[b].ncat);
             const unsigned fb = (unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
             if (fb == 0) continue;

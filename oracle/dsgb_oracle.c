@@ -717,12 +717,14 @@ static void draw_one_line(int32_t layout, int64_t L, int64_t nrows, int64_t nv, 
 
 static size_t stage2_elem(int kind) {
     switch (kind) {
-    case ORK_COUNT: case ORK_ANY: return 4;                 /* float32 when antialiased */
+    case ORK_COUNT: case ORK_ANY: case ORK_COUNT_IGNORE_AA: return 4;   /* float32 / uint32 */
     case ORK_SUM: case ORK_MIN: case ORK_MAX: case ORK_FIRST: case ORK_LAST:
-    case ORK_MIN_ROW: case ORK_MAX_ROW: return 8;
+    case ORK_MIN_ROW: case ORK_MAX_ROW: case ORK_SUM_ZERO: case ORK_MEAN: return 8;
     default: return 0;                                      /* no stage-2 fold restated here */
     }
 }
+/* MEAN's second aggregate: the uint32 counts of _count_ignore_antialiasing */
+static size_t stage2_elem2(int kind) { return kind == ORK_MEAN ? 4 : 0; }
 
 /* ret <- combine(ret, other): nansum_in_place (utils.py:885-897, float32 for the
  * float32 count), nanmax_in_place / nanmin_in_place (:639-668),
@@ -732,6 +734,21 @@ static size_t stage2_elem(int kind) {
  * MIN / MAX over -1 (reductions.py:545-549, 1040-1045, 837, 1173, 1218, 1396,
  * 1434, 2257, 2311). */
 static void stage2_fold(int kind, void *ret, const void *other, int64_t n) {
+    if (kind == ORK_COUNT_IGNORE_AA) {
+        /* SUM_2AGG over zero-initialised uint32 counts (reductions.py:673-677) */
+        uint32_t *r = (uint32_t *)ret;
+        const uint32_t *o = (const uint32_t *)other;
+        for (int64_t k = 0; k < n; ++k) r[k] += o[k];
+        return;
+    }
+    if (kind == ORK_SUM_ZERO || kind == ORK_MEAN) {
+        /* SUM_2AGG over zero-initialised float64 sums (reductions.py:944-948); no NaN
+         * reaches them, so nansum_in_place is the plain sum */
+        double *r = (double *)ret;
+        const double *o = (const double *)other;
+        for (int64_t k = 0; k < n; ++k) r[k] = r[k] + o[k];
+        return;
+    }
     if (kind == ORK_COUNT || kind == ORK_ANY) {
         float *r = (float *)ret;
         const float *o = (const float *)other;
@@ -779,9 +796,9 @@ int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double 
     const int64_t nlines = layout == 1 ? nv : nrows;
     for (int r = 0; r < nreds; ++r)
         if (stage2_elem(reds[r].kind) == 0) return -2;
-    void *acc[64];
+    void *acc[64], *acc2[64];
     if (nreds > 64) return -2;
-    for (int r = 0; r < nreds; ++r) acc[r] = NULL;
+    for (int r = 0; r < nreds; ++r) { acc[r] = NULL; acc2[r] = NULL; }
     for (int64_t L = 0; L < nlines; ++L) {
         if (L > 0) oracle_init(reds, nreds, ncells, 1);
         draw_one_line(layout, L, nrows, nv, xs, ys, xrow, yrow, cols, row_offset, width, sx, tx, sy, ty,
@@ -790,11 +807,14 @@ int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double 
         for (int r = 0; r < nreds; ++r) {
             const int64_t n = red_cells(ncells, &reds[r]);
             const size_t bytes = (size_t)n * stage2_elem(reds[r].kind);
+            const size_t bytes2 = (size_t)n * stage2_elem2(reds[r].kind);
             if (L == 0) {
                 acc[r] = malloc(bytes ? bytes : 1);
                 memcpy(acc[r], reds[r].agg, bytes);
+                if (bytes2) { acc2[r] = malloc(bytes2); memcpy(acc2[r], reds[r].agg2, bytes2); }
             } else {
                 stage2_fold(reds[r].kind, acc[r], reds[r].agg, n);
+                if (bytes2) stage2_fold(ORK_COUNT_IGNORE_AA, acc2[r], reds[r].agg2, n);
             }
         }
     }
@@ -802,6 +822,7 @@ int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double 
         const int64_t n = red_cells(ncells, &reds[r]);
         memcpy(reds[r].agg, acc[r], (size_t)n * stage2_elem(reds[r].kind));
         free(acc[r]);
+        if (acc2[r]) { memcpy(reds[r].agg2, acc2[r], (size_t)n * stage2_elem2(reds[r].kind)); free(acc2[r]); }
     }
     return 0;
 }

@@ -186,8 +186,15 @@ def test_two_stage_summary_and_unserved_plans():
             assert_same(to_numpy(got[k]), r, rtol=3e-7, atol=1e-7, what=k)
         else:
             assert_same(to_numpy(got[k]), r, what=k)
-    with pytest.raises(NotImplementedError):
-        cvs.line(frame, agg=ds.summary(m=ds.mean("v"), f=ds.first("v")), line_width=1.5, **kw)
+    # mean and _count_ignore_antialiasing inside a two-stage plan: additive within and across lines
+    agg = ds.summary(m=ds.mean("v"), f=ds.first("v"), k=ds._count_ignore_antialiasing("v"))
+    got = cvs.line(frame, agg=agg, line_width=1.5, **kw)
+    ref = oracle.lines({"v": cols["v"]}, layout, xs, ys, 70, 50, xr, yr,
+                       [oracle.spec("mean", "v"), oracle.spec("first", "v"), oracle.spec("count_ignore_aa", "v")],
+                       line_width=1.5)
+    assert_same(to_numpy(got["m"]), ref[0], rtol=1e-12, atol=1e-15, what="mean")
+    assert_same(to_numpy(got["f"]), ref[1], what="first")
+    assert_same(to_numpy(got["k"]), ref[2], what="count_ignore_aa")
     with pytest.raises(NotImplementedError):
         cvs.line(frame, agg=ds.where(ds.min("v")), line_width=1.5, **kw)
 
