@@ -130,6 +130,7 @@ BASEF_UNWEIGHTED = 0x1
 # finalize ops (dsgb_fin_op)
 FIN_SUM_NAN, FIN_MEAN, FIN_KEY_F64, FIN_ROW, FIN_GATHER, FIN_KEY_F32, FIN_SUM_F32, FIN_COPY = range(1, 9)
 FOLD_SUM, FOLD_SUM_F32, FOLD_MAX, FOLD_MIN, FOLD_FIRST, FOLD_LAST, FOLD_ROW_MIN, FOLD_ADD = range(1, 9)
+FOLD_WHERE_MAX, FOLD_WHERE_MIN, FOLD_WHERE_FIRST, FOLD_WHERE_LAST = range(9, 13)
 
 FLAG_NO_INIT, FLAG_NO_FINALIZE, FLAG_EXACT_BIN, FLAG_WARP_AGG, FLAG_DETERMINISTIC = 0x1, 0x2, 0x4, 0x8, 0x10
 

@@ -134,9 +134,21 @@ def _stage2_fold(red):
     reductions.py: count and sum SUM_2AGG, any and max MAX, min MIN, first
     FIRST, last LAST, the row indexes MIN / MAX over -1; mean, _sum_zero and
     _count_ignore_antialiasing append additively in either mode and fold by
-    SUM_2AGG over zeros, a plain sum); 0 where it has none here (where)."""
+    SUM_2AGG over zeros, a plain sum; where folds its {selector, row} pair by
+    the selector's own append, reductions.py:1992-2018)."""
     if isinstance(red, (rd._count_ignore_antialiasing, rd._sum_zero, rd.mean)):
         return N.FOLD_ADD
+    if isinstance(red, rd.where):
+        sel = red.selector
+        if isinstance(sel, rd._min_row_index):
+            return N.FOLD_ROW_MIN
+        if isinstance(sel, rd._max_row_index):
+            return N.FOLD_MAX
+        for cls, fold in ((rd.max, N.FOLD_WHERE_MAX), (rd.min, N.FOLD_WHERE_MIN), (rd.first, N.FOLD_WHERE_FIRST),
+                          (rd.last, N.FOLD_WHERE_LAST)):
+            if isinstance(sel, cls):
+                return fold
+        return 0
     if isinstance(red, rd.count):
         return N.FOLD_SUM_F32          # float32 aggregate (reductions.py:542-543)
     if isinstance(red, rd.any):

@@ -413,9 +413,8 @@ class Canvas:
             from .compiler import compile_plan as _cp
             plan = _cp(agg, as_frame(source), antialias=True)
             if plan.use_2_stage and (isinstance(glyph, LinesAxis1Ragged) or any(b.fold == 0 for b in plan.bases)):
-                # folded line by line for every reduction but where
-                raise NotImplementedError("this two-stage antialiased plan over several lines is not on the GPU "
-                                          "path (ragged lines or where)")
+                # every reduction folds line by line; ragged lines are not drawn one at a time here
+                raise NotImplementedError("two-stage antialiased plans over ragged lines are not on the GPU path")
         return bypixel(source, self, glyph, agg, antialias=glyph.antialiased)
 
     def validate_ranges(self, x_range, y_range):

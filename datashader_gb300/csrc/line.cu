@@ -779,7 +779,32 @@ __global__ void stage2_fold_kernel(int fold, long long *acc, const long long *pa
     }
 }
 
+// where's stage-2 combine (reductions.py:1992-2018) on the {key, row} pairs
+// of AA_ARGMAX (empty key KEY_EMPTY_MAX): the other line's selector key, when
+// present, replaces the accumulated pair where the selector's own
+// non-antialiased append would update (max / min strict, first only into an
+// empty cell, last always), carrying that line's row.
+__global__ void stage2_fold_pairs_kernel(int fold, long long *acc, const long long *part, int64_t n) {
+    for (int64_t c = gtid(); c < n; c += gstride()) {
+        const long long ok = part[2 * c];
+        if (ok == KEY_EMPTY_MAX) continue;
+        const long long ak = acc[2 * c];
+        bool take = false;
+        switch (fold) {
+        case DSGB_FOLD_WHERE_MAX: take = ok > ak; break;
+        case DSGB_FOLD_WHERE_MIN: take = ak == KEY_EMPTY_MAX || ok < ak; break;
+        case DSGB_FOLD_WHERE_FIRST: take = ak == KEY_EMPTY_MAX; break;
+        case DSGB_FOLD_WHERE_LAST: take = true; break;
+        default: break;
+        }
+        if (take) { acc[2 * c] = ok; acc[2 * c + 1] = part[2 * c + 1]; }
+    }
+}
+
 static bool fold_fits(int op, int fold) {
+    if (op == DSGB_BASE_AA_ARGMAX)
+        return fold == DSGB_FOLD_WHERE_MAX || fold == DSGB_FOLD_WHERE_MIN || fold == DSGB_FOLD_WHERE_FIRST ||
+               fold == DSGB_FOLD_WHERE_LAST;
     if (op == DSGB_BASE_AA_SUM || op == DSGB_BASE_AA_CNT0) return fold == DSGB_FOLD_ADD;
     if (op == DSGB_BASE_AA_MAX)
         return fold == DSGB_FOLD_MAX || fold == DSGB_FOLD_MIN || fold == DSGB_FOLD_FIRST || fold == DSGB_FOLD_LAST ||
@@ -872,8 +897,12 @@ extern "C" int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t
             const int64_t n = ncells * (bases[b].ncat < 1 ? 1 : bases[b].ncat);
             const unsigned fb = (unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
             if (fb == 0) continue;
-            stage2_fold_kernel<<<fb, 256, 0, st>>>(folds[b], (long long *)bases[b].agg,
-                                                  (const long long *)line_aggs[b], n);
+            if (bases[b].op == DSGB_BASE_AA_ARGMAX)
+                stage2_fold_pairs_kernel<<<fb, 256, 0, st>>>(folds[b], (long long *)bases[b].agg,
+                                                            (const long long *)line_aggs[b], n);
+            else
+                stage2_fold_kernel<<<fb, 256, 0, st>>>(folds[b], (long long *)bases[b].agg,
+                                                      (const long long *)line_aggs[b], n);
             DSGB_CHECK_LAUNCH("stage-2 fold");
         }
     }

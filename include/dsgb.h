@@ -280,7 +280,8 @@ int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t ro
  * plans draw every segment as if it started a line, line.py:1170, 1266).
  * Supported bases and folds: DSGB_BASE_AA_MAX with any value fold,
  * DSGB_BASE_MIN_ROW with DSGB_FOLD_ROW_MIN, DSGB_BASE_MAX_ROW with
- * DSGB_FOLD_MAX, DSGB_BASE_AA_SUM / DSGB_BASE_AA_CNT0 with DSGB_FOLD_ADD.  Cost: one launch per line plus one initialisation and one
+ * DSGB_FOLD_MAX, DSGB_BASE_AA_SUM / DSGB_BASE_AA_CNT0 with DSGB_FOLD_ADD,
+ * DSGB_BASE_AA_ARGMAX with DSGB_FOLD_WHERE_*.  Cost: one launch per line plus one initialisation and one
  * fold of each base over the canvas per line after the first. */
 enum {
     DSGB_FOLD_SUM      = 1,  /* nansum_in_place, float64 (count / sum, self_intersect=False) */
@@ -290,9 +291,13 @@ enum {
     DSGB_FOLD_FIRST    = 5,  /* nanfirst_in_place (first)                                   */
     DSGB_FOLD_LAST     = 6,  /* nanlast_in_place (last)                                     */
     DSGB_FOLD_ROW_MIN  = 7,  /* row_min_in_place (MIN_ROW)                                  */
-    DSGB_FOLD_ADD      = 8   /* nansum_in_place of zero-initialised additive bases (AA_SUM,
+    DSGB_FOLD_ADD      = 8,  /* nansum_in_place of zero-initialised additive bases (AA_SUM,
                                 AA_CNT0 of mean / _sum_zero / _count_ignore_antialiasing): every
                                 line draws straight into the accumulator; line_aggs[b] unused */
+    DSGB_FOLD_WHERE_MAX   = 9,   /* where(max | min | first | last) on AA_ARGMAX pairs: the   */
+    DSGB_FOLD_WHERE_MIN   = 10,  /* selector's own append decides, the row follows           */
+    DSGB_FOLD_WHERE_FIRST = 11,  /* (reductions.py:1992-2018)                                 */
+    DSGB_FOLD_WHERE_LAST  = 12
 };
 int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
                       int32_t layout, const double *xs, const double *ys, int64_t nv,

@@ -719,12 +719,37 @@ static size_t stage2_elem(int kind) {
     switch (kind) {
     case ORK_COUNT: case ORK_ANY: case ORK_COUNT_IGNORE_AA: return 4;   /* float32 / uint32 */
     case ORK_SUM: case ORK_MIN: case ORK_MAX: case ORK_FIRST: case ORK_LAST:
-    case ORK_MIN_ROW: case ORK_MAX_ROW: case ORK_SUM_ZERO: case ORK_MEAN: return 8;
+    case ORK_MIN_ROW: case ORK_MAX_ROW: case ORK_SUM_ZERO: case ORK_MEAN: case ORK_WHERE: return 8;
     default: return 0;                                      /* no stage-2 fold restated here */
     }
 }
-/* MEAN's second aggregate: the uint32 counts of _count_ignore_antialiasing */
-static size_t stage2_elem2(int kind) { return kind == ORK_MEAN ? 4 : 0; }
+/* The second aggregate: MEAN's uint32 counts, WHERE's selector (float64 or int64) */
+static size_t stage2_elem2(int kind) { return kind == ORK_MEAN ? 4 : kind == ORK_WHERE ? 8 : 0; }
+
+/* where's stage-2 combine (reductions.py:1992-2018, combine_cpu_2d): the other
+ * line's selector value, when valid, is offered to the accumulated selector
+ * through the selector's own (non-antialiased) append, and where that append
+ * updates, the other line's where value is taken. */
+static void stage2_fold_where(const oracle_red *rd, void *ret, void *ret_sel, const void *other,
+                              const void *other_sel, int64_t n) {
+    const int k = rd->sel_kind;
+    const int row_sel = sel_is_row(k);
+    for (int64_t c = 0; c < n; ++c) {
+        int take = 0;
+        if (row_sel) {
+            int64_t *a = (int64_t *)ret_sel;
+            const int64_t v = ((const int64_t *)other_sel)[c];
+            if (v == -1) continue;
+            take = app_selector(k, a, c, 0.0, v) >= 0;
+        } else {
+            double *a = (double *)ret_sel;
+            const double v = ((const double *)other_sel)[c];
+            if (isnull_d(v)) continue;
+            take = app_selector(k, a, c, v, 0) >= 0;
+        }
+        if (take) ((int64_t *)ret)[c] = ((const int64_t *)other)[c];   /* 8-byte where value, row or float64 */
+    }
+}
 
 /* ret <- combine(ret, other): nansum_in_place (utils.py:885-897, float32 for the
  * float32 count), nanmax_in_place / nanmin_in_place (:639-668),
@@ -812,6 +837,8 @@ int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double 
                 acc[r] = malloc(bytes ? bytes : 1);
                 memcpy(acc[r], reds[r].agg, bytes);
                 if (bytes2) { acc2[r] = malloc(bytes2); memcpy(acc2[r], reds[r].agg2, bytes2); }
+            } else if (reds[r].kind == ORK_WHERE) {
+                stage2_fold_where(&reds[r], acc[r], acc2[r], reds[r].agg, reds[r].agg2, n);
             } else {
                 stage2_fold(reds[r].kind, acc[r], reds[r].agg, n);
                 if (bytes2) stage2_fold(ORK_COUNT_IGNORE_AA, acc2[r], reds[r].agg2, n);

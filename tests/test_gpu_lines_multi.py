@@ -195,8 +195,22 @@ def test_two_stage_summary_and_unserved_plans():
     assert_same(to_numpy(got["m"]), ref[0], rtol=1e-12, atol=1e-15, what="mean")
     assert_same(to_numpy(got["f"]), ref[1], what="first")
     assert_same(to_numpy(got["k"]), ref[2], what="count_ignore_aa")
+    # where(min | first | last) are two-stage; where(max) folds inside a two-stage summary
+    w = np.arange(300.0) * 0.5
+    frame_w = _frame(dict(cols, w=w))
+    for sel, cls in (("min", ds.min), ("first", ds.first), ("last", ds.last), ("max", ds.max)):
+        agg = ds.summary(r=ds.where(cls("v")), l=ds.where(cls("v"), "w"), f=ds.first("v"))
+        got = cvs.line(frame_w, agg=agg, line_width=1.5, **kw)
+        ref = oracle.lines({"v": cols["v"], "w": w}, layout, xs, ys, 70, 50, xr, yr,
+                           [oracle.spec("where", selector=oracle.spec(sel, "v")),
+                            oracle.spec("where", selector=oracle.spec(sel, "v"), lookup="w"),
+                            oracle.spec("first", "v")], line_width=1.5)
+        assert_same(to_numpy(got["r"]), ref[0], what=f"where({sel}) row")
+        assert_same(to_numpy(got["l"]), ref[1], what=f"where({sel}, w)")
+    ragged = ds.TensorFrame({"x": ds.RaggedColumn([[0.1, 0.5, 0.9]]), "y": ds.RaggedColumn([[0.2, 0.6, 0.3]]),
+                             "v": torch.ones(1, dtype=torch.float64, device="cuda")})
     with pytest.raises(NotImplementedError):
-        cvs.line(frame, agg=ds.where(ds.min("v")), line_width=1.5, **kw)
+        cvs.line(ragged, x="x", y="y", axis=1, agg=ds.first("v"), line_width=1.5)
 
 
 @pytest.mark.parametrize("nv", [2, 6])
