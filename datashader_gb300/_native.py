@@ -139,7 +139,7 @@ EXPORTED = (
     "dsgb_abi_version", "dsgb_last_error", "dsgb_device_sm_count", "dsgb_bases_init", "dsgb_combine",
     "dsgb_finalize", "dsgb_finalize_partitioned", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_workspace_size_flags",
     "dsgb_points_ws", "dsgb_points_segments",
-    "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_workspace_size", "dsgb_line_axis0_ws", "dsgb_lines", "dsgb_lines_2stage", "dsgb_lines_ragged", "dsgb_line_axis0_backward", "dsgb_line_axis0_backward_ws",
+    "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_workspace_size", "dsgb_line_axis0_ws", "dsgb_lines", "dsgb_lines_2stage", "dsgb_lines_ragged", "dsgb_lines_ragged_2stage", "dsgb_line_axis0_backward", "dsgb_line_axis0_backward_ws",
     "dsgb_points_backward", "dsgb_bounds", "dsgb_eq_hist_workspace_size", "dsgb_eq_hist_u32",
     "dsgb_eq_hist_f64", "dsgb_eq_hist_u32_static", "dsgb_shade_workspace_size", "dsgb_shade_u32", "dsgb_shade_f64", "dsgb_composite", "dsgb_pyramid_tile_offset", "dsgb_pyramid_workspace_size", "dsgb_pyramid", "dsgb_pyramid_status",
 )
@@ -188,6 +188,9 @@ def _declare(L):
                                     i32, PB, i32, ctypes.POINTER(i32), ctypes.POINTER(P), PO, i32, u32, P]
     L.dsgb_lines_ragged.argtypes = [PC, i32, i64, i64, P, i64, P, P, i64, P, ctypes.POINTER(CanvasDesc), dbl, i32,
                                     PB, i32, PO, i32, u32, P]
+    L.dsgb_lines_ragged_2stage.argtypes = [PC, i32, i64, i64, P, i64, P, P, i64, P, ctypes.POINTER(CanvasDesc),
+                                           dbl, i32, PB, i32, ctypes.POINTER(i32), ctypes.POINTER(P), PO, i32,
+                                           u32, P]
     L.dsgb_line_axis0_backward.argtypes = [PC, i32, i64, i32, i32, i32, ctypes.POINTER(CanvasDesc), dbl, i32,
                                            P, P, P, P, P]
     L.dsgb_line_axis0_backward_ws.argtypes = [PC, i32, i64, i32, i32, i32, ctypes.POINTER(CanvasDesc), dbl, i32,

@@ -128,10 +128,14 @@ def aa_stage_flags(agg):
     return si, overwrite, use_2
 
 
-def _stage2_fold(red):
+def _stage2_fold(red, si=False):
     """The stage-2 fold that a two-stage plan over several lines applies to the
-    single base of ``red`` (compiler.py:153-196 with the combinations of
-    reductions.py: count and sum SUM_2AGG, any and max MAX, min MIN, first
+    bases of ``red`` (compiler.py:153-196 with the combinations of
+    reductions.py: count and sum SUM_2AGG, or SUM_1AGG when the plan keeps
+    self_intersect (a two-stage plan whose only two-stage reductions are where,
+    which does not ask for self_intersect=False, reductions.py:1842-1915): both
+    combinations fold by nansum, so the additive self-intersecting bases (sum
+    and count of the row mask) add up; any and max MAX, min MIN, first
     FIRST, last LAST, the row indexes MIN / MAX over -1; mean, _sum_zero and
     _count_ignore_antialiasing append additively in either mode and fold by
     SUM_2AGG over zeros, a plain sum; where folds its {selector, row} pair by
@@ -150,11 +154,11 @@ def _stage2_fold(red):
                 return fold
         return 0
     if isinstance(red, rd.count):
-        return N.FOLD_SUM_F32          # float32 aggregate (reductions.py:542-543)
+        return N.FOLD_ADD if si else N.FOLD_SUM_F32   # float32 aggregate (reductions.py:542-543)
     if isinstance(red, rd.any):
         return N.FOLD_MAX
     if isinstance(red, rd.sum) and not isinstance(red, rd._sum_zero):
-        return N.FOLD_SUM
+        return N.FOLD_ADD if si else N.FOLD_SUM
     if isinstance(red, rd.max):
         return N.FOLD_MAX
     if isinstance(red, rd.min):
@@ -171,10 +175,11 @@ def _stage2_fold(red):
 
 
 class _Builder:
-    def __init__(self, schema, antialias, si):
+    def __init__(self, schema, antialias, si, use_2=False):
         self.schema = schema
         self.antialias = antialias
         self.si = si
+        self.use_2 = use_2
         self.bases = []
         self.index = {}
         self.columns = []
@@ -214,7 +219,7 @@ class _Builder:
             name, n, cats, dim = self.categorizer(red)
             return self.reduction(red.reduction, name, n, cats, dim)
         kw = dict(categories=categories, cat_dim=cat_dim)
-        fold = _stage2_fold(red) if (self.antialias and not self.si) else 0
+        fold = _stage2_fold(red, self.si) if (self.antialias and self.use_2) else 0
         B = lambda op, col, flags=0: self.base(op, col, cat, ncat, flags, fold)  # noqa: E731
         c = red.column if not isinstance(red, rd._max_or_min_row_index) else None
         aa = self.antialias
@@ -297,7 +302,7 @@ def compile_plan(agg, schema, *, antialias=False):
         si, overwrite, use_2 = aa_stage_flags(agg)
     else:
         si, overwrite, use_2 = True, False, False
-    b = _Builder(schema, antialias, si)
+    b = _Builder(schema, antialias, si, use_2)
     if isinstance(agg, rd.summary):
         outs = [(k, b.reduction(v)) for k, v in zip(agg.keys, agg.values)]
     else:

@@ -412,9 +412,8 @@ class Canvas:
         if glyph.antialiased and isinstance(glyph, _MultiLine):
             from .compiler import compile_plan as _cp
             plan = _cp(agg, as_frame(source), antialias=True)
-            if plan.use_2_stage and (isinstance(glyph, LinesAxis1Ragged) or any(b.fold == 0 for b in plan.bases)):
-                # every reduction folds line by line; ragged lines are not drawn one at a time here
-                raise NotImplementedError("two-stage antialiased plans over ragged lines are not on the GPU path")
+            if plan.use_2_stage and any(b.fold == 0 for b in plan.bases):
+                raise NotImplementedError("a reduction of this two-stage antialiased plan has no stage-2 fold")
         return bypixel(source, self, glyph, agg, antialias=glyph.antialiased)
 
     def validate_ranges(self, x_range, y_range):
@@ -642,11 +641,24 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
         if ncols == 0:                       # count() / any(): no field column, any valid pointer
             cols = (N.Column * 1)(N.Column(xr.starts.data_ptr(), N.I64, 0))   # one entry a row
             ncols = 1
-        rc = L.dsgb_lines_ragged(cols, ncols, len(frame), frame.row_offset, xr.flat.data_ptr(), xr.flat.numel(),
-                                 xr.starts.data_ptr(), yr.flat.data_ptr(), yr.flat.numel(), yr.starts.data_ptr(),
-                                 ctypes.byref(cv), float(glyph.line_width), int(plan.overwrite),
-                                 ex.bases, len(plan.bases), ex.outs, ex.nouts, flags, stream)
-        N.check(rc, "dsgb_lines_ragged")
+        if antialias and plan.use_2_stage:
+            # one row at a time, folded row by row (line.py:1616-1693)
+            line_aggs = [torch.empty_like(t) for t in ex.base_tensors]
+            folds = (ctypes.c_int32 * max(1, len(plan.bases)))(*[b.fold for b in plan.bases])
+            ptrs = (ctypes.c_void_p * max(1, len(plan.bases)))(*[t.data_ptr() for t in line_aggs])
+            rc = L.dsgb_lines_ragged_2stage(cols, ncols, len(frame), frame.row_offset, xr.flat.data_ptr(),
+                                            xr.flat.numel(), xr.starts.data_ptr(), yr.flat.data_ptr(),
+                                            yr.flat.numel(), yr.starts.data_ptr(), ctypes.byref(cv),
+                                            float(glyph.line_width), int(plan.overwrite), ex.bases,
+                                            len(plan.bases), folds, ptrs, ex.outs, ex.nouts, flags, stream)
+            N.check(rc, "dsgb_lines_ragged_2stage")
+        else:
+            rc = L.dsgb_lines_ragged(cols, ncols, len(frame), frame.row_offset, xr.flat.data_ptr(),
+                                     xr.flat.numel(), xr.starts.data_ptr(), yr.flat.data_ptr(), yr.flat.numel(),
+                                     yr.starts.data_ptr(), ctypes.byref(cv), float(glyph.line_width),
+                                     int(plan.overwrite), ex.bases, len(plan.bases), ex.outs, ex.nouts, flags,
+                                     stream)
+            N.check(rc, "dsgb_lines_ragged")
     elif isinstance(glyph, _MultiLine):
         if glyph.layout == 1:
             nv, xrow, yrow = xs.shape[1], xs.shape[1], ys.shape[1]

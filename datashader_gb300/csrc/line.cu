@@ -539,6 +539,24 @@ __global__ void __launch_bounds__(256, 1) lines_ragged_kernel(const LineParams p
     }
 }
 
+// One ragged row alone (two-stage plans, line.py:1616-1693): the row's slice
+// bounds are read on the device, its segments split over a small grid; the
+// previous vertex is never read.
+__global__ void __launch_bounds__(256, 1) lines_ragged_row_kernel(const LineParams p, const RaggedGeom g, int64_t i) {
+    const bool last = i == g.nrows - 1;
+    const int64_t xa = min(max(g.xs[i], (int64_t)0), g.nx);
+    const int64_t xb = max(min(last ? g.nx : g.xs[i + 1], g.nx), xa);
+    const int64_t ya = min(max(g.ys[i], (int64_t)0), g.ny);
+    const int64_t yb = max(min(last ? g.ny : g.ys[i + 1], g.ny), ya);
+    const int64_t len = min(xb - xa, yb - ya);
+    const double *X = g.xf + xa, *Y = g.yf + ya;
+    for (int64_t j = gtid(); j + 1 < len; j += gstride()) {
+        const bool segment_start = (j == 0) || isnull(X[j - 1]) || isnull(Y[j - 1]);
+        const bool segment_end = (j == len - 2) || isnull(X[j + 2]) || isnull(Y[j + 2]);
+        draw_segment(p, i, X[j], Y[j], X[j + 1], Y[j + 1], segment_start, segment_end, 0.0, 0.0);
+    }
+}
+
 // Visit keys (j * nrows + r, plus the row offset) held by the row-index
 // bases back to rows (r plus the row offset); empty cells keep their marker.
 __global__ void unkey_rows_kernel(int op, void *agg, int64_t n, int64_t nrows, int64_t row_offset) {
@@ -805,13 +823,71 @@ static bool fold_fits(int op, int fold) {
     if (op == DSGB_BASE_AA_ARGMAX)
         return fold == DSGB_FOLD_WHERE_MAX || fold == DSGB_FOLD_WHERE_MIN || fold == DSGB_FOLD_WHERE_FIRST ||
                fold == DSGB_FOLD_WHERE_LAST;
-    if (op == DSGB_BASE_AA_SUM || op == DSGB_BASE_AA_CNT0) return fold == DSGB_FOLD_ADD;
+    if (op == DSGB_BASE_AA_SUM || op == DSGB_BASE_AA_CNT0 || op == DSGB_BASE_COUNT) return fold == DSGB_FOLD_ADD;
     if (op == DSGB_BASE_AA_MAX)
         return fold == DSGB_FOLD_MAX || fold == DSGB_FOLD_MIN || fold == DSGB_FOLD_FIRST || fold == DSGB_FOLD_LAST ||
                fold == DSGB_FOLD_SUM || fold == DSGB_FOLD_SUM_F32;
     if (op == DSGB_BASE_MIN_ROW) return fold == DSGB_FOLD_ROW_MIN;
     if (op == DSGB_BASE_MAX_ROW) return fold == DSGB_FOLD_MAX;
     return false;
+}
+
+}  // namespace dsgb
+
+namespace dsgb {
+
+// The stage-2 driver shared by the two-stage entry points: draw(params, L)
+// draws line L alone; line 0 goes into the bases, every later line into the
+// re-initialised per-line aggregates, folded in line order (additive bases
+// keep drawing into their accumulators).
+template <class DrawLine>
+static int run_two_stage(LineParams &p, const dsgb_base *bases, int32_t nbases, const int32_t *folds,
+                         void *const *line_aggs, int64_t nlines, int64_t ncells, cudaStream_t st, DrawLine draw) {
+    if (nbases > 0 && (!folds || !line_aggs)) { set_error("two-stage lines: folds / line_aggs missing"); return DSGB_E_INVALID; }
+    dsgb_base line_bases[MAX_BASES];      // the per-line aggregates to re-initialise for every line
+    int32_t nline_bases = 0;
+    for (int32_t b = 0; b < nbases; ++b) {
+        if (!fold_fits(bases[b].op, folds[b]) || (folds[b] != DSGB_FOLD_ADD && !line_aggs[b])) {
+            set_error("two-stage lines: base %d (op %d) has no stage-2 fold %d", b, bases[b].op, folds[b]);
+            return DSGB_E_UNSUPPORTED;
+        }
+        if (folds[b] == DSGB_FOLD_ADD) continue;
+        line_bases[nline_bases] = bases[b];
+        line_bases[nline_bases].agg = line_aggs[b];
+        ++nline_bases;
+    }
+    p.use_2_stage = 1;                     // the previous vertex is not read (line.py:1170, 1266)
+    // the same plan drawing into the per-line aggregates; additive bases (the
+    // zero-initialised sums and counts of mean, _sum_zero and
+    // _count_ignore_antialiasing, whose stage-2 nansum is a plain sum) keep
+    // drawing into their accumulators
+    LineParams pl = p;
+    for (int32_t b = 0; b < nbases; ++b)
+        if (folds[b] != DSGB_FOLD_ADD) pl.bases[b].agg = line_aggs[b];
+    int rc = bases_init(bases, nbases, ncells, st);
+    if (rc) return rc;
+    for (int64_t L = 0; L < nlines && nbases > 0; ++L) {
+        if (L > 0 && nline_bases > 0) {
+            rc = bases_init(line_bases, nline_bases, ncells, st);
+            if (rc) return rc;
+        }
+        draw(L > 0 ? pl : p, L);
+        DSGB_CHECK_LAUNCH("two-stage lines kernel");
+        for (int32_t b = 0; b < nbases && L > 0; ++b) {
+            if (folds[b] == DSGB_FOLD_ADD) continue;
+            const int64_t n = ncells * (bases[b].ncat < 1 ? 1 : bases[b].ncat);
+            const unsigned fb = (unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+            if (fb == 0) continue;
+            if (bases[b].op == DSGB_BASE_AA_ARGMAX)
+                stage2_fold_pairs_kernel<<<fb, 256, 0, st>>>(folds[b], (long long *)bases[b].agg,
+                                                            (const long long *)line_aggs[b], n);
+            else
+                stage2_fold_kernel<<<fb, 256, 0, st>>>(folds[b], (long long *)bases[b].agg,
+                                                      (const long long *)line_aggs[b], n);
+            DSGB_CHECK_LAUNCH("stage-2 fold");
+        }
+    }
+    return DSGB_OK;
 }
 
 }  // namespace dsgb
@@ -839,73 +915,73 @@ extern "C" int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t
         set_error("dsgb_lines_2stage: a two-stage plan cannot accumulate across calls");
         return DSGB_E_INVALID;
     }
-    if (nbases > 0 && (!folds || !line_aggs)) { set_error("dsgb_lines_2stage: folds / line_aggs missing"); return DSGB_E_INVALID; }
     LineParams p;
     int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
     if (rc) return rc;
-    dsgb_base line_bases[MAX_BASES];      // the per-line aggregates to re-initialise for every line
-    int32_t nline_bases = 0;
-    for (int32_t b = 0; b < nbases; ++b) {
-        if (!fold_fits(bases[b].op, folds[b]) || (folds[b] != DSGB_FOLD_ADD && !line_aggs[b])) {
-            set_error("dsgb_lines_2stage: base %d (op %d) has no stage-2 fold %d", b, bases[b].op, folds[b]);
-            return DSGB_E_UNSUPPORTED;
-        }
-        if (folds[b] == DSGB_FOLD_ADD) continue;
-        line_bases[nline_bases] = bases[b];
-        line_bases[nline_bases].agg = line_aggs[b];
-        ++nline_bases;
-    }
     p.line_width = line_width;
     p.plot_start = 1;
     p.overwrite = overwrite;
-    p.use_2_stage = 1;                     // the previous vertex is not read (line.py:1170, 1266)
-    // the same plan drawing into the per-line aggregates; additive bases (the
-    // zero-initialised sums and counts of mean, _sum_zero and
-    // _count_ignore_antialiasing, whose stage-2 nansum is a plain sum) keep
-    // drawing into their accumulators
-    LineParams pl = p;
-    for (int32_t b = 0; b < nbases; ++b)
-        if (folds[b] != DSGB_FOLD_ADD) pl.bases[b].agg = line_aggs[b];
     LinesGeom g;
     g.xs = xs; g.ys = ys; g.nrows = nrows; g.nv = nv;
     g.xrow = layout == 1 ? nv : x_row_stride;
     g.yrow = layout == 1 ? nv : y_row_stride;
+    g.only_line = -1;
     cudaStream_t st = as_stream(stream);
     const int64_t ncells = (int64_t)canvas->width * canvas->height;
-    rc = bases_init(bases, nbases, ncells, st);
-    if (rc) return rc;
-    const int64_t nlines = layout == 1 ? nv : nrows;
     const int64_t nseg = layout == 1 ? nrows - 1 : nv - 1;   // segments of one line
     int sms = sm_count();
     if (sms <= 0) sms = 148;
     int64_t blocks = (nseg + 255) / 256;
     if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
-    for (int64_t L = 0; L < nlines && nseg > 0 && nbases > 0; ++L) {
-        // line 0 draws straight into the accumulators (the first pass copies,
-        // compiler.py:218-222); every later line into freshly initialised
-        // per-line aggregates, folded in line order
-        g.only_line = L;
-        if (L > 0 && nline_bases > 0) {
-            rc = bases_init(line_bases, nline_bases, ncells, st);
-            if (rc) return rc;
-        }
-        if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(L > 0 ? pl : p, g);
-        else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(L > 0 ? pl : p, g);
-        DSGB_CHECK_LAUNCH("two-stage lines kernel");
-        for (int32_t b = 0; b < nbases && L > 0; ++b) {
-            if (folds[b] == DSGB_FOLD_ADD) continue;
-            const int64_t n = ncells * (bases[b].ncat < 1 ? 1 : bases[b].ncat);
-            const unsigned fb = (unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
-            if (fb == 0) continue;
-            if (bases[b].op == DSGB_BASE_AA_ARGMAX)
-                stage2_fold_pairs_kernel<<<fb, 256, 0, st>>>(folds[b], (long long *)bases[b].agg,
-                                                            (const long long *)line_aggs[b], n);
-            else
-                stage2_fold_kernel<<<fb, 256, 0, st>>>(folds[b], (long long *)bases[b].agg,
-                                                      (const long long *)line_aggs[b], n);
-            DSGB_CHECK_LAUNCH("stage-2 fold");
-        }
+    if (blocks < 1) blocks = 1;
+    rc = run_two_stage(p, bases, nbases, folds, line_aggs, nseg > 0 ? (layout == 1 ? nv : nrows) : 0, ncells, st,
+                       [&](const LineParams &pp, int64_t L) {
+                           g.only_line = L;
+                           if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(pp, g);
+                           else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(pp, g);
+                       });
+    if (rc) return rc;
+    if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+        rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+    return rc;
+}
+
+extern "C" int dsgb_lines_ragged_2stage(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
+                                        const double *x_flat, int64_t nx, const int64_t *x_start,
+                                        const double *y_flat, int64_t ny, const int64_t *y_start,
+                                        const dsgb_canvas *canvas, double line_width, int32_t overwrite,
+                                        const dsgb_base *bases, int32_t nbases, const int32_t *folds,
+                                        void *const *line_aggs, const dsgb_output *outs, int32_t nouts,
+                                        uint32_t flags, void *stream) {
+    if (nrows < 0 || nx < 0 || ny < 0 || (nrows > 0 && (!x_start || !y_start)) || (nx > 0 && !x_flat) ||
+        (ny > 0 && !y_flat)) {
+        set_error("dsgb_lines_ragged_2stage: invalid vertex arrays");
+        return DSGB_E_INVALID;
     }
+    if (!(line_width > 0.0)) {
+        set_error("dsgb_lines_ragged_2stage: two-stage plans are antialiased (line_width > 0)");
+        return DSGB_E_INVALID;
+    }
+    if (flags & DSGB_FLAG_NO_INIT) {
+        set_error("dsgb_lines_ragged_2stage: a two-stage plan cannot accumulate across calls");
+        return DSGB_E_INVALID;
+    }
+    LineParams p;
+    int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
+    if (rc) return rc;
+    p.line_width = line_width;
+    p.plot_start = 1;
+    p.overwrite = overwrite;
+    RaggedGeom g;
+    g.xf = x_flat; g.yf = y_flat; g.xs = x_start; g.ys = y_start; g.nrows = nrows; g.nx = nx; g.ny = ny;
+    cudaStream_t st = as_stream(stream);
+    const int64_t ncells = (int64_t)canvas->width * canvas->height;
+    // a row's length is known on the device only: a small grid strides over its segments
+    rc = run_two_stage(p, bases, nbases, folds, line_aggs, nx > 1 ? nrows : 0, ncells, st,
+                       [&](const LineParams &pp, int64_t L) {
+                           lines_ragged_row_kernel<<<32, 256, 0, st>>>(pp, g, L);
+                       });
+    if (rc) return rc;
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
         rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
     return rc;

@@ -280,7 +280,7 @@ int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t ro
  * plans draw every segment as if it started a line, line.py:1170, 1266).
  * Supported bases and folds: DSGB_BASE_AA_MAX with any value fold,
  * DSGB_BASE_MIN_ROW with DSGB_FOLD_ROW_MIN, DSGB_BASE_MAX_ROW with
- * DSGB_FOLD_MAX, DSGB_BASE_AA_SUM / DSGB_BASE_AA_CNT0 with DSGB_FOLD_ADD,
+ * DSGB_FOLD_MAX, DSGB_BASE_AA_SUM / DSGB_BASE_AA_CNT0 / DSGB_BASE_COUNT with DSGB_FOLD_ADD,
  * DSGB_BASE_AA_ARGMAX with DSGB_FOLD_WHERE_*.  Cost: one launch per line plus one initialisation and one
  * fold of each base over the canvas per line after the first. */
 enum {
@@ -291,9 +291,10 @@ enum {
     DSGB_FOLD_FIRST    = 5,  /* nanfirst_in_place (first)                                   */
     DSGB_FOLD_LAST     = 6,  /* nanlast_in_place (last)                                     */
     DSGB_FOLD_ROW_MIN  = 7,  /* row_min_in_place (MIN_ROW)                                  */
-    DSGB_FOLD_ADD      = 8,  /* nansum_in_place of zero-initialised additive bases (AA_SUM,
-                                AA_CNT0 of mean / _sum_zero / _count_ignore_antialiasing): every
-                                line draws straight into the accumulator; line_aggs[b] unused */
+    DSGB_FOLD_ADD      = 8,  /* nansum_in_place of additive bases (AA_SUM, AA_CNT0 and the COUNT
+                                row mask: mean / _sum_zero / _count_ignore_antialiasing, and
+                                count / sum in a plan that keeps self_intersect): every line
+                                draws straight into the accumulator; line_aggs[b] unused */
     DSGB_FOLD_WHERE_MAX   = 9,   /* where(max | min | first | last) on AA_ARGMAX pairs: the   */
     DSGB_FOLD_WHERE_MIN   = 10,  /* selector's own append decides, the row follows           */
     DSGB_FOLD_WHERE_FIRST = 11,  /* (reductions.py:1992-2018)                                 */
@@ -305,6 +306,17 @@ int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t nrows, int
                       double line_width, int32_t overwrite, const dsgb_base *bases, int32_t nbases,
                       const int32_t *folds, void *const *line_aggs, const dsgb_output *outs,
                       int32_t nouts, uint32_t flags, void *stream);
+
+/* dsgb_lines_ragged's two-stage antialiased form (the reference's
+ * extend_cpu_antialias_2agg of LinesAxis1Ragged, line.py:1616-1693): one row
+ * at a time, folds and per-line aggregates as dsgb_lines_2stage. */
+int dsgb_lines_ragged_2stage(const dsgb_column *cols, int32_t ncols, int64_t nrows, int64_t row_offset,
+                             const double *x_flat, int64_t nx, const int64_t *x_start,
+                             const double *y_flat, int64_t ny, const int64_t *y_start,
+                             const dsgb_canvas *canvas, double line_width, int32_t overwrite,
+                             const dsgb_base *bases, int32_t nbases, const int32_t *folds,
+                             void *const *line_aggs, const dsgb_output *outs, int32_t nouts,
+                             uint32_t flags, void *stream);
 
 /* Canvas.line(axis=1) over ragged x / y columns (LinesAxis1Ragged,
  * line.py:457-523 and 1538-1612): row i's vertices are x_flat[x_start[i] ..

@@ -89,6 +89,7 @@ def lib():
                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                 ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 9 + [
                 ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
+            L.oracle_lines_ragged_2stage.argtypes = L.oracle_lines_ragged.argtypes
             L.oracle_bounds.argtypes = [ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             _lib = L
@@ -363,18 +364,20 @@ def lines_ragged(cols, x_rows, y_rows, width, height, x_range, y_range, specs, l
     sy, ty = scale_translate(y_range, height)
     antialias = line_width > 0
     overwrite = False
+    use_2_stage = False
     if antialias:
         self_intersect, overwrite, use_2_stage = aa_flags(specs)
-        if use_2_stage:
-            raise NotImplementedError("two-stage antialiased reductions over several lines")
         specs = [dict(s, self_intersect=self_intersect) for s in specs]
     reds, keep, colarrs, ptrs = _prepare(cols, specs, (height, width), antialias)
     L = lib()
     L.oracle_init(reds, len(specs), height * width, 1 if antialias else 0)
-    L.oracle_lines_ragged(nrows, xf.ctypes.data, xf.size, xstart.ctypes.data, yf.ctypes.data, yf.size,
-                          ystart.ctypes.data, ptrs, row_offset, width, height, sx, tx, sy, ty,
-                          float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]),
-                          float(line_width), 1 if overwrite else 0, reds, len(specs))
+    fn = L.oracle_lines_ragged_2stage if use_2_stage else L.oracle_lines_ragged
+    rc = fn(nrows, xf.ctypes.data, xf.size, xstart.ctypes.data, yf.ctypes.data, yf.size,
+            ystart.ctypes.data, ptrs, row_offset, width, height, sx, tx, sy, ty,
+            float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]),
+            float(line_width), 1 if overwrite else 0, reds, len(specs))
+    if rc == -2:
+        raise NotImplementedError("a reduction of this two-stage antialiased plan has no stage-2 fold in the oracle")
     return _finalize(specs, keep)
 
 

@@ -811,14 +811,14 @@ static void stage2_fold(int kind, void *ret, const void *other, int64_t n) {
     }
 }
 
-/* Returns 0, or -2 when a reduction has no stage-2 fold restated here. */
-int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double *xs, const double *ys,
-                        int64_t xrow, int64_t yrow, const double *const *cols, int64_t row_offset,
-                        int32_t width, int32_t height, double sx, double tx, double sy, double ty,
-                        double xmin, double xmax, double ymin, double ymax,
-                        double line_width, int32_t plot_start, int32_t overwrite, oracle_red *reds, int nreds) {
-    const int64_t ncells = (int64_t)width * height;
-    const int64_t nlines = layout == 1 ? nv : nrows;
+/* The stage-2 driver shared by every two-stage loop: draw line L into the
+ * aggregates (initialised by the caller for L = 0, re-initialised here after),
+ * copy them on the first pass and fold them afterwards, then copy back.
+ * Returns 0, or -2 when a reduction has no stage-2 fold restated here. */
+typedef void (*draw_line_fn)(const void *ctx, int64_t L, oracle_red *reds, int nreds);
+
+static int run_two_stage(int64_t nlines, int64_t ncells, draw_line_fn draw, const void *ctx,
+                         oracle_red *reds, int nreds) {
     for (int r = 0; r < nreds; ++r)
         if (stage2_elem(reds[r].kind) == 0) return -2;
     void *acc[64], *acc2[64];
@@ -826,8 +826,7 @@ int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double 
     for (int r = 0; r < nreds; ++r) { acc[r] = NULL; acc2[r] = NULL; }
     for (int64_t L = 0; L < nlines; ++L) {
         if (L > 0) oracle_init(reds, nreds, ncells, 1);
-        draw_one_line(layout, L, nrows, nv, xs, ys, xrow, yrow, cols, row_offset, width, sx, tx, sy, ty,
-                      xmin, xmax, ymin, ymax, line_width, plot_start, overwrite, reds, nreds);
+        draw(ctx, L, reds, nreds);
         if (nlines == 1) return 0;
         for (int r = 0; r < nreds; ++r) {
             const int64_t n = red_cells(ncells, &reds[r]);
@@ -854,33 +853,81 @@ int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double 
     return 0;
 }
 
+typedef struct {
+    int32_t layout; int64_t nrows, nv; const double *xs, *ys; int64_t xrow, yrow;
+    const double *const *cols; int64_t row_offset; int32_t width;
+    double sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width; int32_t plot_start, overwrite;
+} multi_ctx;
+
+static void draw_multi(const void *c, int64_t L, oracle_red *reds, int nreds) {
+    const multi_ctx *m = (const multi_ctx *)c;
+    draw_one_line(m->layout, L, m->nrows, m->nv, m->xs, m->ys, m->xrow, m->yrow, m->cols, m->row_offset, m->width,
+                  m->sx, m->tx, m->sy, m->ty, m->xmin, m->xmax, m->ymin, m->ymax, m->line_width, m->plot_start,
+                  m->overwrite, reds, nreds);
+}
+
+int oracle_lines_2stage(int32_t layout, int64_t nrows, int64_t nv, const double *xs, const double *ys,
+                        int64_t xrow, int64_t yrow, const double *const *cols, int64_t row_offset,
+                        int32_t width, int32_t height, double sx, double tx, double sy, double ty,
+                        double xmin, double xmax, double ymin, double ymax,
+                        double line_width, int32_t plot_start, int32_t overwrite, oracle_red *reds, int nreds) {
+    const multi_ctx m = {layout, nrows, nv, xs, ys, xrow, yrow, cols, row_offset, width,
+                         sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, plot_start, overwrite};
+    return run_two_stage(layout == 1 ? nv : nrows, (int64_t)width * height, draw_multi, &m, reds, nreds);
+}
+
 /* line.py:1538-1612 -- LinesAxis1Ragged (_build_extend_line_axis1_ragged,
  * single-stage form): row i runs over its own slices of the flat x and y
  * arrays (start indices; the last row ends at the flat length), through
  * the shorter of the two; segment j appends row i. */
+typedef struct {
+    int64_t nrows; const double *xf; int64_t nx; const int64_t *xstart; const double *yf; int64_t ny;
+    const int64_t *ystart; const double *const *cols; int64_t row_offset; int32_t width;
+    double sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width; int32_t overwrite, two_stage;
+} ragged_ctx;
+
+/* one ragged row: its slices of the flat arrays, through the shorter of the two;
+ * the two-stage form never reads the previous vertex (line.py:1662-1684) */
+static void draw_ragged_row(const void *c, int64_t i, oracle_red *reds, int nreds) {
+    const ragged_ctx *g = (const ragged_ctx *)c;
+    const int64_t x0i = g->xstart[i], x1i = i < g->nrows - 1 ? g->xstart[i + 1] : g->nx;
+    const int64_t y0i = g->ystart[i], y1i = i < g->nrows - 1 ? g->ystart[i + 1] : g->ny;
+    const int64_t len = (x1i - x0i) < (y1i - y0i) ? (x1i - x0i) : (y1i - y0i);
+    const double *X = g->xf + x0i, *Y = g->yf + y0i;
+    for (int64_t j = 0; j + 1 < len; ++j) {
+        int segment_start = (j == 0) || isnull_d(X[j - 1]) || isnull_d(Y[j - 1]);
+        int segment_end = (j == len - 2) || isnull_d(X[j + 2]) || isnull_d(Y[j + 2]);
+        double xm = 0.0, ym = 0.0;
+        if (!segment_start && !g->two_stage) { xm = X[j - 1]; ym = Y[j - 1]; }
+        draw_segment(i, g->row_offset, X[j], Y[j], X[j + 1], Y[j + 1], segment_start, segment_end, xm, ym,
+                     g->cols, g->width, g->sx, g->tx, g->sy, g->ty, g->xmin, g->xmax, g->ymin, g->ymax,
+                     g->line_width, g->overwrite, reds, nreds);
+    }
+}
+
 int oracle_lines_ragged(int64_t nrows, const double *xf, int64_t nx, const int64_t *xstart,
                         const double *yf, int64_t ny, const int64_t *ystart,
                         const double *const *cols, int64_t row_offset,
                         int32_t width, int32_t height, double sx, double tx, double sy, double ty,
                         double xmin, double xmax, double ymin, double ymax,
                         double line_width, int32_t overwrite, oracle_red *reds, int nreds) {
-    for (int64_t i = 0; i < nrows; ++i) {
-        const int64_t x0i = xstart[i], x1i = i < nrows - 1 ? xstart[i + 1] : nx;
-        const int64_t y0i = ystart[i], y1i = i < nrows - 1 ? ystart[i + 1] : ny;
-        const int64_t len = (x1i - x0i) < (y1i - y0i) ? (x1i - x0i) : (y1i - y0i);
-        const double *X = xf + x0i, *Y = yf + y0i;
-        for (int64_t j = 0; j + 1 < len; ++j) {
-            int segment_start = (j == 0) || isnull_d(X[j - 1]) || isnull_d(Y[j - 1]);
-            int segment_end = (j == len - 2) || isnull_d(X[j + 2]) || isnull_d(Y[j + 2]);
-            double xm = 0.0, ym = 0.0;
-            if (!segment_start) { xm = X[j - 1]; ym = Y[j - 1]; }
-            draw_segment(i, row_offset, X[j], Y[j], X[j + 1], Y[j + 1], segment_start, segment_end, xm, ym,
-                         cols, width, sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite,
-                         reds, nreds);
-        }
-    }
+    const ragged_ctx g = {nrows, xf, nx, xstart, yf, ny, ystart, cols, row_offset, width,
+                          sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite, 0};
+    for (int64_t i = 0; i < nrows; ++i) draw_ragged_row(&g, i, reds, nreds);
     (void)height;
     return 0;
+}
+
+/* line.py:1616-1693 -- the two-stage ragged loop: one row at a time, folded. */
+int oracle_lines_ragged_2stage(int64_t nrows, const double *xf, int64_t nx, const int64_t *xstart,
+                               const double *yf, int64_t ny, const int64_t *ystart,
+                               const double *const *cols, int64_t row_offset,
+                               int32_t width, int32_t height, double sx, double tx, double sy, double ty,
+                               double xmin, double xmax, double ymin, double ymax,
+                               double line_width, int32_t overwrite, oracle_red *reds, int nreds) {
+    const ragged_ctx g = {nrows, xf, nx, xstart, yf, ny, ystart, cols, row_offset, width,
+                          sx, tx, sy, ty, xmin, xmax, ymin, ymax, line_width, overwrite, 1};
+    return run_two_stage(nrows, (int64_t)width * height, draw_ragged_row, &g, reds, nreds);
 }
 
 /* glyph.py:66-78 -- _compute_bounds_numba: NaN-skipping min/max. */

@@ -207,10 +207,56 @@ def test_two_stage_summary_and_unserved_plans():
                             oracle.spec("first", "v")], line_width=1.5)
         assert_same(to_numpy(got["r"]), ref[0], what=f"where({sel}) row")
         assert_same(to_numpy(got["l"]), ref[1], what=f"where({sel}, w)")
-    ragged = ds.TensorFrame({"x": ds.RaggedColumn([[0.1, 0.5, 0.9]]), "y": ds.RaggedColumn([[0.2, 0.6, 0.3]]),
-                             "v": torch.ones(1, dtype=torch.float64, device="cuda")})
-    with pytest.raises(NotImplementedError):
-        cvs.line(ragged, x="x", y="y", axis=1, agg=ds.first("v"), line_width=1.5)
+
+
+@pytest.mark.parametrize("name", [t[0] for t in TWO_STAGE] + ["where_last", "mean", "si_count_where"])
+def test_two_stage_ragged_vs_oracle(name):
+    """Two-stage plans over ragged rows (line.py:1616-1693): one row at a time, folded."""
+    rng = np.random.default_rng(29)
+    lens = rng.integers(0, 40, 30)
+    xr_rows = [list(np.sort(rng.uniform(0, 1, k))) for k in lens]
+    yr_rows = [list(np.cumsum(rng.normal(0, 0.08, k))) for k in lens]
+    for r in yr_rows[::7]:
+        if len(r) > 3:
+            r[2] = np.nan
+    v = rng.uniform(0, 1, 30)
+    frame = ds.TensorFrame({"x": ds.RaggedColumn(xr_rows), "y": ds.RaggedColumn(yr_rows),
+                            "v": torch.from_numpy(v).cuda()})
+    if name == "where_last":
+        red, spec = ds.where(ds.last("v")), oracle.spec("where", selector=oracle.spec("last", "v"))
+    elif name == "mean":
+        red, spec = ds.summary(m=ds.mean("v"), f=ds.first("v")), None
+    elif name == "si_count_where":
+        # where alone keeps self_intersect: a two-stage plan whose count and sum stay additive
+        red, spec = ds.summary(c=ds.count(), s=ds.sum("v"), w=ds.where(ds.first("v"))), None
+    else:
+        _, red, spec = next(t for t in TWO_STAGE if t[0] == name)
+    yall = np.concatenate([np.asarray(r) for r in yr_rows if len(r)])
+    xrng, yrng = (0.0, 1.0), (float(np.nanmin(yall)), float(np.nanmax(yall)))
+    cvs = ds.Canvas(plot_width=80, plot_height=60, x_range=xrng, y_range=yrng)
+    got = cvs.line(frame, x="x", y="y", axis=1, agg=red, line_width=1.5)
+    if name == "si_count_where":
+        ref = oracle.lines_ragged({"v": v}, xr_rows, yr_rows, 80, 60, xrng, yrng,
+                                  [oracle.spec("count"), oracle.spec("sum", "v"),
+                                   oracle.spec("where", selector=oracle.spec("first", "v"))], line_width=1.5)
+        assert_same(to_numpy(got["c"]), ref[0], rtol=3e-7, atol=1e-7)
+        assert_same(to_numpy(got["s"]), ref[1], rtol=1e-12, atol=1e-15)
+        assert_same(to_numpy(got["w"]), ref[2])
+        return
+    if spec is None:
+        ref = oracle.lines_ragged({"v": v}, xr_rows, yr_rows, 80, 60, xrng, yrng,
+                                  [oracle.spec("mean", "v"), oracle.spec("first", "v")], line_width=1.5)
+        assert_same(to_numpy(got["m"]), ref[0], rtol=1e-12, atol=1e-15)
+        assert_same(to_numpy(got["f"]), ref[1])
+        return
+    ref = oracle.lines_ragged({"v": v}, xr_rows, yr_rows, 80, 60, xrng, yrng, [spec], line_width=1.5)[0]
+    got = to_numpy(got)
+    if ref.dtype == np.float32:
+        assert_same(got, ref, rtol=3e-7, atol=1e-7, what=name)
+    elif ref.dtype.kind == "f":
+        assert_same(got, ref, rtol=1e-12, what=name)
+    else:
+        assert_same(got, ref, what=name)
 
 
 @pytest.mark.parametrize("nv", [2, 6])
