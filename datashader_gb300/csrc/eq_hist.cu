@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(1024) eqh_scan(EqHeader *hp, const unsigned in
 }
 
 struct Cmap {
-    double r[16], g[16], b[16];
+    double r[256], g[256], b[256];   // float64 channels as given (a tuple may hold floats)
     int n;
     int alpha;
 };
@@ -277,22 +277,23 @@ struct Cmap {
 template <typename T>
 __global__ void __launch_bounds__(256) eqh_apply(const T *data, int64_t n, const EqHeader *hp,
                                                  const double *cdf, const double *centers, double *out,
-                                                 uint32_t *rgba, const Cmap cm, int nbins) {
+                                                 uint32_t *rgba, const __grid_constant__ Cmap cm, int nbins) {
     const EqHeader h = *hp;
-    // np.linspace(span0, span1, ncolors) (:320)
-    double xs[16];
+    // np.linspace(span0, span1, ncolors) (:320) and the colours, shared by the block
+    __shared__ double xs[256], cr[256], cg[256], cb[256];
     if (rgba) {
         const int div = cm.n - 1;
         const double delta = __dsub_rn(h.span1, h.span0);
         const double step = div > 0 ? __ddiv_rn(delta, (double)div) : 0.0;
-        for (int k = 0; k < cm.n; ++k) {
+        for (int k = threadIdx.x; k < cm.n; k += blockDim.x) {
             double y;
             if (div > 0 && step == 0.0) y = __dmul_rn(__ddiv_rn((double)k, (double)div), delta);
             else y = __dmul_rn((double)k, step);
-            xs[k] = __dadd_rn(y, h.span0);
+            xs[k] = (div > 0 && k == div) ? h.span1 : __dadd_rn(y, h.span0);
+            cr[k] = cm.r[k]; cg[k] = cm.g[k]; cb[k] = cm.b[k];
         }
-        if (div > 0) xs[cm.n - 1] = h.span1;
     }
+    __syncthreads();
     for (int64_t i = gtid(); i < n; i += gstride()) {
         T v = data[i];
         double o;
@@ -308,9 +309,9 @@ __global__ void __launch_bounds__(256) eqh_apply(const T *data, int64_t n, const
             uint32_t px = 0;
             if (o == o) {
                 // interp(data, span, chan, left=255), nan_to_num, astype(uint8)
-                double r = np_interp(o, xs, cm.r, cm.n, 255.0, cm.r[cm.n - 1]);
-                double g = np_interp(o, xs, cm.g, cm.n, 255.0, cm.g[cm.n - 1]);
-                double b = np_interp(o, xs, cm.b, cm.n, 255.0, cm.b[cm.n - 1]);
+                double r = np_interp(o, xs, cr, cm.n, 255.0, cr[cm.n - 1]);
+                double g = np_interp(o, xs, cg, cm.n, 255.0, cg[cm.n - 1]);
+                double b = np_interp(o, xs, cb, cm.n, 255.0, cb[cm.n - 1]);
                 px = (uint32_t)(uint8_t)(int)r | ((uint32_t)(uint8_t)(int)g << 8) |
                      ((uint32_t)(uint8_t)(int)b << 16) | ((uint32_t)(uint8_t)cm.alpha << 24);
             }
@@ -334,7 +335,7 @@ static unsigned grid_cap(int64_t n, int threads, int mult) {
 
 template <typename T>
 static int eq_hist_impl(const T *data, int64_t n, int32_t nbins, double *out, int64_t *levels,
-                        uint32_t *rgba, const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                        uint32_t *rgba, const double *cmap_rgb, int32_t ncolors, int32_t alpha,
                         int32_t rescale, void *workspace, size_t wsb, void *stream) {
     if ((!data && n > 0) || n < 0 || !out || !levels || nbins < 1 || nbins > (1 << 24) || !workspace) {
         set_error("dsgb_eq_hist: invalid arguments");
@@ -344,8 +345,8 @@ static int eq_hist_impl(const T *data, int64_t n, int32_t nbins, double *out, in
         set_error("dsgb_eq_hist: workspace of %zu bytes, %zu needed", wsb, ws_bytes(nbins));
         return DSGB_E_NOSPACE;
     }
-    if (rgba && (!cmap_rgb || ncolors < 1 || ncolors > 16)) {
-        set_error("dsgb_eq_hist: colormap must have 1..16 colours");
+    if (rgba && (!cmap_rgb || ncolors < 1 || ncolors > 256)) {
+        set_error("dsgb_eq_hist: colormap must have 1..256 colours");
         return DSGB_E_INVALID;
     }
     Cmap cm;
@@ -414,7 +415,7 @@ static int static_scratch(void **ptr) {
 using namespace dsgb;
 
 extern "C" int dsgb_eq_hist_u32_static(const uint32_t *data, int64_t n, int32_t nbins, double *out,
-                                       int64_t *levels, uint32_t *rgba, const uint8_t *cmap_rgb,
+                                       int64_t *levels, uint32_t *rgba, const double *cmap_rgb,
                                        int32_t ncolors, int32_t alpha, int32_t rescale, void *stream) {
     if (nbins < 1 || nbins > STATIC_MAX_BINS) {
         set_error("dsgb_eq_hist_u32_static: nbins=%d is outside 1..%d, the size of the static scratch",
@@ -431,14 +432,14 @@ extern "C" int dsgb_eq_hist_u32_static(const uint32_t *data, int64_t n, int32_t 
 extern "C" size_t dsgb_eq_hist_workspace_size(int32_t nbins) { return ws_bytes(nbins < 1 ? 1 : nbins); }
 
 extern "C" int dsgb_eq_hist_u32(const uint32_t *data, int64_t n, int32_t nbins, double *out, int64_t *levels,
-                                uint32_t *rgba, const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                                uint32_t *rgba, const double *cmap_rgb, int32_t ncolors, int32_t alpha,
                                 int32_t rescale, void *workspace, size_t wsb, void *stream) {
     return eq_hist_impl<unsigned int>((const unsigned int *)data, n, nbins, out, levels, rgba, cmap_rgb,
                                       ncolors, alpha, rescale, workspace, wsb, stream);
 }
 
 extern "C" int dsgb_eq_hist_f64(const double *data, int64_t n, int32_t nbins, double *out, int64_t *levels,
-                                uint32_t *rgba, const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                                uint32_t *rgba, const double *cmap_rgb, int32_t ncolors, int32_t alpha,
                                 int32_t rescale, void *workspace, size_t wsb, void *stream) {
     return eq_hist_impl<double>(data, n, nbins, out, levels, rgba, cmap_rgb, ncolors, alpha, rescale,
                                 workspace, wsb, stream);

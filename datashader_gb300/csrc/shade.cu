@@ -41,7 +41,7 @@ struct ShadeArgs {
     double span0, span1;
     int cmap_kind;                   // 0 = list of colours, 1 = single colour + alpha ramp
     int ncolors;                     // list: colours; single: alpha steps (alpha - min_alpha + 1)
-    double r[16], g[16], b[16];
+    double r[256], g[256], b[256];   // list colours, float64 channels as given (a tuple may hold floats)
     int alpha, min_alpha;
     int sr, sg, sb;                  // single colour
 };
@@ -119,7 +119,7 @@ __device__ __forceinline__ void s_offsets(const ShadeArgs &a, const ShadeHeader 
 }
 
 template <typename T>
-__global__ void shade_span(const T *data, int64_t n, const ShadeArgs a, ShadeHeader *hp) {
+__global__ void shade_span(const T *data, int64_t n, const __grid_constant__ ShadeArgs a, ShadeHeader *hp) {
     const ShadeHeader h = *hp;
     if (h.total == 0 || a.has_span) return;
     T offset, clo, chi;
@@ -148,7 +148,7 @@ __global__ void shade_span(const T *data, int64_t n, const ShadeArgs a, ShadeHea
 __device__ __forceinline__ uint32_t s_u8(double x) { return (uint32_t)(uint8_t)(int)x; }
 
 template <typename T>
-__global__ void __launch_bounds__(256) shade_apply(const T *data, int64_t n, const ShadeArgs a,
+__global__ void __launch_bounds__(256) shade_apply(const T *data, int64_t n, const __grid_constant__ ShadeArgs a,
                                                    const ShadeHeader *hp, uint32_t *rgba) {
     const ShadeHeader h = *hp;
     if (h.total == 0) {                              // everything masked: a zero image
@@ -166,8 +166,8 @@ __global__ void __launch_bounds__(256) shade_apply(const T *data, int64_t n, con
         s0 = unord64(h.tlo);
         s1 = unord64(h.thi);
     }
-    // np.linspace(span, num) and the alpha ramp, shared by the block
-    __shared__ double xs[256], ramp[256];
+    // np.linspace(span, num), the alpha ramp and the colours, shared by the block
+    __shared__ double xs[256], ramp[256], cr[256], cg[256], cb[256];
     const int m = a.ncolors < 256 ? a.ncolors : 256;
     {
         const int div = m - 1;
@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(256) shade_apply(const T *data, int64_t n, con
             else y = __dmul_rn((double)k, step);
             xs[k] = (div > 0 && k == div) ? s1 : __dadd_rn(y, s0);
             ramp[k] = (double)(a.min_alpha + k);
+            if (a.cmap_kind == 0) { cr[k] = a.r[k]; cg[k] = a.g[k]; cb[k] = a.b[k]; }
         }
     }
     __syncthreads();
@@ -190,9 +191,9 @@ __global__ void __launch_bounds__(256) shade_apply(const T *data, int64_t n, con
         if (a.cmap_kind == 0) {
             px = 0u;
             if (t == t) {
-                const double r = np_interp(t, xs, a.r, m, 255.0, a.r[m - 1]);
-                const double g = np_interp(t, xs, a.g, m, 255.0, a.g[m - 1]);
-                const double b = np_interp(t, xs, a.b, m, 255.0, a.b[m - 1]);
+                const double r = np_interp(t, xs, cr, m, 255.0, cr[m - 1]);
+                const double g = np_interp(t, xs, cg, m, 255.0, cg[m - 1]);
+                const double b = np_interp(t, xs, cb, m, 255.0, cb[m - 1]);
                 px = s_u8(r) | (s_u8(g) << 8) | (s_u8(b) << 16) | ((uint32_t)(uint8_t)a.alpha << 24);
             }
         } else {
@@ -215,7 +216,7 @@ static unsigned s_grid(int64_t n) {
 }
 
 template <typename T>
-static int shade_impl(const T *data, int64_t n, int32_t how, const double *span, const uint8_t *cmap_rgb,
+static int shade_impl(const T *data, int64_t n, int32_t how, const double *span, const double *cmap_rgb,
                       int32_t ncolors, const uint8_t *single_rgb, int32_t alpha, int32_t min_alpha, uint32_t *rgba,
                       void *ws, size_t ws_bytes, void *stream) {
     if (n < 0 || (n > 0 && (!data || !rgba)) || how < 0 || how > 2 || alpha < 0 || alpha > 255 || min_alpha < 0 ||
@@ -242,8 +243,8 @@ static int shade_impl(const T *data, int64_t n, int32_t how, const double *span,
         a.sr = single_rgb[0]; a.sg = single_rgb[1]; a.sb = single_rgb[2];
         a.ncolors = alpha - min_alpha + 1;
     } else {
-        if (!cmap_rgb || ncolors < 1 || ncolors > 16) {
-            set_error("dsgb_shade: a list colormap has 1..16 colours");
+        if (!cmap_rgb || ncolors < 1 || ncolors > 256) {
+            set_error("dsgb_shade: a list colormap has 1..256 colours");
             return DSGB_E_INVALID;
         }
         a.ncolors = ncolors;
@@ -349,7 +350,7 @@ extern "C" int dsgb_composite(const uint32_t *src, const uint32_t *dst, uint32_t
 extern "C" size_t dsgb_shade_workspace_size(void) { return 256; }
 
 extern "C" int dsgb_shade_u32(const uint32_t *data, int64_t n, int32_t how, const double *span,
-                              const uint8_t *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb, int32_t alpha,
+                              const double *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb, int32_t alpha,
                               int32_t min_alpha, uint32_t *rgba, void *workspace, size_t workspace_bytes,
                               void *stream) {
     return shade_impl<unsigned int>((const unsigned int *)data, n, how, span, cmap_rgb, ncolors, single_rgb, alpha,
@@ -357,7 +358,7 @@ extern "C" int dsgb_shade_u32(const uint32_t *data, int64_t n, int32_t how, cons
 }
 
 extern "C" int dsgb_shade_f64(const double *data, int64_t n, int32_t how, const double *span,
-                              const uint8_t *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb, int32_t alpha,
+                              const double *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb, int32_t alpha,
                               int32_t min_alpha, uint32_t *rgba, void *workspace, size_t workspace_bytes,
                               void *stream) {
     return shade_impl<double>(data, n, how, span, cmap_rgb, ncolors, single_rgb, alpha, min_alpha, rgba, workspace,

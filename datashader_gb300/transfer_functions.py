@@ -93,10 +93,10 @@ def _run_eq_hist(data, nbins=256 * 256, cmap=None, alpha=255, rescale_discrete_l
     ncol = 0
     if cmap is not None:
         cols = [rgb(c) for c in cmap]
-        if not 1 <= len(cols) <= 16:
-            raise ValueError("colormap must have 1..16 colours")
+        if not 1 <= len(cols) <= 256:
+            raise ValueError("colormap must have 1..256 colours")
         ncol = len(cols)
-        cmap_buf = (ctypes.c_uint8 * (3 * ncol))(*[v for c in cols for v in c])
+        cmap_buf = (ctypes.c_double * (3 * ncol))(*[float(v) for c in cols for v in c])
         rgba = torch.empty(data.shape, dtype=torch.uint32, device=dev)
     ws = _workspace(dev, nbins)
     rc = fn(data.data_ptr(), data.numel(), nbins, out.data_ptr(), levels.data_ptr(),
@@ -137,10 +137,10 @@ def _run_shade(data, how, cmap, alpha, min_alpha, span, stream=None):
         single_buf = (ctypes.c_uint8 * 3)(*rgb(cmap))
     else:
         cols = [rgb(c) for c in cmap]
-        if not 1 <= len(cols) <= 16:
-            raise ValueError("colormap must have 1..16 colours")
+        if not 1 <= len(cols) <= 256:
+            raise ValueError("colormap must have 1..256 colours")
         ncol = len(cols)
-        cmap_buf = (ctypes.c_uint8 * (3 * ncol))(*[v for c in cols for v in c])
+        cmap_buf = (ctypes.c_double * (3 * ncol))(*[float(v) for c in cols for v in c])
     span_buf = (ctypes.c_double * 2)(float(span[0]), float(span[1])) if span is not None else None
     rgba = torch.empty(data.shape, dtype=torch.uint32, device=dev)
     size = int(N.lib().dsgb_shade_workspace_size())

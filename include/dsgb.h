@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define DSGB_ABI_VERSION 1
+#define DSGB_ABI_VERSION 2   /* 2: list colormaps as float64 channels, up to 256 colours */
 
 /* Status codes. */
 #define DSGB_OK             0
@@ -372,17 +372,19 @@ int dsgb_bounds(const dsgb_column *col, int64_t n, double *out_minmax, void *str
  * 0 (uint32) or NaN (float64).  Output: out (f64, NaN where masked) = the
  * equalised value; *levels (device int64) = discrete_levels; when rgba != NULL
  * the list-colormap RGBA image (uint32) is also written, with `ncolors` colour
- * stops in `cmap_rgb` (host, 3*ncolors bytes) and `alpha`, `rescale` as in
+ * stops in `cmap_rgb` (host, 3*ncolors float64 channels, 1 <= ncolors <= 256: a
+ * colour tuple may hold floats, interpolated before the uint8 truncation as
+ * numpy does) and `alpha`, `rescale` as in
  * tf.shade.  `workspace` must hold dsgb_eq_hist_workspace_size() bytes. */
 size_t dsgb_eq_hist_workspace_size(int32_t nbins);
 int dsgb_eq_hist_u32(const uint32_t *data, int64_t n, int32_t nbins,
                      double *out, int64_t *levels, uint32_t *rgba,
-                     const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                     const double *cmap_rgb, int32_t ncolors, int32_t alpha,
                      int32_t rescale_discrete_levels,
                      void *workspace, size_t workspace_bytes, void *stream);
 int dsgb_eq_hist_f64(const double *data, int64_t n, int32_t nbins,
                      double *out, int64_t *levels, uint32_t *rgba,
-                     const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                     const double *cmap_rgb, int32_t ncolors, int32_t alpha,
                      int32_t rescale_discrete_levels,
                      void *workspace, size_t workspace_bytes, void *stream);
 
@@ -398,22 +400,22 @@ int dsgb_eq_hist_f64(const double *data, int64_t n, int32_t nbins,
  * on one device) corrupt each other: serialise them. */
 int dsgb_eq_hist_u32_static(const uint32_t *data, int64_t n, int32_t nbins,
                             double *out, int64_t *levels, uint32_t *rgba,
-                            const uint8_t *cmap_rgb, int32_t ncolors, int32_t alpha,
+                            const double *cmap_rgb, int32_t ncolors, int32_t alpha,
                             int32_t rescale_discrete_levels, void *stream);
 
 /* tf.shade(how='linear' | 'log' | 'cbrt') of a 2-D aggregate
  * (transfer_functions/__init__.py:220-356): how 0 = linear, 1 = log,
- * 2 = cbrt; span (host, 2 doubles) or NULL; a list colormap (cmap_rgb,
- * ncolors <= 16) or, when single_rgb != NULL, one colour with an alpha
+ * 2 = cbrt; span (host, 2 doubles) or NULL; a list colormap (cmap_rgb: host,
+ * 3*ncolors float64 channels, ncolors <= 256) or, when single_rgb != NULL, one colour with an alpha
  * ramp from min_alpha to alpha.  rgba: uint32 per pixel.  The workspace is
  * dsgb_shade_workspace_size() bytes, 256-byte aligned. */
 size_t dsgb_shade_workspace_size(void);
 int dsgb_shade_u32(const uint32_t *data, int64_t n, int32_t how, const double *span,
-                   const uint8_t *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb,
+                   const double *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb,
                    int32_t alpha, int32_t min_alpha, uint32_t *rgba,
                    void *workspace, size_t workspace_bytes, void *stream);
 int dsgb_shade_f64(const double *data, int64_t n, int32_t how, const double *span,
-                   const uint8_t *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb,
+                   const double *cmap_rgb, int32_t ncolors, const uint8_t *single_rgb,
                    int32_t alpha, int32_t min_alpha, uint32_t *rgba,
                    void *workspace, size_t workspace_bytes, void *stream);
 

@@ -21,7 +21,12 @@ Reads (as text, via ``ast``; nothing from the reference is imported or run):
   replayed in order (they are plain numpy on literals), the operator under
   test never called;
 * ``datashader/tests/test_tiles.py`` -- the extent, zoom and expected tile
-  of ``test_meters_to_tile``.
+  of ``test_meters_to_tile``;
+* ``datashader/tests/data/test_00{1..7}_{antialias,noaa}_{normal,clipped}.png``
+  -- the shaded images of ``test_antialias.py`` (the PNG files the test module
+  writes beside its NetCDF copies), decoded with zlib and the PNG filters of
+  the PNG specification and stored as uint32 RGBA in aggregate orientation
+  (row 0 = y minimum: the PNG rows flipped back, as ``Image.to_pil`` flips them).
 
 Usage::
 
@@ -85,6 +90,59 @@ def _jsonable(a):
         return {"dtype": str(a.dtype), "shape": list(a.shape),
                 "data": [None if np.isnan(v) else float(v) for v in a.ravel()]}
     return {"dtype": str(a.dtype), "shape": list(a.shape), "data": [int(v) for v in a.ravel()]}
+
+
+def _paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    if pa <= pb and pa <= pc:
+        return a
+    return b if pb <= pc else c
+
+
+def _decode_png_rgba(path):
+    """8-bit RGBA PNG -> uint8 [h][w][4] (filter types 0-4 of the PNG specification)."""
+    import struct
+    import zlib
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, chunks = 8, {}
+    while pos < len(data):
+        (n,) = struct.unpack(">I", data[pos:pos + 4])
+        tag = data[pos + 4:pos + 8]
+        chunks[tag] = chunks.get(tag, b"") + data[pos + 8:pos + 8 + n]
+        pos += 12 + n
+    w, h, depth, ctype, _, _, interlace = struct.unpack(">IIBBBBB", chunks[b"IHDR"])
+    assert (depth, ctype, interlace) == (8, 6, 0), (depth, ctype, interlace)
+    raw = zlib.decompress(chunks[b"IDAT"])
+    stride, bpp = 4 * w, 4
+    out = np.zeros((h, stride), dtype=np.int64)
+    prev = [0] * stride
+    for y in range(h):
+        ftype = raw[y * (stride + 1)]
+        line = raw[y * (stride + 1) + 1:(y + 1) * (stride + 1)]
+        cur = [0] * stride
+        for i in range(stride):
+            a = cur[i - bpp] if i >= bpp else 0
+            b = prev[i]
+            c = prev[i - bpp] if i >= bpp else 0
+            pred = (0, a, b, (a + b) // 2, _paeth(a, b, c))[ftype]
+            cur[i] = (line[i] + pred) & 0xFF
+        out[y] = cur
+        prev = cur
+    return out.astype(np.uint8).reshape(h, w, 4)
+
+
+def _antialias_images(tests):
+    images = {}
+    for t in range(1, 8):
+        for aa in ("antialias", "noaa"):
+            for cv in ("normal", "clipped"):
+                name = f"test_{t:03d}_{aa}_{cv}"
+                rgba = _decode_png_rgba(os.path.join(tests, "data", name + ".png"))
+                u32 = np.ascontiguousarray(np.flipud(rgba)).view("<u4")[..., 0]
+                images[name] = dict(_jsonable(u32), source=f"datashader/tests/data/{name}.png")
+    return images
 
 
 def main(ref_root):
@@ -159,6 +217,9 @@ def main(ref_root):
     tiles = _meters_to_tile_case(os.path.join(tests, "test_tiles.py"))
     with open(os.path.join(HERE, "tiles.json"), "w") as f:
         json.dump(tiles, f, indent=0)
+    aa_images = _antialias_images(tests)
+    with open(os.path.join(HERE, "antialias_images.json"), "w") as f:
+        json.dump(aa_images, f, indent=0)
     print("wrote", sorted(goldens), sorted(eq), sorted(shade), sorted(lines), len(comp["cases"]), "composite cases",
           sorted(tiles))
 

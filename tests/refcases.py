@@ -321,6 +321,82 @@ def both_lines_cases():
     return src, canvas, out
 
 
+def binary_cmap50():
+    """test_antialias.py:40-42 ``cmap01``: matplotlib's ``cm.binary`` sampled at
+    np.linspace(0, 1) (50 points), each channel times 255.  matplotlib is not a
+    dependency here, so its published colormap steps are restated: the 'binary'
+    segment data ((0, 1, 1), (1, 0, 0)) per channel expanded into a 256-entry
+    lookup table as LinearSegmentedColormap builds it (x scaled by N - 1, the
+    sample points (N - 1) * linspace(0, 1, N), linear pieces between the
+    anchors, clipped to [0, 1]), then Colormap.__call__'s float lookup (x * N
+    truncated, x == 1 taking the last entry)."""
+    n = 256
+    x = np.array([0.0, 1.0]) * (n - 1)
+    y0 = np.array([1.0, 0.0])
+    y1 = np.array([1.0, 0.0])
+    xind = (n - 1) * np.linspace(0, 1, n) ** 1.0
+    ind = np.searchsorted(x, xind)[1:-1]
+    distance = (xind[1:-1] - x[ind - 1]) / (x[ind] - x[ind - 1])
+    lut = np.clip(np.concatenate([[y1[0]], distance * (y0[ind] - y1[ind - 1]) + y1[ind - 1], [y0[-1]]]), 0.0, 1.0)
+    xa = np.linspace(0, 1) * n
+    xa[xa == n] = n - 1
+    return [tuple(float(lut[i]) * 255. for _ in range(3)) for i in xa.astype(int)]
+
+
+def antialias_image_cases():
+    """test_antialias.py:141-408: the 7 line sets x {antialiased, not} x {the
+    50 x 50 canvas over [0, 49]^2, the clipped 20 x 20 canvas over [14, 34]^2}.
+    Sets 001-005 and 007 are separate two-vertex lines, each its own
+    Canvas.line(max('val')) aggregate, summed as xr.concat(...).sum('stack')
+    sums them (NaN counts as 0, so an empty pixel is 0); set 006 is one line
+    through its vertices.  The image is tf.shade(agg, cmap=cmap01) (eq_hist)
+    over a white background.  Expected: the PNG the module wrote, decoded
+    (tests/golden/antialias_images.json)."""
+    g = load_golden("antialias_images.json")
+    sets = {
+        "test_001": [((1, 1), (49, a)) for a in range(1, 55, 6)],
+        "test_002": [((1, 1), (a, 49)) for a in range(1, 55, 6)],
+        "test_003": [((49, 49), (1, a)) for a in range(1, 55, 6)],
+        "test_004": [((49, 49), (a, 1)) for a in range(1, 55, 6)],
+        "test_005": [((1, 1), (1, 49)), ((1, 49), (2, 1)), ((2, 1), (2, 49)), ((2, 49), (4, 1)),
+                     ((4, 1), (4, 49)), ((4, 49), (8, 1)), ((8, 1), (8, 49)), ((8, 49), (16, 1)),
+                     ((16, 1), (16, 49)), ((16, 49), (32, 1)), ((32, 1), (32, 49)), ((32, 49), (49, 1)),
+                     ((49, 1), (49, 49))],
+        "test_006": [(1, 1), (1, 49), (2, 1), (2, 49), (4, 1), (4, 49), (8, 1), (8, 49), (16, 1), (16, 49),
+                     (32, 1), (32, 49), (49, 1), (49, 49)],
+        "test_007": [((0.5, 0.5), (1.5, 48.5)), ((0.5, 0.5), (48.5, 1.5)), ((48.5, 48.5), (47.5, 0.5)),
+                     ((48.5, 48.5), (0.5, 47.5))],
+    }
+    canvases = {"normal": dict(plot_width=50, plot_height=50, x_range=(0, 49), y_range=(0, 49)),
+                "clipped": dict(plot_width=20, plot_height=20, x_range=(14, 34), y_range=(14, 34))}
+    cases = []
+    for name, pts in sets.items():
+        if name == "test_006":
+            frames = [{"x": np.array([p[0] for p in pts], dtype=np.float64),
+                       "y": np.array([p[1] for p in pts], dtype=np.float64)}]
+        else:
+            frames = [{"x": np.array([a[0], b[0]], dtype=np.float64), "y": np.array([a[1], b[1]], dtype=np.float64)}
+                      for a, b in pts]
+        for f in frames:
+            f["val"] = np.full(f["x"].size, 5.0)
+        for aa in ("antialias", "noaa"):
+            for cv in ("normal", "clipped"):
+                key = f"{name}_{aa}_{cv}"
+                cases.append(dict(id=key, frames=frames, canvas=canvases[cv], line_width=1.0 if aa == "antialias" else 0.0,
+                                  expected=golden_array(g[key])))
+    return cases
+
+
+def stack_sum(aggs):
+    """xr.concat(aggs, 'stack').sum(dim='stack'): NaN skipped, the float64 sum
+    taken along the stack in order (an all-NaN pixel sums to 0)."""
+    acc = None
+    for a in aggs:
+        a = np.where(np.isnan(a), 0.0, a)
+        acc = a if acc is None else acc + a
+    return acc
+
+
 def eq_hist_agg_a():
     """test_transfer_functions.py:23-37 build_agg 'a' (uint32, zero diagonal)."""
     a = np.arange(10, 19, dtype="u4").reshape((3, 3))

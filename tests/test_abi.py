@@ -32,7 +32,7 @@ def test_library_loads_and_exports_every_symbol():
 
 def test_abi_version_and_error_string():
     L = N.lib()
-    assert L.dsgb_abi_version() == 1
+    assert L.dsgb_abi_version() == 2
     assert isinstance(L.dsgb_last_error(), bytes)
 
 

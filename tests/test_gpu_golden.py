@@ -157,3 +157,22 @@ def test_gpu_shade_large_vs_oracle(how):
                 np.testing.assert_array_equal(got, ref)
             else:
                 assert np.abs(got.view(np.uint8).astype(int) - ref.view(np.uint8).astype(int)).max() <= 1
+
+
+AA_IMAGE_CASES = refcases.antialias_image_cases()
+
+
+@pytest.mark.parametrize("case", AA_IMAGE_CASES, ids=[c["id"] for c in AA_IMAGE_CASES])
+def test_gpu_antialias_images(case):
+    """test_antialias.py::test_antialiasing through the GPU path: each line's
+    Canvas.line(max('val')) aggregate, their NaN-skipping sum (the test's own
+    xr.concat(...).sum('stack'), host glue), tf.shade with the 50-colour binary
+    colormap (eq_hist) and set_background white; exactly the reference's PNG."""
+    cvs = ds.Canvas(**case["canvas"])
+    aggs = [to_numpy(cvs.line(frame_from_numpy(f), "x", "y", agg=ds.max("val"), line_width=case["line_width"]))
+            for f in case["frames"]]
+    total = torch.from_numpy(refcases.stack_sum(aggs)).cuda()
+    agg = ds.Aggregate(total, ["y", "x"], {}, dict(x_range=case["canvas"]["x_range"], y_range=case["canvas"]["y_range"]))
+    img = ds.tf.set_background(ds.tf.shade(agg, cmap=refcases.binary_cmap50()), "#ffffff")
+    got = img.data.view(torch.int32).cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(got, case["expected"], err_msg=case["id"])

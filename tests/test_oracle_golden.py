@@ -227,3 +227,19 @@ def test_oracle_both_lines_golden(case):
                        cv["x_range"], cv["y_range"], specs, line_width=1)[0]
     assert oracle.aa_flags(specs)[2] == case["two_stage"]
     _check(got, case["expected"], got.dtype.kind == "f")
+
+
+AA_IMAGE_CASES = refcases.antialias_image_cases()
+
+
+@pytest.mark.parametrize("case", AA_IMAGE_CASES, ids=[c["id"] for c in AA_IMAGE_CASES])
+def test_oracle_antialias_images(case):
+    """test_antialias.py::test_antialiasing: every image of the 28, exactly."""
+    from oracle import composite
+    cv = case["canvas"]
+    aggs = [oracle.line_axis0(f, "x", "y", cv["plot_width"], cv["plot_height"], cv["x_range"], cv["y_range"],
+                              [oracle.spec("max", "val")], line_width=case["line_width"])[0] for f in case["frames"]]
+    img = oracle.shade_eq_hist(refcases.stack_sum(aggs), refcases.binary_cmap50())
+    white = np.array([0xFFFFFFFF], dtype=np.uint32)[0]
+    got = composite.over(img, white)
+    np.testing.assert_array_equal(got, case["expected"])

@@ -19,7 +19,7 @@ from datashader_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
 
-CMAP = (ctypes.c_uint8 * 6)(0xAD, 0xD8, 0xE6, 0x00, 0x00, 0x8B)   # lightblue -> darkblue
+CMAP = (ctypes.c_double * 6)(0xAD, 0xD8, 0xE6, 0x00, 0x00, 0x8B)   # lightblue -> darkblue
 
 
 def _aggregate(seed, shape=(700, 900)):
