@@ -314,3 +314,43 @@ def test_ragged_random_vs_oracle(lw, red):
     auto = ds.Canvas(plot_width=64, plot_height=48).line(frame, "x", "y", agg=ds.count(), axis=1)
     ref_auto = oracle.lines_ragged({}, xr, yr, 64, 48, None, None, [oracle.spec("count")])[0]
     assert_same(to_numpy(auto), ref_auto)
+
+
+def test_two_stage_categorical_and_y_constant():
+    """Two-stage folds over categorical aggregates (by(cat, ...): the fold runs
+    over every category cell) on LineAxis0Multi, and a LinesAxis1YConstant
+    frame (one y array shared by every row)."""
+    cols, kw = _random_case("axis0multi", 350, 3, 31)
+    rng = np.random.default_rng(32)
+    cols["cat"] = rng.integers(0, 3, 350).astype(np.float64)
+    layout, xs, ys = refcases.multi_line_arrays(cols, kw)
+    xr, yr = (0.0, 1.0), (float(np.nanmin(ys)), float(np.nanmax(ys)))
+    t = {k: torch.from_numpy(np.asarray(v, dtype=np.float64)).cuda() for k, v in cols.items() if k != "cat"}
+    t["cat"] = torch.from_numpy(cols["cat"].astype(np.int8)).cuda()
+    frame = ds.TensorFrame(t, categories={"cat": [0, 1, 2]})
+    cvs = ds.Canvas(plot_width=60, plot_height=40, x_range=xr, y_range=yr)
+    for red, spec in ((ds.by("cat", ds.count(self_intersect=False)), oracle.spec("count", cat="cat", ncat=3,
+                                                                                  self_intersect=False)),
+                      (ds.by("cat", ds.first("v")), oracle.spec("first", "v", cat="cat", ncat=3))):
+        got = to_numpy(cvs.line(frame, agg=red, line_width=1.5, **kw))
+        ref = oracle.lines({"v": cols["v"], "cat": cols["cat"]}, layout, xs, ys, 60, 40, xr, yr, [spec],
+                           line_width=1.5)[0]
+        if ref.dtype == np.float32:
+            assert_same(got, ref, rtol=3e-7, atol=1e-7)
+        else:
+            assert_same(got, ref)
+    # LinesAxis1YConstant: x per row, one shared y
+    rng = np.random.default_rng(33)
+    nv = 50
+    xcols = {f"x{j}": np.linspace(0, 1, 40) * 0.02 + j / nv + rng.normal(0, 0.003, 40) for j in range(nv)}
+    xcols["v"] = rng.uniform(0, 1, 40)
+    yconst = np.sin(np.linspace(0, 3, nv))
+    kw = dict(x=[f"x{j}" for j in range(nv)], y=yconst, axis=1)
+    frame = _frame(xcols)
+    xs = np.stack([xcols[f"x{j}"] for j in range(nv)], axis=1)
+    yr = (float(yconst.min()), float(yconst.max()))
+    cvs = ds.Canvas(plot_width=70, plot_height=30, x_range=(0.0, 1.05), y_range=yr)
+    for red, spec in ((ds.min("v"), oracle.spec("min", "v")), (ds.last("v"), oracle.spec("last", "v"))):
+        got = to_numpy(cvs.line(frame, agg=red, line_width=1.5, **kw))
+        ref = oracle.lines({"v": xcols["v"]}, 2, xs, yconst, 70, 30, (0.0, 1.05), yr, [spec], line_width=1.5)[0]
+        assert_same(got, ref)
