@@ -133,6 +133,7 @@ FOLD_SUM, FOLD_SUM_F32, FOLD_MAX, FOLD_MIN, FOLD_FIRST, FOLD_LAST, FOLD_ROW_MIN,
 FOLD_WHERE_MAX, FOLD_WHERE_MIN, FOLD_WHERE_FIRST, FOLD_WHERE_LAST = range(9, 13)
 
 FLAG_NO_INIT, FLAG_NO_FINALIZE, FLAG_EXACT_BIN, FLAG_WARP_AGG, FLAG_DETERMINISTIC = 0x1, 0x2, 0x4, 0x8, 0x10
+FLAG_ROW_ORDER = 0x20
 
 # every symbol include/dsgb.h declares
 EXPORTED = (

@@ -493,6 +493,15 @@ def bypixel(source, canvas, glyph, agg, *, antialias=False, flags=0):
     return gpu_pipeline(frame, canvas, glyph, agg, antialias=antialias, flags=flags)
 
 
+def _raw_array_bounds(t, stream):
+    """NaN-skipping (min, max) of a float64 vertex array, unexpanded."""
+    t = t.contiguous()
+    col = N.Column(t.data_ptr(), N.F64, 0)
+    out = torch.empty(2, dtype=torch.float64, device=t.device)
+    N.check(N.lib().dsgb_bounds(ctypes.byref(col), t.numel(), out.data_ptr(), stream), "dsgb_bounds")
+    return tuple(out.cpu().tolist())
+
+
 def _column_raw_bounds(frame, name, stream):
     """Glyph._compute_bounds (glyph.py:51-78) on the device: NaN-skipping (min, max)."""
     t = frame[name]
@@ -717,23 +726,32 @@ def _line_chunks(parts):
 def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
     """dask.py:86-219 on one GPU: every partition into its own partial bases,
     an elementwise combine, one finalize.  LineAxis0 partitions are drawn as
-    the reference's dask line path draws them (dask.py:222-266)."""
+    the reference's dask line path draws them (dask.py:222-266); the
+    multi-line glyphs take the generic path (dask.py:86-219): each partition's
+    rows drawn alone, first / last / where by global row (row-index
+    reductions), not by the line-major visit order of one frame."""
     is_line = isinstance(glyph, LineAxis0)
-    if isinstance(glyph, _MultiLine):
-        raise NotImplementedError("partitioned sources are supported for Canvas.points and LineAxis0 lines")
+    multi = isinstance(glyph, _MultiLine)
+    if isinstance(glyph, LinesAxis1Ragged):
+        raise NotImplementedError("partitioned sources of ragged lines are not supported")
     if flags & N.FLAG_DETERMINISTIC:
         raise NotImplementedError("the deterministic mode sums one frame in row order; concatenate the partitions")
     parts = pframe.partitions
     dev = pframe.device
     if stream is None:
         stream = torch.cuda.current_stream(dev).cuda_stream
-    plan = compile_plan(agg, parts[0], antialias=is_line and glyph.antialiased)
-    if is_line and plan.use_2_stage:
+    plan = compile_plan(agg, parts[0], antialias=(is_line or multi) and glyph.antialiased)
+    if (is_line or multi) and plan.use_2_stage:
         raise NotImplementedError("two-stage antialiased plans are not supported on partitioned sources")
     if any(o.fin == N.FIN_GATHER for _, o in plan.outputs) and len(parts) > 64:
         raise NotImplementedError("first/last/where with a lookup column gather from at most 64 partitions")
     if canvas.x_range is not None and canvas.y_range is not None:
         x_range, y_range = canvas.x_range, canvas.y_range
+    elif multi:
+        bx = [_raw_array_bounds(_vertex_array(p, glyph.x, len(p)), stream) for p in parts] or [(np.inf, -np.inf)]
+        by = [_raw_array_bounds(_vertex_array(p, glyph.y, len(p)), stream) for p in parts] or [(np.inf, -np.inf)]
+        x_range = canvas.x_range or _expand_bounds(min(b[0] for b in bx), max(b[1] for b in bx))
+        y_range = canvas.y_range or _expand_bounds(min(b[0] for b in by), max(b[1] for b in by))
     else:
         bx = [_column_raw_bounds(p, glyph.x, stream) for p in parts] or [(np.inf, -np.inf)]
         by = [_column_raw_bounds(p, glyph.y, stream) for p in parts] or [(np.inf, -np.inf)]
@@ -752,7 +770,25 @@ def partitioned_pipeline(pframe, canvas, glyph, agg, *, flags=0, stream=None):
     for part, plot_start in chunks:
         ex = Executor(part, plan, glyph)
         ex.allocate(height, width, dev)
-        if is_line:
+        if multi:
+            xs = _vertex_array(part, glyph.x, len(part))
+            ys = _vertex_array(part, glyph.y, len(part))
+            if glyph.layout == 1:
+                nv, xrow, yrow = xs.shape[1], xs.shape[1], ys.shape[1]
+            else:
+                nv = xs.shape[-1] if xs.dim() == 2 else ys.shape[-1]
+                xrow = nv if xs.dim() == 2 else 0
+                yrow = nv if ys.dim() == 2 else 0
+            cols, ncols = ex.cols, len(ex.names)
+            if ncols == 0:                   # count() / any(): no field column, any valid pointer
+                cols = (N.Column * 1)(N.Column(ys.data_ptr(), N.F64, 0))
+                ncols = 1
+            N.check(L.dsgb_lines(cols, ncols, len(part), part.row_offset, glyph.layout, xs.data_ptr(), ys.data_ptr(),
+                                 nv, xrow, yrow, ctypes.byref(cv), float(glyph.line_width), 1, int(plan.overwrite),
+                                 ex.bases, len(plan.bases), ex.outs, ex.nouts,
+                                 flags | N.FLAG_NO_FINALIZE | N.FLAG_ROW_ORDER, stream), "dsgb_lines (partition)")
+            ex.keep = (xs, ys)           # the vertex arrays live until the stream has used them
+        elif is_line:
             wsz = int(L.dsgb_line_workspace_size(len(part))) if glyph.line_width > 0 else 0
             ws = workspace(dev, stream, wsz) if wsz else None
             N.check(L.dsgb_line_axis0_ws(ex.cols, len(ex.names), len(part), part.row_offset, 0, 1, ctypes.byref(cv),

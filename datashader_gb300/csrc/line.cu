@@ -720,7 +720,7 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
     p.plot_start = plot_start;
     p.overwrite = overwrite;
     p.use_2_stage = 0;
-    if (layout == 1 && nv > 1) p.field_mod = nrows;
+    if (layout == 1 && nv > 1 && !(flags & DSGB_FLAG_ROW_ORDER)) p.field_mod = nrows;
     LinesGeom g;
     g.xs = xs; g.ys = ys; g.nrows = nrows; g.nv = nv;
     g.xrow = layout == 1 ? nv : x_row_stride;

@@ -135,6 +135,9 @@ typedef struct {
 #define DSGB_FLAG_DETERMINISTIC 0x10u /* float64 sums in row order (bit-identical to the
                                          reference's CPU loop and run to run); needs the
                                          workspace of dsgb_points_workspace_size_flags */
+#define DSGB_FLAG_ROW_ORDER    0x20u /* dsgb_lines, layout 1: row-index bases (first / last / where) keep
+                                       global rows, the semantics of a partitioned source (dask.py:86-219,
+                                       row-index reductions), instead of the line-major visit order */
 
 /* ---- informational ---------------------------------------------------- */
 int dsgb_abi_version(void);

@@ -126,3 +126,62 @@ def test_partitioned_lines_follow_the_reference_dask_path(lw, red):
     want = want.astype(partials[0].dtype)
     rtol = 0.0 if red == "max" or (red == "count" and lw == 0) else (3e-7 if partials[0].dtype == np.float32 else 1e-12)
     assert_same(got, want, rtol=rtol, what=f"{red} lw={lw}")
+
+
+def _multi_cols(nrows, nv, seed):
+    rng = np.random.default_rng(seed)
+    cols = {}
+    for j in range(nv):
+        cols[f"x{j}"] = np.linspace(0, 1, nrows) + 0.01 * j
+        cols[f"y{j}"] = np.cumsum(rng.normal(0, 0.05, nrows))
+    cols["v"] = rng.uniform(0, 1, nrows)
+    return cols
+
+
+@pytest.mark.parametrize("lw", [0.0, 1.5])
+def test_partitioned_lines_axis1_equal_one_frame(lw):
+    """The LinesAxis1 family over row partitions (the generic dask path,
+    dask.py:86-219): a line is one row, so partitions lose nothing and the
+    combined result equals the single-frame one (first / last by global row,
+    which for one line per row is the visit order too)."""
+    cols = _multi_cols(300, 40, 41)
+    xs = [f"x{j}" for j in range(40)]
+    ys = [f"y{j}" for j in range(40)]
+    whole = _line_frame(cols, 0, None)
+    cuts = [0, 1, 77, 150, 299, 300]
+    parts = ds.PartitionedFrame([_line_frame(cols, a, b) for a, b in zip(cuts[:-1], cuts[1:])])
+    aggs = {"count": ds.count(), "sum": ds.sum("v"), "max": ds.max("v"), "any": ds.any()}
+    if lw == 0:
+        aggs.update(first=ds.first("v"), last=ds.last("v"), where=ds.where(ds.min("v")))
+    cvs = ds.Canvas(plot_width=120, plot_height=80)
+    for axis, kx in ((1, xs), (1, np.linspace(0, 1, 40))):
+        for name, agg in aggs.items():
+            got = to_numpy(cvs.line(parts, x=kx, y=ys, axis=axis, agg=agg, line_width=lw))
+            ref = to_numpy(cvs.line(whole, x=kx, y=ys, axis=axis, agg=agg, line_width=lw))
+            rtol = 1e-12 if name == "sum" else (3e-7 if ref.dtype == np.float32 else 0.0)
+            assert_same(got, ref, rtol=rtol, atol=1e-7 if ref.dtype == np.float32 else 0.0, what=name)
+
+
+def test_partitioned_line_axis0_multi_by_partition():
+    """LineAxis0Multi over row partitions: each partition's segments drawn
+    alone (the generic dask path has no overlap for these glyphs), partials
+    combined; first by the smallest global row (a row-index reduction), against
+    the oracle run per partition and combined the reference's way."""
+    import oracle
+    import refcases
+    cols = _multi_cols(500, 3, 43)
+    kw = dict(x=[f"x{j}" for j in range(3)], y=[f"y{j}" for j in range(3)])
+    cuts = [0, 120, 121, 333, 500]
+    parts = ds.PartitionedFrame([_line_frame(cols, a, b) for a, b in zip(cuts[:-1], cuts[1:])])
+    layout, xs, ys = refcases.multi_line_arrays(cols, kw)
+    xr, yr = (0.0, 1.1), (float(ys.min()), float(ys.max()))
+    cvs = ds.Canvas(plot_width=150, plot_height=90, x_range=xr, y_range=yr)
+    specs = [oracle.spec("count"), oracle.spec("max", "v"), oracle.spec("min_row")]
+    partials = [oracle.lines({"v": cols["v"][a:b]}, 1, xs[a:b], ys[a:b], 150, 90, xr, yr, specs, row_offset=a)
+                for a, b in zip(cuts[:-1], cuts[1:])]
+    got = cvs.line(parts, agg=ds.summary(c=ds.count(), m=ds.max("v"), f=ds.first("v")), **kw)
+    assert_same(to_numpy(got["c"]), np.sum([p[0] for p in partials], axis=0).astype(np.uint32))
+    assert_same(to_numpy(got["m"]), np.fmax.reduce(np.stack([p[1] for p in partials]), axis=0))
+    rows = np.stack([np.where(p[2] < 0, np.iinfo(np.int64).max, p[2]) for p in partials]).min(axis=0)
+    want_first = np.where(rows == np.iinfo(np.int64).max, np.nan, cols["v"][np.minimum(rows, 499)])
+    assert_same(to_numpy(got["f"]), want_first)
