@@ -233,6 +233,11 @@ class HostFrame(TensorFrame):
         t = t.cpu().contiguous()
         return t if t.is_pinned() else t.pin_memory()
 
+    def on_device(self):
+        """The same columns as a TensorFrame on the aggregating GPU (one copy
+        each, from the pinned host memory)."""
+        return TensorFrame(self._cols, categories=self._cats, device=self.gpu, row_offset=self.row_offset)
+
 
 def as_frame(source):
     if isinstance(source, (TensorFrame, PartitionedFrame)):
@@ -489,6 +494,9 @@ def bypixel(source, canvas, glyph, agg, *, antialias=False, flags=0):
     if isinstance(frame, PartitionedFrame):
         return partitioned_pipeline(frame, canvas, glyph, agg, flags=flags)
     if isinstance(frame, HostFrame):
+        if not isinstance(glyph, Point):
+            # a line reads its neighbouring vertices and crosses any chunk edge: copy the frame once
+            return gpu_pipeline(frame.on_device(), canvas, glyph, agg, antialias=antialias, flags=flags)
         return streamed_pipeline(frame, canvas, glyph, agg, flags=flags)
     return gpu_pipeline(frame, canvas, glyph, agg, antialias=antialias, flags=flags)
 

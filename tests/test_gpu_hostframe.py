@@ -61,8 +61,31 @@ def test_host_frame_edges():
     assert out.shape == (8, 16) and not out.any()
     h = ds.HostFrame({"x": np.float32([0.5]), "y": np.float32([0.5])}, chunk_rows=1)
     with pytest.raises(NotImplementedError):
-        ds.Canvas(plot_width=8, plot_height=8).line(h, "x", "y")
-    with pytest.raises(NotImplementedError):
         ds.Canvas(plot_width=8, plot_height=8, x_range=(0, 1), y_range=(0, 1)).points(h, "x", "y", deterministic=True)
     with pytest.raises(ValueError):
         ds.HostFrame({"x": np.float32([0.5])}, chunk_rows=0)
+
+
+@pytest.mark.parametrize("lw", [0.0, 1.5])
+def test_host_frame_lines_equal_device_frame(lw):
+    """Canvas.line over a HostFrame: the frame is copied to the GPU once (a line
+    reads its neighbours across any chunk edge), then the device path; equal to
+    the same columns given as a device frame, for LineAxis0 and a multi-line glyph."""
+    from datashader_gb300 import synthetic as S
+    x, y, v, _ = S.time_series_np(6, 400, seed=9)
+    cols = {"x": x, "y": y, "v": v}
+    host = ds.HostFrame(cols, chunk_rows=100)
+    dev = ds.TensorFrame({k: torch.from_numpy(a).cuda() for k, a in cols.items()})
+    cvs = ds.Canvas(plot_width=90, plot_height=60)
+    agg = ds.summary(c=ds.count(), s=ds.sum("v"), m=ds.max("v"))
+    got = cvs.line(host, "x", "y", agg=agg, line_width=lw)
+    ref = cvs.line(dev, "x", "y", agg=agg, line_width=lw)
+    for k in ("c", "s", "m"):
+        assert_same(to_numpy(got[k]), to_numpy(ref[k]), rtol=1e-12 if k == "s" else 0.0, what=k)
+    rng = np.random.default_rng(3)
+    mcols = {f"y{j}": np.cumsum(rng.normal(0, 0.1, 200)) for j in range(4)}
+    mcols["x"] = np.linspace(0, 1, 200)
+    hm = ds.HostFrame(mcols)
+    dm = ds.TensorFrame({k: torch.from_numpy(a).cuda() for k, a in mcols.items()})
+    kw = dict(x="x", y=[f"y{j}" for j in range(4)], axis=0, agg=ds.count(), line_width=lw)
+    assert_same(to_numpy(cvs.line(hm, **kw)), to_numpy(cvs.line(dm, **kw)))
