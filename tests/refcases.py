@@ -321,6 +321,49 @@ def both_lines_cases():
     return src, canvas, out
 
 
+def both_lines_summary_cases():
+    """TestLineAntialiasSummary (test_pandas.py:2802-2890): summaries over the
+    same two lines, mixing self_intersect settings (a plan turns two-stage, and
+    every count / sum in it non-self-intersecting, as soon as one reduction asks
+    for it).  Returns (columns, canvas, cases) with a dict of expected arrays."""
+    src, canvas, _ = both_lines_cases()
+    g = load_golden("line_antialias.json")
+    A = {k: golden_array(v) for k, v in g.items() if k.startswith("line_antialias_sol")}
+    s0, s1, s0i = A["line_antialias_sol_0"], A["line_antialias_sol_1"], A["line_antialias_sol_0_intersect"]
+
+    def nansum(a, b):
+        r = np.nan_to_num(a) + np.nan_to_num(b)
+        r[np.isnan(a) & np.isnan(b)] = np.nan
+        return r
+
+    def nanmin(a, b):
+        r = np.minimum(np.nan_to_num(a, nan=1e10), np.nan_to_num(b, nan=1e10))
+        r[np.isnan(a) & np.isnan(b)] = np.nan
+        return r
+
+    cnt, cnt_i = nansum(s0, s1), nansum(s0i, s1)
+    first = 3 * np.where(np.isnan(s0), s1, s0)
+    last = 3 * np.where(np.isnan(s1), s0, s1)
+    cases = [
+        ("count_sum_intersect_true", ds.summary(count=ds.count("value", self_intersect=True),
+                                                sum=ds.sum("value", self_intersect=True)),
+         {"count": cnt_i, "sum": 3 * cnt_i}),
+        ("count_sum_intersect_false", ds.summary(count=ds.count("value", self_intersect=False),
+                                                 sum=ds.sum("value", self_intersect=False)),
+         {"count": cnt, "sum": 3 * cnt}),
+        ("count_sum_intersect_mixed", ds.summary(count=ds.count("value", self_intersect=True),
+                                                 sum=ds.sum("value", self_intersect=False)),
+         {"count": cnt, "sum": 3 * cnt}),
+        ("count_min", ds.summary(count=ds.count("value", self_intersect=True), min=ds.min("value")),
+         {"count": cnt, "min": 3 * nanmin(s0, s1)}),
+        ("count_first", ds.summary(count=ds.count("value", self_intersect=True), first=ds.first("value")),
+         {"count": cnt, "first": first}),
+        ("count_last", ds.summary(count=ds.count("value", self_intersect=True), last=ds.last("value")),
+         {"count": cnt, "last": last}),
+    ]
+    return src, canvas, [dict(id=f"both_lines_summary_{c}", agg=a, expected=e) for c, a, e in cases]
+
+
 def binary_cmap50():
     """test_antialias.py:40-42 ``cmap01``: matplotlib's ``cm.binary`` sampled at
     np.linspace(0, 1) (50 points), each channel times 255.  matplotlib is not a

@@ -354,3 +354,15 @@ def test_two_stage_categorical_and_y_constant():
         got = to_numpy(cvs.line(frame, agg=red, line_width=1.5, **kw))
         ref = oracle.lines({"v": xcols["v"]}, 2, xs, yconst, 70, 30, (0.0, 1.05), yr, [spec], line_width=1.5)[0]
         assert_same(got, ref)
+
+
+SUMMARY_SRC, SUMMARY_CANVAS, SUMMARY_CASES = refcases.both_lines_summary_cases()
+
+
+@pytest.mark.parametrize("case", SUMMARY_CASES, ids=[c["id"] for c in SUMMARY_CASES])
+def test_both_lines_summary_golden(case):
+    """TestLineAntialiasSummary (test_pandas.py:2802-2890) through the GPU path."""
+    got = ds.Canvas(**SUMMARY_CANVAS).line(_frame(SUMMARY_SRC), x=["x0", "x1"], y=["y0", "y1"], agg=case["agg"],
+                                           line_width=1)
+    for k, exp in case["expected"].items():
+        np.testing.assert_array_almost_equal(to_numpy(got[k]), exp, decimal=5, err_msg=f"{case['id']} {k}")

@@ -243,3 +243,19 @@ def test_oracle_antialias_images(case):
     white = np.array([0xFFFFFFFF], dtype=np.uint32)[0]
     got = composite.over(img, white)
     np.testing.assert_array_equal(got, case["expected"])
+
+
+SUMMARY_SRC, SUMMARY_CANVAS, SUMMARY_CASES = refcases.both_lines_summary_cases()
+
+
+@pytest.mark.parametrize("case", SUMMARY_CASES, ids=[c["id"] for c in SUMMARY_CASES])
+def test_oracle_both_lines_summary_golden(case):
+    from oracle_bridge import specs_of
+    keys, specs, _ = specs_of(case["agg"], SUMMARY_SRC, {})
+    xs = np.stack([SUMMARY_SRC["x0"], SUMMARY_SRC["x1"]], axis=1)
+    ys = np.stack([SUMMARY_SRC["y0"], SUMMARY_SRC["y1"]], axis=1)
+    cv = SUMMARY_CANVAS
+    res = oracle.lines({"value": SUMMARY_SRC["value"]}, 1, xs, ys, cv["plot_width"], cv["plot_height"],
+                       cv["x_range"], cv["y_range"], specs, line_width=1)
+    for k, r in zip(keys, res):
+        np.testing.assert_array_almost_equal(r, case["expected"][k], decimal=5, err_msg=f"{case['id']} {k}")
