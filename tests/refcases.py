@@ -364,6 +364,34 @@ def both_lines_summary_cases():
     return src, canvas, [dict(id=f"both_lines_summary_{c}", agg=a, expected=e) for c, a, e in cases]
 
 
+def antialias_nan_multi_cases():
+    """test_line_antialias_nan (test_pandas.py:2931-3024), the multi-line entries:
+    two lines with a NaN vertex each, float32 columns, on a 12 x 12 canvas over
+    [-1, 11]^2, line_width 2, count(self_intersect=False | True); every layout
+    expects line_antialias_nan_sol_intersect (transposed for YConstant, whose
+    lines run along y).  Each case: (id, kind, columns, kwargs, expected)."""
+    g = load_golden("line_antialias.json")
+    sol = golden_array(g["line_antialias_nan_sol_intersect"])
+    f32 = lambda v: np.asarray(v, dtype=np.float32)    # noqa: E731
+    nan = np.nan
+    a, b = [0.5, 1.5, nan, 4.5, 9.5], [9.5, 8.5, nan, 5.5, 0.5]
+    cases = [
+        ("multi_axis0", dict(x0=f32(a), x1=f32(a), y0=f32(a), y1=f32(b)),
+         dict(x=["x0", "x1"], y=["y0", "y1"], axis=0), sol),
+        ("lines_axis1", {**{f"x{j}": f32([a[j], a[j]]) for j in range(5)},
+                         **{f"y{j}": f32([a[j], b[j]]) for j in range(5)}},
+         dict(x=[f"x{j}" for j in range(5)], y=[f"y{j}" for j in range(5)], axis=1), sol),
+        ("x_constant", {f"y{j}": f32([a[j], b[j]]) for j in range(5)},
+         dict(x=np.array(a), y=[f"y{j}" for j in range(5)], axis=1), sol),
+        ("y_constant", {f"x{j}": f32([a[j], b[j]]) for j in range(5)},
+         dict(y=np.array(a), x=[f"x{j}" for j in range(5)], axis=1), sol.T),
+        ("ragged", dict(x=[list(map(float, f32(a))), list(map(float, f32(a)))],
+                        y=[list(map(float, f32(a))), list(map(float, f32(b)))]),
+         dict(x="x", y="y", axis=1), sol),
+    ]
+    return [dict(id=c, columns=cols, kwargs=kw, expected=e) for c, cols, kw, e in cases]
+
+
 def binary_cmap50():
     """test_antialias.py:40-42 ``cmap01``: matplotlib's ``cm.binary`` sampled at
     np.linspace(0, 1) (50 points), each channel times 255.  matplotlib is not a

@@ -366,3 +366,21 @@ def test_both_lines_summary_golden(case):
                                            line_width=1)
     for k, exp in case["expected"].items():
         np.testing.assert_array_almost_equal(to_numpy(got[k]), exp, decimal=5, err_msg=f"{case['id']} {k}")
+
+
+NAN_CASES = refcases.antialias_nan_multi_cases()
+
+
+@pytest.mark.parametrize("si", [False, True])
+@pytest.mark.parametrize("case", NAN_CASES, ids=[c["id"] for c in NAN_CASES])
+def test_antialias_nan_multi_golden(case, si):
+    """test_line_antialias_nan's multi-line entries (test_pandas.py:2931-3024):
+    end caps at NaN vertices; self_intersect=False is a two-stage plan."""
+    cols = case["columns"]
+    if case["id"] == "ragged":
+        frame = ds.TensorFrame({k: ds.RaggedColumn(v) for k, v in cols.items()})
+    else:
+        frame = ds.TensorFrame({k: torch.from_numpy(v).cuda() for k, v in cols.items()})
+    cvs = ds.Canvas(plot_width=12, plot_height=12, x_range=(-1, 11), y_range=(-1, 11))
+    got = to_numpy(cvs.line(frame, line_width=2, agg=ds.count(self_intersect=si), **case["kwargs"]))
+    np.testing.assert_array_almost_equal(got, case["expected"], decimal=5)

@@ -259,3 +259,19 @@ def test_oracle_both_lines_summary_golden(case):
                        cv["x_range"], cv["y_range"], specs, line_width=1)
     for k, r in zip(keys, res):
         np.testing.assert_array_almost_equal(r, case["expected"][k], decimal=5, err_msg=f"{case['id']} {k}")
+
+
+NAN_CASES = refcases.antialias_nan_multi_cases()
+
+
+@pytest.mark.parametrize("si", [False, True])
+@pytest.mark.parametrize("case", NAN_CASES, ids=[c["id"] for c in NAN_CASES])
+def test_oracle_antialias_nan_multi_golden(case, si):
+    spec = oracle.spec("count", self_intersect=si)
+    cols, kw = case["columns"], case["kwargs"]
+    if case["id"] == "ragged":
+        got = oracle.lines_ragged({}, cols["x"], cols["y"], 12, 12, (-1, 11), (-1, 11), [spec], line_width=2)[0]
+    else:
+        layout, xs, ys = refcases.multi_line_arrays(cols, kw)
+        got = oracle.lines({}, layout, xs, ys, 12, 12, (-1, 11), (-1, 11), [spec], line_width=2)[0]
+    np.testing.assert_array_almost_equal(got, case["expected"], decimal=5)
