@@ -9,7 +9,8 @@ Reads (as text, via ``ast``; nothing from the reference is imported or run):
 * ``datashader/tests/test_pandas.py`` -- the multi-line cases of
   ``line_manual_range_params`` / ``line_autorange_params`` (ragged-array
   entries skipped) and the ``sol`` arrays of ``test_line_manual_range``,
-  ``test_line_autorange``, ``test_line_autorange_axis1_x_constant`` and
+  ``test_line_autorange``, ``test_line_autorange_axis1_x_constant``,
+  ``test_line_autorange_axis1_ragged`` and
   ``test_line_agg_sum_axis1_none_constant`` (with its frame);
 * ``datashader/tests/test_transfer_functions.py`` -- ``eq_hist_sol`` and
   ``eq_hist_sol_rescale_discrete_levels`` (uint32 RGBA images), the
@@ -198,7 +199,8 @@ def main(ref_root):
         lines[name] = {"source": f"datashader/tests/test_pandas.py:{line}", "cases": cases}
     for fn, sols in _function_all_sols(pandas_path, ("test_line_manual_range", "test_line_autorange",
                                                      "test_line_autorange_axis1_x_constant",
-                                                     "test_line_agg_sum_axis1_none_constant")).items():
+                                                     "test_line_agg_sum_axis1_none_constant",
+                                                     "test_line_autorange_axis1_ragged")).items():
         lines[fn] = [dict(_jsonable(np.asarray(v)), source=f"datashader/tests/test_pandas.py:{ln}") for v, ln in sols]
     with open(os.path.join(HERE, "lines_multi.json"), "w") as f:
         json.dump(lines, f, indent=0)

@@ -384,3 +384,51 @@ def test_antialias_nan_multi_golden(case, si):
     cvs = ds.Canvas(plot_width=12, plot_height=12, x_range=(-1, 11), y_range=(-1, 11))
     got = to_numpy(cvs.line(frame, line_width=2, agg=ds.count(self_intersect=si), **case["kwargs"]))
     np.testing.assert_array_almost_equal(got, case["expected"], decimal=5)
+
+
+def _ragged_autorange_frame():
+    """test_line_autorange_axis1_ragged (test_pandas.py:1935-1966): two float32 ragged rows."""
+    x = [[4.0, 0.0], [0.0, -4.0, 0.0, 4.0]]
+    y = [[0.0, -4.0], [-4.0, 0.0, 4.0, 0.0]]
+    return x, y
+
+
+def test_ragged_autorange_golden():
+    x, y = _ragged_autorange_frame()
+    frame = ds.TensorFrame({"x": ds.RaggedColumn(x), "y": ds.RaggedColumn(y)})
+    agg = ds.Canvas(plot_width=9, plot_height=9).line(frame, "x", "y", ds.count(), axis=1)
+    sol = refcases.golden_array(refcases.lines_golden("test_line_autorange_axis1_ragged")[0])
+    np.testing.assert_array_equal(to_numpy(agg), sol)
+    assert agg.x_range == (-4.0, 4.0) and agg.y_range == (-4.0, 4.0)
+
+
+@pytest.mark.parametrize("si", [False, True])
+def test_antialias_duplicate_points(si):
+    """test_line_antialias_duplicate_points (test_pandas.py:3050-3064): a repeated
+    vertex draws the same image as the line without it (no division by zero)."""
+    cvs = ds.Canvas(plot_width=10, plot_height=10, x_range=(-0.1, 1.1), y_range=(0.9, 2.1))
+    a = cvs.line(_frame({"x": [0.0, 1.0], "y": [1.0, 2.0]}), "x", "y", line_width=1, agg=ds.count(self_intersect=si))
+    b = cvs.line(_frame({"x": [0.0, 0.0, 1.0], "y": [1.0, 1.0, 2.0]}), "x", "y", line_width=1,
+                 agg=ds.count(self_intersect=si))
+    np.testing.assert_array_equal(to_numpy(a), to_numpy(b))
+
+
+def test_line_coordinate_lengths():
+    """test_line_coordinate_lengths (test_pandas.py:3310-3334): mismatched x / y
+    lists or constant arrays raise ValueError('x and y coordinate lengths do not match')."""
+    cvs = ds.Canvas(plot_width=10, plot_height=6)
+    msg = r"^x and y coordinate lengths do not match"
+    df = _frame(dict(x0=[0, 0.2, 1], y0=[0, 0.4, 1], x1=[0, 0.6, 1], y1=[1, 0.8, 1]))
+    for axis in (0, 1):
+        with pytest.raises(ValueError, match=msg):
+            cvs.line(source=df, x=["x0"], y=["y0", "y1"], axis=axis)
+        with pytest.raises(ValueError, match=msg):
+            cvs.line(source=df, x=["x0", "x1"], y=["y0"], axis=axis)
+    df = _frame(dict(y0=[0, 1, 0, 1], y1=[0, 1, 1, 0]))
+    for nx in (1, 3):
+        with pytest.raises(ValueError, match=msg):
+            cvs.line(source=df, x=np.arange(nx), y=["y0", "y1"], axis=1)
+    df = _frame(dict(x0=[0, 1, 0, 1], x1=[0, 1, 1, 0]))
+    for ny in (1, 3):
+        with pytest.raises(ValueError, match=msg):
+            cvs.line(source=df, x=["x0", "x1"], y=np.arange(ny), axis=1)

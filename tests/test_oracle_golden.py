@@ -275,3 +275,22 @@ def test_oracle_antialias_nan_multi_golden(case, si):
         layout, xs, ys = refcases.multi_line_arrays(cols, kw)
         got = oracle.lines({}, layout, xs, ys, 12, 12, (-1, 11), (-1, 11), [spec], line_width=2)[0]
     np.testing.assert_array_almost_equal(got, case["expected"], decimal=5)
+
+
+def test_oracle_ragged_autorange_golden():
+    """test_line_autorange_axis1_ragged (test_pandas.py:1935-1966)."""
+    x = [[4.0, 0.0], [0.0, -4.0, 0.0, 4.0]]
+    y = [[0.0, -4.0], [-4.0, 0.0, 4.0, 0.0]]
+    got = oracle.lines_ragged({}, x, y, 9, 9, None, None, [oracle.spec("count")])[0]
+    np.testing.assert_array_equal(got, refcases.golden_array(refcases.lines_golden("test_line_autorange_axis1_ragged")[0]))
+
+
+@pytest.mark.parametrize("si", [False, True])
+def test_oracle_antialias_duplicate_points(si):
+    """test_line_antialias_duplicate_points (test_pandas.py:3050-3064)."""
+    spec = [oracle.spec("count", self_intersect=si)]
+    a = oracle.line_axis0({"x": np.array([0.0, 1.0]), "y": np.array([1.0, 2.0])}, "x", "y", 10, 10, (-0.1, 1.1),
+                          (0.9, 2.1), spec, line_width=1)[0]
+    b = oracle.line_axis0({"x": np.array([0.0, 0.0, 1.0]), "y": np.array([1.0, 1.0, 2.0])}, "x", "y", 10, 10,
+                          (-0.1, 1.1), (0.9, 2.1), spec, line_width=1)[0]
+    np.testing.assert_array_equal(a, b)
