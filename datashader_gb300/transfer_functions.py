@@ -153,6 +153,21 @@ def _run_shade(data, how, cmap, alpha, min_alpha, span, stream=None):
     return rgba
 
 
+def _shade_input(data):
+    """The aggregate as the kernels take it: uint32 or float64.  A bool
+    aggregate (any()) becomes 0 / 1 uint32, which masks and offsets exactly as
+    the reference's bool prologue (mask = ~data, data as int8, offset 1:
+    transfer_functions/__init__.py:263-268); a float32 one (antialiased count /
+    any) is widened to float64 exactly (the reference subtracts the offset and
+    applies log1p / cbrt in float32, so those steps can differ in the last
+    float32 bit, one colour step at most)."""
+    if data.dtype == torch.bool:
+        return data.to(torch.int32).view(torch.uint32)
+    if data.dtype == torch.float32:
+        return data.to(torch.float64)
+    return data
+
+
 def shade(agg, cmap=("lightblue", "darkblue"), color_key=None, how="eq_hist", alpha=255,
           min_alpha=40, span=None, name=None, color_baseline=None, rescale_discrete_levels=False):
     """tf.shade for a 2-D aggregate (transfer_functions/__init__.py:616-745):
@@ -165,10 +180,11 @@ def shade(agg, cmap=("lightblue", "darkblue"), color_key=None, how="eq_hist", al
         raise ValueError(f"min_alpha ({min_alpha}) and alpha ({alpha}) must be between 0 and 255")
     if agg.ndim != 2:
         raise NotImplementedError("only 2-D aggregates are shaded on the GPU path")
+    data = _shade_input(agg.data)
     if how in _HOW_CODE:
         if span is not None and not span[0] <= span[1]:
             raise ValueError("span must be (low, high)")
-        rgba = _run_shade(agg.data, how, cmap, alpha, min_alpha, span)
+        rgba = _run_shade(data, how, cmap, alpha, min_alpha, span)
         return Image(rgba, agg.dims, agg.coords, agg.attrs, name=name)
     if how != "eq_hist":
         raise ValueError(f"Unknown interpolation method: {how}")
@@ -176,7 +192,7 @@ def shade(agg, cmap=("lightblue", "darkblue"), color_key=None, how="eq_hist", al
         raise ValueError("span is not (yet) valid to use with eq_hist")
     if isinstance(cmap, str) or not isinstance(cmap, (list, tuple)):
         raise NotImplementedError("only list colormaps are on the GPU path")
-    _, _, rgba = _run_eq_hist(agg.data, cmap=list(cmap), alpha=alpha,
+    _, _, rgba = _run_eq_hist(data, cmap=list(cmap), alpha=alpha,
                               rescale_discrete_levels=rescale_discrete_levels)
     return Image(rgba, agg.dims, agg.coords, agg.attrs, name=name)
 

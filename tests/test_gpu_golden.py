@@ -16,6 +16,7 @@ import pytest
 import datashader_gb300 as ds
 import oracle
 import refcases
+from datashader_gb300 import synthetic
 from gpu_helpers import assert_same, frame_from_numpy, to_numpy
 from oracle_bridge import run_line, run_points
 
@@ -176,3 +177,33 @@ def test_gpu_antialias_images(case):
     img = ds.tf.set_background(ds.tf.shade(agg, cmap=refcases.binary_cmap50()), "#ffffff")
     got = img.data.view(torch.int32).cpu().numpy().view(np.uint32)
     np.testing.assert_array_equal(got, case["expected"], err_msg=case["id"])
+
+
+def test_gpu_shade_bool_golden():
+    """test_shade_bool (test_transfer_functions.py:260-272): a bool aggregate, every
+    `how`, cmap ['pink', 'red'] -> opaque red where True, transparent elsewhere."""
+    data = ~np.eye(3, dtype=bool)
+    agg = ds.Aggregate(torch.from_numpy(data).cuda(), ["y", "x"], {}, {})
+    sol = np.where(data, 4278190335, 0).astype(np.uint32)
+    for how in ("log", "cbrt", "linear", "eq_hist"):
+        img = ds.tf.shade(agg, cmap=["pink", "red"], how=how)
+        np.testing.assert_array_equal(img.data.view(torch.int32).cpu().numpy().view(np.uint32), sol, err_msg=how)
+
+
+@pytest.mark.parametrize("how", ["linear", "log", "cbrt", "eq_hist"])
+def test_gpu_shade_float32_line_aggregate(how):
+    """Shading the float32 aggregate of an antialiased line count: against the
+    oracle's numpy restatement run on the float32 array itself, within one colour
+    step per channel (the reference's float32 offset / log1p / cbrt steps)."""
+    x, y, v, _ = synthetic.time_series_np(20, 300, seed=5)
+    agg = ds.Canvas(plot_width=160, plot_height=90).line(frame_from_numpy({"x": x, "y": y}), "x", "y",
+                                                         agg=ds.count(), line_width=1.5)
+    assert agg.data.dtype == torch.float32
+    img = ds.tf.shade(agg, cmap=["lightblue", "darkblue"], how=how)
+    got = img.data.view(torch.int32).cpu().numpy().view(np.uint32)
+    a = agg.data.cpu().numpy()
+    ref = (oracle.shade_eq_hist(a, ["lightblue", "darkblue"]) if how == "eq_hist"
+           else oracle.shade_interp(a, how=how, cmap=["lightblue", "darkblue"]))
+    g8, r8 = got.view(np.uint8).astype(int), ref.view(np.uint8).astype(int)
+    assert np.abs(g8 - r8).max() <= 1
+    assert (got != ref).mean() < 0.01
