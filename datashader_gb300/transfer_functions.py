@@ -153,6 +153,21 @@ def _run_shade(data, how, cmap, alpha, min_alpha, span, stream=None):
     return rgba
 
 
+def _check_cmap(cmap):
+    """Colour validation before any device work: colors.rgb's ValueError /
+    TypeError for an unknown colour (colors.py:99-126), and a ValueError for an
+    empty list (the reference fails unpacking its channels,
+    transfer_functions/__init__.py:317-320)."""
+    if isinstance(cmap, str) or (isinstance(cmap, tuple) and len(cmap) == 3 and not isinstance(cmap[0], str)):
+        rgb(cmap)
+        return
+    if isinstance(cmap, (list, tuple)):
+        if len(cmap) == 0:
+            raise ValueError("not enough values to unpack: the colormap is empty")
+        for c in cmap:
+            rgb(c)
+
+
 def _shade_input(data):
     """The aggregate as the kernels take it: uint32 or float64.  A bool
     aggregate (any()) becomes 0 / 1 uint32, which masks and offsets exactly as
@@ -180,6 +195,7 @@ def shade(agg, cmap=("lightblue", "darkblue"), color_key=None, how="eq_hist", al
         raise ValueError(f"min_alpha ({min_alpha}) and alpha ({alpha}) must be between 0 and 255")
     if agg.ndim != 2:
         raise NotImplementedError("only 2-D aggregates are shaded on the GPU path")
+    _check_cmap(cmap)
     data = _shade_input(agg.data)
     if how in _HOW_CODE:
         if span is not None and not span[0] <= span[1]:
