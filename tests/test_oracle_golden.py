@@ -294,3 +294,23 @@ def test_oracle_antialias_duplicate_points(si):
     b = oracle.line_axis0({"x": np.array([0.0, 0.0, 1.0]), "y": np.array([1.0, 1.0, 2.0])}, "x", "y", 10, 10,
                           (-0.1, 1.1), (0.9, 2.1), spec, line_width=1)[0]
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("kind", ["first", "count", "min", "where_last", "mean", "sum"])
+def test_oracle_two_stage_ragged_equals_axis1(kind):
+    """Property of the two restated loops: ragged rows that all have the same
+    length are a LinesAxis1 frame, so their two-stage results agree exactly
+    (line.py:1300-1318 against :1616-1693)."""
+    rng = np.random.default_rng(5)
+    xs = np.linspace(0, 1, 40)[None, :] + rng.normal(0, 0.002, (25, 40))
+    ys = np.cumsum(rng.normal(0, 0.05, (25, 40)), axis=1)
+    ys[rng.random(ys.shape) < 0.03] = np.nan
+    v = rng.uniform(0, 1, 25)
+    xr, yr = (0.0, 1.0), (float(np.nanmin(ys)), float(np.nanmax(ys)))
+    spec = {"first": oracle.spec("first", "v"), "count": oracle.spec("count", self_intersect=False),
+            "min": oracle.spec("min", "v"), "where_last": oracle.spec("where", selector=oracle.spec("last", "v")),
+            "mean": oracle.spec("mean", "v"), "sum": oracle.spec("sum", "v", self_intersect=False)}[kind]
+    specs = [spec, oracle.spec("first", "v")]                # first makes every plan two-stage
+    a = oracle.lines({"v": v}, 2, xs, ys, 50, 40, xr, yr, specs, line_width=1.5)[0]
+    b = oracle.lines_ragged({"v": v}, list(xs), list(ys), 50, 40, xr, yr, specs, line_width=1.5)[0]
+    np.testing.assert_array_equal(a, b)
