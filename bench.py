@@ -48,19 +48,29 @@ def workload(n):
             "1024x1024 canvas over [-4,4]^2")
 
 
-# DRAM bytes (read + write) of one hot-tile count launch, from an ncu capture
-# of cached_main at 2e7 rows (163.31 MB read, 3.09 MB written; profiles/
-# cached_main_count_2e7_1024_full.md): reads scale with rows, writes with the
-# touched pixels of the 1024x1024 canvas.
+# DRAM bytes (read + write) of one hot-tile count launch, measured by ncu on a
+# 2e7-row launch of the same kernel (163.31 MB read, 3.09 MB written): reads
+# scale with rows, writes with the touched pixels of the 1024x1024 canvas.
 def count_traffic(n):
     return 163.31e6 / 2e7 * n + 3.09e6
 
 
-# The same for the hot-tile mean('v') launch (x/y float32 + v float64), from
-# an ncu capture of cached_mean_main at 2e7 rows (329.75 MB read, 3.51 MB
-# written; profiles/cached_mean_main_mean_2e7_1024_full.md).
+# The same for the hot-tile mean('v') launch (x/y float32 + v float64): ncu on
+# a 2e7-row launch (329.75 MB read, 3.51 MB written).
 def mean_traffic(n):
     return 329.75e6 / 2e7 * n + 3.51e6
+
+
+def bench_config(n, world):
+    """The config dict both arms print (the driver compares them)."""
+    return {"workload": workload(n), "n_points": n, "canvas": [1024, 1024], "x_range": [-4, 4],
+            "coords": "float32", "reduction": "count",
+            "l2": "inputs (800 MB) larger than L2, no flush",
+            "parallelism": "replicas" if world > 1 else "one device"}
+
+
+CFG1 = {"workload": "Canvas.points count, 10,000,000 float64 points (5-Gaussian mixture), 512x512 canvas over "
+                    "[-4,4]^2", "n_points": 10_000_000, "canvas": [512, 512], "coords": "float64"}
 
 
 def measured_peak():
@@ -172,8 +182,7 @@ def _oracle_count_threads(xs, ys, threads, width, height, x_range, y_range):
 
 def cpu_baseline(sample_n=20_000_000, threads=1):
     from datashader_gb300 import synthetic
-    x, y = synthetic.gaussian_mixture_np(sample_n, seed=0, dtype=np.float32)
-    xs, ys = x.astype(np.float64), y.astype(np.float64)
+    xs, ys = synthetic.gaussian_mixture_np(sample_n, seed=0, dtype=np.float32)
     _oracle_count_threads(xs[:100_000], ys[:100_000], 1, 1024, 1024, (-4, 4), (-4, 4))   # warm
     t0 = time.perf_counter()
     _oracle_count_threads(xs, ys, threads, 1024, 1024, (-4, 4), (-4, 4))
@@ -181,33 +190,59 @@ def cpu_baseline(sample_n=20_000_000, threads=1):
     return sample_n / dt / 1e9, dt
 
 
+def _oracle_mean_threads(xs, ys, vs, threads):
+    import oracle
+    return oracle.points_parallel({"x": xs, "y": ys, "v": vs}, "x", "y", 1024, 1024, (-4, 4), (-4, 4),
+                                  [oracle.spec("mean", "v")], threads=threads)[0]
+
+
 def run_reference(args):
+    """The reference's CPU algorithm (the oracle port of datashader's numba
+    loop) over the same workload: float32 x/y read as float32 and widened in
+    the loop as numba does, one row partition per host thread, partials
+    summed as datashader's dask path does."""
     world, rank, _ = _dist_init(args)
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     from datashader_gb300 import synthetic
     n = min(args.n, args.reference_sample)
-    x, y = synthetic.gaussian_mixture_np(n, seed=0, dtype=np.float32)
-    xs, ys = x.astype(np.float64), y.astype(np.float64)
-    for _ in range(args.warmup):
-        _oracle_count_threads(xs, ys, threads, 1024, 1024, (-4, 4), (-4, 4))
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        _oracle_count_threads(xs, ys, threads, 1024, 1024, (-4, 4), (-4, 4))
-    dt = time.perf_counter() - t0
-    v = n * args.steps / dt / 1e9
-    sample = f"{n} rows of the same distribution per step, {threads} threads, one row partition per thread"
+    xs, ys = synthetic.gaussian_mixture_np(n, seed=0, dtype=np.float32)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fn()
+        return (time.perf_counter() - t0) / steps
+
+    dt = timed(lambda: _oracle_count_threads(xs, ys, threads, 1024, 1024, (-4, 4), (-4, 4)),
+               args.steps, args.warmup)
+    v = n / dt / 1e9
+    extras = {}
+    if args.ref_extras:
+        vs = np.random.default_rng(1).lognormal(0.0, 1.0, n)
+        mdt = timed(lambda: _oracle_mean_threads(xs, ys, vs, threads), max(1, args.steps // 4), 1)
+        extras["mean"] = {"value": n / mdt / 1e9, "unit": "Gpoints/s", "ms_per_step": mdt * 1e3}
+        del vs
+        x1, y1 = synthetic.gaussian_mixture_np(CFG1["n_points"], seed=0, dtype=np.float64)
+        cdt = timed(lambda: _oracle_count_threads(x1, y1, threads, 512, 512, (-4, 4), (-4, 4)),
+                    max(1, args.steps // 4), 1)
+        extras["cfg1"] = dict(CFG1, value=CFG1["n_points"] / cdt / 1e9, unit="Gpoints/s", ms_per_step=cdt * 1e3)
+    sample = (f"all {n:,} rows of the workload per step (float32 x/y), {threads} threads, one row partition "
+              "per thread")
     line = {"metric": METRIC, "value": v, "unit": "Gpoints/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": workload(n), "n_points": n, "canvas": [1024, 1024]},
+            "config": bench_config(n, world),
             "cpu_baseline": {"value": v, "unit": "Gpoints/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "datashader cannot be imported here (numba/pandas/xarray absent): the timed CPU "
                     "implementation is the C restatement of its numba CPU loop (oracle/)"}
+    line.update(extras)
     print(json.dumps(line))
     return 0
 
@@ -550,8 +585,50 @@ def run_gpu(args):
            "path": f"HostFrame streamed in chunks of {hframe.chunk_rows} rows",
            "copy_then_compute_gpoints_per_s": n * world * args.steps / ctc_s / 1e9}
 
+    # ---- parity of the timed workload (untimed): the 1e8-row count against the
+    # oracle on every host thread, bit for bit
+    parity = None
+    if rank == 0 and args.parity:
+        import oracle
+        got = step_count().data.view(torch.int32).cpu().numpy().view(np.uint32)
+        t0 = time.perf_counter()
+        ref = oracle.points_parallel({"x": xh.numpy(), "y": yh.numpy()}, "x", "y", 1024, 1024, (-4, 4), (-4, 4),
+                                     [oracle.spec("count")])[0]
+        parity = {"count_bit_exact_vs_oracle": bool(np.array_equal(got, ref)), "rows": n,
+                  "oracle_threads": os.cpu_count() or 1, "oracle_s": round(time.perf_counter() - t0, 3)}
+
     del x, y, v, cat, frame, xh, yh, xd, yd, hframe
     torch.cuda.empty_cache()
+
+    # ---- the 1e7 float64 512^2 count configuration
+    cfg1 = None
+    if args.cfg1:
+        n1 = CFG1["n_points"]
+        x1, y1 = synthetic.gaussian_mixture_torch(n1, seed=rank, dtype=torch.float64, device=dev)
+        f1 = ds.TensorFrame({"x": x1, "y": y1})
+        c1 = ds.Canvas(plot_width=512, plot_height=512, x_range=(-4, 4), y_range=(-4, 4))
+        for _ in range(3):
+            c1.points(f1, "x", "y", ds.count())
+        t1 = _events_time(lambda: c1.points(f1, "x", "y", ds.count()), args.steps, stream)
+        ms1 = sum(t1) / len(t1)
+        alg1 = n1 * 16 + 512 * 512 * 4
+        cfg1 = dict(CFG1, value=n1 / (ms1 / 1e3) / 1e9, unit="Gpoints/s", ms_per_step=ms1,
+                    roofline={"bound": "hbm", "achieved": alg1 / (ms1 / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                              "frac": alg1 / (ms1 / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
+                              "algorithmic_bytes_per_step": alg1,
+                              "note": "16 B/point (x, y float64) + 4 B/pixel, public API call time"})
+        if rank == 0 and not args.no_cpu_baseline:
+            import oracle
+            xn, yn = x1.cpu().numpy(), y1.cpu().numpy()
+            t0 = time.perf_counter()
+            r1 = oracle.points({"x": xn, "y": yn}, "x", "y", 512, 512, (-4, 4), (-4, 4), [oracle.spec("count")])[0]
+            dt1 = time.perf_counter() - t0
+            cfg1["cpu_baseline"] = {"value": n1 / dt1 / 1e9, "unit": "Gpoints/s", "cores": 1, "kind": "port",
+                                    "sample": f"all {n1:,} rows, one thread, {dt1:.2f} s"}
+            g1 = c1.points(f1, "x", "y", ds.count()).data.view(torch.int32).cpu().numpy().view(np.uint32)
+            cfg1["count_bit_exact_vs_oracle"] = bool(np.array_equal(g1, r1))
+        del x1, y1, f1
+        torch.cuda.empty_cache()
     extras = {}
     if world == 1 and args.pyramid_n > 0:
         extras["pyramid"] = bench_pyramid(args, dev, peak, peak_kind)
@@ -577,10 +654,7 @@ def run_gpu(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": workload(n), "n_points": n, "canvas": [1024, 1024],
-                       "x_range": [-4, 4], "coords": "float32", "reduction": "count",
-                       "l2": "inputs (800 MB) larger than L2, no flush",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": bench_config(n, world),
             "roofline": {k: rl_count[k] for k in ("bound", "achieved", "peak", "unit", "frac", "traffic")},
             "roofline_detail": rl_count,
             "mean": {"value": n / (mean_ms / 1e3) / 1e9, "unit": "Gpoints/s", "ms_per_step": mean_ms,
@@ -589,6 +663,8 @@ def run_gpu(args):
                          "reductions": "count,sum,mean,max,min,first,where(max),by(cat,count) + eq_hist"},
             "cpu_baseline": base,
             "e2e": e2e,
+            "parity": parity,
+            "cfg1": cfg1,
             "gpu_launches": args.steps * kernels_per_count,
             "clocks": clk.summary(),
         }
@@ -609,6 +685,9 @@ def main():
     ap.add_argument("--n", type=int, default=100_000_000)
     ap.add_argument("--cpu-sample", type=int, default=20_000_000)
     ap.add_argument("--reference-sample", type=int, default=100_000_000)
+    ap.add_argument("--ref-extras", type=int, default=1, help="reference arm: also time mean and the 512^2 config")
+    ap.add_argument("--parity", type=int, default=1, help="compare the timed count with the oracle (untimed)")
+    ap.add_argument("--cfg1", type=int, default=1, help="also time the 1e7 float64 512^2 count configuration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--pyramid-n", type=int, default=200_000_000, help="0 skips the tile-pyramid workload")
     ap.add_argument("--serving-n", type=int, default=500_000_000, help="0 skips the viewport workload")

@@ -15,6 +15,7 @@ Usage mirrors ``import datashader as ds``::
 from __future__ import annotations
 
 from .core import Canvas, TensorFrame, PartitionedFrame, HostFrame, RaggedColumn, Aggregate, AggregateSet, bypixel, LinearAxis, LogAxis  # noqa: F401
+from .core import debug_checks, check_device_status  # noqa: F401
 from .reductions import (  # noqa: F401
     count, any, sum, mean, min, max, first, last, where, by, count_cat, summary,
     _sum_zero, _count_ignore_antialiasing, _min_row_index, _max_row_index,

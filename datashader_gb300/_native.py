@@ -134,10 +134,12 @@ FOLD_WHERE_MAX, FOLD_WHERE_MIN, FOLD_WHERE_FIRST, FOLD_WHERE_LAST = range(9, 13)
 
 FLAG_NO_INIT, FLAG_NO_FINALIZE, FLAG_EXACT_BIN, FLAG_WARP_AGG, FLAG_DETERMINISTIC = 0x1, 0x2, 0x4, 0x8, 0x10
 FLAG_ROW_ORDER = 0x20
+FLAG_DEBUG_CHECKS = 0x40
+STATUS_CAS_GUARD, STATUS_INDEX = 0x1, 0x2
 
 # every symbol include/dsgb.h declares
 EXPORTED = (
-    "dsgb_abi_version", "dsgb_last_error", "dsgb_device_sm_count", "dsgb_bases_init", "dsgb_combine",
+    "dsgb_abi_version", "dsgb_last_error", "dsgb_device_status", "dsgb_device_sm_count", "dsgb_bases_init", "dsgb_combine",
     "dsgb_finalize", "dsgb_finalize_partitioned", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_workspace_size_flags",
     "dsgb_points_ws", "dsgb_points_segments",
     "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_workspace_size", "dsgb_line_axis0_ws", "dsgb_lines", "dsgb_lines_2stage", "dsgb_lines_ragged", "dsgb_lines_ragged_2stage", "dsgb_line_axis0_backward", "dsgb_line_axis0_backward_ws",
@@ -160,6 +162,7 @@ def _declare(L):
     L.dsgb_abi_version.restype = ctypes.c_int
     L.dsgb_last_error.restype = ctypes.c_char_p
     L.dsgb_device_sm_count.restype = ctypes.c_int
+    L.dsgb_device_status.argtypes = [ctypes.POINTER(u32), i32]
     L.dsgb_bases_init.argtypes = [PB, i32, i64, P]
     L.dsgb_combine.argtypes = [PB, PB, i32, i64, P]
     L.dsgb_finalize.argtypes = [PC, i32, i64, PB, i32, PO, i32, i64, P]
@@ -235,6 +238,13 @@ def lib(build_if_missing: bool = True):
                 build()
             _lib = _declare(ctypes.CDLL(LIB_PATH))
     return _lib
+
+
+def device_status(clear: bool = True) -> int:
+    """Wait for the current device and return the DSGB_STATUS_* bits its kernels raised."""
+    bits = ctypes.c_uint32(0)
+    check(lib().dsgb_device_status(ctypes.byref(bits), int(clear)), "dsgb_device_status")
+    return int(bits.value)
 
 
 def check(rc: int, what: str = "dsgb call"):

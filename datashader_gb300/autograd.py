@@ -45,7 +45,11 @@ class _PointsAgg(torch.autograd.Function):
         red = rd.mean("v") if mean else rd.sum("v")
         out = Canvas(canvas.plot_width, canvas.plot_height, x_range, y_range).points(
             frame, "x", "y", rd.summary(agg=red, cnt=rd.count("v")))
-        ctx.save_for_backward(x, y, v)
+        # The frame's columns are contiguous and on the aggregation device: the
+        # backward kernel reads these, never the caller's (possibly strided,
+        # expanded or host) tensors.
+        ctx.save_for_backward(frame["x"], frame["y"], frame["v"])
+        ctx.v_like = (v.dtype, v.device)
         ctx.canvas = canvas
         ctx.counts = out["cnt"].data if mean else None
         return out["agg"].data
@@ -64,7 +68,8 @@ class _PointsAgg(torch.autograd.Function):
                                              counts, gv.data_ptr(), 0,
                                              torch.cuda.current_stream(v.device).cuda_stream),
                 "dsgb_points_backward")
-        return gv.to(v.dtype), None, None, None, None
+        dtype, device = ctx.v_like
+        return gv.to(device=device, dtype=dtype), None, None, None, None
 
 
 def points_sum(x, y, v, canvas):
@@ -86,7 +91,9 @@ class _LineSum(torch.autograd.Function):
         frame = TensorFrame({"x": x, "y": y.detach(), "v": v.detach()})
         out = Canvas(canvas.plot_width, canvas.plot_height, x_range, y_range).line(
             frame, "x", "y", agg=rd.sum("v"), line_width=line_width)
-        ctx.save_for_backward(x, y, v)
+        # contiguous device copies (the frame's columns), as in _PointsAgg
+        ctx.save_for_backward(frame["x"], frame["y"], frame["v"])
+        ctx.like = ((v.dtype, v.device), (y.dtype, y.device))
         ctx.canvas = canvas
         ctx.line_width = line_width
         return out.data
@@ -109,7 +116,8 @@ class _LineSum(torch.autograd.Function):
                                               grad.data_ptr(), None, gv.data_ptr(), gy.data_ptr(),
                                               ws.data_ptr(), wsz, torch.cuda.current_stream(v.device).cuda_stream),
                 "dsgb_line_axis0_backward_ws")
-        return gv.to(v.dtype), gy.to(y.dtype), None, None, None
+        (vd, vdev), (yd, ydev) = ctx.like
+        return gv.to(device=vdev, dtype=vd), gy.to(device=ydev, dtype=yd), None, None, None
 
 
 def line_sum(x, y, v, canvas, line_width=1.5):

@@ -302,6 +302,63 @@ class LogAxis(Axis):
 _axis_lookup = {"linear": LinearAxis(), "log": LogAxis()}
 
 
+# ------------------------------------------------------------ instrumentation
+
+class _NvtxRange:
+    """An NVTX range (visible in Nsight Systems / ncu --nvtx) around one
+    pipeline stage; a no-op when torch has no NVTX support."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        try:
+            torch.cuda.nvtx.range_push(self.name)
+            self.pushed = True
+        except Exception:
+            self.pushed = False
+        return self
+
+    def __exit__(self, *exc):
+        if self.pushed:
+            torch.cuda.nvtx.range_pop()
+
+
+_DEBUG = [False]
+
+
+class debug_checks:
+    """Within this context (or after ``debug_checks(True)`` without ``with``),
+    every Canvas.points / Canvas.line call checks each append's aggregate
+    index on the device (``DSGB_FLAG_DEBUG_CHECKS``: the generic kernels,
+    no hot-tile path), then waits for the device and raises ``DsgbError`` if
+    any kernel raised a status bit (an index outside its base, a CAS loop at
+    its iteration guard).  The reference's numba appends are unchecked."""
+
+    def __init__(self, enabled=True):
+        self.prev = _DEBUG[0]
+        _DEBUG[0] = bool(enabled)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        _DEBUG[0] = self.prev
+
+
+def _raise_on_status(bits):
+    if bits:
+        names = [n for b, n in ((N.STATUS_CAS_GUARD, "a where() CAS loop reached its iteration guard"),
+                                (N.STATUS_INDEX, "an append index fell outside its aggregate")) if bits & b]
+        raise N.DsgbError(f"device status {bits:#x}: " + "; ".join(names))
+
+
+def check_device_status(clear=True):
+    """Wait for the device and raise ``DsgbError`` if a kernel of the
+    library raised a status bit since the last check."""
+    _raise_on_status(N.device_status(clear))
+
+
 # ----------------------------------------------------------------- results
 
 class Aggregate:
@@ -487,10 +544,20 @@ def _array_bounds(t, stream):
 
 def bypixel(source, canvas, glyph, agg, *, antialias=False, flags=0):
     """core.py:1334-1359: validate, then run the GPU pipeline."""
-    frame = as_frame(source)
-    glyph.validate(frame)
-    agg.validate(frame)
-    canvas.validate()
+    if _DEBUG[0]:
+        N.device_status(clear=True)            # start from a clean status word
+        out = _bypixel(source, canvas, glyph, agg, antialias=antialias, flags=flags | N.FLAG_DEBUG_CHECKS)
+        check_device_status()
+        return out
+    return _bypixel(source, canvas, glyph, agg, antialias=antialias, flags=flags)
+
+
+def _bypixel(source, canvas, glyph, agg, *, antialias=False, flags=0):
+    with _NvtxRange("dsgb validate"):
+        frame = as_frame(source)
+        glyph.validate(frame)
+        agg.validate(frame)
+        canvas.validate()
     if isinstance(frame, PartitionedFrame):
         return partitioned_pipeline(frame, canvas, glyph, agg, flags=flags)
     if isinstance(frame, HostFrame):
@@ -620,7 +687,8 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
     """pandas.py:26-66 on the GPU: ranges, scale/translate, create+extend+finalize."""
     if stream is None:
         stream = torch.cuda.current_stream(frame.device).cuda_stream
-    plan = compile_plan(agg, frame, antialias=antialias)
+    with _NvtxRange("dsgb plan"):
+        plan = compile_plan(agg, frame, antialias=antialias)
     if isinstance(glyph, LinesAxis1Ragged):
         xr, yr = frame[glyph.x], frame[glyph.y]
         x_range = canvas.x_range or _array_bounds(xr.flat, stream)
@@ -712,7 +780,8 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
         N.check(rc, "dsgb_points_ws")
     coords = {glyph.x_label: x_axis, glyph.y_label: y_axis}
     dims = [glyph.y_label, glyph.x_label]
-    return _results(plan, ex, coords, dims, dict(x_range=x_range, y_range=y_range))
+    with _NvtxRange("dsgb results"):
+        return _results(plan, ex, coords, dims, dict(x_range=x_range, y_range=y_range))
 
 
 def _line_chunks(parts):

@@ -224,6 +224,7 @@ static int base_elem_bytes(int op) {
 int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
                      const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
                      int64_t ncells, cudaStream_t st, int64_t ncol_rows) {
+    NvtxRange range("dsgb finalize");
     for (int o = 0; o < nouts; ++o) {
         const dsgb_output &O = outs[o];
         if (!O.out || O.base0 < 0 || O.base0 >= nbases) {
@@ -318,6 +319,26 @@ using namespace dsgb;
 
 extern "C" int dsgb_abi_version(void) { return DSGB_ABI_VERSION; }
 extern "C" const char *dsgb_last_error(void) { return g_err; }
+namespace dsgb {
+int status_points(unsigned *bits, bool clear);
+int status_line(unsigned *bits, bool clear);
+}
+
+extern "C" int dsgb_device_status(uint32_t *bits, int32_t clear) {
+    if (!bits) {
+        set_error("dsgb_device_status: null bits");
+        return DSGB_E_INVALID;
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_status(e, "dsgb_device_status synchronize");
+    unsigned v = 0;
+    int rc = status_points(&v, clear != 0);
+    if (rc == DSGB_OK) rc = status_line(&v, clear != 0);
+    if (rc != DSGB_OK) return rc;
+    *bits |= v;
+    return DSGB_OK;
+}
+
 extern "C" int dsgb_device_sm_count(void) {
     int n = sm_count();
     if (n < 0) { set_error("no CUDA device"); return DSGB_E_CUDA; }

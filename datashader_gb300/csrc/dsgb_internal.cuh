@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
@@ -23,6 +24,15 @@ int sm_count();
 
 static inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// An NVTX range over one host-side stage of an entry point (plan, launch,
+// finalize); free when no profiler is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // Blocks of 256 threads for a grid-stride loop over n items (at most 16 per SM).
 static inline unsigned grid_of(int64_t n) {
     int sms = sm_count();
@@ -42,6 +52,30 @@ static inline int dtype_size(int32_t dt) {
     default: return 0;
     }
 }
+
+// ------------------------------------------------------- device status
+// Kernels never trap: a condition that a correct input cannot produce (a CAS
+// retry loop that reached its iteration guard, an aggregate index outside
+// its base in debug mode) sets a bit in a device status word, which
+// dsgb_device_status reads.  Each translation unit is its own device module
+// and keeps its own word (a static __device__ variable); the units that can
+// raise a bit expose it through DSGB_STATUS_READER.
+static __device__ unsigned g_unit_status;
+__device__ __forceinline__ void raise_status(unsigned bits) { atomicOr(&g_unit_status, bits); }
+
+static inline int unit_status_take(unsigned *bits, bool clear) {
+    unsigned v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_unit_status, sizeof(v));
+    if (e == cudaSuccess && clear && v) {
+        const unsigned zero = 0;
+        e = cudaMemcpyToSymbol(g_unit_status, &zero, sizeof(zero));
+    }
+    if (e != cudaSuccess) return cuda_status(e, "device status word");
+    *bits |= v;
+    return DSGB_OK;
+}
+#define DSGB_STATUS_READER(name) \
+    int name(unsigned *bits, bool clear) { return unit_status_take(bits, clear); }
 
 // ------------------------------------------------------- device helpers
 constexpr int MAX_BASES = 16;
@@ -166,7 +200,8 @@ __device__ __forceinline__ void pair_update(long long *slot, long long key, long
     long long orow = v[1];
     // Each failed CAS observes a strictly better pair written by another
     // thread; improvements are bounded by the rows landing on this slot, so
-    // the loop ends.  The iteration limit is a guard, not a wait.
+    // the loop ends.  The iteration limit is a guard, not a wait: reaching it
+    // leaves this row's update undone and raises DSGB_STATUS_CAS_GUARD.
     for (int guard = 0; guard < (1 << 24); ++guard) {
         long long rk, rr;
         if (!pair_better<MAX>(key, row, ok, orow)) {
@@ -179,6 +214,7 @@ __device__ __forceinline__ void pair_update(long long *slot, long long key, long
         }
         ok = rk; orow = rr;
     }
+    raise_status(DSGB_STATUS_CAS_GUARD);
 }
 
 __device__ __forceinline__ void atomic_max_key(long long *slot, long long key) {

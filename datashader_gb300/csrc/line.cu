@@ -29,6 +29,7 @@ struct LineParams {
     double line_width;
     int32_t plot_start, overwrite, use_2_stage;
     int64_t field_mod;      // > 0: appends carry a visit key (row = key % field_mod); 0: the row itself
+    int32_t debug;          // DSGB_FLAG_DEBUG_CHECKS
 };
 
 // One append of row i (field row = segment start) at pixel (x, y).
@@ -39,7 +40,10 @@ struct LineParams {
 template <bool KEYED>
 __device__ void line_append(const LineParams &p, int64_t key, long long x, long long y,
                             double aa, double pa) {
-    if (x < 0 || y < 0 || x >= p.width || y >= p.height) return;  // memory safety only
+    if (x < 0 || y < 0 || x >= p.width || y >= p.height) {   // memory safety only
+        if (p.debug) raise_status(DSGB_STATUS_INDEX);
+        return;
+    }
     const int64_t pix = (int64_t)y * p.width + x;
     const int64_t i = KEYED ? key % p.field_mod : key;
     const long long row = (long long)(key + p.row_offset);
@@ -50,7 +54,10 @@ __device__ void line_append(const LineParams &p, int64_t key, long long x, long 
         if (B.cat_col >= 0) {
             long long c = load_i64(p.cols[B.cat_col], i);
             if (c < 0) c += B.ncat;
-            if (c < 0 || c >= B.ncat) continue;
+            if (c < 0 || c >= B.ncat) {
+                if (p.debug) raise_status(DSGB_STATUS_INDEX);
+                continue;
+            }
             cell = pix * B.ncat + c;
         }
         double field = 1.0;
@@ -614,6 +621,10 @@ int build_line_params(LineParams &p, const dsgb_column *cols, int32_t ncols, int
 
 }  // namespace dsgb
 
+namespace dsgb {
+DSGB_STATUS_READER(status_line)
+}
+
 using namespace dsgb;
 
 extern "C" size_t dsgb_line_workspace_size(int64_t n) { return line_work_order_bytes(n); }
@@ -655,9 +666,11 @@ static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, in
                            const dsgb_base *bases, int32_t nbases,
                            const dsgb_output *outs, int32_t nouts,
                            void *workspace, size_t ws_bytes, uint32_t flags, void *stream) {
+    NvtxRange range("dsgb_line_axis0");
     LineParams p;
     int rc = build_line_params(p, cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases);
     if (rc) return rc;
+    p.debug = (flags & DSGB_FLAG_DEBUG_CHECKS) != 0;
     if (!(line_width >= 0.0)) { set_error("dsgb_line_axis0: line_width must be >= 0"); return DSGB_E_INVALID; }
     p.line_width = line_width;
     p.plot_start = plot_start;
@@ -715,6 +728,7 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
     // the field columns are indexed by row; x/y come from xs / ys
     int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
     if (rc) return rc;
+    p.debug = (flags & DSGB_FLAG_DEBUG_CHECKS) != 0;
     if (!(line_width >= 0.0)) { set_error("dsgb_lines: line_width must be >= 0"); return DSGB_E_INVALID; }
     p.line_width = line_width;
     p.plot_start = plot_start;
@@ -918,6 +932,7 @@ extern "C" int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t
     LineParams p;
     int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
     if (rc) return rc;
+    p.debug = (flags & DSGB_FLAG_DEBUG_CHECKS) != 0;
     p.line_width = line_width;
     p.plot_start = 1;
     p.overwrite = overwrite;
@@ -969,6 +984,7 @@ extern "C" int dsgb_lines_ragged_2stage(const dsgb_column *cols, int32_t ncols, 
     LineParams p;
     int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
     if (rc) return rc;
+    p.debug = (flags & DSGB_FLAG_DEBUG_CHECKS) != 0;
     p.line_width = line_width;
     p.plot_start = 1;
     p.overwrite = overwrite;
@@ -1001,6 +1017,7 @@ extern "C" int dsgb_lines_ragged(const dsgb_column *cols, int32_t ncols, int64_t
     LineParams p;
     int rc = build_line_params(p, cols, ncols, nrows, row_offset, 0, 0, canvas, bases, nbases);
     if (rc) return rc;
+    p.debug = (flags & DSGB_FLAG_DEBUG_CHECKS) != 0;
     if (!(line_width >= 0.0)) { set_error("dsgb_lines_ragged: line_width must be >= 0"); return DSGB_E_INVALID; }
     p.line_width = line_width;
     p.plot_start = 1;

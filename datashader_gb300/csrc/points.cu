@@ -312,6 +312,10 @@ int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
 
 }  // namespace dsgb
 
+namespace dsgb {
+DSGB_STATUS_READER(status_points)
+}
+
 using namespace dsgb;
 
 static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
@@ -319,9 +323,12 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
                        const dsgb_base *bases, int32_t nbases,
                        const dsgb_output *outs, int32_t nouts,
                        void *workspace, size_t ws_bytes, uint32_t flags, void *stream) {
+    NvtxRange range("dsgb_points");
     PointsParams p;
     int rc = build_params(p, cols, ncols, n, row_offset, x_col, y_col, canvas, bases, nbases);
     if (rc) return rc;
+    p.debug = (flags & DSGB_FLAG_DEBUG_CHECKS) != 0;
+    if (p.debug) workspace = nullptr;       // the checked appends live in the generic kernels
     cudaStream_t st = as_stream(stream);
     const int64_t ncells = (int64_t)canvas->width * canvas->height;
     if ((flags & DSGB_FLAG_DETERMINISTIC) && has_sum_base(p)) {
@@ -428,6 +435,7 @@ extern "C" int dsgb_points_segments(const dsgb_column *cols, int32_t ncols, int6
     PointsParams p;
     int rc = build_params(p, cols, ncols, n, 0, x_col, y_col, canvas, bases, nbases);
     if (rc) return rc;
+    p.debug = (flags & DSGB_FLAG_DEBUG_CHECKS) != 0;
     SegList s;
     memset(&s, 0, sizeof(s));
     int64_t maxlen = 0;

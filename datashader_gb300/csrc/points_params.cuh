@@ -20,6 +20,7 @@ struct PointsParams {
     double xmin, xmax, ymin, ymax;
     BinAxis ax, ay;                    // float32 fast path (binning.cuh)
     BinBounds bb;
+    int32_t debug;                     // DSGB_FLAG_DEBUG_CHECKS
 };
 
 // ------------------------------------------------------------------ binning
@@ -54,7 +55,10 @@ __device__ __forceinline__ void accumulate(const PointsParams &p, int64_t i, int
             // compiler.py:379-390 -- agg[:, :, int(code)], negative codes wrap
             long long c = load_i64(p.cols[B.cat_col], i);
             if (c < 0) c += B.ncat;
-            if (c < 0 || c >= B.ncat) continue;
+            if (c < 0 || c >= B.ncat) {
+                if (p.debug) raise_status(DSGB_STATUS_INDEX);
+                continue;
+            }
             cell = pix * B.ncat + c;
         }
         double field = 0.0;
@@ -84,6 +88,10 @@ enum Mode { MODE_GENERIC = 0, MODE_COUNT = 1, MODE_MEAN = 2 };
 // Per-row work of one kernel instantiation.  MEAN: bases[0] = SUM(v), bases[1] = COUNT(v).
 template <int MODE>
 __device__ __forceinline__ void emit(const PointsParams &p, int64_t i, int xi, int yi, double v) {
+    if (p.debug && ((unsigned)xi >= (unsigned)p.width || (unsigned)yi >= (unsigned)p.height)) {
+        raise_status(DSGB_STATUS_INDEX);
+        return;
+    }
     int64_t pix = (int64_t)yi * p.width + xi;
     if (MODE == MODE_COUNT) {
         atomicAdd((unsigned *)p.bases[0].agg + pix, 1u);

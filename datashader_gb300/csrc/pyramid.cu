@@ -960,7 +960,7 @@ extern "C" size_t dsgb_pyramid_workspace_size(int64_t n, int32_t has_v, const ds
 extern "C" int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n, int32_t x_col, int32_t y_col,
                             int32_t v_col, const dsgb_pyramid_config *config, uint32_t *counts, double *max_out,
                             void *workspace, size_t workspace_bytes, uint32_t flags, void *stream) {
-    (void)flags;
+    const int cap_shift = (int)((flags >> 8) & 31u);
     if (!cols || !config || !counts || x_col < 0 || y_col < 0 || x_col >= ncols || y_col >= ncols ||
         v_col >= ncols || (v_col >= 0 && !max_out)) {
         set_error("dsgb_pyramid: invalid arguments");
@@ -1028,9 +1028,9 @@ extern "C" int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n, i
                    ex > -100 && ex < 100 && ey > -100 && ey < 100;
     }
     p.partials = (unsigned *)(w + L.off_partials);
-    p.slot_cap = L.slot_cap;
+    p.slot_cap = L.slot_cap >> cap_shift;
     p.spill = (PyrSpill *)(w + L.off_spill);
-    p.spill_cap = L.spill_cap;
+    p.spill_cap = L.spill_cap >> cap_shift;
     p.footprint = L.footprint;
     const int bl = L.bls + p.split;
     int fo = 0;

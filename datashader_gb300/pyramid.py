@@ -44,7 +44,13 @@ class TilePyramid:
     """count (uint32) and, with ``v``, max(v) (float64) for every tile."""
 
     def __init__(self, x, y, v=None, *, zmin=0, zmax=6, tile_size=256, x_range=(0.0, 1.0),
-                 y_range=(0.0, 1.0), config=None, graph=True):
+                 y_range=(0.0, 1.0), config=None, graph=True, capacity_shift=0):
+        """``capacity_shift`` k renders with 1/2^k of the workspace's edge
+        queue and partial-slot capacities (DSGB_PYRAMID_CAP_SHIFT); a render
+        that overflows them is incomplete and :meth:`check` raises."""
+        if not 0 <= int(capacity_shift) <= 31:
+            raise ValueError("capacity_shift must be in 0..31")
+        self._flags = int(capacity_shift) << 8
         for t in (x, y) + ((v,) if v is not None else ()):
             if not (t.is_cuda and t.dtype == torch.float32 and t.dim() == 1 and t.is_contiguous()):
                 raise TypeError("x, y and v must be contiguous 1-D float32 CUDA tensors")
@@ -83,7 +89,7 @@ class TilePyramid:
         L = N.lib()
         N.check(L.dsgb_pyramid(self._cols, 3, self.n, 0, 1, 2 if self.v is not None else -1, ctypes.byref(self._c),
                                self.counts.data_ptr(), self.max.data_ptr() if self.max is not None else None,
-                               self.workspace.data_ptr(), self.workspace.numel(), 0, stream.cuda_stream),
+                               self.workspace.data_ptr(), self.workspace.numel(), self._flags, stream.cuda_stream),
                 "dsgb_pyramid")
 
     def _capture(self):

@@ -138,10 +138,26 @@ typedef struct {
 #define DSGB_FLAG_ROW_ORDER    0x20u /* dsgb_lines, layout 1: row-index bases (first / last / where) keep
                                        global rows, the semantics of a partitioned source (dask.py:86-219,
                                        row-index reductions), instead of the line-major visit order */
+#define DSGB_FLAG_DEBUG_CHECKS 0x40u /* dsgb_points / dsgb_line_axis0 / dsgb_lines: every append checks its
+                                       aggregate index against the base (pixel inside the canvas, category
+                                       code inside 0..ncat-1); an append that fails is skipped and raises
+                                       DSGB_STATUS_INDEX.  Takes the generic kernels (no hot-tile path).
+                                       The reference's numba appends do no such check. */
+
+/* Device status bits, read by dsgb_device_status.  Kernels never trap: a
+ * condition that no valid input produces sets a bit instead. */
+#define DSGB_STATUS_CAS_GUARD  0x1u  /* a where(max|min) {key,row} CAS loop reached its iteration guard and
+                                       left one row's update undone */
+#define DSGB_STATUS_INDEX      0x2u  /* DSGB_FLAG_DEBUG_CHECKS: an append's index fell outside its base */
 
 /* ---- informational ---------------------------------------------------- */
 int dsgb_abi_version(void);
 const char *dsgb_last_error(void);
+/* Waits for the current device (cudaDeviceSynchronize), then ORs into *bits
+ * the DSGB_STATUS_* bits that any kernel of this library raised on it since
+ * the last clear, and clears them when `clear` is non-zero.  No counterpart
+ * in the reference, whose appends run unchecked. */
+int dsgb_device_status(uint32_t *bits, int32_t clear);
 /* Number of SMs of the current device (grid sizing), or a negative code. */
 int dsgb_device_sm_count(void);
 
@@ -453,6 +469,10 @@ typedef struct {
 } dsgb_pyramid_config;
 int64_t dsgb_pyramid_tile_offset(int32_t zmin, int32_t z, int32_t tile_size);
 size_t dsgb_pyramid_workspace_size(int64_t n, int32_t has_v, const dsgb_pyramid_config *config);
+/* flags: DSGB_PYRAMID_CAP_SHIFT(k) uses 1/2^k of the workspace's queue and
+ * slot capacities (k = 0..31; a smaller workspace footprint for callers
+ * that know their data, and the way to test the overflow status bits). */
+#define DSGB_PYRAMID_CAP_SHIFT(k) (((uint32_t)(k) & 31u) << 8)
 int dsgb_pyramid(const dsgb_column *cols, int32_t ncols, int64_t n,
                  int32_t x_col, int32_t y_col, int32_t v_col,
                  const dsgb_pyramid_config *config,

@@ -74,6 +74,7 @@ def lib():
                 ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                 ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 8 + [
                 ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_Red), ctypes.c_int]
+            L.oracle_points_xy32.argtypes = L.oracle_points.argtypes
             L.oracle_line_axis0.argtypes = [
                 ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                 ctypes.c_int32, ctypes.c_int32] + [ctypes.c_double] * 9 + [
@@ -210,10 +211,16 @@ def _finalize(specs, keep):
 
 
 def points(cols, x, y, width, height, x_range, y_range, specs, row_offset=0,
-           x_axis="linear", y_axis="linear"):
-    """Canvas.points via pandas.default + Point.extend_cpu (pandas.py:26-66, points.py:182-212)."""
-    xs = np.ascontiguousarray(cols[x], dtype=np.float64)
-    ys = np.ascontiguousarray(cols[y], dtype=np.float64)
+           x_axis="linear", y_axis="linear", raw=False):
+    """Canvas.points via pandas.default + Point.extend_cpu (pandas.py:26-66, points.py:182-212).
+
+    float32 x and y columns are read as float32 and widened row by row inside
+    the C loop, as numba does; other coordinate dtypes are converted to
+    float64 first."""
+    f32 = (np.asarray(cols[x]).dtype == np.float32 and np.asarray(cols[y]).dtype == np.float32)
+    cdt = np.float32 if f32 else np.float64
+    xs = np.ascontiguousarray(cols[x], dtype=cdt)
+    ys = np.ascontiguousarray(cols[y], dtype=cdt)
     if x_range is None:
         x_range = maybe_expand_bounds(compute_bounds(xs))
     if y_range is None:
@@ -223,12 +230,86 @@ def points(cols, x, y, width, height, x_range, y_range, specs, row_offset=0,
     reds, keep, colarrs, ptrs = _prepare(cols, specs, (height, width), False)
     L = lib()
     L.oracle_init(reds, len(specs), height * width, 0)
-    L.oracle_points(xs.size, xs.ctypes.data, ys.ctypes.data, ptrs, row_offset, width, height,
+    loop = L.oracle_points_xy32 if f32 else L.oracle_points
+    loop(xs.size, xs.ctypes.data, ys.ctypes.data, ptrs, row_offset, width, height,
                     sx, tx, sy, ty, float(x_range[0]), float(x_range[1]),
                     float(y_range[0]), float(y_range[1]),
                     1 if x_axis == "log" else 0, 1 if y_axis == "log" else 0,
                     reds, len(specs))
-    return _finalize(specs, keep)
+    return keep if raw else _finalize(specs, keep)
+
+
+def combine_partials(specs, parts):
+    """Fold the raw (agg, agg2) bases of row partitions, in row order, the way
+    datashader's dask path combines partition aggregates (compiler.py:478-507,
+    reductions.py `_combine` of each base; dask.py:168-217), then finalize.
+    ``parts``: one list of (agg, agg2) per partition, earlier rows first."""
+    acc = [tuple(None if a is None else a.copy() for a in pair) for pair in parts[0]]
+    for part in parts[1:]:
+        for k, s in enumerate(specs):
+            (a, a2), (b, b2) = acc[k], part[k]
+            kind = s["kind"]
+            if kind in ("count", "count_ignore_aa", "sum_zero"):
+                a += b
+            elif kind == "any":
+                np.maximum(a, b, out=a)
+            elif kind == "mean":
+                a += b
+                a2 += b2
+            elif kind == "sum":                 # nansum, NaN where both are empty
+                both = np.isnan(a) & np.isnan(b)
+                a[...] = np.where(both, np.nan, np.nan_to_num(a, nan=0.0) + np.nan_to_num(b, nan=0.0))
+            elif kind == "max":
+                np.fmax(a, b, out=a)
+            elif kind == "min":
+                np.fmin(a, b, out=a)
+            elif kind == "first":               # the earlier partition's value wins
+                a[...] = np.where(np.isnan(a), b, a)
+            elif kind == "last":
+                a[...] = np.where(np.isnan(b), a, b)
+            elif kind == "min_row":
+                a[...] = np.where(a < 0, b, np.where(b < 0, a, np.minimum(a, b)))
+            elif kind == "max_row":
+                np.maximum(a, b, out=a)
+            elif kind == "where":
+                sk = s["selector"]["kind"]
+                if sk in ("max", "min"):        # strictly better selector value wins; ties keep the earlier rows
+                    better = (~np.isnan(b2)) & (np.isnan(a2) | ((b2 > a2) if sk == "max" else (b2 < a2)))
+                elif sk == "first":
+                    better = np.isnan(a2) & ~np.isnan(b2)
+                elif sk == "last":
+                    better = ~np.isnan(b2)
+                elif sk == "min_row":
+                    better = (b2 >= 0) & (a2 < 0)
+                else:                            # max_row
+                    better = b2 > a2
+                a[...] = np.where(better, b, a)
+                a2[...] = np.where(better, b2, a2)
+            else:
+                raise NotImplementedError(kind)
+    return _finalize(specs, acc)
+
+
+def points_parallel(cols, x, y, width, height, x_range, y_range, specs, threads=None):
+    """oracle.points over one row partition per host thread (the C loop
+    releases the GIL), partial bases folded by :func:`combine_partials`.
+    Fixed ranges only."""
+    threads = threads or os.cpu_count() or 1
+    n = len(cols[x])
+    bounds = np.linspace(0, n, threads + 1).astype(np.int64)
+    parts = [None] * threads
+
+    def work(k):
+        a, b = bounds[k], bounds[k + 1]
+        sub = {c: v[a:b] for c, v in cols.items()}
+        parts[k] = points(sub, x, y, width, height, x_range, y_range, specs, row_offset=int(a), raw=True)
+
+    ts = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return combine_partials(specs, parts)
 
 
 # AntialiasCombination values (antialias.py:8-14).

@@ -211,7 +211,31 @@ static void append_row(oracle_red *reds, int nreds, const double *const *cols,
 }
 
 /* glyphs/points.py:190-212 -- Point._build_extend, CPU loop.
- * Bounds test, `int(x * sx + tx)` (truncation toward zero), upper-edge clamp. */
+ * Bounds test, `int(x * sx + tx)` (truncation toward zero), upper-edge clamp.
+ * Returns the pixel index, or -1 when the row is outside the bounds. */
+static inline int64_t point_pixel(double x, double y, int32_t width, int32_t height,
+                                  double sx, double tx, double sy, double ty,
+                                  double xmin, double xmax, double ymin, double ymax,
+                                  int32_t x_log, int32_t y_log) {
+    if (!((xmin <= x && x <= xmax) && (ymin <= y && y <= ymax))) return -1;
+    /* core.py:131-134 LogAxis.mapper = log10(float(val)) */
+    double mx = x_log ? log10(x) : x;
+    double my = y_log ? log10(y) : y;
+    double fx = mx * sx;
+    fx = fx + tx;
+    double fy = my * sy;
+    fy = fy + ty;
+    int64_t xx = (int64_t)fx;  /* Python int(): truncation toward zero */
+    int64_t yy = (int64_t)fy;
+    int64_t xi = xx >= width ? width - 1 : xx;
+    int64_t yi = yy >= height ? height - 1 : yy;
+    /* numba indexes negative positions from the end. */
+    if (xi < 0) xi += width;
+    if (yi < 0) yi += height;
+    if (xi < 0 || yi < 0) return -1;
+    return yi * (int64_t)width + xi;
+}
+
 int oracle_points(int64_t n, const double *xs, const double *ys,
                   const double *const *cols, int64_t row_offset,
                   int32_t width, int32_t height,
@@ -220,25 +244,27 @@ int oracle_points(int64_t n, const double *xs, const double *ys,
                   int32_t x_log, int32_t y_log,
                   oracle_red *reds, int nreds) {
     for (int64_t i = 0; i < n; ++i) {
-        double x = xs[i], y = ys[i];
-        if ((xmin <= x && x <= xmax) && (ymin <= y && y <= ymax)) {
-            /* core.py:131-134 LogAxis.mapper = log10(float(val)) */
-            double mx = x_log ? log10(x) : x;
-            double my = y_log ? log10(y) : y;
-            double fx = mx * sx;
-            fx = fx + tx;
-            double fy = my * sy;
-            fy = fy + ty;
-            int64_t xx = (int64_t)fx;  /* Python int(): truncation toward zero */
-            int64_t yy = (int64_t)fy;
-            int64_t xi = xx >= width ? width - 1 : xx;
-            int64_t yi = yy >= height ? height - 1 : yy;
-            /* numba indexes negative positions from the end. */
-            if (xi < 0) xi += width;
-            if (yi < 0) yi += height;
-            if (xi < 0 || yi < 0) continue;
-            append_row(reds, nreds, cols, i, i + row_offset, yi * (int64_t)width + xi);
-        }
+        const int64_t pix = point_pixel(xs[i], ys[i], width, height, sx, tx, sy, ty, xmin, xmax, ymin, ymax,
+                                        x_log, y_log);
+        if (pix >= 0) append_row(reds, nreds, cols, i, i + row_offset, pix);
+    }
+    return 0;
+}
+
+/* The same loop over float32 coordinate columns: each value is widened to
+ * float64 inside the loop, where numba widens a float32 column element that
+ * meets the float64 bounds and scale (glyphs/points.py:193-204). */
+int oracle_points_xy32(int64_t n, const float *xs, const float *ys,
+                       const double *const *cols, int64_t row_offset,
+                       int32_t width, int32_t height,
+                       double sx, double tx, double sy, double ty,
+                       double xmin, double xmax, double ymin, double ymax,
+                       int32_t x_log, int32_t y_log,
+                       oracle_red *reds, int nreds) {
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t pix = point_pixel((double)xs[i], (double)ys[i], width, height, sx, tx, sy, ty,
+                                        xmin, xmax, ymin, ymax, x_log, y_log);
+        if (pix >= 0) append_row(reds, nreds, cols, i, i + row_offset, pix);
     }
     return 0;
 }

@@ -45,6 +45,7 @@ def test_argument_errors_return_codes_without_a_gpu():
     assert b"invalid" in L.dsgb_last_error()
     rc = L.dsgb_eq_hist_u32(None, 0, 0, None, None, None, None, 0, 255, 0, None, 0, None)
     assert rc == -1
+    assert L.dsgb_device_status(None, 1) == -1
 
 
 def test_struct_layouts_match_header():

@@ -177,3 +177,48 @@ def test_line_adjoint_work_order_matches_row_order():
     assert np.array_equal(gv0, gv1)
     np.testing.assert_allclose(gy1, gy0, rtol=1e-12, atol=1e-12 * np.abs(gy0).max())
     assert np.abs(gv0).max() > 0 and np.abs(gy0).max() > 0
+
+
+@pytest.mark.parametrize("mean", [False, True])
+def test_points_adjoint_strided_and_host_inputs(mean):
+    """Strided views (columns of an (n, 2) array), a stride-0 expanded value
+    column and host x/y give the gradients of the contiguous device inputs:
+    the backward reads the frame's device copies, not the caller's tensors."""
+    n = 4096
+    x, y = synthetic.gaussian_mixture_np(n, seed=6, dtype=np.float32)
+    v = np.random.default_rng(6).lognormal(0, 1, n)
+    cvs = ds.Canvas(plot_width=32, plot_height=32, x_range=(-4, 4), y_range=(-4, 4))
+    f = ag.points_mean if mean else ag.points_sum
+    w = torch.randn(32, 32, dtype=torch.float64, device="cuda")
+    X, Y = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    V = torch.from_numpy(v).cuda().requires_grad_(True)
+    (torch.nan_to_num(f(X, Y, V, cvs)) * w).sum().backward()
+    ref = V.grad.clone()
+    xy = torch.stack([X, Y], dim=1)                     # x, y as stride-2 views
+    V2 = torch.from_numpy(v).cuda().requires_grad_(True)
+    (torch.nan_to_num(f(xy[:, 0], xy[:, 1], V2, cvs)) * w).sum().backward()
+    assert torch.equal(V2.grad, ref)
+    V3 = torch.from_numpy(v).cuda().requires_grad_(True)
+    (torch.nan_to_num(f(X.cpu(), Y.cpu(), V3, cvs)) * w).sum().backward()   # host x/y, device v
+    assert torch.equal(V3.grad, ref)
+    c = torch.tensor([1.5], dtype=torch.float64, device="cuda", requires_grad=True)
+    (torch.nan_to_num(f(X, Y, c.expand(n), cvs)) * w).sum().backward()        # stride-0 value column
+    assert c.grad is not None and torch.isfinite(c.grad).all()
+    if not mean:   # d/dc of sum_px w * (c * count) is sum_i w[pixel(i)]
+        torch.testing.assert_close(c.grad, ref.sum().reshape(1), rtol=1e-12, atol=0)
+
+
+def test_line_adjoint_strided_inputs():
+    x, y, v = _series(4, 100, seed=9)
+    cvs = _canvas(y)
+    X, Y0, V0 = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (x, y, v))
+    Y = Y0.clone().requires_grad_(True)
+    V = V0.clone().requires_grad_(True)
+    w = torch.randn(cvs.plot_height, cvs.plot_width, dtype=torch.float64, device="cuda")
+    (torch.nan_to_num(ag.line_sum(X, Y, V, cvs)) * w).sum().backward()
+    big = torch.stack([X, Y0, V0], dim=1)               # every column a stride-3 view
+    Ys = big[:, 1].detach().requires_grad_(True)
+    Vs = big[:, 2].detach().requires_grad_(True)
+    (torch.nan_to_num(ag.line_sum(big[:, 0], Ys, Vs, cvs)) * w).sum().backward()
+    assert torch.equal(Vs.grad, V.grad)
+    torch.testing.assert_close(Ys.grad, Y.grad, rtol=1e-12, atol=1e-12 * float(Y.grad.abs().max()))

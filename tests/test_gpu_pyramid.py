@@ -142,3 +142,24 @@ def test_pyramid_count_only_and_autotune():
         assert m is None
         rc, _ = _plain_tile(frame, pyr, z, tx, ty)
         assert_same(c.view(torch.int32).cpu().numpy().view(np.uint32), rc, what=f"count {(z, tx, ty)}")
+
+
+def test_pyramid_overflow_status_raises():
+    """With the edge queue and slot capacities shrunk to nothing, a render
+    that needs them reports an incomplete pyramid: check() raises, and the
+    full capacity renders the same data completely."""
+    x, y, v = _data(300_000, seed=21)
+    # a dense cluster so that buckets split into chunks (partial slots)
+    x = np.concatenate([x, np.full(200_000, 0.3001, np.float32)])
+    y = np.concatenate([y, np.full(200_000, 0.7003, np.float32)])
+    v = np.concatenate([v, np.ones(200_000, np.float32)])
+    X, Y, V = (torch.from_numpy(a).cuda() for a in (x, y, v))
+    cfg = dict(split=0, threads=512, chunk=16384)
+    bad = P.TilePyramid(X, Y, V, zmax=4, tile_size=64, config=cfg, graph=False, capacity_shift=31).render()
+    with pytest.raises(ds._native.DsgbError, match="incomplete render"):
+        bad.check()
+    assert bad.status() & 0x5          # queue overflow and / or slots exhausted
+    good = P.TilePyramid(X, Y, V, zmax=4, tile_size=64, config=cfg, graph=False).render()
+    good.check()
+    with pytest.raises(ValueError):
+        P.TilePyramid(X, Y, V, zmax=4, tile_size=64, capacity_shift=32)
