@@ -140,7 +140,7 @@ STATUS_CAS_GUARD, STATUS_INDEX = 0x1, 0x2
 # every symbol include/dsgb.h declares
 EXPORTED = (
     "dsgb_abi_version", "dsgb_last_error", "dsgb_device_status", "dsgb_device_sm_count", "dsgb_bases_init", "dsgb_combine",
-    "dsgb_finalize", "dsgb_finalize_partitioned", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_workspace_size_flags",
+    "dsgb_finalize", "dsgb_finalize_partitioned", "dsgb_select_by_owner", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_workspace_size_flags",
     "dsgb_points_ws", "dsgb_points_segments",
     "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_workspace_size", "dsgb_line_axis0_ws", "dsgb_lines", "dsgb_lines_2stage", "dsgb_lines_ragged", "dsgb_lines_ragged_2stage", "dsgb_line_axis0_backward", "dsgb_line_axis0_backward_ws",
     "dsgb_points_backward", "dsgb_bounds", "dsgb_eq_hist_workspace_size", "dsgb_eq_hist_u32",
@@ -168,6 +168,8 @@ def _declare(L):
     L.dsgb_finalize.argtypes = [PC, i32, i64, PB, i32, PO, i32, i64, P]
     L.dsgb_finalize_partitioned.argtypes = [PC, i32, i32, ctypes.POINTER(i64), ctypes.POINTER(i64), PB, i32, PO, i32,
                                             i64, P]
+    L.dsgb_select_by_owner.argtypes = [PB, i32, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(P), P,
+                                       i64, P]
     L.dsgb_points.argtypes = [PC, i32, i64, i64, i32, i32, ctypes.POINTER(CanvasDesc), PB, i32, PO, i32, u32, P]
     L.dsgb_points_workspace_size.argtypes = [i64, ctypes.POINTER(CanvasDesc), PB, i32]
     L.dsgb_points_workspace_size.restype = ctypes.c_size_t

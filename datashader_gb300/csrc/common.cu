@@ -212,6 +212,32 @@ __global__ void gather_parts_kernel(const __grid_constant__ GatherParts g) {
     }
 }
 
+// Cross-process form: partition p looked its gather up itself (vals[p], one
+// float64 per cell, NaN where empty); the owner of the selected row gives
+// the value.  A cell that no partition selected reads partition 0 (NaN).
+struct SelectParts {
+    int32_t nparts, b0op;
+    const void *b0;
+    double *out;
+    int64_t n;
+    const double *vals[FIN_MAX_PARTS];
+    int64_t first[FIN_MAX_PARTS], rows[FIN_MAX_PARTS];
+};
+
+__global__ void select_owner_kernel(const __grid_constant__ SelectParts g) {
+    for (int64_t i = gtid(); i < g.n; i += gstride()) {
+        const long long r = base_row(g.b0op, g.b0, i);
+        int owner = 0;
+        if (r >= 0) {
+            for (int p = 0; p < g.nparts; ++p) {
+                const long long j = r - g.first[p];
+                if (j >= 0 && j < g.rows[p]) { owner = p; break; }
+            }
+        }
+        g.out[i] = g.vals[owner][i];
+    }
+}
+
 static int base_elem_bytes(int op) {
     switch (op) {
     case DSGB_BASE_COUNT: case DSGB_BASE_AA_CNT0: return 4;
@@ -415,6 +441,42 @@ extern "C" int dsgb_finalize(const dsgb_column *cols, int32_t ncols, int64_t row
                              const dsgb_output *outs, int32_t nouts, int64_t ncells, void *stream) {
     if ((nbases > 0 && !bases) || (nouts > 0 && !outs) || ncells < 0) { set_error("dsgb_finalize: bad args"); return DSGB_E_INVALID; }
     return finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, as_stream(stream));
+}
+
+extern "C" int dsgb_select_by_owner(const dsgb_base *row_base, int32_t nparts, const int64_t *part_first,
+                                    const int64_t *part_rows, const double *const *part_vals, double *out,
+                                    int64_t ncells, void *stream) {
+    if (!row_base || !row_base->agg || !part_first || !part_rows || !part_vals || !out || ncells < 0 ||
+        nparts < 1) {
+        set_error("dsgb_select_by_owner: bad args");
+        return DSGB_E_INVALID;
+    }
+    if (nparts > FIN_MAX_PARTS) {
+        set_error("dsgb_select_by_owner: at most %d partitions", FIN_MAX_PARTS);
+        return DSGB_E_UNSUPPORTED;
+    }
+    const int op = row_base->op;
+    if (op != DSGB_BASE_MIN_ROW && op != DSGB_BASE_MAX_ROW && op != DSGB_BASE_ARGMAX && op != DSGB_BASE_ARGMIN &&
+        op != DSGB_BASE_AA_ARGMAX) {
+        set_error("dsgb_select_by_owner: base op %d carries no row", op);
+        return DSGB_E_INVALID;
+    }
+    SelectParts g;
+    memset(&g, 0, sizeof(g));
+    g.nparts = nparts;
+    g.b0op = op;
+    g.b0 = row_base->agg;
+    g.out = out;
+    g.n = ncells * (row_base->ncat < 1 ? 1 : row_base->ncat);
+    for (int p = 0; p < nparts; ++p) {
+        if (!part_vals[p]) { set_error("dsgb_select_by_owner: partition %d values null", p); return DSGB_E_INVALID; }
+        g.vals[p] = part_vals[p];
+        g.first[p] = part_first[p];
+        g.rows[p] = part_rows[p];
+    }
+    if (g.n > 0) select_owner_kernel<<<grid_for(g.n), 256, 0, as_stream(stream)>>>(g);
+    DSGB_CHECK_LAUNCH("dsgb_select_by_owner");
+    return DSGB_OK;
 }
 
 // dsgb_finalize for bases combined from row partitions: every output but the

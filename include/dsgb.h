@@ -179,6 +179,17 @@ int dsgb_finalize_partitioned(const dsgb_column *part_cols, int32_t ncols, int32
                               const int64_t *part_first, const int64_t *part_rows,
                               const dsgb_base *bases, int32_t nbases, const dsgb_output *outs,
                               int32_t nouts, int64_t ncells, void *stream);
+/* The gather outputs of partitions held by different processes: partition p
+ * (global rows [part_first[p], part_first[p] + part_rows[p])) finalized its
+ * own gather output (part_vals[p], device float64, one value per cell);
+ * out[i] takes the value of the partition holding the row that the combined
+ * row_base (MIN_ROW / MAX_ROW or a {key,row} pair base) selected at cell i,
+ * so no process needs another's columns.  Replaces the paired selector /
+ * lookup combine of where, first and last across partitions
+ * (reductions.py:1992-2018, dask.py:168-217).  nparts <= 64. */
+int dsgb_select_by_owner(const dsgb_base *row_base, int32_t nparts, const int64_t *part_first,
+                         const int64_t *part_rows, const double *const *part_vals, double *out,
+                         int64_t ncells, void *stream);
 
 /* ---- Canvas.points ------------------------------------------------------
  * Replaces points.py:182-242 (+ compiler.py create/append/finalize).

@@ -39,8 +39,8 @@ def test_debug_checks_equal_results_and_clean_status():
     with ds.debug_checks():
         checked = cvs.points(f, "x", "y", red)
         line = cvs.line(f, "x", "y", agg=ds.sum("v"), line_width=1.5)
-    for k in ("c", "m", "w", "b"):
-        assert torch.equal(plain[k].data, checked[k].data)
+    for k in ("c", "m", "w", "b"):                  # NaN-aware equality
+        np.testing.assert_array_equal(plain[k].data.cpu().numpy(), checked[k].data.cpu().numpy(), err_msg=k)
     torch.testing.assert_close(plain["s"].data, checked["s"].data, rtol=1e-12, atol=0, equal_nan=True)
     assert torch.isfinite(torch.nan_to_num(line.data)).all()
     ds.check_device_status()
