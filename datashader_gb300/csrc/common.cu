@@ -348,6 +348,7 @@ extern "C" const char *dsgb_last_error(void) { return g_err; }
 namespace dsgb {
 int status_points(unsigned *bits, bool clear);
 int status_line(unsigned *bits, bool clear);
+int status_points_hot(unsigned *bits, bool clear);
 }
 
 extern "C" int dsgb_device_status(uint32_t *bits, int32_t clear) {
@@ -360,6 +361,7 @@ extern "C" int dsgb_device_status(uint32_t *bits, int32_t clear) {
     unsigned v = 0;
     int rc = status_points(&v, clear != 0);
     if (rc == DSGB_OK) rc = status_line(&v, clear != 0);
+    if (rc == DSGB_OK) rc = status_points_hot(&v, clear != 0);
     if (rc != DSGB_OK) return rc;
     *bits |= v;
     return DSGB_OK;

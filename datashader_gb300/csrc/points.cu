@@ -273,6 +273,9 @@ static int launch_points_segments(const PointsParams &p, const SegList &s, int n
 
 int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st);
 size_t cached_workspace_size(int64_t n, int width, int height);
+int launch_points_hot(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
+                      const BinAxis &ax, const BinAxis &ay, const BinBounds &bb, uint32_t *out, bool accumulate,
+                      cudaStream_t st);
 int launch_points_cached(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
                          const BinAxis &ax, const BinAxis &ay, const BinBounds &bb,
                          uint32_t *out, bool accumulate, void *ws, size_t ws_bytes, cudaStream_t st);
@@ -353,6 +356,12 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
         if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
             rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
         return rc;
+    }
+    if (cached_eligible(p, flags)) {
+        // float32 coordinates, count(): the per-SM hot-tile kernel (points_hot.cu)
+        rc = launch_points_hot(p.cols[x_col], p.cols[y_col], n, canvas, p.ax, p.ay, p.bb,
+                               (uint32_t *)p.bases[0].agg, (flags & DSGB_FLAG_NO_INIT) != 0, st);
+        if (rc != DSGB_E_UNSUPPORTED) return rc;
     }
     if (workspace && cached_eligible(p, flags)) {
         rc = launch_points_cached(p.cols[x_col], p.cols[y_col], n, canvas, p.ax, p.ay, p.bb,
