@@ -521,12 +521,9 @@ def run_gpu(args):
                 "kernel_gpts": n / (avg_ms / 1e3) / 1e9}
 
     rl_count = roofline(ds.count(), 8, 4, args.steps, traffic=count_traffic(n))
-    # kernels of one count call: the hot-tile path launches sample (with the
-    # tile selection in its last block) and main; the single-kernel path one
-    _probe = Executor(frame, compile_plan(ds.count(), frame), Point("x", "y"))
-    _probe.allocate(1024, 1024, dev)
-    _cv = N.CanvasDesc(1024, 1024, 0, 0, 128.0, 512.0, 128.0, 512.0, -4.0, 4.0, -4.0, 4.0)
-    kernels_per_count = 2 if N.lib().dsgb_points_workspace_size(n, ctypes.byref(_cv), _probe.bases, 1) else 1
+    # kernels of one count call: the hot-tile kernel (the output is cleared by
+    # cudaMemsetAsync, not a kernel of this library)
+    kernels_per_count = 1
     rl_mean = roofline(ds.mean("v"), 16, 12, args.steps, traffic=mean_traffic(n))
 
     # mean through the public API

@@ -276,6 +276,9 @@ size_t cached_workspace_size(int64_t n, int width, int height);
 int launch_points_hot(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
                       const BinAxis &ax, const BinAxis &ay, const BinBounds &bb, uint32_t *out, bool accumulate,
                       cudaStream_t st);
+int launch_points_hot_mean(const ColumnRef &xc, const ColumnRef &yc, const ColumnRef &vc, int64_t n,
+                           const dsgb_canvas *cv, const BinAxis &ax, const BinAxis &ay, const BinBounds &bb,
+                           double *sum, uint32_t *count, bool accumulate, cudaStream_t st);
 int launch_points_cached(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
                          const BinAxis &ax, const BinAxis &ay, const BinBounds &bb,
                          uint32_t *out, bool accumulate, void *ws, size_t ws_bytes, cudaStream_t st);
@@ -367,6 +370,15 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
         rc = launch_points_cached(p.cols[x_col], p.cols[y_col], n, canvas, p.ax, p.ay, p.bb,
                                   (uint32_t *)p.bases[0].agg, (flags & DSGB_FLAG_NO_INIT) != 0,
                                   workspace, ws_bytes, st);
+        if (rc != DSGB_E_UNSUPPORTED) return rc;
+    }
+    if (cached_mean_eligible(p, flags)) {
+        // float32 coordinates, mean(v) with a float64 v: the per-SM hot-tile kernel (points_hot.cu)
+        rc = launch_points_hot_mean(p.cols[x_col], p.cols[y_col], p.cols[p.bases[0].col], n, canvas, p.ax, p.ay,
+                                    p.bb, (double *)p.bases[0].agg, (uint32_t *)p.bases[1].agg,
+                                    (flags & DSGB_FLAG_NO_INIT) != 0, st);
+        if (rc == DSGB_OK && !(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
+            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
         if (rc != DSGB_E_UNSUPPORTED) return rc;
     }
     if (workspace && cached_mean_eligible(p, flags)) {

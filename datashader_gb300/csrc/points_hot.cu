@@ -56,9 +56,11 @@ struct Params {
     float ex_lo, ex_hi, ey_lo, ey_hi;       // window of the fractional part that proves a bin
     float xminf, xmaxf, yminf, ymaxf;       // float32 images of the inclusive bounds
     double sx, tx, sy, ty;
-    uint32_t *out;
+    uint32_t *out;                          // count (the COUNT base of mean)
+    const double *vs;                       // mean: the value column
+    double *sum_out;                        // mean: the float64 SUM base
     int use_tma;
-    int tab_off, st_off;                    // byte offsets of the tile table and slot list
+    int cnt_off, tab_off, st_off;           // byte offsets of the 16-bit counters, tile table, slot list
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -388,6 +390,240 @@ __global__ void __launch_bounds__(THREADS, 1) hot_count_kernel(const __grid_cons
     }
 }
 
+
+// ================================================================== mean('v')
+// The same pass for mean('v') (reductions.py:1280-1297: bases _sum_zero and
+// _count_ignore_antialiasing, rows with a NaN value add nothing): per cached
+// pixel a float64 sum (shared-memory add) beside the 16-bit count; other rows
+// add their value and one into the output bases by L2 reductions.
+__device__ __forceinline__ void mean_row(const RowConsts &k, unsigned sums, unsigned long long sout, float x,
+                                         float y, double v, unsigned bit, unsigned &slowm, unsigned &ovf) {
+    asm volatile(
+        "{\n\t"
+        ".reg .f32 vx, vy, tx, ty, kxf, kyf, fx, fy;\n\t"
+        ".reg .b32 kx, ky, a, b, t, s, c, pix, inc, old, cs;\n\t"
+        ".reg .b64 ga, gs;\n\t"
+        ".reg .pred pw, pf, pm, ps, pc, pu, pn;\n\t"
+        "testp.notanumber.f64 pn, %21;\n\t"
+        "fma.rn.f32 vx, %2, %4, %5;\n\t"
+        "fma.rn.f32 vy, %3, %6, %7;\n\t"
+        "add.rz.f32 tx, vx, 0f4B400000;\n\t"
+        "add.rz.f32 ty, vy, 0f4B400000;\n\t"
+        "sub.rn.f32 kxf, tx, 0f4B400000;\n\t"
+        "sub.rn.f32 kyf, ty, 0f4B400000;\n\t"
+        "sub.rn.f32 fx, vx, kxf;\n\t"
+        "sub.rn.f32 fy, vy, kyf;\n\t"
+        "setp.gt.f32 pw, fx, %8;\n\t"
+        "setp.lt.and.f32 pw, fx, %9, pw;\n\t"
+        "setp.gt.and.f32 pw, fy, %10, pw;\n\t"
+        "setp.lt.and.f32 pw, fy, %11, pw;\n\t"
+        "mov.b32 kx, tx;\n\t"
+        "mov.b32 ky, ty;\n\t"
+        "sub.s32 kx, kx, 0x4B400000;\n\t"
+        "sub.s32 ky, ky, 0x4B400000;\n\t"
+        "setp.lt.u32 pf, kx, %12;\n\t"
+        "setp.lt.and.u32 pf, ky, %13, pf;\n\t"
+        "add.s32 a, kx, 1;\n\t"
+        "add.s32 b, ky, 1;\n\t"
+        "setp.lt.u32 pm, a, %14;\n\t"
+        "setp.lt.and.u32 pm, b, %15, pm;\n\t"
+        "and.pred pf, pf, pw;\n\t"
+        "not.pred ps, pf;\n\t"
+        "and.pred ps, ps, pm;\n\t"
+        "not.pred pn, pn;\n\t"
+        "and.pred ps, ps, pn;\n\t"
+        "and.pred pf, pf, pn;\n\t"
+        "@ps or.b32 %0, %0, %20;\n\t"
+        "shr.u32 a, ky, 4;\n\t"
+        "shr.u32 b, kx, 4;\n\t"
+        "mad.lo.u32 t, a, %16, %17;\n\t"
+        "mad.lo.u32 t, b, 2, t;\n\t"
+        "@!pf mov.u32 t, %17;\n\t"
+        "ld.shared.s16 s, [t];\n\t"
+        "setp.ge.and.s32 pc, s, 0, pf;\n\t"
+        "setp.lt.and.s32 pu, s, 0, pf;\n\t"
+        "and.b32 a, ky, 15;\n\t"
+        "and.b32 b, kx, 15;\n\t"
+        "mad.lo.u32 c, a, 16, b;\n\t"
+        "mad.lo.u32 c, s, 256, c;\n\t"
+        "mad.lo.u32 cs, c, 8, %22;\n\t"
+        "@pc red.shared.add.f64 [cs], %21;\n\t"
+        "and.b32 inc, c, 1;\n\t"
+        "mad.lo.u32 inc, inc, 65535, 1;\n\t"
+        "and.b32 c, c, -2;\n\t"
+        "mad.lo.u32 c, c, 2, %18;\n\t"
+        "@pc atom.shared.add.u32 old, [c], inc;\n\t"
+        "@pc or.b32 %1, %1, old;\n\t"
+        "mad.lo.u32 pix, ky, %12, kx;\n\t"
+        "mad.wide.u32 ga, pix, 4, %19;\n\t"
+        "mad.wide.u32 gs, pix, 8, %23;\n\t"
+        "@pu red.global.add.f64 [gs], %21;\n\t"
+        "@pu red.global.add.u32 [ga], 1;\n\t"
+        "}"
+        : "+r"(slowm), "+r"(ovf)
+        : "f"(x), "f"(y), "f"(k.sxf), "f"(k.txf), "f"(k.syf), "f"(k.tyf), "f"(k.exlo), "f"(k.exhi),
+          "f"(k.eylo), "f"(k.eyhi), "r"(k.W), "r"(k.H), "r"(k.W2), "r"(k.H2), "r"(k.tx2), "r"(k.tab),
+          "r"(k.cache), "l"(k.out), "r"(bit), "d"(v), "r"(sums), "l"(sout)
+        : "memory");
+}
+
+// Exact path of one mean row; returns the old count word of a shared increment.
+static __device__ __noinline__ unsigned slow_row_mean(const Params *pp, const short *tab, double *sums,
+                                                      unsigned *cw, int64_t row) {
+    const Params &p = *pp;
+    const double v = p.vs[row];
+    if (isnull(v)) return 0u;
+    const unsigned long long r = exact_bin(p.xs[row], p.ys[row], pp);
+    if (r == ~0ull) return 0u;
+    const int xi = (int)(unsigned)r, yi = (int)(unsigned)(r >> 32);
+    const int s = tab[(yi >> TS) * p.tiles_x + (xi >> TS)];
+    if (s >= 0) {
+        const unsigned h = half_index(s, xi, yi);
+        atomicAdd(&sums[h], v);
+        return atomicAdd(&cw[h >> 1], (h & 1u) ? 0x10000u : 1u);
+    }
+    const int64_t pix = (int64_t)yi * p.W + xi;
+    atomicAdd(&p.sum_out[pix], v);
+    atomicAdd(&p.out[pix], 1u);
+    return 0u;
+}
+
+__global__ void __launch_bounds__(THREADS, 1) hot_mean_kernel(const __grid_constant__ Params p,
+                                                              const __grid_constant__ CUtensorMap tmap) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    double *sums = (double *)smem;                            // K tiles of float64 sums
+    unsigned *cw = (unsigned *)(smem + p.cnt_off);            // K tiles of 16-bit counts
+    short *tab = (short *)(smem + p.tab_off);
+    short *slot_tile = (short *)(smem + p.st_off);
+    const float4 *x4 = (const float4 *)p.xs;
+    const float4 *y4 = (const float4 *)p.ys;
+    const double2 *v2 = (const double2 *)p.vs;
+    const int64_t g0 = p.n4 * blockIdx.x / gridDim.x, g1 = p.n4 * (blockIdx.x + 1) / gridDim.x;
+
+    unsigned *hist = (unsigned *)smem;
+    for (int i = threadIdx.x; i < p.ntiles; i += THREADS) hist[i] = 0;
+    __syncthreads();
+    if (g1 > g0) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int64_t g = g0 + (g1 - g0) * (threadIdx.x + j * THREADS) / (2 * THREADS);
+            const float4 a = __ldg(x4 + g), b = __ldg(y4 + g);
+            const float xs[4] = {a.x, a.y, a.z, a.w};
+            const float ys[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float x = xs[k], y = ys[k];
+                if (!(x >= p.xminf && x <= p.xmaxf && y >= p.yminf && y <= p.ymaxf)) continue;
+                const int xi = min(max(__float_as_int(__fadd_rz(__fmaf_rn(x, p.sxf, p.txf), MAGIC)) - MAGIC_BITS, 0),
+                                   p.W - 1);
+                const int yi = min(max(__float_as_int(__fadd_rz(__fmaf_rn(y, p.syf, p.tyf), MAGIC)) - MAGIC_BITS, 0),
+                                   p.H - 1);
+                atomicAdd(&hist[(yi >> TS) * p.tiles_x + (xi >> TS)], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    select_tiles(p, hist, tab, slot_tile);
+    {
+        uint4 *c4 = (uint4 *)smem;
+        const int words = p.cnt_off / 16 + p.K * (TILE_PX / 8);
+        for (int i = threadIdx.x; i < words; i += THREADS) c4[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __syncthreads();
+
+    RowConsts rk;
+    rk.sxf = p.sxf; rk.txf = p.txf; rk.syf = p.syf; rk.tyf = p.tyf;
+    rk.exlo = p.ex_lo; rk.exhi = p.ex_hi; rk.eylo = p.ey_lo; rk.eyhi = p.ey_hi;
+    rk.W = p.W; rk.H = p.H; rk.W2 = p.W + 2; rk.H2 = p.H + 2; rk.tx2 = 2 * p.tiles_x;
+    rk.tab = smem_addr(tab); rk.cache = smem_addr(cw);
+    rk.out = (unsigned long long)p.out;
+    const unsigned sums_s = smem_addr(sums);
+    const unsigned long long sout = (unsigned long long)p.sum_out;
+    for (int64_t g = g0 + threadIdx.x; g < g1; g += THREADS) {
+        const float4 a = __ldcs(x4 + g), b = __ldcs(y4 + g);
+        const double2 c0 = __ldcs(v2 + 2 * g), c1 = __ldcs(v2 + 2 * g + 1);
+        unsigned slowm = 0, ovf = 0;
+        mean_row(rk, sums_s, sout, a.x, b.x, c0.x, 1u, slowm, ovf);
+        mean_row(rk, sums_s, sout, a.y, b.y, c0.y, 2u, slowm, ovf);
+        mean_row(rk, sums_s, sout, a.z, b.z, c1.x, 4u, slowm, ovf);
+        mean_row(rk, sums_s, sout, a.w, b.w, c1.y, 8u, slowm, ovf);
+        if (slowm) {
+#pragma unroll 1
+            for (int k = 0; k < 4; ++k)
+                if ((slowm >> k) & 1u) ovf |= slow_row_mean(&p, tab, sums, cw, 4 * g + k);
+        }
+        if (ovf & 0x80008000u) fix_words(&p, tab, slot_tile, cw, 4 * g);
+    }
+    if (blockIdx.x == gridDim.x - 1) {
+        for (int64_t row = 4 * p.n4 + threadIdx.x; row < p.n; row += THREADS) {
+            const double v = p.vs[row];
+            if (isnull(v)) continue;
+            const unsigned long long r = exact_bin(p.xs[row], p.ys[row], &p);
+            if (r == ~0ull) continue;
+            const int64_t pix = (int64_t)(unsigned)(r >> 32) * p.W + (unsigned)r;
+            atomicAdd(&p.sum_out[pix], v);
+            atomicAdd(&p.out[pix], 1u);
+        }
+    }
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (p.use_tma) {
+        // sums: one bulk float64 reduction per tile row (16 values, 128 bytes)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        bool issued = false;
+        for (int r = threadIdx.x; r < p.K * 16; r += THREADS) {
+            const int slot = r >> 4, ry = r & 15;
+            const int t = slot_tile[slot];
+            if (t < 0) continue;
+            const int yi = (t / p.tiles_x) * 16 + ry, x0 = (t % p.tiles_x) * 16;
+            if (yi >= p.H) continue;
+            const int ncols = p.W - x0 < 16 ? p.W - x0 : 16;       // even: W is a multiple of 4 here
+            const double *src = sums + (size_t)slot * TILE_PX + ry * 16;
+            asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f64 [%0], [%1], %2;"
+                         :: "l"(p.sum_out + (int64_t)yi * p.W + x0), "r"(smem_addr(src)), "r"(ncols * 8)
+                         : "memory");
+            issued = true;
+        }
+        if (issued) asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        // counts: 16-bit pairs widened in place, a tensor reduction per tile
+        for (int j = warp; 2 * j < p.K; j += THREADS / 32) {
+            unsigned char *region = (unsigned char *)cw + (size_t)j * 1024;
+            const uint4 q0 = *(const uint4 *)(region + 16 * lane);
+            const uint4 q1 = *(const uint4 *)(region + 512 + 16 * lane);
+            __syncwarp();
+            const int t0 = slot_tile[2 * j];
+            const int t1 = 2 * j + 1 < p.K ? slot_tile[2 * j + 1] : -1;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint4 q = h ? q1 : q0;
+                const int t = h ? t1 : t0;
+                if (t < 0) continue;
+                *(uint4 *)(region + 32 * lane) = make_uint4(q.x & 0xffffu, q.x >> 16, q.y & 0xffffu, q.y >> 16);
+                *(uint4 *)(region + 32 * lane + 16) = make_uint4(q.z & 0xffffu, q.z >> 16, q.w & 0xffffu, q.w >> 16);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) tma_reduce_tile(&tmap, t, p.tiles_x, smem_addr(region));
+                __syncwarp();
+            }
+        }
+        if (issued) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        return;
+    }
+    for (int i = threadIdx.x; i < p.K * TILE_PX; i += THREADS) {
+        const unsigned c = (cw[i >> 1] >> ((i & 1) * 16)) & 0xffffu;
+        if (!c) continue;
+        const int t = slot_tile[i >> (2 * TS)];
+        if (t < 0) continue;
+        const int within = i & (TILE_PX - 1);
+        const int64_t pix = (int64_t)(((t / p.tiles_x) << TS) + (within >> TS)) * p.W + ((t % p.tiles_x) << TS) +
+                            (within & 15);
+        atomicAdd(&p.out[pix], c);
+        atomicAdd(&p.sum_out[pix], sums[i]);
+    }
+}
+
 // ------------------------------------------------------------------ host
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -423,14 +659,11 @@ static bool edges_ok(float lo, float hi, double s, double t, int n) {
            image64(hi, s, t) < n + 0.5 && image64(nextafterf(hi, INFINITY), s, t) >= (double)n;
 }
 
-}  // namespace hot
-
-// DSGB_E_UNSUPPORTED when the case is not covered (the caller then takes
-// another path).  No workspace.
-int launch_points_hot(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
-                      const BinAxis &ax, const BinAxis &ay, const BinBounds &bb, uint32_t *out, bool accumulate,
-                      cudaStream_t st) {
-    using namespace hot;
+// Common set-up of both kernels; px_bytes is the shared memory a cached
+// pixel takes (2: count; 10: mean's float64 sum and 16-bit count).
+static int hot_setup(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv, const BinAxis &ax,
+                     const BinAxis &ay, const BinBounds &bb, uint32_t *out, int px_bytes, Params &p, int &smem,
+                     CUtensorMap &tmap) {
     if (xc.dtype != DSGB_F32 || yc.dtype != DSGB_F32 || n < MIN_ROWS) return DSGB_E_UNSUPPORTED;
     if (((uintptr_t)xc.data | (uintptr_t)yc.data) & 15u) return DSGB_E_UNSUPPORTED;
     if (cv->x_log || cv->y_log || !fast_path_ok(ax, ay)) return DSGB_E_UNSUPPORTED;
@@ -439,7 +672,6 @@ int launch_points_hot(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const
     if ((int64_t)tiles_x * tiles_y > MAX_TILES) return DSGB_E_UNSUPPORTED;
     if (!edges_ok(bb.xminf, bb.xmaxf, cv->sx, cv->tx, W) || !edges_ok(bb.yminf, bb.ymaxf, cv->sy, cv->ty, H))
         return DSGB_E_UNSUPPORTED;
-    Params p;
     memset(&p, 0, sizeof(p));
     p.xs = (const float *)xc.data; p.ys = (const float *)yc.data; p.n = n; p.n4 = n / 4;
     p.W = W; p.H = H; p.tiles_x = tiles_x; p.ntiles = tiles_x * tiles_y;
@@ -451,19 +683,20 @@ int launch_points_hot(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const
     p.out = out;
     const int tab_bytes = (p.ntiles * 2 + 127) & ~127;
     const int st_bytes = MAX_SLOTS * 2;
-    int K = (DYN_SMEM - tab_bytes - st_bytes) / (TILE_PX * 2);
+    int K = (DYN_SMEM - tab_bytes - st_bytes - 1024) / (TILE_PX * px_bytes);
     K = std::min(K, MAX_SLOTS);
     K = std::min(K, p.ntiles);
     K &= ~1;                                          // slot pairs in the flush
     if (K < 2) return DSGB_E_UNSUPPORTED;
     p.K = K;
-    int cache_bytes = K * TILE_PX * 2;                // a multiple of 1 KB
+    const int sum_bytes = px_bytes > 2 ? K * TILE_PX * 8 : 0;
+    p.cnt_off = sum_bytes;                            // multiples of 1 KB
+    int cache_bytes = sum_bytes + K * TILE_PX * 2;
     if (cache_bytes < p.ntiles * 4) cache_bytes = (p.ntiles * 4 + 1023) & ~1023;   // the prologue's histogram
     p.tab_off = cache_bytes;
     p.st_off = cache_bytes + tab_bytes;
-    const int smem = p.st_off + st_bytes;
+    smem = p.st_off + st_bytes;
     if (smem > DYN_SMEM) return DSGB_E_UNSUPPORTED;
-    CUtensorMap tmap;
     memset(&tmap, 0, sizeof(tmap));
     if ((W % 4) == 0 && (((uintptr_t)out) & 15u) == 0) {
         auto fn = encode_fn();
@@ -478,15 +711,60 @@ int launch_points_hot(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const
                 p.use_tma = 1;
         }
     }
+    return DSGB_OK;
+}
+
+}  // namespace hot
+
+// DSGB_E_UNSUPPORTED when the case is not covered (the caller then takes
+// another path).  No workspace.
+int launch_points_hot(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv,
+                      const BinAxis &ax, const BinAxis &ay, const BinBounds &bb, uint32_t *out, bool accumulate,
+                      cudaStream_t st) {
+    using namespace hot;
+    Params p;
+    int smem = 0;
+    CUtensorMap tmap;
+    int rc = hot_setup(xc, yc, n, cv, ax, ay, bb, out, 2, p, smem, tmap);
+    if (rc) return rc;
     const int sms = sm_count();
     if (sms <= 0) return cuda_status(cudaErrorNoDevice, "points hot: device");
     cudaError_t e = cudaSuccess;
-    if (!accumulate) e = cudaMemsetAsync(out, 0, (size_t)W * H * 4, st);
+    if (!accumulate) e = cudaMemsetAsync(out, 0, (size_t)p.W * p.H * 4, st);
     if (e != cudaSuccess) return cuda_status(e, "points hot: memset");
     e = cudaFuncSetAttribute(hot_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_status(e, "points hot: shared memory attribute");
     hot_count_kernel<<<sms, THREADS, smem, st>>>(p, tmap);
     DSGB_CHECK_LAUNCH("points hot: launch");
+    return DSGB_OK;
+}
+
+// mean('v') of float32 x/y and a float64 value column: sum into the SUM base,
+// non-NaN count into the COUNT base.
+int launch_points_hot_mean(const ColumnRef &xc, const ColumnRef &yc, const ColumnRef &vc, int64_t n,
+                           const dsgb_canvas *cv, const BinAxis &ax, const BinAxis &ay, const BinBounds &bb,
+                           double *sum, uint32_t *count, bool accumulate, cudaStream_t st) {
+    using namespace hot;
+    if (vc.dtype != DSGB_F64 || ((uintptr_t)vc.data & 15u) || (((uintptr_t)sum) & 15u) || (cv->width & 1))
+        return DSGB_E_UNSUPPORTED;
+    Params p;
+    int smem = 0;
+    CUtensorMap tmap;
+    int rc = hot_setup(xc, yc, n, cv, ax, ay, bb, count, 10, p, smem, tmap);
+    if (rc) return rc;
+    p.vs = (const double *)vc.data;
+    p.sum_out = sum;
+    const int sms = sm_count();
+    if (sms <= 0) return cuda_status(cudaErrorNoDevice, "points hot mean: device");
+    const size_t cells = (size_t)p.W * p.H;
+    cudaError_t e = cudaSuccess;
+    if (!accumulate) e = cudaMemsetAsync(count, 0, cells * 4, st);
+    if (e == cudaSuccess && !accumulate) e = cudaMemsetAsync(sum, 0, cells * 8, st);
+    if (e != cudaSuccess) return cuda_status(e, "points hot mean: memset");
+    e = cudaFuncSetAttribute(hot_mean_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return cuda_status(e, "points hot mean: shared memory attribute");
+    hot_mean_kernel<<<sms, THREADS, smem, st>>>(p, tmap);
+    DSGB_CHECK_LAUNCH("points hot mean: launch");
     return DSGB_OK;
 }
 
