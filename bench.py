@@ -61,6 +61,31 @@ def mean_traffic(n):
     return 329.75e6 / 2e7 * n + 3.51e6
 
 
+# float64 operations of the antialiased line forward per segment (adds + muls +
+# 2 x fmas, lanes with the predicate on), counted by ncu on 200 series x
+# 10,000 vertices of the same workload: 873.1 M operations for 1,999,800
+# segments.  The work per segment does not depend on the series count.
+LINE_FP64_FLOPS_PER_SEGMENT = 436.6
+
+
+def fp64_peak(dev):
+    """float64 FMA throughput of this GPU (TFLOP/s): the dsgb_fp64_probe
+    kernel timed with CUDA events, best of 5."""
+    import torch
+    from datashader_gb300 import _native as N
+    L = N.lib()
+    stream = torch.cuda.current_stream(dev)
+    sink = torch.zeros(1, dtype=torch.float64, device=dev)
+    fl = ctypes.c_int64(0)
+
+    def probe():
+        N.check(L.dsgb_fp64_probe(sink.data_ptr(), 4096, 8, ctypes.byref(fl), stream.cuda_stream), "fp64 probe")
+
+    probe()
+    times = _events_time(probe, 5, stream)
+    return fl.value / (min(times) / 1e3) / 1e12
+
+
 def bench_config(n, world):
     """The config dict both arms print (the driver compares them)."""
     return {"workload": workload(n), "n_points": n, "canvas": [1024, 1024], "x_range": [-4, 4],
@@ -324,6 +349,14 @@ def bench_pyramid(args, dev, peak, peak_kind):
     return res
 
 
+def _line_roofline(nseg, f_ms, dev):
+    peak = fp64_peak(dev)
+    achieved = LINE_FP64_FLOPS_PER_SEGMENT * nseg / (f_ms / 1e3) / 1e12
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_kind": "measured (dsgb_fp64_probe, float64 FMA chains)", "traffic": None,
+            "flops_per_segment": LINE_FP64_FLOPS_PER_SEGMENT}
+
+
 def bench_line(args, dev):
     """The differentiation workload: Canvas.line (LineAxis0, line_width 1.5,
     antialiased) of 1000 series x 10,000 float64 vertices (NaN separators,
@@ -380,6 +413,7 @@ def bench_line(args, dev):
     res = {"workload": f"Canvas.line LineAxis0 AA lw=1.5, {nseries} series x {length} float64 vertices, "
                        "1024x512, sum('v')",
            "forward_ms": f_ms, "forward_gsegments_per_s": nseg / (f_ms / 1e3) / 1e9,
+           "roofline": _line_roofline(nseg, f_ms, dev),
            "forward_backward_ms": fb_ms,
            "cpu_baseline": {"value": ns * (length - 1) / cpu_s / 1e9, "unit": "Gsegments/s", "cores": 1,
                             "kind": "port", "sample": f"{ns} series, one thread, {cpu_s:.2f} s"},
@@ -428,7 +462,8 @@ def bench_serving(args, dev):
     for rate in (int(r) for r in args.serving_rates.split(",")):
         per = {}
         for mode in args.serving_modes.split(","):
-            reqs = S.generate_requests(args.serving_requests, rate=rate, seed=rate)
+            nreq = args.serving_requests if mode != "plain" else min(args.serving_requests, args.serving_plain_requests)
+            reqs = S.generate_requests(nreq, rate=rate, seed=rate)
             server.peak_inflight = 0
             server.run(reqs, mode=mode)
             torch.cuda.synchronize()
@@ -688,7 +723,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--pyramid-n", type=int, default=200_000_000, help="0 skips the tile-pyramid workload")
     ap.add_argument("--serving-n", type=int, default=500_000_000, help="0 skips the viewport workload")
-    ap.add_argument("--serving-requests", type=int, default=1000)
+    ap.add_argument("--serving-requests", type=int, default=10000)
+    ap.add_argument("--serving-plain-requests", type=int, default=500,
+                    help="plain mode (one whole-frame call per request) runs this prefix of each stream")
     ap.add_argument("--line-series", type=int, default=1000, help="0 skips the line workload")
     ap.add_argument("--line-cpu-series", type=int, default=20)
     ap.add_argument("--serving-slots", type=int, default=8)

@@ -139,7 +139,7 @@ STATUS_CAS_GUARD, STATUS_INDEX = 0x1, 0x2
 
 # every symbol include/dsgb.h declares
 EXPORTED = (
-    "dsgb_abi_version", "dsgb_last_error", "dsgb_device_status", "dsgb_device_sm_count", "dsgb_bases_init", "dsgb_combine",
+    "dsgb_abi_version", "dsgb_last_error", "dsgb_device_status", "dsgb_fp64_probe", "dsgb_device_sm_count", "dsgb_bases_init", "dsgb_combine",
     "dsgb_finalize", "dsgb_finalize_partitioned", "dsgb_select_by_owner", "dsgb_points", "dsgb_points_workspace_size", "dsgb_points_workspace_size_flags",
     "dsgb_points_ws", "dsgb_points_segments",
     "dsgb_bucket_sort_workspace_size", "dsgb_bucket_sort", "dsgb_line_axis0", "dsgb_line_workspace_size", "dsgb_line_axis0_ws", "dsgb_lines", "dsgb_lines_2stage", "dsgb_lines_ragged", "dsgb_lines_ragged_2stage", "dsgb_line_axis0_backward", "dsgb_line_axis0_backward_ws",
@@ -163,6 +163,7 @@ def _declare(L):
     L.dsgb_last_error.restype = ctypes.c_char_p
     L.dsgb_device_sm_count.restype = ctypes.c_int
     L.dsgb_device_status.argtypes = [ctypes.POINTER(u32), i32]
+    L.dsgb_fp64_probe.argtypes = [P, i32, i32, ctypes.POINTER(i64), P]
     L.dsgb_bases_init.argtypes = [PB, i32, i64, P]
     L.dsgb_combine.argtypes = [PB, PB, i32, i64, P]
     L.dsgb_finalize.argtypes = [PC, i32, i64, PB, i32, PO, i32, i64, P]

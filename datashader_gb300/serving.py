@@ -267,12 +267,13 @@ class ViewportServer:
     light load large ones do not slow each other down by sharing the GPU."""
 
     def __init__(self, executor, slots=8, mem_budget=8 << 30, device=None, streams=None,
-                 heavy_bytes=256 << 20, max_heavy=1, max_heavy_backlogged=None):
+                 heavy_bytes=256 << 20, max_heavy=1, max_heavy_backlogged=None, exclusive_heavy=True):
         self.ex = executor
         self.slots = slots
         self.mem_budget = mem_budget
         self.heavy_bytes = heavy_bytes
         self.max_heavy = max_heavy
+        self.exclusive_heavy = exclusive_heavy
         # with more arrived requests waiting than there are slots, throughput
         # matters more than one request's latency: let heavy ones overlap
         self.max_heavy_backlogged = slots if max_heavy_backlogged is None else max_heavy_backlogged
@@ -315,8 +316,11 @@ class ViewportServer:
             while backlog < len(pending) and pending[backlog].arrival <= now:
                 backlog += 1
             heavy_cap = self.max_heavy if backlog <= self.slots else self.max_heavy_backlogged
+            light_load = backlog <= self.slots
             k = 0
             while k < len(pending) and free and pending[k].arrival <= now:
+                if mode == "batched" and self.exclusive_heavy and light_load and heavy_now > 0:
+                    break                      # a heavy request runs alone at light load
                 req = pending[k]
                 nbytes = self.ex.agg_bytes(req)
                 if inflight and mem + nbytes > self.mem_budget:
@@ -325,6 +329,8 @@ class ViewportServer:
                 if heavy and heavy_now >= heavy_cap:
                     k += 1                     # lighter requests behind it may go first
                     continue
+                if heavy and self.exclusive_heavy and light_load and inflight:
+                    break                      # starts once those in flight are done; later arrivals wait
                 del pending[k]
                 slot = free.pop()
                 req.admitted = clock() - t0

@@ -158,6 +158,12 @@ const char *dsgb_last_error(void);
  * the last clear, and clears them when `clear` is non-zero.  No counterpart
  * in the reference, whose appends run unchecked. */
 int dsgb_device_status(uint32_t *bits, int32_t clear);
+/* Launches a float64 FMA throughput probe (8 independent chains a thread,
+ * iters FMAs each, blocks_per_sm blocks of 256 threads an SM) and returns
+ * the FLOPs it performs in *flops; the caller times the launch with CUDA
+ * events.  A measurement aid for the roofline of the float64-bound kernels;
+ * no counterpart in the reference. */
+int dsgb_fp64_probe(double *sink, int32_t iters, int32_t blocks_per_sm, int64_t *flops, void *stream);
 /* Number of SMs of the current device (grid sizing), or a negative code. */
 int dsgb_device_sm_count(void);
 
