@@ -56,6 +56,8 @@ struct Params {
     float ex_lo, ex_hi, ey_lo, ey_hi;       // window of the fractional part that proves a bin
     float xminf, xmaxf, yminf, ymaxf;       // float32 images of the inclusive bounds
     double sx, tx, sy, ty;
+    double xmin, xmax, ymin, ymax;          // the inclusive bounds (the exact path's test)
+    int coord64;                            // x / y are float64 columns
     uint32_t *out;                          // count (the COUNT base of mean)
     const double *vs;                       // mean: the value column
     double *sum_out;                        // mean: the float64 SUM base
@@ -203,12 +205,27 @@ __device__ __forceinline__ void count_row(const RowConsts &k, float x, float y, 
 
 // The reference formula (bounds, then int(x*sx + tx) in float64, clamp) for
 // one row; returns packed (xi, yi) or ~0 when outside the bounds.
-static __device__ __noinline__ unsigned long long exact_bin(float x, float y, const Params *pp) {
+static __device__ __noinline__ unsigned long long exact_bin(int64_t row, const Params *pp) {
     const Params &p = *pp;
-    if (!(x >= p.xminf && x <= p.xmaxf && y >= p.yminf && y <= p.ymaxf)) return ~0ull;
-    const unsigned xi = (unsigned)bin_exact64_st((double)x, p.sx, p.tx, p.W);
-    const unsigned yi = (unsigned)bin_exact64_st((double)y, p.sy, p.ty, p.H);
+    const double x = p.coord64 ? ((const double *)p.xs)[row] : (double)p.xs[row];
+    const double y = p.coord64 ? ((const double *)p.ys)[row] : (double)p.ys[row];
+    if (!(p.xmin <= x && x <= p.xmax && p.ymin <= y && y <= p.ymax)) return ~0ull;
+    const unsigned xi = (unsigned)bin_exact64_st(x, p.sx, p.tx, p.W);
+    const unsigned yi = (unsigned)bin_exact64_st(y, p.sy, p.ty, p.H);
     return (unsigned long long)xi | ((unsigned long long)yi << 32);
+}
+
+// float32 image of a float64 coordinate by mantissa truncation (integer
+// operations): within 2^-23 relative, the truncation term of the error bound
+// E; magnitudes below the float32 normal range become +-0 (an absolute
+// error far below E), above it +-inf, NaN stays NaN.
+__device__ __forceinline__ float trunc_f32(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e >= 1 && e <= 254) return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+    if (e > 254) return __uint_as_float(sign | 0x7f800000u | (((b << 12) != 0) ? 0x400000u : 0u));
+    return __uint_as_float(sign);
 }
 
 __device__ __forceinline__ unsigned half_index(int s, int xi, int yi) {
@@ -219,7 +236,7 @@ __device__ __forceinline__ unsigned half_index(int s, int xi, int yi) {
 // of a shared increment (0 for an L2 one or an outside row).
 static __device__ __noinline__ unsigned slow_row(const Params *pp, const short *tab, unsigned *cw, int64_t row) {
     const Params &p = *pp;
-    const unsigned long long r = exact_bin(p.xs[row], p.ys[row], pp);
+    const unsigned long long r = exact_bin(row, pp);
     if (r == ~0ull) return 0u;
     const int xi = (int)(unsigned)r, yi = (int)(unsigned)(r >> 32);
     const int s = tab[(yi >> TS) * p.tiles_x + (xi >> TS)];
@@ -243,7 +260,7 @@ static __device__ __noinline__ void fix_words(const Params *pp, const short *tab
     for (int k = 0; k < 4; ++k) {
         const int64_t row = row0 + k;
         if (row >= p.n) continue;
-        const unsigned long long r = exact_bin(p.xs[row], p.ys[row], pp);
+        const unsigned long long r = exact_bin(row, pp);
         if (r == ~0ull) continue;
         const int xi = (int)(unsigned)r, yi = (int)(unsigned)(r >> 32);
         const int s = tab[(yi >> TS) * p.tiles_x + (xi >> TS)];
@@ -278,14 +295,31 @@ __device__ __forceinline__ void tma_reduce_tile(const CUtensorMap *map, int tile
     asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
+// Rows 4g .. 4g+3 of x and y as float32 images (float64 columns truncated).
+template <bool C64, bool STREAM>
+__device__ __forceinline__ void load_rows4(const Params &p, int64_t g, float4 &a, float4 &b) {
+    if (C64) {
+        const double2 *x2 = (const double2 *)p.xs, *y2 = (const double2 *)p.ys;
+        const double2 u0 = STREAM ? __ldcs(x2 + 2 * g) : __ldg(x2 + 2 * g);
+        const double2 u1 = STREAM ? __ldcs(x2 + 2 * g + 1) : __ldg(x2 + 2 * g + 1);
+        const double2 w0 = STREAM ? __ldcs(y2 + 2 * g) : __ldg(y2 + 2 * g);
+        const double2 w1 = STREAM ? __ldcs(y2 + 2 * g + 1) : __ldg(y2 + 2 * g + 1);
+        a = make_float4(trunc_f32(u0.x), trunc_f32(u0.y), trunc_f32(u1.x), trunc_f32(u1.y));
+        b = make_float4(trunc_f32(w0.x), trunc_f32(w0.y), trunc_f32(w1.x), trunc_f32(w1.y));
+    } else {
+        const float4 *x4 = (const float4 *)p.xs, *y4 = (const float4 *)p.ys;
+        a = STREAM ? __ldcs(x4 + g) : __ldg(x4 + g);
+        b = STREAM ? __ldcs(y4 + g) : __ldg(y4 + g);
+    }
+}
+
+template <bool C64>
 __global__ void __launch_bounds__(THREADS, 1) hot_count_kernel(const __grid_constant__ Params p,
                                                                const __grid_constant__ CUtensorMap tmap) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned *cw = (unsigned *)smem;                          // K tiles of 16-bit counters
     short *tab = (short *)(smem + p.tab_off);
     short *slot_tile = (short *)(smem + p.st_off);
-    const float4 *x4 = (const float4 *)p.xs;
-    const float4 *y4 = (const float4 *)p.ys;
     const int64_t g0 = p.n4 * blockIdx.x / gridDim.x, g1 = p.n4 * (blockIdx.x + 1) / gridDim.x;
     const int64_t full = g0 + ((g1 - g0) / THREADS) * THREADS;
 
@@ -295,7 +329,8 @@ __global__ void __launch_bounds__(THREADS, 1) hot_count_kernel(const __grid_cons
     __syncthreads();
     if (g1 > g0) {
         const int64_t g = g0 + (g1 - g0) * threadIdx.x / THREADS;
-        const float4 a = __ldg(x4 + g), b = __ldg(y4 + g);
+        float4 a, b;
+        load_rows4<C64, false>(p, g, a, b);
         const float xs[4] = {a.x, a.y, a.z, a.w};
         const float ys[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
@@ -325,7 +360,8 @@ __global__ void __launch_bounds__(THREADS, 1) hot_count_kernel(const __grid_cons
     rk.tab = smem_addr(tab); rk.cache = smem_addr(cw);
     rk.out = (unsigned long long)p.out;
     for (int64_t g = g0 + threadIdx.x; g < full; g += THREADS) {
-        const float4 a = __ldcs(x4 + g), b = __ldcs(y4 + g);
+        float4 a, b;
+        load_rows4<C64, true>(p, g, a, b);
         unsigned slowm = 0, ovf = 0;
         count_row(rk, a.x, b.x, 1u, slowm, ovf);
         count_row(rk, a.y, b.y, 2u, slowm, ovf);
@@ -344,7 +380,7 @@ __global__ void __launch_bounds__(THREADS, 1) hot_count_kernel(const __grid_cons
     }
     if (blockIdx.x == gridDim.x - 1) {
         for (int64_t row = 4 * p.n4 + threadIdx.x; row < p.n; row += THREADS) {
-            const unsigned long long r = exact_bin(p.xs[row], p.ys[row], &p);
+            const unsigned long long r = exact_bin(row, &p);
             if (r != ~0ull) atomicAdd(&p.out[(int64_t)(unsigned)(r >> 32) * p.W + (unsigned)r], 1u);
         }
     }
@@ -473,7 +509,7 @@ static __device__ __noinline__ unsigned slow_row_mean(const Params *pp, const sh
     const Params &p = *pp;
     const double v = p.vs[row];
     if (isnull(v)) return 0u;
-    const unsigned long long r = exact_bin(p.xs[row], p.ys[row], pp);
+    const unsigned long long r = exact_bin(row, pp);
     if (r == ~0ull) return 0u;
     const int xi = (int)(unsigned)r, yi = (int)(unsigned)(r >> 32);
     const int s = tab[(yi >> TS) * p.tiles_x + (xi >> TS)];
@@ -558,7 +594,7 @@ __global__ void __launch_bounds__(THREADS, 1) hot_mean_kernel(const __grid_const
         for (int64_t row = 4 * p.n4 + threadIdx.x; row < p.n; row += THREADS) {
             const double v = p.vs[row];
             if (isnull(v)) continue;
-            const unsigned long long r = exact_bin(p.xs[row], p.ys[row], &p);
+            const unsigned long long r = exact_bin(row, &p);
             if (r == ~0ull) continue;
             const int64_t pix = (int64_t)(unsigned)(r >> 32) * p.W + (unsigned)r;
             atomicAdd(&p.sum_out[pix], v);
@@ -659,19 +695,36 @@ static bool edges_ok(float lo, float hi, double s, double t, int n) {
            image64(hi, s, t) < n + 0.5 && image64(nextafterf(hi, INFINITY), s, t) >= (double)n;
 }
 
+// The same for float64 coordinates: the bounds themselves and the doubles
+// next to them.
+static double image64d(double v, double s, double t) {
+    volatile double a = v * s;
+    volatile double b = a + t;
+    return b;
+}
+static bool edges_ok64(double lo, double hi, double s, double t, int n) {
+    if (!(s > 0.0) || !std::isfinite(lo) || !std::isfinite(hi) || !(hi >= lo)) return false;
+    return image64d(nextafter(lo, -INFINITY), s, t) <= 0.0 && image64d(lo, s, t) >= 0.0 &&
+           image64d(hi, s, t) < n + 0.5 && image64d(nextafter(hi, INFINITY), s, t) >= (double)n;
+}
+
 // Common set-up of both kernels; px_bytes is the shared memory a cached
 // pixel takes (2: count; 10: mean's float64 sum and 16-bit count).
 static int hot_setup(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const dsgb_canvas *cv, const BinAxis &ax,
                      const BinAxis &ay, const BinBounds &bb, uint32_t *out, int px_bytes, Params &p, int &smem,
                      CUtensorMap &tmap) {
-    if (xc.dtype != DSGB_F32 || yc.dtype != DSGB_F32 || n < MIN_ROWS) return DSGB_E_UNSUPPORTED;
+    const bool c64 = xc.dtype == DSGB_F64 && yc.dtype == DSGB_F64;
+    if (!(c64 || (xc.dtype == DSGB_F32 && yc.dtype == DSGB_F32)) || n < MIN_ROWS) return DSGB_E_UNSUPPORTED;
     if (((uintptr_t)xc.data | (uintptr_t)yc.data) & 15u) return DSGB_E_UNSUPPORTED;
     if (cv->x_log || cv->y_log || !fast_path_ok(ax, ay)) return DSGB_E_UNSUPPORTED;
     const int W = cv->width, H = cv->height;
     const int tiles_x = (W + 15) >> 4, tiles_y = (H + 15) >> 4;
     if ((int64_t)tiles_x * tiles_y > MAX_TILES) return DSGB_E_UNSUPPORTED;
-    if (!edges_ok(bb.xminf, bb.xmaxf, cv->sx, cv->tx, W) || !edges_ok(bb.yminf, bb.ymaxf, cv->sy, cv->ty, H))
-        return DSGB_E_UNSUPPORTED;
+    const bool edges = c64 ? edges_ok64(cv->xmin, cv->xmax, cv->sx, cv->tx, W) &&
+                                 edges_ok64(cv->ymin, cv->ymax, cv->sy, cv->ty, H)
+                           : edges_ok(bb.xminf, bb.xmaxf, cv->sx, cv->tx, W) &&
+                                 edges_ok(bb.yminf, bb.ymaxf, cv->sy, cv->ty, H);
+    if (!edges) return DSGB_E_UNSUPPORTED;
     memset(&p, 0, sizeof(p));
     p.xs = (const float *)xc.data; p.ys = (const float *)yc.data; p.n = n; p.n4 = n / 4;
     p.W = W; p.H = H; p.tiles_x = tiles_x; p.ntiles = tiles_x * tiles_y;
@@ -680,6 +733,8 @@ static int hot_setup(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const 
     p.ey_lo = float_ceil_of((double)ay.e); p.ey_hi = float_floor_of(1.0 - (double)ay.e);
     p.xminf = bb.xminf; p.xmaxf = bb.xmaxf; p.yminf = bb.yminf; p.ymaxf = bb.ymaxf;
     p.sx = cv->sx; p.tx = cv->tx; p.sy = cv->sy; p.ty = cv->ty;
+    p.xmin = cv->xmin; p.xmax = cv->xmax; p.ymin = cv->ymin; p.ymax = cv->ymax;
+    p.coord64 = c64;
     p.out = out;
     const int tab_bytes = (p.ntiles * 2 + 127) & ~127;
     const int st_bytes = MAX_SLOTS * 2;
@@ -732,9 +787,15 @@ int launch_points_hot(const ColumnRef &xc, const ColumnRef &yc, int64_t n, const
     cudaError_t e = cudaSuccess;
     if (!accumulate) e = cudaMemsetAsync(out, 0, (size_t)p.W * p.H * 4, st);
     if (e != cudaSuccess) return cuda_status(e, "points hot: memset");
-    e = cudaFuncSetAttribute(hot_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return cuda_status(e, "points hot: shared memory attribute");
-    hot_count_kernel<<<sms, THREADS, smem, st>>>(p, tmap);
+    if (p.coord64) {
+        e = cudaFuncSetAttribute(hot_count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return cuda_status(e, "points hot: shared memory attribute");
+        hot_count_kernel<true><<<sms, THREADS, smem, st>>>(p, tmap);
+    } else {
+        e = cudaFuncSetAttribute(hot_count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return cuda_status(e, "points hot: shared memory attribute");
+        hot_count_kernel<false><<<sms, THREADS, smem, st>>>(p, tmap);
+    }
     DSGB_CHECK_LAUNCH("points hot: launch");
     return DSGB_OK;
 }
@@ -752,6 +813,7 @@ int launch_points_hot_mean(const ColumnRef &xc, const ColumnRef &yc, const Colum
     CUtensorMap tmap;
     int rc = hot_setup(xc, yc, n, cv, ax, ay, bb, count, 10, p, smem, tmap);
     if (rc) return rc;
+    if (p.coord64) return DSGB_E_UNSUPPORTED;         // float32 coordinates only
     p.vs = (const double *)vc.data;
     p.sum_out = sum;
     const int sms = sm_count();

@@ -267,13 +267,13 @@ class ViewportServer:
     light load large ones do not slow each other down by sharing the GPU."""
 
     def __init__(self, executor, slots=8, mem_budget=8 << 30, device=None, streams=None,
-                 heavy_bytes=256 << 20, max_heavy=1, max_heavy_backlogged=None, exclusive_heavy=True):
+                 heavy_bytes=256 << 20, max_heavy=1, max_heavy_backlogged=None, solo_bytes=32 << 20):
         self.ex = executor
         self.slots = slots
         self.mem_budget = mem_budget
         self.heavy_bytes = heavy_bytes
         self.max_heavy = max_heavy
-        self.exclusive_heavy = exclusive_heavy
+        self.solo_bytes = solo_bytes
         # with more arrived requests waiting than there are slots, throughput
         # matters more than one request's latency: let heavy ones overlap
         self.max_heavy_backlogged = slots if max_heavy_backlogged is None else max_heavy_backlogged
@@ -302,7 +302,7 @@ class ViewportServer:
             now = clock() - t0
             progressed = False
             for slot in list(inflight):
-                req, ev, nbytes, _ = inflight[slot]
+                req, ev, nbytes, _, _ = inflight[slot]
                 if ev.query():
                     req.done = clock() - t0
                     if not keep_results:
@@ -311,7 +311,8 @@ class ViewportServer:
                     free.append(slot)
                     mem -= nbytes
                     progressed = True
-            heavy_now = sum(1 for _, _, _, h in inflight.values() if h)
+            heavy_now = sum(1 for _, _, _, h, _ in inflight.values() if h)
+            solo_now = any(so for _, _, _, _, so in inflight.values())
             backlog = 0
             while backlog < len(pending) and pending[backlog].arrival <= now:
                 backlog += 1
@@ -319,8 +320,8 @@ class ViewportServer:
             light_load = backlog <= self.slots
             k = 0
             while k < len(pending) and free and pending[k].arrival <= now:
-                if mode == "batched" and self.exclusive_heavy and light_load and heavy_now > 0:
-                    break                      # a heavy request runs alone at light load
+                if light_load and solo_now:
+                    break                      # a large request runs alone at light load
                 req = pending[k]
                 nbytes = self.ex.agg_bytes(req)
                 if inflight and mem + nbytes > self.mem_budget:
@@ -329,7 +330,8 @@ class ViewportServer:
                 if heavy and heavy_now >= heavy_cap:
                     k += 1                     # lighter requests behind it may go first
                     continue
-                if heavy and self.exclusive_heavy and light_load and inflight:
+                solo = mode == "batched" and light_load and self.ex.work_bytes(req) > self.solo_bytes
+                if solo and inflight:
                     break                      # starts once those in flight are done; later arrivals wait
                 del pending[k]
                 slot = free.pop()
@@ -339,7 +341,8 @@ class ViewportServer:
                 else:
                     ev, result = self.ex.launch(req, self.streams[slot])
                 req.result = result
-                inflight[slot] = (req, ev, nbytes, heavy)
+                inflight[slot] = (req, ev, nbytes, heavy, solo)
+                solo_now = solo_now or solo
                 heavy_now += heavy
                 mem += nbytes
                 self.peak_mem = max(self.peak_mem, mem)

@@ -382,3 +382,35 @@ def test_cached_paths_adversarial_coordinates(w, h, xr, yr):
     assert_same(got, run_points(cols, {}, ds.count(), canvas))
     got = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", ds.mean("v")))
     assert_same(got, run_points(cols, {}, ds.mean("v"), canvas), rtol=1e-12)
+
+
+def _edge_coords64(lo, hi, npx, rng, m):
+    """float64 coordinates for the same decisions: pixel edges and the
+    doubles next to them, the bounds and beyond, values below the float32
+    normal range (1e-40, 1e-310) and beyond its top (1e39, 1e300), non-finite."""
+    px = (hi - lo) / npx
+    edges = lo + np.arange(npx + 1) * px
+    specials = [lo, hi, np.nextafter(lo, -np.inf), np.nextafter(lo, np.inf), np.nextafter(hi, -np.inf),
+                np.nextafter(hi, np.inf)]
+    for f in (-2.0, -1.0, -0.5, -1e-9, 1e-9, 0.5, 0.75):
+        specials += [lo + f * px, hi - f * px]
+    specials += [np.nan, np.inf, -np.inf, 1e39, -1e39, 1e300, -1e300, 0.0, -0.0, 1e-40, -1e-40, 1e-310, 5e-324]
+    probe = np.concatenate([edges, np.nextafter(edges, np.inf), np.nextafter(edges, -np.inf),
+                            edges + 1e-8 * px, edges - 1e-8 * px, np.asarray(specials, np.float64)])
+    out = rng.normal((lo + hi) / 2, (hi - lo) / 5, m)
+    idx = rng.choice(m, size=min(m // 3, 40 * probe.size), replace=False)
+    out[idx] = probe[rng.integers(0, probe.size, idx.size)]
+    return out
+
+
+@pytest.mark.parametrize("w,h,xr,yr", [(512, 512, (-4.0, 4.0), (-4.0, 4.0)),
+                                       (1024, 768, (-1e-3, 2e-3), (-3.3, 2.7))])
+def test_hot_count_float64_adversarial_coordinates(w, h, xr, yr):
+    """float64 coordinates through the hot-tile count kernel (float32 images
+    by truncation, proven by the error bound): bit-exact against the oracle."""
+    n = 1_500_000
+    rng = np.random.default_rng(w * 7 + h)
+    cols = {"x": _edge_coords64(xr[0], xr[1], w, rng, n), "y": _edge_coords64(yr[0], yr[1], h, rng, n)}
+    canvas = dict(plot_width=w, plot_height=h, x_range=xr, y_range=yr)
+    got = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols), "x", "y", ds.count()))
+    assert_same(got, run_points(cols, {}, ds.count(), canvas))
