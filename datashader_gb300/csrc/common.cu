@@ -349,6 +349,7 @@ namespace dsgb {
 int status_points(unsigned *bits, bool clear);
 int status_line(unsigned *bits, bool clear);
 int status_points_hot(unsigned *bits, bool clear);
+int status_points_part(unsigned *bits, bool clear);
 }
 
 extern "C" int dsgb_device_status(uint32_t *bits, int32_t clear) {
@@ -362,6 +363,7 @@ extern "C" int dsgb_device_status(uint32_t *bits, int32_t clear) {
     int rc = status_points(&v, clear != 0);
     if (rc == DSGB_OK) rc = status_line(&v, clear != 0);
     if (rc == DSGB_OK) rc = status_points_hot(&v, clear != 0);
+    if (rc == DSGB_OK) rc = status_points_part(&v, clear != 0);
     if (rc != DSGB_OK) return rc;
     *bits |= v;
     return DSGB_OK;

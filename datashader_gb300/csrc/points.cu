@@ -305,6 +305,8 @@ static bool cached_eligible(const PointsParams &p, uint32_t flags) {
 
 size_t det_workspace_size(int64_t n);
 int det_sums(const PointsParams &p, bool fast, void *ws, size_t ws_bytes, cudaStream_t st);
+size_t part_workspace_size(int64_t n, const dsgb_canvas *cv, const dsgb_base *bases, int32_t nbases);
+int launch_points_part(const PointsParams &p, const dsgb_base *bases, void *ws, size_t ws_bytes, cudaStream_t st);
 
 static bool has_sum_base(const PointsParams &p) {
     for (int b = 0; b < p.nbases; ++b)
@@ -393,8 +395,16 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
         rc = bases_init(bases, nbases, ncells, st);
         if (rc) return rc;
     }
-    rc = launch_points(p, flags, st);
-    if (rc) return rc;
+    rc = DSGB_E_UNSUPPORTED;
+    if (workspace && !(flags & (DSGB_FLAG_EXACT_BIN | DSGB_FLAG_WARP_AGG))) {
+        // plans of several bases: rows partitioned by canvas block, bases in shared memory (points_part.cu)
+        rc = launch_points_part(p, bases, workspace, ws_bytes, st);
+        if (rc != DSGB_OK && rc != DSGB_E_UNSUPPORTED) return rc;
+    }
+    if (rc == DSGB_E_UNSUPPORTED) {
+        rc = launch_points(p, flags, st);
+        if (rc) return rc;
+    }
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
         rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
     return rc;
@@ -416,7 +426,7 @@ extern "C" size_t dsgb_points_workspace_size(int64_t n, const dsgb_canvas *canva
     const bool mean = nbases == 2 && bases[0].op == DSGB_BASE_SUM && bases[1].op == DSGB_BASE_COUNT &&
                       bases[0].col >= 0 && bases[0].col == bases[1].col && bases[0].cat_col < 0 &&
                       bases[1].cat_col < 0;
-    if (!count && !mean) return 0;
+    if (!count && !mean) return part_workspace_size(n, canvas, bases, nbases);
     return cached_workspace_size(n, canvas->width, canvas->height);
 }
 

@@ -1,0 +1,688 @@
+// points_part.cu -- Canvas.points for plans of several bases over float32
+// coordinates (a summary of count / sum / mean / min / max / first / last /
+// where / by): rows partitioned by canvas block, each block aggregated in
+// shared memory.
+//
+// Replaces Point._build_extend (datashader/glyphs/points.py:182-242) with the
+// fused append of compiler.make_append (datashader/compiler.py:321-475) for
+// these plans.  With one L2 atomic per base and row, such a plan is bound by
+// the L2 atomic rate (about 2e11 a second on GB300: 8 bases over 1e8 rows take
+// 4 ms).  Here the atomics move into shared memory:
+//
+//   part_hist    -- bin every row (the exact binning of binning.cuh) and count
+//                   rows per canvas block (a block is a power-of-two rectangle
+//                   of pixels sized so that every base of the plan fits in
+//                   shared memory for the whole block);
+//   part_plan    -- one CTA: block offsets by an exclusive scan, and the work
+//                   items (a block's rows, split into items of at most 2^18);
+//   part_scatter -- bin the rows again (the same function, so the same block)
+//                   and write one 16-byte record per row {value, row, pixel in
+//                   the block, category} into its block's range: a CTA ranks a
+//                   batch of 2048 rows by block in shared memory and writes
+//                   each block's run contiguously;
+//   part_reduce  -- persistent CTAs take work items; each initialises every
+//                   base over its block in shared memory, applies the item's
+//                   records with shared-memory atomics, and adds the block into
+//                   the bases: plain read-modify-write when the block is one
+//                   item (no other CTA touches it), atomics otherwise.
+//
+// Every base combines order-independently (counts and sums add, min / max /
+// first / last / where keep the smaller row on ties: reductions.py:1178-1182,
+// 1223-1227), so the result is the reference's; float64 sums add in another
+// order than the reference's row loop (the 1e-12 tolerance of every atomic
+// sum).  Rows are processed in chunks of 2^27 so that a record's row fits in
+// 32 bits and the records take at most 2 GiB of workspace.
+#include "points_params.cuh"
+
+namespace dsgb {
+namespace part {
+
+constexpr int HIST_THREADS = 256;
+constexpr int SC_THREADS = 512;
+constexpr int SC_BATCH = 4 * SC_THREADS;        // rows a scatter CTA ranks at once
+constexpr int RD_THREADS = 1024;
+constexpr int PLAN_THREADS = 1024;
+constexpr int MAX_BLOCKS = 16384;
+constexpr int64_t CHUNK = (int64_t)1 << 27;
+constexpr int64_t ITEM = (int64_t)1 << 18;
+constexpr int64_t MAX_ITEMS = CHUNK / ITEM + MAX_BLOCKS + 1;
+constexpr int64_t MIN_ROWS = (int64_t)1 << 20;
+constexpr int STATE_BUDGET = 200 * 1024;         // shared memory for the bases of one block
+constexpr uint8_t CAT_NONE = 0xff;
+
+struct Rec {                                     // 16 bytes
+    double v;
+    uint32_t row;                                // row within the chunk
+    uint16_t lpix;                               // pixel within the block
+    uint8_t cat;                                 // category code, CAT_NONE when invalid
+    uint8_t pad;
+};
+
+struct PBase {
+    int32_t op, has_col, has_cat, ncat;
+    int32_t off;                                 // byte offset of its block state in shared memory
+    int32_t esize;
+    void *agg;
+};
+
+struct Params {
+    const float *xs, *ys;                        // the chunk's first row
+    ColumnRef vcol, ccol;                        // value / category column at the chunk's first row (data null: none)
+    int64_t n, row0;                             // rows of the chunk, global row of its first row
+    int W, H, bw_log, bh_log, bx, nblk;
+    int ncat;                                    // categories of the record's code (0: no category column)
+    BinAxis ax, ay;
+    BinBounds bb;
+    uint32_t *blk_count, *blk_start, *blk_cursor;
+    Rec *recs;
+    int4 *items;                                 // {block, begin, end, owned}
+    uint32_t *counters;                          // [0] items, [1] next item
+    int nbases, state_bytes;
+    PBase bases[MAX_BASES];
+};
+
+__device__ __forceinline__ bool bin_row(const Params &p, float x, float y, int &xi, int &yi) {
+    const int r = bin_try_f32(x, y, p.bb, p.ax, p.ay, xi, yi);
+    if (r == 2) bin_exact_f32(x, y, p.ax, p.ay, xi, yi);
+    return r != 0;
+}
+
+__device__ __forceinline__ int block_of(const Params &p, int xi, int yi) {
+    return (yi >> p.bh_log) * p.bx + (xi >> p.bw_log);
+}
+
+__device__ __forceinline__ unsigned local_pixel(const Params &p, int xi, int yi) {
+    return ((unsigned)(yi & ((1 << p.bh_log) - 1)) << p.bw_log) | (unsigned)(xi & ((1 << p.bw_log) - 1));
+}
+
+// ------------------------------------------------------------ part_hist
+__global__ void __launch_bounds__(HIST_THREADS) part_hist(const __grid_constant__ Params p) {
+    extern __shared__ unsigned hist[];
+    for (int i = threadIdx.x; i < p.nblk; i += HIST_THREADS) hist[i] = 0;
+    __syncthreads();
+    const int64_t n4 = p.n >> 2;
+    const float4 *x4 = (const float4 *)p.xs, *y4 = (const float4 *)p.ys;
+    for (int64_t g = (int64_t)blockIdx.x * HIST_THREADS + threadIdx.x; g < n4; g += (int64_t)gridDim.x * HIST_THREADS) {
+        const float4 a = __ldcs(x4 + g), b = __ldcs(y4 + g);
+        const float xs[4] = {a.x, a.y, a.z, a.w}, ys[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int xi, yi;
+            if (bin_row(p, xs[k], ys[k], xi, yi)) atomicAdd(&hist[block_of(p, xi, yi)], 1u);
+        }
+    }
+    if (blockIdx.x == 0) {
+        for (int64_t i = 4 * n4 + threadIdx.x; i < p.n; i += HIST_THREADS) {
+            int xi, yi;
+            if (bin_row(p, p.xs[i], p.ys[i], xi, yi)) atomicAdd(&hist[block_of(p, xi, yi)], 1u);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < p.nblk; i += HIST_THREADS)
+        if (hist[i]) atomicAdd(&p.blk_count[i], hist[i]);
+}
+
+// Exclusive scan of one value per thread over the CTA; returns the prefix
+// and leaves the total in *total.
+template <int T>
+__device__ __forceinline__ unsigned block_scan(unsigned v, unsigned *warp_sums, unsigned *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += t;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < T / 32 ? warp_sums[lane] : 0u;
+        unsigned wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, wi, d);
+            if (lane >= d) wi += t;
+        }
+        if (lane < T / 32) warp_sums[lane] = wi - w;
+        if (lane == 31) *total = wi;
+    }
+    __syncthreads();
+    return warp_sums[warp] + incl - v;
+}
+
+// ------------------------------------------------------------ part_plan
+__global__ void __launch_bounds__(PLAN_THREADS) part_plan(const __grid_constant__ Params p) {
+    __shared__ unsigned ws1[32], ws2[32];
+    __shared__ unsigned tot1, tot2;
+    constexpr int PER = MAX_BLOCKS / PLAN_THREADS;
+    unsigned c[PER], m[PER];
+    unsigned s1 = 0, s2 = 0;
+    const int b0 = threadIdx.x * PER;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int b = b0 + k;
+        c[k] = b < p.nblk ? p.blk_count[b] : 0u;
+        m[k] = (unsigned)((c[k] + ITEM - 1) / ITEM);
+        s1 += c[k];
+        s2 += m[k];
+    }
+    unsigned o1 = block_scan<PLAN_THREADS>(s1, ws1, &tot1);
+    unsigned o2 = block_scan<PLAN_THREADS>(s2, ws2, &tot2);
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int b = b0 + k;
+        if (b >= p.nblk) break;
+        p.blk_start[b] = o1;
+        p.blk_cursor[b] = o1;
+        for (unsigned j = 0; j < m[k]; ++j) {
+            const int64_t lo = (int64_t)c[k] * j / m[k], hi = (int64_t)c[k] * (j + 1) / m[k];
+            p.items[o2 + j] = make_int4(b, (int)(o1 + lo), (int)(o1 + hi), m[k] == 1 ? 1 : 0);
+        }
+        o1 += c[k];
+        o2 += m[k];
+    }
+    if (threadIdx.x == 0) {
+        p.blk_start[p.nblk] = tot1;
+        p.counters[0] = tot2;
+        p.counters[1] = 0;
+    }
+}
+
+// ------------------------------------------------------------ part_scatter
+__device__ __forceinline__ double load_value(const Params &p, int64_t i) {
+    return p.vcol.data ? load_f64(p.vcol, i) : 0.0;
+}
+
+__device__ __forceinline__ uint8_t load_code(const Params &p, int64_t i) {
+    if (!p.ccol.data) return CAT_NONE;
+    long long c = load_i64(p.ccol, i);
+    if (c < 0) c += p.ncat;                       // compiler.py:379-390: negative codes wrap
+    return (c < 0 || c >= p.ncat) ? CAT_NONE : (uint8_t)c;
+}
+
+__global__ void __launch_bounds__(SC_THREADS) part_scatter(const __grid_constant__ Params p) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    Rec *stage = (Rec *)sm;                                       // SC_BATCH records
+    uint16_t *sblk = (uint16_t *)(sm + SC_BATCH * sizeof(Rec));   // block of each staged record
+    unsigned *hist = (unsigned *)(sm + SC_BATCH * (sizeof(Rec) + 2));   // counts, then staging offsets
+    unsigned *delta = hist + p.nblk;                              // record index - staging index of a block's run
+    __shared__ unsigned warp_sums[32];
+    __shared__ unsigned s_total;
+    for (int i = threadIdx.x; i < p.nblk; i += SC_THREADS) hist[i] = 0;
+    __syncthreads();
+    const int64_t n4 = p.n >> 2;
+    const int64_t g0 = n4 * blockIdx.x / gridDim.x, g1 = n4 * (blockIdx.x + 1) / gridDim.x;
+    const float4 *x4 = (const float4 *)p.xs, *y4 = (const float4 *)p.ys;
+    const int per = (p.nblk + SC_THREADS - 1) / SC_THREADS;       // scan entries per thread
+    for (int64_t base = g0; base < g1; base += SC_THREADS) {
+        const int64_t g = base + threadIdx.x;
+        const bool live = g < g1;
+        int blk[4];
+        unsigned lp[4], rank[4];
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+        if (live) { a = __ldcs(x4 + g); b = __ldcs(y4 + g); }
+        const float xs[4] = {a.x, a.y, a.z, a.w}, ys[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int xi, yi;
+            blk[k] = -1;
+            if (live && bin_row(p, xs[k], ys[k], xi, yi)) {
+                blk[k] = block_of(p, xi, yi);
+                lp[k] = local_pixel(p, xi, yi);
+                rank[k] = atomicAdd(&hist[blk[k]], 1u);
+            }
+        }
+        __syncthreads();
+        // offsets of the blocks in the staging area, and their runs' places in the records
+        const int e0 = threadIdx.x * per;
+        {
+            unsigned s = 0;
+            for (int j = 0; j < per; ++j) {
+                const int e = e0 + j;
+                if (e < p.nblk) s += hist[e];
+            }
+            unsigned o = block_scan<SC_THREADS>(s, warp_sums, &s_total);
+            for (int j = 0; j < per; ++j) {
+                const int e = e0 + j;
+                if (e >= p.nblk) break;
+                const unsigned h = hist[e];
+                hist[e] = o;
+                if (h) delta[e] = atomicAdd(&p.blk_cursor[e], h) - o;
+                o += h;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (blk[k] < 0) continue;
+            const int64_t row = 4 * g + k;
+            const unsigned pos = hist[blk[k]] + rank[k];
+            Rec r;
+            r.v = load_value(p, row);
+            r.row = (uint32_t)row;
+            r.lpix = (uint16_t)lp[k];
+            r.cat = load_code(p, row);
+            r.pad = 0;
+            stage[pos] = r;
+            sblk[pos] = (uint16_t)blk[k];
+        }
+        __syncthreads();
+        const unsigned total = s_total;
+        for (unsigned i = threadIdx.x; i < total; i += SC_THREADS) {
+            const uint4 q = *(const uint4 *)(stage + i);
+            const unsigned dst = delta[sblk[i]] + i;
+            // both passes bin alike, so every run stays inside its block's range
+            if (dst < p.n) __stcg((uint4 *)(p.recs + dst), q);
+            else raise_status(DSGB_STATUS_INDEX);
+        }
+        for (int j = 0; j < per; ++j) {
+            const int e = e0 + j;
+            if (e < p.nblk) hist[e] = 0;
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == gridDim.x - 1) {
+        // the rows after the last float4 (at most 3)
+        for (int64_t i = 4 * n4 + threadIdx.x; i < p.n; i += SC_THREADS) {
+            int xi, yi;
+            if (!bin_row(p, p.xs[i], p.ys[i], xi, yi)) continue;
+            const int e = block_of(p, xi, yi);
+            Rec r;
+            r.v = load_value(p, i);
+            r.row = (uint32_t)i;
+            r.lpix = (uint16_t)local_pixel(p, xi, yi);
+            r.cat = load_code(p, i);
+            r.pad = 0;
+            const unsigned dst = atomicAdd(&p.blk_cursor[e], 1u);
+            if (dst < p.n) p.recs[dst] = r;
+            else raise_status(DSGB_STATUS_INDEX);
+        }
+    }
+}
+
+// ------------------------------------------------------------ part_reduce
+
+__device__ __forceinline__ void cas128_shared(unsigned addr, long long cmp_lo, long long cmp_hi, long long new_lo,
+                                              long long new_hi, long long &old_lo, long long &old_hi) {
+    asm volatile(
+        "{\n\t.reg .b128 d, c, n;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 n, {%4, %5};\n\t"
+        "atom.shared.cas.b128 d, [%6], c, n;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}"
+        : "=l"(old_lo), "=l"(old_hi)
+        : "l"(cmp_lo), "l"(cmp_hi), "l"(new_lo), "l"(new_hi), "r"(addr)
+        : "memory");
+}
+
+// pair_update (dsgb_internal.cuh) on a shared-memory pair.
+template <bool MAX>
+__device__ __forceinline__ void pair_update_shared(long long *slot, long long key, long long row) {
+    volatile long long *v = slot;
+    long long ok = v[0];
+    if (MAX ? (ok > key) : (ok < key)) return;
+    long long orow = v[1];
+    const unsigned addr = (unsigned)__cvta_generic_to_shared(slot);
+    for (int guard = 0; guard < (1 << 24); ++guard) {
+        long long rk, rr;
+        if (!pair_better<MAX>(key, row, ok, orow)) {
+            cas128_shared(addr, ok, orow, ok, orow, rk, rr);
+            if (rk == ok && rr == orow) return;
+        } else {
+            cas128_shared(addr, ok, orow, key, row, rk, rr);
+            if (rk == ok && rr == orow) return;
+        }
+        ok = rk; orow = rr;
+    }
+    raise_status(DSGB_STATUS_CAS_GUARD);
+}
+
+__device__ __forceinline__ void init_state(const Params &p, unsigned char *sm, int px) {
+    for (int b = 0; b < p.nbases; ++b) {
+        const PBase &B = p.bases[b];
+        const int cells = px * (B.has_cat ? B.ncat : 1);
+        unsigned char *s = sm + B.off;
+        switch (B.op) {
+        case DSGB_BASE_COUNT:
+            for (int i = threadIdx.x; i < cells; i += RD_THREADS) ((unsigned *)s)[i] = 0u;
+            break;
+        case DSGB_BASE_ANY:
+            for (int i = threadIdx.x; i < cells; i += RD_THREADS) s[i] = 0;
+            break;
+        case DSGB_BASE_SUM:
+            for (int i = threadIdx.x; i < cells; i += RD_THREADS) ((double *)s)[i] = 0.0;
+            break;
+        case DSGB_BASE_MAX:
+            for (int i = threadIdx.x; i < cells; i += RD_THREADS) ((long long *)s)[i] = KEY_EMPTY_MAX;
+            break;
+        case DSGB_BASE_MIN:
+            for (int i = threadIdx.x; i < cells; i += RD_THREADS) ((long long *)s)[i] = KEY_EMPTY_MIN;
+            break;
+        case DSGB_BASE_MIN_ROW:
+            for (int i = threadIdx.x; i < cells; i += RD_THREADS) ((long long *)s)[i] = ROW_EMPTY_MIN;
+            break;
+        case DSGB_BASE_MAX_ROW:
+            for (int i = threadIdx.x; i < cells; i += RD_THREADS) ((long long *)s)[i] = -1;
+            break;
+        case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: {
+            const long long k0 = B.op == DSGB_BASE_ARGMAX ? KEY_EMPTY_MAX : KEY_EMPTY_MIN;
+            for (int i = threadIdx.x; i < cells; i += RD_THREADS) {
+                ((long long *)s)[2 * i] = k0;
+                ((long long *)s)[2 * i + 1] = ROW_EMPTY_MIN;
+            }
+            break;
+        }
+        default: break;
+        }
+    }
+}
+
+// One record into every base's block state.
+__device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const Rec &r) {
+    const bool has = !isnull(r.v);
+    const long long key = f64_key(r.v);
+    const long long row = p.row0 + (long long)r.row;
+#pragma unroll 1
+    for (int b = 0; b < p.nbases; ++b) {
+        const PBase &B = p.bases[b];
+        if (B.has_col && !has) continue;
+        unsigned cell = r.lpix;
+        if (B.has_cat) {
+            if (r.cat == CAT_NONE) continue;
+            cell = cell * (unsigned)B.ncat + r.cat;
+        }
+        unsigned char *s = sm + B.off;
+        switch (B.op) {
+        case DSGB_BASE_COUNT: atomicAdd((unsigned *)s + cell, 1u); break;
+        case DSGB_BASE_ANY: s[cell] = 1; break;
+        case DSGB_BASE_SUM: atomicAdd((double *)s + cell, r.v); break;
+        case DSGB_BASE_MAX: {
+            long long *q = (long long *)s + cell;
+            if (*(volatile long long *)q < key) atomicMax(q, key);
+            break;
+        }
+        case DSGB_BASE_MIN: {
+            long long *q = (long long *)s + cell;
+            if (*(volatile long long *)q > key) atomicMin(q, key);
+            break;
+        }
+        case DSGB_BASE_MIN_ROW: {
+            long long *q = (long long *)s + cell;
+            if (*(volatile long long *)q > row) atomicMin(q, row);
+            break;
+        }
+        case DSGB_BASE_MAX_ROW: {
+            long long *q = (long long *)s + cell;
+            if (*(volatile long long *)q < row) atomicMax(q, row);
+            break;
+        }
+        case DSGB_BASE_ARGMAX: pair_update_shared<true>((long long *)s + 2 * cell, key, row); break;
+        case DSGB_BASE_ARGMIN: pair_update_shared<false>((long long *)s + 2 * cell, key, row); break;
+        default: break;
+        }
+    }
+}
+
+// The block's state into the bases: read-modify-write when this CTA owns
+// the block, atomics otherwise.  Cells holding the identity are skipped.
+__device__ __forceinline__ void flush_state(const Params &p, const unsigned char *sm, int blk, bool owned) {
+    const int bw = 1 << p.bw_log, bh = 1 << p.bh_log;
+    const int x0 = (blk % p.bx) << p.bw_log, y0 = (blk / p.bx) << p.bh_log;
+    const int w = min(bw, p.W - x0), h = min(bh, p.H - y0);
+    for (int b = 0; b < p.nbases; ++b) {
+        const PBase &B = p.bases[b];
+        const int nc = B.has_cat ? B.ncat : 1;
+        const int cells = w * h * nc;
+        const unsigned char *s = sm + B.off;
+        for (int i = threadIdx.x; i < cells; i += RD_THREADS) {
+            // i walks the block's rows inside the canvas, then pixels, then categories
+            const int c = i % nc, q = i / nc;
+            const int lx = q % w, ly = q / w;
+            const int lc = ((ly << p.bw_log) | lx) * nc + c;
+            const int64_t gc = ((int64_t)(y0 + ly) * p.W + (x0 + lx)) * nc + c;
+            switch (B.op) {
+            case DSGB_BASE_COUNT: {
+                const unsigned v = ((const unsigned *)s)[lc];
+                if (!v) break;
+                unsigned *d = (unsigned *)B.agg + gc;
+                if (owned) *d += v; else atomicAdd(d, v);
+                break;
+            }
+            case DSGB_BASE_ANY:
+                if (s[lc]) ((uint8_t *)B.agg)[gc] = 1;
+                break;
+            case DSGB_BASE_SUM: {
+                const double v = ((const double *)s)[lc];
+                if (v == 0.0) break;
+                double *d = (double *)B.agg + gc;
+                if (owned) *d += v; else atomicAdd(d, v);
+                break;
+            }
+            case DSGB_BASE_MAX: case DSGB_BASE_MAX_ROW: {
+                const long long v = ((const long long *)s)[lc];
+                if (v == (B.op == DSGB_BASE_MAX ? KEY_EMPTY_MAX : -1ll)) break;
+                long long *d = (long long *)B.agg + gc;
+                if (owned) { if (v > *d) *d = v; }
+                else atomic_max_key(d, v);
+                break;
+            }
+            case DSGB_BASE_MIN: case DSGB_BASE_MIN_ROW: {
+                const long long v = ((const long long *)s)[lc];
+                if (v == KEY_EMPTY_MIN) break;             // == ROW_EMPTY_MIN
+                long long *d = (long long *)B.agg + gc;
+                if (owned) { if (v < *d) *d = v; }
+                else atomic_min_key(d, v);
+                break;
+            }
+            case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: {
+                const bool mx = B.op == DSGB_BASE_ARGMAX;
+                const long long k = ((const long long *)s)[2 * lc], r = ((const long long *)s)[2 * lc + 1];
+                if (r == ROW_EMPTY_MIN) break;
+                long long *d = (long long *)B.agg + 2 * gc;
+                if (owned) {
+                    if (mx ? pair_better<true>(k, r, d[0], d[1]) : pair_better<false>(k, r, d[0], d[1])) {
+                        d[0] = k;
+                        d[1] = r;
+                    }
+                } else if (mx) {
+                    pair_update<true>(d, k, r);
+                } else {
+                    pair_update<false>(d, k, r);
+                }
+                break;
+            }
+            default: break;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(RD_THREADS, 1) part_reduce(const __grid_constant__ Params p) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ int s_item;
+    const int px = 1 << (p.bw_log + p.bh_log);
+    const unsigned nitems = p.counters[0];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(&p.counters[1], 1u);
+        __syncthreads();
+        const int it = s_item;
+        if ((unsigned)it >= nitems) break;
+        const int4 item = p.items[it];
+        init_state(p, sm, px);
+        __syncthreads();
+        const uint4 *src = (const uint4 *)p.recs;
+        for (int64_t i = (int64_t)item.y + threadIdx.x; i < item.z; i += RD_THREADS) {
+            const uint4 q = __ldcs(src + i);
+            Rec r;
+            r.v = __longlong_as_double((long long)(((unsigned long long)q.y << 32) | q.x));
+            r.row = q.z;
+            r.lpix = (uint16_t)(q.w & 0xffffu);
+            r.cat = (uint8_t)((q.w >> 16) & 0xffu);
+            apply(p, sm, r);
+        }
+        __syncthreads();
+        flush_state(p, sm, item.x, item.w != 0);
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ host
+
+static int elem_size(int op) {
+    switch (op) {
+    case DSGB_BASE_COUNT: return 4;
+    case DSGB_BASE_ANY: return 1;
+    case DSGB_BASE_SUM: case DSGB_BASE_MAX: case DSGB_BASE_MIN: case DSGB_BASE_MIN_ROW: case DSGB_BASE_MAX_ROW:
+        return 8;
+    case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: return 16;
+    default: return 0;
+    }
+}
+
+// Shared-memory bytes of one pixel over all bases (0: a base this path does
+// not serve, or columns it cannot share).
+static int pixel_bytes(const dsgb_base *bases, int nbases, int &vcol, int &ccol, int &ncat) {
+    vcol = -1; ccol = -1; ncat = 0;
+    int total = 0;
+    for (int b = 0; b < nbases; ++b) {
+        const dsgb_base &B = bases[b];
+        const int es = elem_size(B.op);
+        if (!es) return 0;
+        if (B.col >= 0) {
+            if (vcol >= 0 && vcol != B.col) return 0;       // one value column
+            vcol = B.col;
+        }
+        if (B.cat_col >= 0) {
+            if ((ccol >= 0 && (ccol != B.cat_col || ncat != B.ncat)) || B.ncat < 1 || B.ncat > 255) return 0;
+            ccol = B.cat_col;
+            ncat = B.ncat;
+        }
+        total += es * (B.cat_col >= 0 ? B.ncat : 1);
+    }
+    return total;
+}
+
+// Block geometry: the most pixels (a power of two, at most 2^16 so that a
+// pixel fits the record's 16 bits) whose state fits the budget; 64 pixels
+// wide at most.
+static bool geometry(int bpp, int W, int H, int &bw_log, int &bh_log, int &bx, int &nblk) {
+    if (bpp <= 0) return false;
+    int lg = 0;
+    while (lg < 16 && ((int64_t)bpp << (lg + 1)) + 16 * MAX_BASES <= STATE_BUDGET) ++lg;
+    if (lg < 6) return false;
+    bw_log = std::min(lg, 6);
+    bh_log = lg - bw_log;
+    bx = (W + (1 << bw_log) - 1) >> bw_log;
+    const int by = (H + (1 << bh_log) - 1) >> bh_log;
+    if ((int64_t)bx * by > MAX_BLOCKS) return false;
+    nblk = bx * by;
+    return true;
+}
+
+static size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+}  // namespace part
+
+// Workspace of the partitioned path for n rows (0 when the bases are not served).
+size_t part_workspace_size(int64_t n, const dsgb_canvas *cv, const dsgb_base *bases, int32_t nbases) {
+    using namespace part;
+    if (n < MIN_ROWS || !cv || nbases < 1) return 0;
+    int vcol, ccol, ncat, bwl, bhl, bx, nblk;
+    const int bpp = pixel_bytes(bases, nbases, vcol, ccol, ncat);
+    if (!geometry(bpp, cv->width, cv->height, bwl, bhl, bx, nblk)) return 0;
+    const int64_t rows = std::min(n, CHUNK);
+    return align16((size_t)rows * sizeof(Rec)) + align16((size_t)MAX_ITEMS * sizeof(int4)) +
+           align16((size_t)(3 * MAX_BLOCKS + 1) * 4) + 16;
+}
+
+// DSGB_E_UNSUPPORTED when the case is not served (the caller takes the
+// generic kernels).  The bases hold their initial values (or a previous
+// call's, when accumulating); the call adds the rows into them.
+int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws, size_t ws_bytes, cudaStream_t st) {
+    using namespace part;
+    if (!ws || pp.n < MIN_ROWS) return DSGB_E_UNSUPPORTED;
+    const ColumnRef &xc = pp.cols[pp.x_col], &yc = pp.cols[pp.y_col];
+    if (xc.dtype != DSGB_F32 || yc.dtype != DSGB_F32 || (((uintptr_t)xc.data | (uintptr_t)yc.data) & 15u))
+        return DSGB_E_UNSUPPORTED;
+    if (pp.x_log || pp.y_log || !fast_path_ok(pp.ax, pp.ay)) return DSGB_E_UNSUPPORTED;
+    int vcol, ccol, ncat;
+    const int bpp = pixel_bytes(bases, pp.nbases, vcol, ccol, ncat);
+    Params p;
+    memset(&p, 0, sizeof(p));
+    if (!geometry(bpp, pp.width, pp.height, p.bw_log, p.bh_log, p.bx, p.nblk)) return DSGB_E_UNSUPPORTED;
+    const int64_t rows = std::min(pp.n, CHUNK);
+    const size_t rec_bytes = align16((size_t)rows * sizeof(Rec));
+    const size_t item_bytes = align16((size_t)MAX_ITEMS * sizeof(int4));
+    const size_t need = rec_bytes + item_bytes + align16((size_t)(3 * MAX_BLOCKS + 1) * 4) + 16;
+    if (ws_bytes < need || ((uintptr_t)ws & 15u)) return DSGB_E_UNSUPPORTED;
+    unsigned char *w = (unsigned char *)ws;
+    p.recs = (Rec *)w;
+    p.items = (int4 *)(w + rec_bytes);
+    p.blk_count = (uint32_t *)(w + rec_bytes + item_bytes);
+    p.blk_start = p.blk_count + MAX_BLOCKS;
+    p.blk_cursor = p.blk_start + MAX_BLOCKS + 1;
+    p.counters = (uint32_t *)(w + rec_bytes + item_bytes + align16((size_t)(3 * MAX_BLOCKS + 1) * 4));
+    p.W = pp.width; p.H = pp.height;
+    p.ax = pp.ax; p.ay = pp.ay; p.bb = pp.bb;
+    p.ncat = ncat;
+    p.nbases = pp.nbases;
+    const int px = 1 << (p.bw_log + p.bh_log);
+    int off = 0;
+    for (int b = 0; b < pp.nbases; ++b) {
+        const dsgb_base &B = bases[b];
+        PBase &q = p.bases[b];
+        q.op = B.op;
+        q.has_col = B.col >= 0;
+        q.has_cat = B.cat_col >= 0;
+        q.ncat = B.cat_col >= 0 ? B.ncat : 1;
+        q.esize = elem_size(B.op);
+        q.off = off;
+        q.agg = B.agg;
+        off += (int)align16((size_t)px * q.ncat * q.esize);
+    }
+    p.state_bytes = off;
+    const int sms = sm_count();
+    if (sms <= 0) return cuda_status(cudaErrorNoDevice, "points part: device");
+    const size_t sc_smem = (size_t)SC_BATCH * (sizeof(Rec) + 2) + (size_t)2 * p.nblk * 4;
+    cudaError_t e = cudaFuncSetAttribute(part_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, p.state_bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(part_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, p.nblk * 4);
+    if (e != cudaSuccess) return cuda_status(e, "points part: shared memory attribute");
+    int sc_per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sc_per_sm, part_scatter, SC_THREADS, sc_smem);
+    if (e != cudaSuccess || sc_per_sm < 1) return cuda_status(e, "points part: scatter occupancy");
+    for (int64_t c0 = 0; c0 < pp.n; c0 += CHUNK) {
+        const int64_t m = std::min(CHUNK, pp.n - c0);
+        p.n = m;
+        p.row0 = pp.row_offset + c0;
+        p.xs = (const float *)xc.data + c0;
+        p.ys = (const float *)yc.data + c0;
+        p.vcol.data = nullptr;
+        p.ccol.data = nullptr;
+        if (vcol >= 0) {
+            p.vcol.dtype = pp.cols[vcol].dtype;
+            p.vcol.data = (const unsigned char *)pp.cols[vcol].data + c0 * dtype_size(p.vcol.dtype);
+        }
+        if (ccol >= 0) {
+            p.ccol.dtype = pp.cols[ccol].dtype;
+            p.ccol.data = (const unsigned char *)pp.cols[ccol].data + c0 * dtype_size(p.ccol.dtype);
+        }
+        e = cudaMemsetAsync(p.blk_count, 0, (size_t)p.nblk * 4, st);
+        if (e != cudaSuccess) return cuda_status(e, "points part: memset");
+        const int64_t n4 = m >> 2;
+        int hist_grid = (int)std::min<int64_t>((int64_t)sms * 8, std::max<int64_t>(1, (n4 + HIST_THREADS - 1) / HIST_THREADS));
+        part_hist<<<hist_grid, HIST_THREADS, (size_t)p.nblk * 4, st>>>(p);
+        part_plan<<<1, PLAN_THREADS, 0, st>>>(p);
+        const int sc_grid = (int)std::min<int64_t>((int64_t)sms * sc_per_sm, std::max<int64_t>(1, n4 / SC_THREADS));
+        part_scatter<<<sc_grid, SC_THREADS, sc_smem, st>>>(p);
+        part_reduce<<<sms, RD_THREADS, p.state_bytes, st>>>(p);
+        DSGB_CHECK_LAUNCH("points part: launch");
+    }
+    return DSGB_OK;
+}
+
+DSGB_STATUS_READER(status_points_part)
+
+}  // namespace dsgb
