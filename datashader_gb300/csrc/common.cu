@@ -143,8 +143,8 @@ __device__ __forceinline__ bool base_hit(int op, const void *b, int64_t i, unsig
     return cnt != 0;
 }
 
-__global__ void finalize_kernel(const FinArgs a) {
-    for (int64_t i = gtid(); i < a.n; i += gstride()) {
+__device__ __forceinline__ void finalize_cell(const FinArgs &a, int64_t i) {
+    {
         switch (a.op) {
         case DSGB_FIN_SUM_NAN: {
             unsigned c; bool hit = base_hit(a.b1op, a.b1, i, c);
@@ -182,6 +182,23 @@ __global__ void finalize_kernel(const FinArgs a) {
             break; }
         default: break;
         }
+    }
+}
+
+// Every output of a plan in one launch: a thread finalizes cell i of each
+// output that has one.
+constexpr int FIN_BATCH = 16;
+struct FinBatch {
+    int32_t count;
+    int64_t n;                      // the largest output
+    FinArgs a[FIN_BATCH];
+};
+
+__global__ void finalize_kernel(const __grid_constant__ FinBatch b) {
+    for (int64_t i = gtid(); i < b.n; i += gstride()) {
+#pragma unroll 1
+        for (int k = 0; k < b.count; ++k)
+            if (i < b.a[k].n) finalize_cell(b.a[k], i);
     }
 }
 
@@ -251,6 +268,8 @@ int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
                      const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
                      int64_t ncells, cudaStream_t st, int64_t ncol_rows) {
     NvtxRange range("dsgb finalize");
+    FinBatch batch;
+    memset(&batch, 0, sizeof(batch));
     for (int o = 0; o < nouts; ++o) {
         const dsgb_output &O = outs[o];
         if (!O.out || O.base0 < 0 || O.base0 >= nbases) {
@@ -276,8 +295,14 @@ int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
         a.out = O.out;
         a.n = ncells * (B0.ncat < 1 ? 1 : B0.ncat);
         a.out_bytes = base_elem_bytes(B0.op);
-        finalize_kernel<<<grid_for(a.n), 256, 0, st>>>(a);
-        DSGB_CHECK_LAUNCH("finalize kernel");
+        batch.a[batch.count++] = a;
+        if (a.n > batch.n) batch.n = a.n;
+        if (batch.count == FIN_BATCH || o == nouts - 1) {
+            finalize_kernel<<<grid_for(batch.n), 256, 0, st>>>(batch);
+            DSGB_CHECK_LAUNCH("finalize kernel");
+            batch.count = 0;
+            batch.n = 0;
+        }
     }
     return DSGB_OK;
 }

@@ -274,13 +274,52 @@ struct Cmap {
     int alpha;
 };
 
+// np.interp of one x against the three colour channels: one interval search
+// and, per channel, numpy's slope (fp[j+1] - fp[j]) / (xp[j+1] - xp[j])
+// (compiled_base.c arr_interp, which also precomputes the slopes when the
+// table is not longer than x) taken from a per-block table, then
+// slope * (x - xp[j]) + fp[j] with numpy's NaN fallbacks: the same operations
+// in the same order as np_interp per channel.
+__device__ __forceinline__ void np_interp_rgb(double x, const double *xp, const double (*fp)[256],
+                                              const double (*sl)[256], int len, double left, double out[3]) {
+    if (x > xp[len - 1]) {
+        for (int c = 0; c < 3; ++c) out[c] = fp[c][len - 1];
+        return;
+    }
+    if (x < xp[0]) {
+        for (int c = 0; c < 3; ++c) out[c] = left;
+        return;
+    }
+    int lo = 0, hi = len - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (xp[mid] <= x) lo = mid; else hi = mid;
+    }
+    int j = lo;
+    if (x >= xp[len - 1]) j = len - 1;
+    if (j == len - 1 || xp[j] == x) {
+        for (int c = 0; c < 3; ++c) out[c] = fp[c][j];
+        return;
+    }
+    const double dx = __dsub_rn(x, xp[j]);
+    for (int c = 0; c < 3; ++c) {
+        const double slope = sl[c][j];
+        double r = __dadd_rn(__dmul_rn(slope, dx), fp[c][j]);
+        if (r != r) {
+            r = __dadd_rn(__dmul_rn(slope, __dsub_rn(x, xp[j + 1])), fp[c][j + 1]);
+            if (r != r && fp[c][j] == fp[c][j + 1]) r = fp[c][j];
+        }
+        out[c] = r;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) eqh_apply(const T *data, int64_t n, const EqHeader *hp,
                                                  const double *cdf, const double *centers, double *out,
                                                  uint32_t *rgba, const __grid_constant__ Cmap cm, int nbins) {
     const EqHeader h = *hp;
-    // np.linspace(span0, span1, ncolors) (:320) and the colours, shared by the block
-    __shared__ double xs[256], cr[256], cg[256], cb[256];
+    // np.linspace(span0, span1, ncolors) (:320), the colours and their slopes, shared by the block
+    __shared__ double xs[256], ch[3][256], sl[3][256];
     if (rgba) {
         const int div = cm.n - 1;
         const double delta = __dsub_rn(h.span1, h.span0);
@@ -290,7 +329,12 @@ __global__ void __launch_bounds__(256) eqh_apply(const T *data, int64_t n, const
             if (div > 0 && step == 0.0) y = __dmul_rn(__ddiv_rn((double)k, (double)div), delta);
             else y = __dmul_rn((double)k, step);
             xs[k] = (div > 0 && k == div) ? h.span1 : __dadd_rn(y, h.span0);
-            cr[k] = cm.r[k]; cg[k] = cm.g[k]; cb[k] = cm.b[k];
+            ch[0][k] = cm.r[k]; ch[1][k] = cm.g[k]; ch[2][k] = cm.b[k];
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < 3 * (cm.n - 1); k += blockDim.x) {
+            const int c = k / (cm.n - 1), j = k % (cm.n - 1);
+            sl[c][j] = __ddiv_rn(__dsub_rn(ch[c][j + 1], ch[c][j]), __dsub_rn(xs[j + 1], xs[j]));
         }
     }
     __syncthreads();
@@ -309,11 +353,10 @@ __global__ void __launch_bounds__(256) eqh_apply(const T *data, int64_t n, const
             uint32_t px = 0;
             if (o == o) {
                 // interp(data, span, chan, left=255), nan_to_num, astype(uint8)
-                double r = np_interp(o, xs, cr, cm.n, 255.0, cr[cm.n - 1]);
-                double g = np_interp(o, xs, cg, cm.n, 255.0, cg[cm.n - 1]);
-                double b = np_interp(o, xs, cb, cm.n, 255.0, cb[cm.n - 1]);
-                px = (uint32_t)(uint8_t)(int)r | ((uint32_t)(uint8_t)(int)g << 8) |
-                     ((uint32_t)(uint8_t)(int)b << 16) | ((uint32_t)(uint8_t)cm.alpha << 24);
+                double c[3];
+                np_interp_rgb(o, xs, ch, sl, cm.n, 255.0, c);
+                px = (uint32_t)(uint8_t)(int)c[0] | ((uint32_t)(uint8_t)(int)c[1] << 8) |
+                     ((uint32_t)(uint8_t)(int)c[2] << 16) | ((uint32_t)(uint8_t)cm.alpha << 24);
             }
             rgba[i] = px;
         }
@@ -367,7 +410,7 @@ static int eq_hist_impl(const T *data, int64_t n, int32_t nbins, double *out, in
     eqh_plan<T><<<1, 32, 0, st>>>(L.hdr, nbins);
     if (n > 0) eqh_hist<T><<<grid_cap(n, 512, 2), 512, 0, st>>>(data, n, L.hdr, L.hist, nbins);
     eqh_scan<<<1, 1024, 0, st>>>(L.hdr, L.hist, L.cdf, L.centers, nbins, rescale);
-    if (n > 0) eqh_apply<T><<<grid_cap(n, 256, 8), 256, 0, st>>>(data, n, L.hdr, L.cdf, L.centers, out, rgba, cm, nbins);
+    if (n > 0) eqh_apply<T><<<grid_cap(n, 256, 2), 256, 0, st>>>(data, n, L.hdr, L.cdf, L.centers, out, rgba, cm, nbins);
     eqh_levels<<<1, 32, 0, st>>>(L.hdr, (long long *)levels);
     DSGB_CHECK_LAUNCH("dsgb_eq_hist");
     return DSGB_OK;

@@ -79,6 +79,24 @@ struct Params {
     uint32_t *counters;                          // [0] items, [1] next item
     int nbases, state_bytes;
     PBase bases[MAX_BASES];
+    // The common bases by kind, applied by straight-line code: a bit of
+    // fast_mask and the shared-memory offset of each; the other bases
+    // (rest) take the generic loop.
+    unsigned fast_mask;
+    int fast_off[16];
+    int fast_ncat;                               // categories of KF_COUNT_C
+    int nrest;
+    int rest[MAX_BASES];
+};
+
+enum FastKind {
+    KF_COUNT = 0,                                // count() of every row
+    KF_COUNT_V,                                  // count('v'): rows with a value
+    KF_SUM_V, KF_MAX_V, KF_MIN_V,
+    KF_MINROW_V, KF_MAXROW_V,                    // first / last
+    KF_ARGMAX_V, KF_ARGMIN_V,                    // where(max / min)
+    KF_COUNT_C,                                  // by(cat, count())
+    KF_N
 };
 
 __device__ __forceinline__ bool bin_row(const Params &p, float x, float y, int &xi, int &yi) {
@@ -200,9 +218,51 @@ __device__ __forceinline__ uint8_t load_code(const Params &p, int64_t i) {
     return (c < 0 || c >= p.ncat) ? CAT_NONE : (uint8_t)c;
 }
 
+// Value loads: VK 0 no value column, 1 float64 column (16-byte aligned: two
+// double2 per four rows), 2 any other (load_f64).  Code loads: CK 0 none,
+// 1 int8 / uint8 (4-byte aligned: one word per four rows), 2 any other.
+template <int VK>
+__device__ __forceinline__ void load_values4(const Params &p, int64_t g, double (&v)[4]) {
+    if (VK == 1) {
+        const double2 *v2 = (const double2 *)p.vcol.data;
+        const double2 a = __ldcs(v2 + 2 * g), b = __ldcs(v2 + 2 * g + 1);
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = VK == 2 ? load_f64(p.vcol, 4 * g + k) : 0.0;
+    }
+}
+
+__device__ __forceinline__ unsigned wrap_code(const Params &p, long long c) {
+    if (c < 0) c += p.ncat;                       // compiler.py:379-390: negative codes wrap
+    return (c < 0 || c >= p.ncat) ? CAT_NONE : (unsigned)c;
+}
+
+template <int CK>
+__device__ __forceinline__ unsigned load_codes4(const Params &p, int64_t g) {
+    if (CK == 0) return 0xffffffffu;
+    if (CK == 1) {
+        const unsigned w = __ldcs((const unsigned *)p.ccol.data + g);
+        const bool sgn = p.ccol.dtype == DSGB_I8;
+        unsigned out = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const unsigned b = (w >> (8 * k)) & 0xffu;
+            const long long c = sgn ? (long long)(int8_t)b : (long long)b;
+            out |= wrap_code(p, c) << (8 * k);
+        }
+        return out;
+    }
+    unsigned out = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out |= wrap_code(p, load_i64(p.ccol, 4 * g + k)) << (8 * k);
+    return out;
+}
+
+template <int VK, int CK>
 __global__ void __launch_bounds__(SC_THREADS) part_scatter(const __grid_constant__ Params p) {
     extern __shared__ __align__(16) unsigned char sm[];
-    Rec *stage = (Rec *)sm;                                       // SC_BATCH records
+    uint4 *stage = (uint4 *)sm;                                   // SC_BATCH records
     uint16_t *sblk = (uint16_t *)(sm + SC_BATCH * sizeof(Rec));   // block of each staged record
     unsigned *hist = (unsigned *)(sm + SC_BATCH * (sizeof(Rec) + 2));   // counts, then staging offsets
     unsigned *delta = hist + p.nblk;                              // record index - staging index of a block's run
@@ -220,7 +280,14 @@ __global__ void __launch_bounds__(SC_THREADS) part_scatter(const __grid_constant
         int blk[4];
         unsigned lp[4], rank[4];
         float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-        if (live) { a = __ldcs(x4 + g); b = __ldcs(y4 + g); }
+        double v[4] = {0.0, 0.0, 0.0, 0.0};
+        unsigned codes = 0xffffffffu;
+        if (live) {
+            a = __ldcs(x4 + g);
+            b = __ldcs(y4 + g);
+            load_values4<VK>(p, g, v);
+            codes = load_codes4<CK>(p, g);
+        }
         const float xs[4] = {a.x, a.y, a.z, a.w}, ys[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -255,21 +322,16 @@ __global__ void __launch_bounds__(SC_THREADS) part_scatter(const __grid_constant
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (blk[k] < 0) continue;
-            const int64_t row = 4 * g + k;
             const unsigned pos = hist[blk[k]] + rank[k];
-            Rec r;
-            r.v = load_value(p, row);
-            r.row = (uint32_t)row;
-            r.lpix = (uint16_t)lp[k];
-            r.cat = load_code(p, row);
-            r.pad = 0;
-            stage[pos] = r;
+            const unsigned long long vb = (unsigned long long)__double_as_longlong(v[k]);
+            stage[pos] = make_uint4((unsigned)vb, (unsigned)(vb >> 32), (unsigned)(4 * g + k),
+                                    lp[k] | (((codes >> (8 * k)) & 0xffu) << 16));
             sblk[pos] = (uint16_t)blk[k];
         }
         __syncthreads();
         const unsigned total = s_total;
         for (unsigned i = threadIdx.x; i < total; i += SC_THREADS) {
-            const uint4 q = *(const uint4 *)(stage + i);
+            const uint4 q = stage[i];
             const unsigned dst = delta[sblk[i]] + i;
             // both passes bin alike, so every run stays inside its block's range
             if (dst < p.n) __stcg((uint4 *)(p.recs + dst), q);
@@ -377,14 +439,44 @@ __device__ __forceinline__ void init_state(const Params &p, unsigned char *sm, i
     }
 }
 
-// One record into every base's block state.
+// One record into every base's block state: the common kinds first, by
+// warp-uniform tests of fast_mask, then the rest by the generic loop.
 __device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const Rec &r) {
     const bool has = !isnull(r.v);
     const long long key = f64_key(r.v);
     const long long row = p.row0 + (long long)r.row;
+    const unsigned m = p.fast_mask;
+    const unsigned lp = r.lpix;
+    if (m & (1u << KF_COUNT)) atomicAdd((unsigned *)(sm + p.fast_off[KF_COUNT]) + lp, 1u);
+    if ((m & (1u << KF_COUNT_C)) && r.cat != CAT_NONE)
+        atomicAdd((unsigned *)(sm + p.fast_off[KF_COUNT_C]) + lp * (unsigned)p.fast_ncat + r.cat, 1u);
+    if (has) {
+        if (m & (1u << KF_COUNT_V)) atomicAdd((unsigned *)(sm + p.fast_off[KF_COUNT_V]) + lp, 1u);
+        if (m & (1u << KF_SUM_V)) atomicAdd((double *)(sm + p.fast_off[KF_SUM_V]) + lp, r.v);
+        if (m & (1u << KF_MAX_V)) {
+            long long *q = (long long *)(sm + p.fast_off[KF_MAX_V]) + lp;
+            if (*(volatile long long *)q < key) atomicMax(q, key);
+        }
+        if (m & (1u << KF_MIN_V)) {
+            long long *q = (long long *)(sm + p.fast_off[KF_MIN_V]) + lp;
+            if (*(volatile long long *)q > key) atomicMin(q, key);
+        }
+        if (m & (1u << KF_MINROW_V)) {
+            long long *q = (long long *)(sm + p.fast_off[KF_MINROW_V]) + lp;
+            if (*(volatile long long *)q > row) atomicMin(q, row);
+        }
+        if (m & (1u << KF_MAXROW_V)) {
+            long long *q = (long long *)(sm + p.fast_off[KF_MAXROW_V]) + lp;
+            if (*(volatile long long *)q < row) atomicMax(q, row);
+        }
+        if (m & (1u << KF_ARGMAX_V))
+            pair_update_shared<true>((long long *)(sm + p.fast_off[KF_ARGMAX_V]) + 2 * lp, key, row);
+        if (m & (1u << KF_ARGMIN_V))
+            pair_update_shared<false>((long long *)(sm + p.fast_off[KF_ARGMIN_V]) + 2 * lp, key, row);
+    }
 #pragma unroll 1
-    for (int b = 0; b < p.nbases; ++b) {
-        const PBase &B = p.bases[b];
+    for (int j = 0; j < p.nrest; ++j) {
+        const PBase &B = p.bases[p.rest[j]];
         if (B.has_col && !has) continue;
         unsigned cell = r.lpix;
         if (B.has_cat) {
@@ -641,17 +733,53 @@ int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws,
         off += (int)align16((size_t)px * q.ncat * q.esize);
     }
     p.state_bytes = off;
+    for (int b = 0; b < pp.nbases; ++b) {
+        const PBase &q = p.bases[b];
+        int k = -1;
+        if (!q.has_cat) {
+            switch (q.op) {
+            case DSGB_BASE_COUNT: k = q.has_col ? KF_COUNT_V : KF_COUNT; break;
+            case DSGB_BASE_SUM: k = q.has_col ? KF_SUM_V : -1; break;
+            case DSGB_BASE_MAX: k = q.has_col ? KF_MAX_V : -1; break;
+            case DSGB_BASE_MIN: k = q.has_col ? KF_MIN_V : -1; break;
+            case DSGB_BASE_MIN_ROW: k = q.has_col ? KF_MINROW_V : -1; break;
+            case DSGB_BASE_MAX_ROW: k = q.has_col ? KF_MAXROW_V : -1; break;
+            case DSGB_BASE_ARGMAX: k = q.has_col ? KF_ARGMAX_V : -1; break;
+            case DSGB_BASE_ARGMIN: k = q.has_col ? KF_ARGMIN_V : -1; break;
+            default: break;
+            }
+        } else if (q.op == DSGB_BASE_COUNT && !q.has_col) {
+            k = KF_COUNT_C;
+            p.fast_ncat = q.ncat;
+        }
+        if (k >= 0 && !(p.fast_mask & (1u << k))) {
+            p.fast_mask |= 1u << k;
+            p.fast_off[k] = q.off;
+        } else {
+            p.rest[p.nrest++] = b;
+        }
+    }
     const int sms = sm_count();
     if (sms <= 0) return cuda_status(cudaErrorNoDevice, "points part: device");
     const size_t sc_smem = (size_t)SC_BATCH * (sizeof(Rec) + 2) + (size_t)2 * p.nblk * 4;
+    // value and code load forms (the chunk starts keep the columns' alignment: 2^27 rows)
+    const int VK = vcol < 0 ? 0 : (pp.cols[vcol].dtype == DSGB_F64 && !((uintptr_t)pp.cols[vcol].data & 15u)) ? 1 : 2;
+    const int CK = ccol < 0 ? 0
+                 : ((pp.cols[ccol].dtype == DSGB_I8 || pp.cols[ccol].dtype == DSGB_U8) &&
+                    !((uintptr_t)pp.cols[ccol].data & 3u)) ? 1 : 2;
+    void (*scatter)(Params) = nullptr;
+#define DSGB_SC(V, C) if (VK == V && CK == C) scatter = part_scatter<V, C>;
+    DSGB_SC(0, 0) DSGB_SC(0, 1) DSGB_SC(0, 2) DSGB_SC(1, 0) DSGB_SC(1, 1) DSGB_SC(1, 2)
+    DSGB_SC(2, 0) DSGB_SC(2, 1) DSGB_SC(2, 2)
+#undef DSGB_SC
     cudaError_t e = cudaFuncSetAttribute(part_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, p.state_bytes);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
+        e = cudaFuncSetAttribute(scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(part_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, p.nblk * 4);
     if (e != cudaSuccess) return cuda_status(e, "points part: shared memory attribute");
     int sc_per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sc_per_sm, part_scatter, SC_THREADS, sc_smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sc_per_sm, scatter, SC_THREADS, sc_smem);
     if (e != cudaSuccess || sc_per_sm < 1) return cuda_status(e, "points part: scatter occupancy");
     for (int64_t c0 = 0; c0 < pp.n; c0 += CHUNK) {
         const int64_t m = std::min(CHUNK, pp.n - c0);
@@ -676,7 +804,7 @@ int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws,
         part_hist<<<hist_grid, HIST_THREADS, (size_t)p.nblk * 4, st>>>(p);
         part_plan<<<1, PLAN_THREADS, 0, st>>>(p);
         const int sc_grid = (int)std::min<int64_t>((int64_t)sms * sc_per_sm, std::max<int64_t>(1, n4 / SC_THREADS));
-        part_scatter<<<sc_grid, SC_THREADS, sc_smem, st>>>(p);
+        scatter<<<sc_grid, SC_THREADS, sc_smem, st>>>(p);
         part_reduce<<<sms, RD_THREADS, p.state_bytes, st>>>(p);
         DSGB_CHECK_LAUNCH("points part: launch");
     }
