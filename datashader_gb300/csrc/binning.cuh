@@ -208,4 +208,25 @@ static inline bool fast_path_ok(const BinAxis &ax, const BinAxis &ay) {
     return std::isfinite(ax.e) && std::isfinite(ay.e) && ax.e < 0.01f && ay.e < 0.01f;
 }
 
+// The float64 image fl(fl(v * s) + t) of a float32 value, each operation
+// rounded (volatile keeps the host compiler from fusing them).
+static inline double image64(float v, double s, double t) {
+    volatile double a = (double)v * s;
+    volatile double b = a + t;
+    return b;
+}
+
+// Precondition of the integer classification (bins from the float32 image
+// alone: both in [0, n) with the fraction inside the window is inside the
+// bounds; a bin outside [-1, n] is outside them; the rest take the float64
+// formula): the smallest in-bounds float maps to >= 0 and the float below it
+// to <= 0; the largest in-bounds float below n + 0.5 and the float above it
+// to >= n.  The canvas relation of core.py:62-81 (t = -lo * s) gives this;
+// other descriptors take the general binning.
+static inline bool edges_ok(float lo, float hi, double s, double t, int n) {
+    if (!(s > 0.0) || !std::isfinite(lo) || !std::isfinite(hi) || !(hi >= lo)) return false;
+    return image64(nextafterf(lo, -INFINITY), s, t) <= 0.0 && image64(lo, s, t) >= 0.0 &&
+           image64(hi, s, t) < n + 0.5 && image64(nextafterf(hi, INFINITY), s, t) >= (double)n;
+}
+
 }  // namespace dsgb

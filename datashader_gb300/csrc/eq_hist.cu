@@ -37,6 +37,7 @@ struct EqHeader {
     double dmax;                   // largest unmasked value after the offset
     unsigned int uoffset;          // offset (uint32 data)
     unsigned int ptp;
+    double cdf_total;              // integer path: the divisor of the cumulative counts
 };
 
 constexpr int SMEM_BINS = 8192;
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(1024) eqh_scan(EqHeader *hp, const unsigned in
         unsigned int c = hist[j];
         run += c;
         if (path == 1) {
-            cdf[j] = __ddiv_rn((double)run, ftotal);          // (:200-201)
+            cdf[j] = (double)run;                             // divided by eqh_div (:200-201)
         } else if (c) {
             cdf[krun] = __ddiv_rn((double)run, ftotal);
             double e0 = lin_edge(h, j, nbins), e1 = lin_edge(h, j + 1, nbins);
@@ -245,8 +246,9 @@ __global__ void __launch_bounds__(1024) eqh_scan(EqHeader *hp, const unsigned in
         // monotone in the value, so they are the images of the extremes.
         double s0, s1;
         if (path == 1) {
-            s0 = cdf[0];
-            s1 = cdf[h.ptp];
+            h.cdf_total = ftotal;
+            s0 = __ddiv_rn(cdf[0], ftotal);
+            s1 = __ddiv_rn(cdf[h.ptp], ftotal);
         } else {
             // the shifted extremes of the unmasked data are 0 and dmax
             s0 = np_interp(0.0, centers, cdf, nkept, cdf[0], cdf[nkept - 1]);
@@ -266,6 +268,17 @@ __global__ void __launch_bounds__(1024) eqh_scan(EqHeader *hp, const unsigned in
         h.span0 = s0;
         h.span1 = s1;
     }
+}
+
+// Integer path: cdf = cumsum / cumsum[-1] (:200-201), one correctly rounded
+// division per bin, spread over the GPU (a float64 division is dozens of
+// operations on GB300's float64 pipe; one CTA took ~50 us for 20,000 bins).
+__global__ void eqh_div(const EqHeader *hp, double *cdf) {
+    const EqHeader &h = *hp;
+    if (h.path != 1) return;
+    const int64_t nb = (int64_t)h.ptp + 1;
+    const double t = h.cdf_total;
+    for (int64_t j = gtid(); j < nb; j += gstride()) cdf[j] = __ddiv_rn(cdf[j], t);
 }
 
 struct Cmap {
@@ -410,6 +423,7 @@ static int eq_hist_impl(const T *data, int64_t n, int32_t nbins, double *out, in
     eqh_plan<T><<<1, 32, 0, st>>>(L.hdr, nbins);
     if (n > 0) eqh_hist<T><<<grid_cap(n, 512, 2), 512, 0, st>>>(data, n, L.hdr, L.hist, nbins);
     eqh_scan<<<1, 1024, 0, st>>>(L.hdr, L.hist, L.cdf, L.centers, nbins, rescale);
+    eqh_div<<<grid_cap(nbins, 256, 1), 256, 0, st>>>(L.hdr, L.cdf);
     if (n > 0) eqh_apply<T><<<grid_cap(n, 256, 2), 256, 0, st>>>(data, n, L.hdr, L.cdf, L.centers, out, rgba, cm, nbins);
     eqh_levels<<<1, 32, 0, st>>>(L.hdr, (long long *)levels);
     DSGB_CHECK_LAUNCH("dsgb_eq_hist");

@@ -317,6 +317,11 @@ static bool has_sum_base(const PointsParams &p) {
 int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
                      const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
                      int64_t ncells, cudaStream_t st);
+// The same with the gather bound: a selected row outside [row_offset,
+// row_offset + ncol_rows) (one that an earlier call accumulated) gathers NaN.
+int finalize_outputs(const dsgb_column *cols, int32_t ncols, int64_t row_offset,
+                     const dsgb_base *bases, int32_t nbases, const dsgb_output *outs, int32_t nouts,
+                     int64_t ncells, cudaStream_t st, int64_t ncol_rows);
 
 }  // namespace dsgb
 
@@ -359,7 +364,7 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
         rc = det_sums(p, fast, workspace, ws_bytes, st);
         if (rc) return rc;
         if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
-            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st, n);
         return rc;
     }
     if (cached_eligible(p, flags)) {
@@ -380,7 +385,7 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
                                     p.bb, (double *)p.bases[0].agg, (uint32_t *)p.bases[1].agg,
                                     (flags & DSGB_FLAG_NO_INIT) != 0, st);
         if (rc == DSGB_OK && !(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
-            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st, n);
         if (rc != DSGB_E_UNSUPPORTED) return rc;
     }
     if (workspace && cached_mean_eligible(p, flags)) {
@@ -388,7 +393,7 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
                                        p.bb, (double *)p.bases[0].agg, (uint32_t *)p.bases[1].agg,
                                        (flags & DSGB_FLAG_NO_INIT) != 0, workspace, ws_bytes, st);
         if (rc == DSGB_OK && !(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
-            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+            rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st, n);
         if (rc != DSGB_E_UNSUPPORTED) return rc;
     }
     if (!(flags & DSGB_FLAG_NO_INIT)) {
@@ -406,7 +411,7 @@ static int points_impl(const dsgb_column *cols, int32_t ncols, int64_t n, int64_
         if (rc) return rc;
     }
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
-        rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st);
+        rc = finalize_outputs(cols, ncols, row_offset, bases, nbases, outs, nouts, ncells, st, n);
     return rc;
 }
 

@@ -676,27 +676,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// The float64 image fl(fl(v * s) + t) of a float32 value, each operation
-// rounded (volatile keeps the host compiler from fusing them).
-static double image64(float v, double s, double t) {
-    volatile double a = (double)v * s;
-    volatile double b = a + t;
-    return b;
-}
-
-// The integer classification of the kernel needs: the smallest in-bounds
-// float maps to >= 0 and the float below it to <= 0; the largest in-bounds
-// float below n + 0.5 and the float above it to >= n.  The canvas relation
-// of core.py:62-81 (t = -lo * s) gives this; other descriptors take the
-// general path.
-static bool edges_ok(float lo, float hi, double s, double t, int n) {
-    if (!(s > 0.0) || !std::isfinite(lo) || !std::isfinite(hi) || !(hi >= lo)) return false;
-    return image64(nextafterf(lo, -INFINITY), s, t) <= 0.0 && image64(lo, s, t) >= 0.0 &&
-           image64(hi, s, t) < n + 0.5 && image64(nextafterf(hi, INFINITY), s, t) >= (double)n;
-}
-
-// The same for float64 coordinates: the bounds themselves and the doubles
-// next to them.
+// edges_ok (binning.cuh) for float64 coordinates: the bounds themselves and
+// the doubles next to them.
 static double image64d(double v, double s, double t) {
     volatile double a = v * s;
     volatile double b = a + t;

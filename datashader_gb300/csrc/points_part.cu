@@ -49,6 +49,7 @@ constexpr int64_t MAX_ITEMS = CHUNK / ITEM + MAX_BLOCKS + 1;
 constexpr int64_t MIN_ROWS = (int64_t)1 << 20;
 constexpr int STATE_BUDGET = 200 * 1024;         // shared memory for the bases of one block
 constexpr uint8_t CAT_NONE = 0xff;
+constexpr unsigned SUM_LANES = 0u;               // lanes of part_reduce whose SUM updates go to L2
 
 struct Rec {                                     // 16 bytes
     double v;
@@ -62,6 +63,7 @@ struct PBase {
     int32_t op, has_col, has_cat, ncat;
     int32_t off;                                 // byte offset of its block state in shared memory
     int32_t esize;
+    int32_t key_off;                             // >= 0: max / min taken from the key of this where() pair state
     void *agg;
 };
 
@@ -73,6 +75,10 @@ struct Params {
     int ncat;                                    // categories of the record's code (0: no category column)
     BinAxis ax, ay;
     BinBounds bb;
+    // integer classification of the float32 image (when edges_ok holds for both axes)
+    int lean;
+    float sxf, txf, syf, tyf, exlo, exhi, eylo, eyhi;
+    double sx, tx, sy, ty, xmin, xmax, ymin, ymax;
     uint32_t *blk_count, *blk_start, *blk_cursor;
     Rec *recs;
     int4 *items;                                 // {block, begin, end, owned}
@@ -83,6 +89,8 @@ struct Params {
     // fast_mask and the shared-memory offset of each; the other bases
     // (rest) take the generic loop.
     unsigned fast_mask;
+    unsigned sum_lanes;                          // lanes whose SUM updates go to L2
+    void *sum_agg;
     int fast_off[16];
     int fast_ncat;                               // categories of KF_COUNT_C
     int nrest;
@@ -99,7 +107,44 @@ enum FastKind {
     KF_N
 };
 
+// The reference formula for a row the float32 image cannot decide: the
+// inclusive bounds, then int(x * s + t) in float64 clamped (points.py:199-203);
+// packed (xi, yi), or ~0 outside the bounds.
+static __device__ __noinline__ unsigned long long exact_xy(float x, float y, const Params *pp) {
+    const Params &p = *pp;
+    const double dx = (double)x, dy = (double)y;
+    if (!(p.xmin <= dx && dx <= p.xmax && p.ymin <= dy && dy <= p.ymax)) return ~0ull;
+    const unsigned xi = (unsigned)bin_exact64_st(dx, p.sx, p.tx, p.W);
+    const unsigned yi = (unsigned)bin_exact64_st(dy, p.sy, p.ty, p.H);
+    return (unsigned long long)xi | ((unsigned long long)yi << 32);
+}
+
+// Both passes bin every row with this one function, so they agree on its
+// block.  Lean form (the hot-tile kernels' classification, exact under
+// edges_ok): v = fma32(x, sf, tf); k = floor(v) by the 1.5 * 2^23 addition
+// rounded toward zero; both k in [0, n) with the fraction inside the window
+// (E, 1 - E) decide the pixel; a k outside [-1, n] is outside the bounds;
+// anything else takes the float64 formula.  Otherwise binning.cuh's bounds
+// test and fast path.
 __device__ __forceinline__ bool bin_row(const Params &p, float x, float y, int &xi, int &yi) {
+    if (p.lean) {
+        const float vx = __fmaf_rn(x, p.sxf, p.txf), vy = __fmaf_rn(y, p.syf, p.tyf);
+        const float tx = __fadd_rz(vx, 12582912.0f), ty = __fadd_rz(vy, 12582912.0f);
+        const int kx = __float_as_int(tx) - 0x4B400000, ky = __float_as_int(ty) - 0x4B400000;
+        const float fx = __fsub_rn(vx, __fsub_rn(tx, 12582912.0f)), fy = __fsub_rn(vy, __fsub_rn(ty, 12582912.0f));
+        if ((unsigned)kx < (unsigned)p.W && (unsigned)ky < (unsigned)p.H && fx > p.exlo && fx < p.exhi &&
+            fy > p.eylo && fy < p.eyhi) {
+            xi = kx;
+            yi = ky;
+            return true;
+        }
+        if (!((unsigned)(kx + 1) < (unsigned)(p.W + 2) && (unsigned)(ky + 1) < (unsigned)(p.H + 2))) return false;
+        const unsigned long long r = exact_xy(x, y, &p);
+        if (r == ~0ull) return false;
+        xi = (int)(unsigned)r;
+        yi = (int)(unsigned)(r >> 32);
+        return true;
+    }
     const int r = bin_try_f32(x, y, p.bb, p.ax, p.ay, xi, yi);
     if (r == 2) bin_exact_f32(x, y, p.ax, p.ay, xi, yi);
     return r != 0;
@@ -169,39 +214,34 @@ __device__ __forceinline__ unsigned block_scan(unsigned v, unsigned *warp_sums, 
 }
 
 // ------------------------------------------------------------ part_plan
+// One CTA: blocks in rounds of PLAN_THREADS, one a thread, scanned with the
+// running totals of the previous rounds.  A block of c rows becomes
+// m = ceil(c / ITEM) items of ceil(c / m) rows (the last shorter, none empty).
 __global__ void __launch_bounds__(PLAN_THREADS) part_plan(const __grid_constant__ Params p) {
     __shared__ unsigned ws1[32], ws2[32];
     __shared__ unsigned tot1, tot2;
-    constexpr int PER = MAX_BLOCKS / PLAN_THREADS;
-    unsigned c[PER], m[PER];
-    unsigned s1 = 0, s2 = 0;
-    const int b0 = threadIdx.x * PER;
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int b = b0 + k;
-        c[k] = b < p.nblk ? p.blk_count[b] : 0u;
-        m[k] = (unsigned)((c[k] + ITEM - 1) / ITEM);
-        s1 += c[k];
-        s2 += m[k];
-    }
-    unsigned o1 = block_scan<PLAN_THREADS>(s1, ws1, &tot1);
-    unsigned o2 = block_scan<PLAN_THREADS>(s2, ws2, &tot2);
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int b = b0 + k;
-        if (b >= p.nblk) break;
-        p.blk_start[b] = o1;
-        p.blk_cursor[b] = o1;
-        for (unsigned j = 0; j < m[k]; ++j) {
-            const int64_t lo = (int64_t)c[k] * j / m[k], hi = (int64_t)c[k] * (j + 1) / m[k];
-            p.items[o2 + j] = make_int4(b, (int)(o1 + lo), (int)(o1 + hi), m[k] == 1 ? 1 : 0);
+    unsigned carry1 = 0, carry2 = 0;
+    for (int r0 = 0; r0 < p.nblk; r0 += PLAN_THREADS) {
+        const int b = r0 + threadIdx.x;
+        const unsigned c = b < p.nblk ? p.blk_count[b] : 0u;
+        const unsigned m = (unsigned)((c + (unsigned)ITEM - 1) / (unsigned)ITEM);
+        const unsigned o1 = block_scan<PLAN_THREADS>(c, ws1, &tot1) + carry1;
+        const unsigned o2 = block_scan<PLAN_THREADS>(m, ws2, &tot2) + carry2;
+        if (b < p.nblk) {
+            p.blk_start[b] = o1;
+            p.blk_cursor[b] = o1;
+            const unsigned sz = m ? (c + m - 1) / m : 0u;
+            for (unsigned j = 0; j < m; ++j) {
+                const unsigned lo = j * sz, hi = min(c, lo + sz);
+                p.items[o2 + j] = make_int4(b, (int)(o1 + lo), (int)(o1 + hi), m == 1 ? 1 : 0);
+            }
         }
-        o1 += c[k];
-        o2 += m[k];
+        carry1 += tot1;
+        carry2 += tot2;
     }
     if (threadIdx.x == 0) {
-        p.blk_start[p.nblk] = tot1;
-        p.counters[0] = tot2;
+        p.blk_start[p.nblk] = carry1;
+        p.counters[0] = carry2;
         p.counters[1] = 0;
     }
 }
@@ -260,7 +300,7 @@ __device__ __forceinline__ unsigned load_codes4(const Params &p, int64_t g) {
 }
 
 template <int VK, int CK>
-__global__ void __launch_bounds__(SC_THREADS) part_scatter(const __grid_constant__ Params p) {
+__global__ void __launch_bounds__(SC_THREADS, 2) part_scatter(const __grid_constant__ Params p) {
     extern __shared__ __align__(16) unsigned char sm[];
     uint4 *stage = (uint4 *)sm;                                   // SC_BATCH records
     uint16_t *sblk = (uint16_t *)(sm + SC_BATCH * sizeof(Rec));   // block of each staged record
@@ -274,19 +314,29 @@ __global__ void __launch_bounds__(SC_THREADS) part_scatter(const __grid_constant
     const int64_t g0 = n4 * blockIdx.x / gridDim.x, g1 = n4 * (blockIdx.x + 1) / gridDim.x;
     const float4 *x4 = (const float4 *)p.xs, *y4 = (const float4 *)p.ys;
     const int per = (p.nblk + SC_THREADS - 1) / SC_THREADS;       // scan entries per thread
+    // the next batch's columns are loaded while this one is ranked and written
+    float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
+    double nv[4] = {0.0, 0.0, 0.0, 0.0};
+    unsigned ncodes = 0xffffffffu;
+    if (g0 + threadIdx.x < g1) {
+        na = __ldcs(x4 + g0 + threadIdx.x);
+        nb = __ldcs(y4 + g0 + threadIdx.x);
+        load_values4<VK>(p, g0 + threadIdx.x, nv);
+        ncodes = load_codes4<CK>(p, g0 + threadIdx.x);
+    }
     for (int64_t base = g0; base < g1; base += SC_THREADS) {
         const int64_t g = base + threadIdx.x;
         const bool live = g < g1;
         int blk[4];
         unsigned lp[4], rank[4];
-        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-        double v[4] = {0.0, 0.0, 0.0, 0.0};
-        unsigned codes = 0xffffffffu;
-        if (live) {
-            a = __ldcs(x4 + g);
-            b = __ldcs(y4 + g);
-            load_values4<VK>(p, g, v);
-            codes = load_codes4<CK>(p, g);
+        const float4 a = na, b = nb;
+        const double v[4] = {nv[0], nv[1], nv[2], nv[3]};
+        const unsigned codes = ncodes;
+        if (g + SC_THREADS < g1) {
+            na = __ldcs(x4 + g + SC_THREADS);
+            nb = __ldcs(y4 + g + SC_THREADS);
+            load_values4<VK>(p, g + SC_THREADS, nv);
+            ncodes = load_codes4<CK>(p, g + SC_THREADS);
         }
         const float xs[4] = {a.x, a.y, a.z, a.w}, ys[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
@@ -323,6 +373,7 @@ __global__ void __launch_bounds__(SC_THREADS) part_scatter(const __grid_constant
         for (int k = 0; k < 4; ++k) {
             if (blk[k] < 0) continue;
             const unsigned pos = hist[blk[k]] + rank[k];
+            if (pos >= (unsigned)SC_BATCH) { raise_status(DSGB_STATUS_INDEX); continue; }
             const unsigned long long vb = (unsigned long long)__double_as_longlong(v[k]);
             stage[pos] = make_uint4((unsigned)vb, (unsigned)(vb >> 32), (unsigned)(4 * g + k),
                                     lp[k] | (((codes >> (8 * k)) & 0xffu) << 16));
@@ -332,7 +383,9 @@ __global__ void __launch_bounds__(SC_THREADS) part_scatter(const __grid_constant
         const unsigned total = s_total;
         for (unsigned i = threadIdx.x; i < total; i += SC_THREADS) {
             const uint4 q = stage[i];
-            const unsigned dst = delta[sblk[i]] + i;
+            const unsigned e = sblk[i];
+            if (e >= (unsigned)p.nblk) { raise_status(DSGB_STATUS_INDEX); continue; }
+            const unsigned dst = delta[e] + i;
             // both passes bin alike, so every run stays inside its block's range
             if (dst < p.n) __stcg((uint4 *)(p.recs + dst), q);
             else raise_status(DSGB_STATUS_INDEX);
@@ -380,10 +433,12 @@ __device__ __forceinline__ void cas128_shared(unsigned addr, long long cmp_lo, l
 // pair_update (dsgb_internal.cuh) on a shared-memory pair.
 template <bool MAX>
 __device__ __forceinline__ void pair_update_shared(long long *slot, long long key, long long row) {
-    volatile long long *v = slot;
-    long long ok = v[0];
+    // the pre-check may read a stale key: keys only improve, so a stale key
+    // strictly better than ours still proves the slot better
+    long long ok = slot[0];
     if (MAX ? (ok > key) : (ok < key)) return;
-    long long orow = v[1];
+    long long orow = ((volatile long long *)slot)[1];
+    ok = ((volatile long long *)slot)[0];
     const unsigned addr = (unsigned)__cvta_generic_to_shared(slot);
     for (int guard = 0; guard < (1 << 24); ++guard) {
         long long rk, rr;
@@ -439,9 +494,23 @@ __device__ __forceinline__ void init_state(const Params &p, unsigned char *sm, i
     }
 }
 
+__device__ __forceinline__ Rec decode(const uint4 q) {
+    Rec r;
+    r.v = __longlong_as_double((long long)(((unsigned long long)q.y << 32) | q.x));
+    r.row = q.z;
+    r.lpix = (uint16_t)(q.w & 0xffffu);
+    r.cat = (uint8_t)((q.w >> 16) & 0xffu);
+    r.pad = 0;
+    return r;
+}
+
 // One record into every base's block state: the common kinds first, by
 // warp-uniform tests of fast_mask, then the rest by the generic loop.
-__device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const Rec &r) {
+__device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const Rec &r, double *gsum) {
+    if (r.lpix >= (1u << (p.bw_log + p.bh_log)) || (r.cat != CAT_NONE && r.cat >= p.ncat)) {
+        raise_status(DSGB_STATUS_INDEX);        // a record outside its block: never written by part_scatter
+        return;
+    }
     const bool has = !isnull(r.v);
     const long long key = f64_key(r.v);
     const long long row = p.row0 + (long long)r.row;
@@ -452,22 +521,29 @@ __device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const 
         atomicAdd((unsigned *)(sm + p.fast_off[KF_COUNT_C]) + lp * (unsigned)p.fast_ncat + r.cat, 1u);
     if (has) {
         if (m & (1u << KF_COUNT_V)) atomicAdd((unsigned *)(sm + p.fast_off[KF_COUNT_V]) + lp, 1u);
-        if (m & (1u << KF_SUM_V)) atomicAdd((double *)(sm + p.fast_off[KF_SUM_V]) + lp, r.v);
+        if (m & (1u << KF_SUM_V)) {
+            // lanes in sum_lanes add into the base in L2 (red.global.add.f64), the others in
+            // shared memory: the two atomic units work side by side
+            if ((p.sum_lanes >> (threadIdx.x & 31)) & 1u)
+                atomicAdd(gsum + (lp >> p.bw_log) * (unsigned)p.W + (lp & ((1u << p.bw_log) - 1)), r.v);
+            else
+                atomicAdd((double *)(sm + p.fast_off[KF_SUM_V]) + lp, r.v);
+        }
         if (m & (1u << KF_MAX_V)) {
             long long *q = (long long *)(sm + p.fast_off[KF_MAX_V]) + lp;
-            if (*(volatile long long *)q < key) atomicMax(q, key);
+            if (*q < key) atomicMax(q, key);
         }
         if (m & (1u << KF_MIN_V)) {
             long long *q = (long long *)(sm + p.fast_off[KF_MIN_V]) + lp;
-            if (*(volatile long long *)q > key) atomicMin(q, key);
+            if (*q > key) atomicMin(q, key);
         }
         if (m & (1u << KF_MINROW_V)) {
             long long *q = (long long *)(sm + p.fast_off[KF_MINROW_V]) + lp;
-            if (*(volatile long long *)q > row) atomicMin(q, row);
+            if (*q > row) atomicMin(q, row);
         }
         if (m & (1u << KF_MAXROW_V)) {
             long long *q = (long long *)(sm + p.fast_off[KF_MAXROW_V]) + lp;
-            if (*(volatile long long *)q < row) atomicMax(q, row);
+            if (*q < row) atomicMax(q, row);
         }
         if (m & (1u << KF_ARGMAX_V))
             pair_update_shared<true>((long long *)(sm + p.fast_off[KF_ARGMAX_V]) + 2 * lp, key, row);
@@ -490,22 +566,22 @@ __device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const 
         case DSGB_BASE_SUM: atomicAdd((double *)s + cell, r.v); break;
         case DSGB_BASE_MAX: {
             long long *q = (long long *)s + cell;
-            if (*(volatile long long *)q < key) atomicMax(q, key);
+            if (*q < key) atomicMax(q, key);
             break;
         }
         case DSGB_BASE_MIN: {
             long long *q = (long long *)s + cell;
-            if (*(volatile long long *)q > key) atomicMin(q, key);
+            if (*q > key) atomicMin(q, key);
             break;
         }
         case DSGB_BASE_MIN_ROW: {
             long long *q = (long long *)s + cell;
-            if (*(volatile long long *)q > row) atomicMin(q, row);
+            if (*q > row) atomicMin(q, row);
             break;
         }
         case DSGB_BASE_MAX_ROW: {
             long long *q = (long long *)s + cell;
-            if (*(volatile long long *)q < row) atomicMax(q, row);
+            if (*q < row) atomicMax(q, row);
             break;
         }
         case DSGB_BASE_ARGMAX: pair_update_shared<true>((long long *)s + 2 * cell, key, row); break;
@@ -516,74 +592,84 @@ __device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const 
 }
 
 // The block's state into the bases: read-modify-write when this CTA owns
-// the block, atomics otherwise.  Cells holding the identity are skipped.
+// the block, atomics otherwise.  A thread takes a pixel and every base's
+// cells of it; pixels that no record reached (a zero count() when the plan
+// has one) and cells holding the identity are skipped.
 __device__ __forceinline__ void flush_state(const Params &p, const unsigned char *sm, int blk, bool owned) {
-    const int bw = 1 << p.bw_log, bh = 1 << p.bh_log;
     const int x0 = (blk % p.bx) << p.bw_log, y0 = (blk / p.bx) << p.bh_log;
-    const int w = min(bw, p.W - x0), h = min(bh, p.H - y0);
-    for (int b = 0; b < p.nbases; ++b) {
-        const PBase &B = p.bases[b];
-        const int nc = B.has_cat ? B.ncat : 1;
-        const int cells = w * h * nc;
-        const unsigned char *s = sm + B.off;
-        for (int i = threadIdx.x; i < cells; i += RD_THREADS) {
-            // i walks the block's rows inside the canvas, then pixels, then categories
-            const int c = i % nc, q = i / nc;
-            const int lx = q % w, ly = q / w;
-            const int lc = ((ly << p.bw_log) | lx) * nc + c;
-            const int64_t gc = ((int64_t)(y0 + ly) * p.W + (x0 + lx)) * nc + c;
-            switch (B.op) {
-            case DSGB_BASE_COUNT: {
-                const unsigned v = ((const unsigned *)s)[lc];
-                if (!v) break;
-                unsigned *d = (unsigned *)B.agg + gc;
-                if (owned) *d += v; else atomicAdd(d, v);
-                break;
-            }
-            case DSGB_BASE_ANY:
-                if (s[lc]) ((uint8_t *)B.agg)[gc] = 1;
-                break;
-            case DSGB_BASE_SUM: {
-                const double v = ((const double *)s)[lc];
-                if (v == 0.0) break;
-                double *d = (double *)B.agg + gc;
-                if (owned) *d += v; else atomicAdd(d, v);
-                break;
-            }
-            case DSGB_BASE_MAX: case DSGB_BASE_MAX_ROW: {
-                const long long v = ((const long long *)s)[lc];
-                if (v == (B.op == DSGB_BASE_MAX ? KEY_EMPTY_MAX : -1ll)) break;
-                long long *d = (long long *)B.agg + gc;
-                if (owned) { if (v > *d) *d = v; }
-                else atomic_max_key(d, v);
-                break;
-            }
-            case DSGB_BASE_MIN: case DSGB_BASE_MIN_ROW: {
-                const long long v = ((const long long *)s)[lc];
-                if (v == KEY_EMPTY_MIN) break;             // == ROW_EMPTY_MIN
-                long long *d = (long long *)B.agg + gc;
-                if (owned) { if (v < *d) *d = v; }
-                else atomic_min_key(d, v);
-                break;
-            }
-            case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: {
-                const bool mx = B.op == DSGB_BASE_ARGMAX;
-                const long long k = ((const long long *)s)[2 * lc], r = ((const long long *)s)[2 * lc + 1];
-                if (r == ROW_EMPTY_MIN) break;
-                long long *d = (long long *)B.agg + 2 * gc;
-                if (owned) {
-                    if (mx ? pair_better<true>(k, r, d[0], d[1]) : pair_better<false>(k, r, d[0], d[1])) {
-                        d[0] = k;
-                        d[1] = r;
-                    }
-                } else if (mx) {
-                    pair_update<true>(d, k, r);
-                } else {
-                    pair_update<false>(d, k, r);
+    const int w = min(1 << p.bw_log, p.W - x0), h = min(1 << p.bh_log, p.H - y0);
+    const int npx = h << p.bw_log;
+    const bool counted = (p.fast_mask & (1u << KF_COUNT)) != 0;
+    const unsigned *cnt = (const unsigned *)(sm + p.fast_off[KF_COUNT]);
+    for (int q = threadIdx.x; q < npx; q += RD_THREADS) {
+        const int lx = q & ((1 << p.bw_log) - 1), ly = q >> p.bw_log;
+        if (lx >= w) continue;
+        if (counted && cnt[q] == 0) continue;
+        const int64_t gpix = (int64_t)(y0 + ly) * p.W + (x0 + lx);
+#pragma unroll 1
+        for (int b = 0; b < p.nbases; ++b) {
+            const PBase &B = p.bases[b];
+            const int nc = B.ncat;
+            const unsigned char *s = sm + B.off;
+#pragma unroll 1
+            for (int c = 0; c < nc; ++c) {
+                const int lc = q * nc + c;
+                const int64_t gc = gpix * nc + c;
+                switch (B.op) {
+                case DSGB_BASE_COUNT: {
+                    const unsigned v = ((const unsigned *)s)[lc];
+                    if (!v) break;
+                    unsigned *d = (unsigned *)B.agg + gc;
+                    if (owned) *d += v; else atomicAdd(d, v);
+                    break;
                 }
-                break;
-            }
-            default: break;
+                case DSGB_BASE_ANY:
+                    if (s[lc]) ((uint8_t *)B.agg)[gc] = 1;
+                    break;
+                case DSGB_BASE_SUM: {
+                    const double v = ((const double *)s)[lc];
+                    if (v == 0.0) break;
+                    double *d = (double *)B.agg + gc;
+                    if (owned && !p.sum_lanes) *d += v; else atomicAdd(d, v);
+                    break;
+                }
+                case DSGB_BASE_MAX: case DSGB_BASE_MAX_ROW: {
+                    const long long v = B.key_off >= 0 ? ((const long long *)(sm + B.key_off))[2 * lc]
+                                                       : ((const long long *)s)[lc];
+                    if (v == (B.op == DSGB_BASE_MAX ? KEY_EMPTY_MAX : -1ll)) break;
+                    long long *d = (long long *)B.agg + gc;
+                    if (owned) { if (v > *d) *d = v; }
+                    else atomic_max_key(d, v);
+                    break;
+                }
+                case DSGB_BASE_MIN: case DSGB_BASE_MIN_ROW: {
+                    const long long v = B.key_off >= 0 ? ((const long long *)(sm + B.key_off))[2 * lc]
+                                                       : ((const long long *)s)[lc];
+                    if (v == KEY_EMPTY_MIN) break;             // == ROW_EMPTY_MIN
+                    long long *d = (long long *)B.agg + gc;
+                    if (owned) { if (v < *d) *d = v; }
+                    else atomic_min_key(d, v);
+                    break;
+                }
+                case DSGB_BASE_ARGMAX: case DSGB_BASE_ARGMIN: {
+                    const bool mx = B.op == DSGB_BASE_ARGMAX;
+                    const long long k = ((const long long *)s)[2 * lc], r = ((const long long *)s)[2 * lc + 1];
+                    if (r == ROW_EMPTY_MIN) break;
+                    long long *d = (long long *)B.agg + 2 * gc;
+                    if (owned) {
+                        if (mx ? pair_better<true>(k, r, d[0], d[1]) : pair_better<false>(k, r, d[0], d[1])) {
+                            d[0] = k;
+                            d[1] = r;
+                        }
+                    } else if (mx) {
+                        pair_update<true>(d, k, r);
+                    } else {
+                        pair_update<false>(d, k, r);
+                    }
+                    break;
+                }
+                default: break;
+                }
             }
         }
     }
@@ -600,18 +686,28 @@ __global__ void __launch_bounds__(RD_THREADS, 1) part_reduce(const __grid_consta
         const int it = s_item;
         if ((unsigned)it >= nitems) break;
         const int4 item = p.items[it];
+        if (item.x < 0 || item.x >= p.nblk || item.y < 0 || item.y > item.z || (unsigned)item.z > p.blk_start[p.nblk]) {
+            raise_status(DSGB_STATUS_INDEX);
+            __syncthreads();
+            continue;
+        }
+        double *gsum = nullptr;                   // the SUM base at the block's first pixel
+        if (p.sum_lanes)
+            gsum = (double *)p.sum_agg + (int64_t)((item.x / p.bx) << p.bh_log) * p.W + ((item.x % p.bx) << p.bw_log);
         init_state(p, sm, px);
         __syncthreads();
         const uint4 *src = (const uint4 *)p.recs;
-        for (int64_t i = (int64_t)item.y + threadIdx.x; i < item.z; i += RD_THREADS) {
-            const uint4 q = __ldcs(src + i);
-            Rec r;
-            r.v = __longlong_as_double((long long)(((unsigned long long)q.y << 32) | q.x));
-            r.row = q.z;
-            r.lpix = (uint16_t)(q.w & 0xffffu);
-            r.cat = (uint8_t)((q.w >> 16) & 0xffu);
-            apply(p, sm, r);
+        // four records a thread in flight: the loads are issued before the
+        // shared-memory updates of any of them
+        int64_t i = (int64_t)item.y + threadIdx.x;
+        for (; i + 3 * RD_THREADS < item.z; i += 4 * RD_THREADS) {
+            uint4 q[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) q[k] = __ldcs(src + i + k * RD_THREADS);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) apply(p, sm, decode(q[k]), gsum);
         }
+        for (; i < item.z; i += RD_THREADS) apply(p, sm, decode(__ldcs(src + i)), gsum);
         __syncthreads();
         flush_state(p, sm, item.x, item.w != 0);
         __syncthreads();
@@ -716,6 +812,13 @@ int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws,
     p.counters = (uint32_t *)(w + rec_bytes + item_bytes + align16((size_t)(3 * MAX_BLOCKS + 1) * 4));
     p.W = pp.width; p.H = pp.height;
     p.ax = pp.ax; p.ay = pp.ay; p.bb = pp.bb;
+    p.lean = edges_ok(pp.bb.xminf, pp.bb.xmaxf, pp.sx, pp.tx, pp.width) &&
+             edges_ok(pp.bb.yminf, pp.bb.ymaxf, pp.sy, pp.ty, pp.height);
+    p.sxf = pp.ax.sf; p.txf = pp.ax.tf; p.syf = pp.ay.sf; p.tyf = pp.ay.tf;
+    p.exlo = float_ceil_of((double)pp.ax.e); p.exhi = float_floor_of(1.0 - (double)pp.ax.e);
+    p.eylo = float_ceil_of((double)pp.ay.e); p.eyhi = float_floor_of(1.0 - (double)pp.ay.e);
+    p.sx = pp.sx; p.tx = pp.tx; p.sy = pp.sy; p.ty = pp.ty;
+    p.xmin = pp.xmin; p.xmax = pp.xmax; p.ymin = pp.ymin; p.ymax = pp.ymax;
     p.ncat = ncat;
     p.nbases = pp.nbases;
     const int px = 1 << (p.bw_log + p.bh_log);
@@ -757,6 +860,23 @@ int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws,
             p.fast_off[k] = q.off;
         } else {
             p.rest[p.nrest++] = b;
+        }
+    }
+    if (p.fast_mask & (1u << KF_SUM_V)) {
+        p.sum_lanes = SUM_LANES;
+        for (int b = 0; b < pp.nbases; ++b)
+            if (p.bases[b].off == p.fast_off[KF_SUM_V]) p.sum_agg = p.bases[b].agg;
+    }
+    // max('v') beside where(max('v')) (and min beside where(min)): the pair's
+    // key is the maximum, so the max base is not updated per row and its flush
+    // reads the pair's key
+    for (int b = 0; b < pp.nbases; ++b) p.bases[b].key_off = -1;
+    const int pairs[2][2] = {{KF_MAX_V, KF_ARGMAX_V}, {KF_MIN_V, KF_ARGMIN_V}};
+    for (const auto &pr : pairs) {
+        if ((p.fast_mask & (1u << pr[0])) && (p.fast_mask & (1u << pr[1]))) {
+            for (int b = 0; b < pp.nbases; ++b)
+                if (p.bases[b].off == p.fast_off[pr[0]]) p.bases[b].key_off = p.fast_off[pr[1]];
+            p.fast_mask &= ~(1u << pr[0]);
         }
     }
     const int sms = sm_count();
