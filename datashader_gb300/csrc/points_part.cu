@@ -49,7 +49,6 @@ constexpr int64_t MAX_ITEMS = CHUNK / ITEM + MAX_BLOCKS + 1;
 constexpr int64_t MIN_ROWS = (int64_t)1 << 20;
 constexpr int STATE_BUDGET = 200 * 1024;         // shared memory for the bases of one block
 constexpr uint8_t CAT_NONE = 0xff;
-constexpr unsigned SUM_LANES = 0u;               // lanes of part_reduce whose SUM updates go to L2
 
 struct Rec {                                     // 16 bytes
     double v;
@@ -89,8 +88,6 @@ struct Params {
     // fast_mask and the shared-memory offset of each; the other bases
     // (rest) take the generic loop.
     unsigned fast_mask;
-    unsigned sum_lanes;                          // lanes whose SUM updates go to L2
-    void *sum_agg;
     int fast_off[16];
     int fast_ncat;                               // categories of KF_COUNT_C
     int nrest;
@@ -346,8 +343,8 @@ __global__ void __launch_bounds__(SC_THREADS, 2) part_scatter(const __grid_const
             if (live && bin_row(p, xs[k], ys[k], xi, yi)) {
                 blk[k] = block_of(p, xi, yi);
                 lp[k] = local_pixel(p, xi, yi);
-                rank[k] = atomicAdd(&hist[blk[k]], 1u);
             }
+            if (blk[k] >= 0) rank[k] = atomicAdd(&hist[blk[k]], 1u);
         }
         __syncthreads();
         // offsets of the blocks in the staging area, and their runs' places in the records
@@ -506,7 +503,7 @@ __device__ __forceinline__ Rec decode(const uint4 q) {
 
 // One record into every base's block state: the common kinds first, by
 // warp-uniform tests of fast_mask, then the rest by the generic loop.
-__device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const Rec &r, double *gsum) {
+__device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const Rec &r) {
     if (r.lpix >= (1u << (p.bw_log + p.bh_log)) || (r.cat != CAT_NONE && r.cat >= p.ncat)) {
         raise_status(DSGB_STATUS_INDEX);        // a record outside its block: never written by part_scatter
         return;
@@ -521,14 +518,9 @@ __device__ __forceinline__ void apply(const Params &p, unsigned char *sm, const 
         atomicAdd((unsigned *)(sm + p.fast_off[KF_COUNT_C]) + lp * (unsigned)p.fast_ncat + r.cat, 1u);
     if (has) {
         if (m & (1u << KF_COUNT_V)) atomicAdd((unsigned *)(sm + p.fast_off[KF_COUNT_V]) + lp, 1u);
-        if (m & (1u << KF_SUM_V)) {
-            // lanes in sum_lanes add into the base in L2 (red.global.add.f64), the others in
-            // shared memory: the two atomic units work side by side
-            if ((p.sum_lanes >> (threadIdx.x & 31)) & 1u)
-                atomicAdd(gsum + (lp >> p.bw_log) * (unsigned)p.W + (lp & ((1u << p.bw_log) - 1)), r.v);
-            else
-                atomicAdd((double *)(sm + p.fast_off[KF_SUM_V]) + lp, r.v);
-        }
+        if (m & (1u << KF_SUM_V)) atomicAdd((double *)(sm + p.fast_off[KF_SUM_V]) + lp, r.v);
+        // pre-checks read without ordering: keys and rows only improve, so a
+        // stale read costs at most a redundant atomic
         if (m & (1u << KF_MAX_V)) {
             long long *q = (long long *)(sm + p.fast_off[KF_MAX_V]) + lp;
             if (*q < key) atomicMax(q, key);
@@ -630,7 +622,7 @@ __device__ __forceinline__ void flush_state(const Params &p, const unsigned char
                     const double v = ((const double *)s)[lc];
                     if (v == 0.0) break;
                     double *d = (double *)B.agg + gc;
-                    if (owned && !p.sum_lanes) *d += v; else atomicAdd(d, v);
+                    if (owned) *d += v; else atomicAdd(d, v);
                     break;
                 }
                 case DSGB_BASE_MAX: case DSGB_BASE_MAX_ROW: {
@@ -691,9 +683,6 @@ __global__ void __launch_bounds__(RD_THREADS, 1) part_reduce(const __grid_consta
             __syncthreads();
             continue;
         }
-        double *gsum = nullptr;                   // the SUM base at the block's first pixel
-        if (p.sum_lanes)
-            gsum = (double *)p.sum_agg + (int64_t)((item.x / p.bx) << p.bh_log) * p.W + ((item.x % p.bx) << p.bw_log);
         init_state(p, sm, px);
         __syncthreads();
         const uint4 *src = (const uint4 *)p.recs;
@@ -705,9 +694,9 @@ __global__ void __launch_bounds__(RD_THREADS, 1) part_reduce(const __grid_consta
 #pragma unroll
             for (int k = 0; k < 4; ++k) q[k] = __ldcs(src + i + k * RD_THREADS);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) apply(p, sm, decode(q[k]), gsum);
+            for (int k = 0; k < 4; ++k) apply(p, sm, decode(q[k]));
         }
-        for (; i < item.z; i += RD_THREADS) apply(p, sm, decode(__ldcs(src + i)), gsum);
+        for (; i < item.z; i += RD_THREADS) apply(p, sm, decode(__ldcs(src + i)));
         __syncthreads();
         flush_state(p, sm, item.x, item.w != 0);
         __syncthreads();
@@ -861,11 +850,6 @@ int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws,
         } else {
             p.rest[p.nrest++] = b;
         }
-    }
-    if (p.fast_mask & (1u << KF_SUM_V)) {
-        p.sum_lanes = SUM_LANES;
-        for (int b = 0; b < pp.nbases; ++b)
-            if (p.bases[b].off == p.fast_off[KF_SUM_V]) p.sum_agg = p.bases[b].agg;
     }
     // max('v') beside where(max('v')) (and min beside where(min)): the pair's
     // key is the maximum, so the max base is not updated per row and its flush
