@@ -49,16 +49,16 @@ def workload(n):
 
 
 # DRAM bytes (read + write) of one hot-tile count launch, measured by ncu on a
-# 2e7-row launch of the same kernel (163.31 MB read, 3.09 MB written): reads
+# 2e7-row launch of the same kernel (167.70 MB read, 3.51 MB written): reads
 # scale with rows, writes with the touched pixels of the 1024x1024 canvas.
 def count_traffic(n):
-    return 163.31e6 / 2e7 * n + 3.09e6
+    return 167.70e6 / 2e7 * n + 3.51e6
 
 
 # The same for the hot-tile mean('v') launch (x/y float32 + v float64): ncu on
-# a 2e7-row launch (329.75 MB read, 3.51 MB written).
+# a 2e7-row launch (372.78 MB read, 3.58 MB written).
 def mean_traffic(n):
-    return 329.75e6 / 2e7 * n + 3.51e6
+    return 372.78e6 / 2e7 * n + 3.58e6
 
 
 # float64 operations of the antialiased line forward per segment (adds + muls +
