@@ -45,6 +45,7 @@ constexpr int MAX_TILES = 8192;             // tile -> slot table (int16)
 constexpr int MAX_SLOTS = 512;
 constexpr int DYN_SMEM = 232448 - 2048;     // dynamic shared memory; the static arrays take the rest
 constexpr int64_t MIN_ROWS = 1 << 20;
+constexpr int SAMPLE_GROUPS = 1;            // float4 groups of x / y a thread samples for the tile choice
 constexpr float MAGIC = 12582912.0f;        // 1.5 * 2^23
 constexpr int MAGIC_BITS = 0x4B400000;
 
@@ -328,20 +329,23 @@ __global__ void __launch_bounds__(THREADS, 1) hot_count_kernel(const __grid_cons
     for (int i = threadIdx.x; i < p.ntiles; i += THREADS) hist[i] = 0;
     __syncthreads();
     if (g1 > g0) {
-        const int64_t g = g0 + (g1 - g0) * threadIdx.x / THREADS;
-        float4 a, b;
-        load_rows4<C64, false>(p, g, a, b);
-        const float xs[4] = {a.x, a.y, a.z, a.w};
-        const float ys[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float x = xs[k], y = ys[k];
-            if (!(x >= p.xminf && x <= p.xmaxf && y >= p.yminf && y <= p.ymaxf)) continue;
-            const int xi = min(max(__float_as_int(__fadd_rz(__fmaf_rn(x, p.sxf, p.txf), MAGIC)) - MAGIC_BITS, 0),
-                               p.W - 1);
-            const int yi = min(max(__float_as_int(__fadd_rz(__fmaf_rn(y, p.syf, p.tyf), MAGIC)) - MAGIC_BITS, 0),
-                               p.H - 1);
-            atomicAdd(&hist[(yi >> TS) * p.tiles_x + (xi >> TS)], 1u);
+        for (int j = 0; j < SAMPLE_GROUPS; ++j) {
+            const int64_t g = g0 + (g1 - g0) * (threadIdx.x + j * THREADS) / (SAMPLE_GROUPS * THREADS);
+            float4 a, b;
+            load_rows4<C64, false>(p, g, a, b);
+            const float xs[4] = {a.x, a.y, a.z, a.w};
+            const float ys[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float x = xs[k], y = ys[k];
+                if (!(x >= p.xminf && x <= p.xmaxf && y >= p.yminf && y <= p.ymaxf)) continue;
+                const int xi = min(max(__float_as_int(__fadd_rz(__fmaf_rn(x, p.sxf, p.txf), MAGIC)) - MAGIC_BITS, 0),
+                                   p.W - 1);
+                const int yi = min(max(__float_as_int(__fadd_rz(__fmaf_rn(y, p.syf, p.tyf), MAGIC)) - MAGIC_BITS, 0),
+                                   p.H - 1);
+                atomicAdd(&hist[(yi >> TS) * p.tiles_x + (xi >> TS)], 1u);
+            }
         }
     }
     __syncthreads();
