@@ -45,7 +45,8 @@ constexpr int MAX_TILES = 8192;             // tile -> slot table (int16)
 constexpr int MAX_SLOTS = 512;
 constexpr int DYN_SMEM = 232448 - 2048;     // dynamic shared memory; the static arrays take the rest
 constexpr int64_t MIN_ROWS = 1 << 20;
-constexpr int SAMPLE_GROUPS = 1;            // float4 groups of x / y a thread samples for the tile choice
+constexpr int SAMPLE_GROUPS = 4;            // float4 groups of x / y a thread samples for the tile choice (count)
+constexpr int MEAN_SAMPLE_GROUPS = 2;       // the same for mean
 constexpr float MAGIC = 12582912.0f;        // 1.5 * 2^23
 constexpr int MAGIC_BITS = 0x4B400000;
 
@@ -545,8 +546,8 @@ __global__ void __launch_bounds__(THREADS, 1) hot_mean_kernel(const __grid_const
     __syncthreads();
     if (g1 > g0) {
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const int64_t g = g0 + (g1 - g0) * (threadIdx.x + j * THREADS) / (2 * THREADS);
+        for (int j = 0; j < MEAN_SAMPLE_GROUPS; ++j) {
+            const int64_t g = g0 + (g1 - g0) * (threadIdx.x + j * THREADS) / (MEAN_SAMPLE_GROUPS * THREADS);
             const float4 a = __ldg(x4 + g), b = __ldg(y4 + g);
             const float xs[4] = {a.x, a.y, a.z, a.w};
             const float ys[4] = {b.x, b.y, b.z, b.w};
