@@ -17,6 +17,9 @@
 //
 // Four launches: min/max, histogram (shared-memory privatised low bins),
 // one-block scan (cdf, levels, span), apply (cdf lookup / interp + RGBA).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "dsgb_internal.cuh"
 #include "shade_common.cuh"
 
@@ -446,22 +449,43 @@ static __device__ __align__(256) unsigned char g_eq_hist_scratch[HDR_BYTES + (si
 static_assert(sizeof(g_eq_hist_scratch) >= HDR_BYTES + (size_t)STATIC_MAX_BINS * 20 + 64, "scratch size");
 
 // In host code `g_eq_hist_scratch` names a host-side shadow, not device
-// memory, so the device address is looked up once per device, with that
-// device current, and cached.
+// memory, so the device address is looked up with the device current and
+// cached per device together with the context it belongs to: after a
+// cudaDeviceReset the device has a new primary context, the module is
+// loaded again, and the address is looked up again.
 static std::mutex g_scratch_mu;
 static void *g_scratch_ptr[128];
+static CUcontext g_scratch_ctx[128];
+
+static PFN_cuCtxGetCurrent_v4000 ctx_current_fn() {
+    static PFN_cuCtxGetCurrent_v4000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuCtxGetCurrent_v4000)f;
+    }
+    return fn;
+}
 
 static int static_scratch(void **ptr) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_status(e, "dsgb_eq_hist_u32_static: cudaGetDevice");
     if (dev < 0 || dev >= 128) { set_error("dsgb_eq_hist_u32_static: device ordinal %d out of range", dev); return DSGB_E_INVALID; }
+    CUcontext ctx = nullptr;                // null before the runtime made a context current: look up again
+    auto fn = ctx_current_fn();
+    if (fn && fn(&ctx) != CUDA_SUCCESS) ctx = nullptr;
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!g_scratch_ptr[dev] || !ctx || ctx != g_scratch_ctx[dev]) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_eq_hist_scratch);
         if (e != cudaSuccess) return cuda_status(e, "dsgb_eq_hist_u32_static: cudaGetSymbolAddress");
         g_scratch_ptr[dev] = p;
+        g_scratch_ctx[dev] = ctx;
     }
     *ptr = g_scratch_ptr[dev];
     return DSGB_OK;

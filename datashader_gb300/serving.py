@@ -88,11 +88,19 @@ class BucketedStore:
         self.domain = tuple(float(d) for d in domain)
         self.grid = grid
         self.x, self.y = x, y
+        # the sort runs on `stream`: it waits for the work that produced the
+        # columns and the buffers (allocated on the current stream), and the
+        # buffers are marked as used on `stream` for the caching allocator
+        cur = torch.cuda.current_stream(dev)
         out = [torch.empty_like(t) for t in tensors]
         starts = torch.empty(grid * grid + 2, dtype=torch.int64, device=dev)
         L = N.lib()
         ws_size = int(L.dsgb_bucket_sort_workspace_size(grid))
         ws = torch.empty(ws_size, dtype=torch.uint8, device=dev)
+        if stream != cur:
+            stream.wait_stream(cur)
+            for t in out + [starts, ws] + tensors:
+                t.record_stream(stream)
         cols = (N.Column * len(tensors))(*[N.Column(t.data_ptr(), dsgb_dtype(t), 0) for t in tensors])
         outs = (ctypes.c_void_p * len(out))(*[t.data_ptr() for t in out])
         dom = (ctypes.c_double * 4)(*self.domain)
@@ -100,6 +108,7 @@ class BucketedStore:
                                    ws.data_ptr(), ws_size, stream.cuda_stream), "dsgb_bucket_sort")
         cats = {c: frame.categories(c) for c in names if frame.is_categorical(c)}
         self.frame = TensorFrame(dict(zip(names, out)), categories=cats, device=dev)
+        stream.synchronize()                   # the bucket offsets are read on the host
         self.starts = starts.cpu().numpy()
         self.n = len(frame)
 

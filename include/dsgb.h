@@ -430,7 +430,9 @@ int dsgb_eq_hist_f64(const double *data, int64_t n, int32_t nbins,
  * that loads the library until the process exits); larger nbins are
  * rejected with DSGB_E_INVALID.  Nothing is allocated: the first call on a
  * device looks up the array's device address (with that device current)
- * and caches it, so make that first call before any stream capture.  Every
+ * and caches it with the device's current context, so make that first call
+ * before any stream capture; after a cudaDeviceReset (a new context) the
+ * next call looks the address up again.  Every
  * call shares the one array and resets what must start at zero, so calls
  * whose work overlaps on the GPU (different streams, or host threads racing
  * on one device) corrupt each other: serialise them. */
