@@ -993,20 +993,28 @@ def streamed_pipeline(hf, canvas, glyph, agg, *, flags=0):
                       float(x_range[0]), float(x_range[1]), float(y_range[0]), float(y_range[1]))
     L = N.lib()
     head = ex = None
+    cats = {k: v for k, v in hf._cats.items() if k in needed}
+    # without derived columns a chunk's columns are the staging slot's buffers
+    # from their first element: each slot's column array is built once
+    slot_ex = [None, None] if not plan.derived else None
+    wsz = ws = None
     for i, (c0, c1) in enumerate(_chunks(len(hf), staging.rows)):
         cols = staging.stage(i, c0, c1, compute)
-        chunk = TensorFrame(cols, categories={k: v for k, v in hf._cats.items() if k in cols}, device=dev,
-                            row_offset=hf.row_offset + c0)
-        ex = Executor(chunk, plan, glyph)
+        if slot_ex is not None and slot_ex[i % 2] is not None:
+            ex = slot_ex[i % 2]
+        else:
+            chunk = TensorFrame(cols, categories=cats, device=dev, row_offset=hf.row_offset + c0)
+            ex = Executor(chunk, plan, glyph)
+            if slot_ex is not None:
+                slot_ex[i % 2] = ex
         if head is None:
             ex.allocate(height, width, dev)
             head = ex
-        else:
-            ex.base_tensors, ex.bases, ex.out_tensors, ex.outs, ex.nouts = (
-                head.base_tensors, head.bases, head.out_tensors, head.outs, head.nouts)
         m = c1 - c0
-        wsz = int(L.dsgb_points_workspace_size_flags(m, ctypes.byref(cv), head.bases, len(plan.bases), flags))
-        ws = workspace(dev, stream, wsz) if wsz else None
+        if wsz is None:
+            # the first chunk is the longest: its workspace serves every chunk
+            wsz = int(L.dsgb_points_workspace_size_flags(m, ctypes.byref(cv), head.bases, len(plan.bases), flags))
+            ws = workspace(dev, stream, wsz) if wsz else None
         f = flags | N.FLAG_NO_FINALIZE | (N.FLAG_NO_INIT if i > 0 else 0)
         N.check(L.dsgb_points_ws(ex.cols, len(ex.names), m, hf.row_offset + c0, 0, 1, ctypes.byref(cv),
                                  head.bases, len(plan.bases), head.outs, head.nouts,

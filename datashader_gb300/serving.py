@@ -179,6 +179,10 @@ def generate_requests(n, rate, seed=0, domain=(0.0, 1.0, 0.0, 1.0), zoom=(1.0, 1
 
 # --------------------------------------------------------------- execution
 
+def _itemsize(dtype):
+    return torch.empty((), dtype=dtype).element_size()
+
+
 class SegmentExecutor:
     """Runs one request on a stream: plan (cached per reduction), buffers,
     one dsgb_points_segments call (init + aggregate + finalize)."""
@@ -188,6 +192,8 @@ class SegmentExecutor:
         self.value, self.cat = value, cat
         self._plans = {}
         self._glyph = Point(store.x, store.y)
+        self._cell_bytes = {}                  # reduction -> aggregate bytes a pixel
+        self._row_bytes = None
 
     def plan(self, kind):
         p = self._plans.get(kind)
@@ -200,24 +206,30 @@ class SegmentExecutor:
     def work_bytes(self, req):
         """Device bytes a request touches: its rows (13 B each on the store) and
         its aggregate buffers.  Caches the request's segments."""
-        if getattr(req, "segments", None) is None:
-            req.segments = self.store.segments(req.x_range, req.y_range)
-            req.rows = sum(e - b for b, e in req.segments)
-        bytes_per_row = sum(t.element_size() for t in (self.store.frame[c] for c in self.store.frame.columns))
-        return req.rows * bytes_per_row + self.agg_bytes(req)
+        wb = getattr(req, "_work_bytes", None)
+        if wb is None:
+            if getattr(req, "segments", None) is None:
+                req.segments = self.store.segments(req.x_range, req.y_range)
+                req.rows = sum(e - b for b, e in req.segments)
+            if self._row_bytes is None:
+                self._row_bytes = sum(self.store.frame[c].element_size() for c in self.store.frame.columns)
+            wb = req._work_bytes = req.rows * self._row_bytes + self.agg_bytes(req)
+        return wb
 
     def agg_bytes(self, req):
         """Device bytes of the request's aggregate buffers (bases + outputs)."""
-        _, plan = self.plan(req.kind)
-        cells = req.width * req.height
-        total = 0
-        for b in plan.bases:
-            total += cells * b.ncat * b.words * torch.empty((), dtype=b.torch_dtype).element_size()
-        for _, o in plan.outputs:
-            if o.fin != 0:
-                nc = plan.bases[o.b0].ncat if o.categories is not None else 1
-                total += cells * nc * torch.empty((), dtype=o.dtype).element_size()
-        return total
+        per_cell = self._cell_bytes.get(req.kind)
+        if per_cell is None:
+            _, plan = self.plan(req.kind)
+            per_cell = 0
+            for b in plan.bases:
+                per_cell += b.ncat * b.words * _itemsize(b.torch_dtype)
+            for _, o in plan.outputs:
+                if o.fin != 0:
+                    nc = plan.bases[o.b0].ncat if o.categories is not None else 1
+                    per_cell += nc * _itemsize(o.dtype)
+            self._cell_bytes[req.kind] = per_cell
+        return req.width * req.height * per_cell
 
     def launch(self, req, stream, segments=None):
         agg, plan = self.plan(req.kind)
@@ -273,16 +285,22 @@ class ViewportServer:
     fewer than ``max_heavy`` other heavy ones do (``max_heavy_backlogged``
     once more requests wait than there are slots); lighter requests behind
     it may go first, so a large viewport does not hold up small ones, and at
-    light load large ones do not slow each other down by sharing the GPU."""
+    light load large ones do not slow each other down by sharing the GPU.
+    At light load (no more arrived requests than slots) a request of more
+    than ``solo_bytes`` runs alone: it starts once the requests in flight are
+    done, and only requests of at most ``tiny_bytes`` start beside it, so the
+    small viewports that arrive meanwhile do not wait for it."""
 
     def __init__(self, executor, slots=8, mem_budget=8 << 30, device=None, streams=None,
-                 heavy_bytes=256 << 20, max_heavy=1, max_heavy_backlogged=None, solo_bytes=32 << 20):
+                 heavy_bytes=256 << 20, max_heavy=1, max_heavy_backlogged=None, solo_bytes=256 << 20,
+                 tiny_bytes=4 << 20):
         self.ex = executor
         self.slots = slots
         self.mem_budget = mem_budget
         self.heavy_bytes = heavy_bytes
         self.max_heavy = max_heavy
         self.solo_bytes = solo_bytes
+        self.tiny_bytes = tiny_bytes
         # with more arrived requests waiting than there are slots, throughput
         # matters more than one request's latency: let heavy ones overlap
         self.max_heavy_backlogged = slots if max_heavy_backlogged is None else max_heavy_backlogged
@@ -329,9 +347,9 @@ class ViewportServer:
             light_load = backlog <= self.slots
             k = 0
             while k < len(pending) and free and pending[k].arrival <= now:
-                if light_load and solo_now:
-                    break                      # a large request runs alone at light load
                 req = pending[k]
+                if light_load and solo_now and self.ex.work_bytes(req) > self.tiny_bytes:
+                    break                      # a large request runs alone at light load, but for tiny ones
                 nbytes = self.ex.agg_bytes(req)
                 if inflight and mem + nbytes > self.mem_budget:
                     break                      # waits for memory to free up, and so does the rest

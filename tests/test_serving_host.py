@@ -137,3 +137,18 @@ def test_heavy_requests_overlap_when_backlogged():
                               heavy_bytes=1, max_heavy=1)
     server.run(reqs, clock=clock, idle=clock.idle)
     assert server.peak_heavy > 1 and all(np.isfinite(r.done) for r in reqs)
+
+
+def test_solo_request_at_light_load_lets_only_tiny_requests_beside_it():
+    """At light load a large request runs alone, except that requests of at
+    most tiny_bytes start beside it; a medium one waits for it."""
+    clock = _Clock()
+    ex = _FakeExecutor(clock)
+    solo = S.Request(0, 0.0, (0, 1), (0, 1), 4096, 2160, "count")          # 354 MB of work: solo
+    tiny = S.Request(1, 5e-4, (0, 0.01), (0, 0.01), 256, 256, "count")    # 2.6 MB: tiny
+    medium = S.Request(2, 6e-4, (0, 0.1), (0, 0.1), 512, 512, "count")   # 10.5 MB: neither
+    server = S.ViewportServer(ex, slots=4, mem_budget=1 << 40, streams=[None] * 4)
+    server.run([solo, tiny, medium], clock=clock, idle=clock.idle)
+    assert tiny.admitted < solo.done                  # did not wait for the large request
+    assert medium.admitted >= solo.done               # waited
+    assert all(np.isfinite(r.done) for r in (solo, tiny, medium))
