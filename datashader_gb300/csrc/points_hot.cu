@@ -45,7 +45,7 @@ constexpr int MAX_TILES = 8192;             // tile -> slot table (int16)
 constexpr int MAX_SLOTS = 512;
 constexpr int DYN_SMEM = 232448 - 2048;     // dynamic shared memory; the static arrays take the rest
 constexpr int64_t MIN_ROWS = 1 << 20;
-constexpr int SAMPLE_GROUPS = 4;            // float4 groups of x / y a thread samples for the tile choice (count)
+constexpr int SAMPLE_GROUPS = 1;            // float4 groups of x / y a thread samples for the tile choice (count)
 constexpr int MEAN_SAMPLE_GROUPS = 2;       // the same for mean
 constexpr float MAGIC = 12582912.0f;        // 1.5 * 2^23
 constexpr int MAGIC_BITS = 0x4B400000;
