@@ -295,8 +295,9 @@ static bool cached_mean_eligible(const PointsParams &p, uint32_t flags) {
            !p.x_log && !p.y_log && fast_path_ok(p.ax, p.ay);
 }
 
-// The hot-tile path (points_cached.cu) serves a plain count() of every row
-// on a canvas that the float32 fast path may bin.
+// The hot-tile paths serve a plain count() of every row on a canvas that the
+// float32 fast path may bin: the per-CTA kernel of points_hot.cu first, the
+// global-selection kernels of points_cached.cu when it declines.
 static bool cached_eligible(const PointsParams &p, uint32_t flags) {
     return p.nbases == 1 && p.bases[0].op == DSGB_BASE_COUNT && p.bases[0].col < 0 &&
            p.bases[0].cat_col < 0 && !(flags & (DSGB_FLAG_EXACT_BIN | DSGB_FLAG_WARP_AGG)) &&
