@@ -36,12 +36,6 @@ int sm_count() {
 
 // ------------------------------------------------------------------ init
 
-__global__ void fill_u64_kernel(unsigned long long *p, int64_t n, unsigned long long v) {
-    for (int64_t i = gtid(); i < n; i += gstride()) p[i] = v;
-}
-__global__ void fill_pair_kernel(long long *p, int64_t n, long long a, long long b) {
-    for (int64_t i = gtid(); i < n; i += gstride()) { p[2 * i] = a; p[2 * i + 1] = b; }
-}
 
 static unsigned grid_for(int64_t n, int threads = 256) {
     int sms = sm_count();
@@ -53,47 +47,80 @@ static unsigned grid_for(int64_t n, int threads = 256) {
     return (unsigned)g;
 }
 
+// Every base's initial value in one launch: a base is a byte range filled
+// with a 16-byte pattern (two 64-bit words; 8-byte values repeat).
+constexpr int INIT_BATCH = 16;
+struct InitBatch {
+    int32_t count;
+    int64_t chunks;                     // 16-byte chunks of the largest base
+    unsigned char *ptr[INIT_BATCH];
+    int64_t bytes[INIT_BATCH];
+    unsigned long long lo[INIT_BATCH], hi[INIT_BATCH];
+};
+
+__global__ void init_kernel(const __grid_constant__ InitBatch b) {
+    for (int64_t i = gtid(); i < b.chunks; i += gstride()) {
+#pragma unroll 1
+        for (int k = 0; k < b.count; ++k) {
+            const int64_t off = 16 * i;
+            if (off + 16 <= b.bytes[k] && !((uintptr_t)b.ptr[k] & 15u)) {
+                *(ulonglong2 *)(b.ptr[k] + off) = make_ulonglong2(b.lo[k], b.hi[k]);
+            } else if (off < b.bytes[k]) {
+                const int64_t end = off + 16 < b.bytes[k] ? off + 16 : b.bytes[k];
+                for (int64_t j = off; j < end; ++j)
+                    b.ptr[k][j] = (unsigned char)((j & 8 ? b.hi[k] : b.lo[k]) >> (8 * (j & 7)));
+            }
+        }
+    }
+}
+
 int bases_init(const dsgb_base *bases, int32_t nbases, int64_t ncells, cudaStream_t st) {
+    InitBatch ib;
+    memset(&ib, 0, sizeof(ib));
+    auto flush = [&]() -> int {
+        if (!ib.count) return DSGB_OK;
+        init_kernel<<<grid_for(ib.chunks), 256, 0, st>>>(ib);
+        DSGB_CHECK_LAUNCH("dsgb_bases_init");
+        ib.count = 0;
+        ib.chunks = 0;
+        return DSGB_OK;
+    };
     for (int b = 0; b < nbases; ++b) {
         const dsgb_base &B = bases[b];
         const int64_t n = ncells * (B.ncat < 1 ? 1 : B.ncat);
         if (!B.agg) { set_error("dsgb_bases_init: base %d has null agg", b); return DSGB_E_INVALID; }
-        cudaError_t e = cudaSuccess;
+        unsigned long long lo = 0, hi = 0;
+        int64_t bytes = 0;
         switch (B.op) {
-        case DSGB_BASE_COUNT: case DSGB_BASE_AA_CNT0:
-            e = cudaMemsetAsync(B.agg, 0, (size_t)n * 4, st); break;
-        case DSGB_BASE_ANY:
-            e = cudaMemsetAsync(B.agg, 0, (size_t)n, st); break;
-        case DSGB_BASE_SUM: case DSGB_BASE_AA_SUM:
-            e = cudaMemsetAsync(B.agg, 0, (size_t)n * 8, st); break;
+        case DSGB_BASE_COUNT: case DSGB_BASE_AA_CNT0: bytes = n * 4; break;
+        case DSGB_BASE_ANY: bytes = n; break;
+        case DSGB_BASE_SUM: case DSGB_BASE_AA_SUM: bytes = n * 8; break;
         case DSGB_BASE_MAX: case DSGB_BASE_AA_MAX:
-            fill_u64_kernel<<<grid_for(n), 256, 0, st>>>((unsigned long long *)B.agg, n,
-                                                          (unsigned long long)KEY_EMPTY_MAX);
-            break;
-        case DSGB_BASE_MIN:
-            fill_u64_kernel<<<grid_for(n), 256, 0, st>>>((unsigned long long *)B.agg, n,
-                                                          (unsigned long long)KEY_EMPTY_MIN);
-            break;
-        case DSGB_BASE_MIN_ROW:
-            fill_u64_kernel<<<grid_for(n), 256, 0, st>>>((unsigned long long *)B.agg, n,
-                                                          (unsigned long long)ROW_EMPTY_MIN);
-            break;
-        case DSGB_BASE_MAX_ROW:
-            e = cudaMemsetAsync(B.agg, 0xff, (size_t)n * 8, st); break;   // -1
+            bytes = n * 8; lo = hi = (unsigned long long)KEY_EMPTY_MAX; break;
+        case DSGB_BASE_MIN: bytes = n * 8; lo = hi = (unsigned long long)KEY_EMPTY_MIN; break;
+        case DSGB_BASE_MIN_ROW: bytes = n * 8; lo = hi = (unsigned long long)ROW_EMPTY_MIN; break;
+        case DSGB_BASE_MAX_ROW: bytes = n * 8; lo = hi = ~0ull; break;          // -1
         case DSGB_BASE_ARGMAX: case DSGB_BASE_AA_ARGMAX:
-            fill_pair_kernel<<<grid_for(n), 256, 0, st>>>((long long *)B.agg, n, KEY_EMPTY_MAX, ROW_EMPTY_MIN);
-            break;
+            bytes = n * 16; lo = (unsigned long long)KEY_EMPTY_MAX; hi = (unsigned long long)ROW_EMPTY_MIN; break;
         case DSGB_BASE_ARGMIN:
-            fill_pair_kernel<<<grid_for(n), 256, 0, st>>>((long long *)B.agg, n, KEY_EMPTY_MIN, ROW_EMPTY_MIN);
-            break;
+            bytes = n * 16; lo = (unsigned long long)KEY_EMPTY_MIN; hi = (unsigned long long)ROW_EMPTY_MIN; break;
         default:
             set_error("dsgb_bases_init: unknown base op %d", B.op);
             return DSGB_E_INVALID;
         }
-        if (e != cudaSuccess) return cuda_status(e, "dsgb_bases_init memset");
-        DSGB_CHECK_LAUNCH("dsgb_bases_init fill");
+        ib.ptr[ib.count] = (unsigned char *)B.agg;
+        ib.bytes[ib.count] = bytes;
+        ib.lo[ib.count] = lo;
+        ib.hi[ib.count] = hi;
+        ++ib.count;
+        const int64_t ch = (bytes + 15) / 16;
+        if (ch > ib.chunks) ib.chunks = ch;
+        if (ib.count == INIT_BATCH) {
+            const int rc = flush();
+            if (rc) return rc;
+        }
     }
-    return DSGB_OK;
+    return flush();
 }
 
 // -------------------------------------------------------------- finalize
