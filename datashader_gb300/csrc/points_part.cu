@@ -9,17 +9,21 @@
 // the L2 atomic rate (about 2e11 a second on GB300: 8 bases over 1e8 rows take
 // 4 ms).  Here the atomics move into shared memory:
 //
-//   part_hist    -- bin every row (the exact binning of binning.cuh) and count
-//                   rows per canvas block (a block is a power-of-two rectangle
-//                   of pixels sized so that every base of the plan fits in
-//                   shared memory for the whole block);
-//   part_plan    -- one CTA: block offsets by an exclusive scan, and the work
-//                   items (a block's rows, split into items of at most 2^18);
-//   part_scatter -- bin the rows again (the same function, so the same block)
-//                   and write one 16-byte record per row {value, row, pixel in
-//                   the block, category} into its block's range: a CTA ranks a
-//                   batch of 2048 rows by block in shared memory and writes
-//                   each block's run contiguously;
+//   part_sample  -- bin one tile of 1,024 rows in eight (the exact binning of
+//                   binning.cuh) and count them per canvas block (a power-of-two
+//                   rectangle of pixels sized so that every base of the plan
+//                   fits in shared memory for the whole block);
+//   part_plan1   -- one CTA: each block's room, the scaled-up sample count plus
+//                   a margin of six standard deviations and 64 rows, laid out
+//                   by an exclusive scan;
+//   part_scatter -- bin every row (the same function as the sample) and write
+//                   one 16-byte record per row {value, row, pixel in the block,
+//                   category} into its block's room: a CTA ranks a batch of
+//                   2048 rows by block in shared memory and writes each block's
+//                   run contiguously; a row that finds the room full (a sample
+//                   far off; rare) goes straight into the bases with L2 atomics;
+//   part_plan2   -- one CTA: the rows each block holds, split into work items
+//                   of at most 2^18;
 //   part_reduce  -- persistent CTAs take work items; each initialises every
 //                   base over its block in shared memory, applies the item's
 //                   records with shared-memory atomics, and adds the block into
@@ -47,6 +51,8 @@ constexpr int64_t CHUNK = (int64_t)1 << 27;
 constexpr int64_t ITEM = (int64_t)1 << 18;
 constexpr int64_t MAX_ITEMS = CHUNK / ITEM + MAX_BLOCKS + 1;
 constexpr int64_t MIN_ROWS = (int64_t)1 << 20;
+constexpr int SAMPLE_LOG = 3;                    // part_sample bins one tile of rows in 2^SAMPLE_LOG
+constexpr int SAMPLE_TILE = 256;                 // float4 groups of a sampled tile (1,024 rows)
 constexpr int STATE_BUDGET = 200 * 1024;         // shared memory for the bases of one block
 constexpr uint8_t CAT_NONE = 0xff;
 
@@ -78,7 +84,8 @@ struct Params {
     int lean;
     float sxf, txf, syf, tyf, exlo, exhi, eylo, eyhi;
     double sx, tx, sy, ty, xmin, xmax, ymin, ymax;
-    uint32_t *blk_count, *blk_start, *blk_cursor;
+    uint32_t *blk_count, *blk_start, *blk_cursor, *blk_end;
+    int64_t rec_cap;                             // records the workspace holds
     Rec *recs;
     int4 *items;                                 // {block, begin, end, owned}
     uint32_t *counters;                          // [0] items, [1] next item
@@ -155,26 +162,26 @@ __device__ __forceinline__ unsigned local_pixel(const Params &p, int xi, int yi)
     return ((unsigned)(yi & ((1 << p.bh_log) - 1)) << p.bw_log) | (unsigned)(xi & ((1 << p.bw_log) - 1));
 }
 
-// ------------------------------------------------------------ part_hist
-__global__ void __launch_bounds__(HIST_THREADS) part_hist(const __grid_constant__ Params p) {
+// ------------------------------------------------------------ part_sample
+// Rows per block, estimated from one tile of 1,024 consecutive rows in every
+// 2^SAMPLE_LOG (whole cache lines); part_plan1 gives each block room for the
+// estimate and a margin, and part_scatter applies the rows that do not fit
+// straight to the bases.
+__global__ void __launch_bounds__(HIST_THREADS) part_sample(const __grid_constant__ Params p) {
     extern __shared__ unsigned hist[];
     for (int i = threadIdx.x; i < p.nblk; i += HIST_THREADS) hist[i] = 0;
     __syncthreads();
     const int64_t n4 = p.n >> 2;
+    const int64_t ns = ((n4 >> SAMPLE_LOG) / SAMPLE_TILE) * SAMPLE_TILE;     // sampled groups
     const float4 *x4 = (const float4 *)p.xs, *y4 = (const float4 *)p.ys;
-    for (int64_t g = (int64_t)blockIdx.x * HIST_THREADS + threadIdx.x; g < n4; g += (int64_t)gridDim.x * HIST_THREADS) {
+    for (int64_t k = (int64_t)blockIdx.x * HIST_THREADS + threadIdx.x; k < ns; k += (int64_t)gridDim.x * HIST_THREADS) {
+        const int64_t g = ((k / SAMPLE_TILE) << SAMPLE_LOG) * SAMPLE_TILE + k % SAMPLE_TILE;
         const float4 a = __ldcs(x4 + g), b = __ldcs(y4 + g);
         const float xs[4] = {a.x, a.y, a.z, a.w}, ys[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int j = 0; j < 4; ++j) {
             int xi, yi;
-            if (bin_row(p, xs[k], ys[k], xi, yi)) atomicAdd(&hist[block_of(p, xi, yi)], 1u);
-        }
-    }
-    if (blockIdx.x == 0) {
-        for (int64_t i = 4 * n4 + threadIdx.x; i < p.n; i += HIST_THREADS) {
-            int xi, yi;
-            if (bin_row(p, p.xs[i], p.ys[i], xi, yi)) atomicAdd(&hist[block_of(p, xi, yi)], 1u);
+            if (bin_row(p, xs[j], ys[j], xi, yi)) atomicAdd(&hist[block_of(p, xi, yi)], 1u);
         }
     }
     __syncthreads();
@@ -210,36 +217,109 @@ __device__ __forceinline__ unsigned block_scan(unsigned v, unsigned *warp_sums, 
     return warp_sums[warp] + incl - v;
 }
 
-// ------------------------------------------------------------ part_plan
-// One CTA: blocks in rounds of PLAN_THREADS, one a thread, scanned with the
-// running totals of the previous rounds.  A block of c rows becomes
-// m = ceil(c / ITEM) items of ceil(c / m) rows (the last shorter, none empty).
-__global__ void __launch_bounds__(PLAN_THREADS) part_plan(const __grid_constant__ Params p) {
-    __shared__ unsigned ws1[32], ws2[32];
-    __shared__ unsigned tot1, tot2;
-    unsigned carry1 = 0, carry2 = 0;
+// ------------------------------------------------------------ part_plan1
+// One CTA, blocks in rounds of PLAN_THREADS: each block's room is its
+// estimated rows (the sampled count scaled up) plus a margin of six standard
+// deviations of the estimate and 64 rows; the rooms are laid out by an
+// exclusive scan.  Room past the workspace's records is cut to nothing (those
+// rows then take the direct path).
+__device__ __forceinline__ unsigned block_room(unsigned sampled) {
+    const double est = (double)sampled * (double)(1 << SAMPLE_LOG);
+    return (unsigned)(est + 6.0 * sqrt(est * (double)((1 << SAMPLE_LOG) - 1)) + 64.0);
+}
+
+__global__ void __launch_bounds__(PLAN_THREADS) part_plan1(const __grid_constant__ Params p) {
+    __shared__ unsigned ws1[32];
+    __shared__ unsigned tot1;
+    unsigned long long carry = 0;
     for (int r0 = 0; r0 < p.nblk; r0 += PLAN_THREADS) {
         const int b = r0 + threadIdx.x;
-        const unsigned c = b < p.nblk ? p.blk_count[b] : 0u;
+        const unsigned cap = b < p.nblk ? block_room(p.blk_count[b]) : 0u;
+        const unsigned o = block_scan<PLAN_THREADS>(cap, ws1, &tot1);
+        if (b < p.nblk) {
+            const unsigned long long start = carry + o;
+            const unsigned long long end = start + cap;
+            const unsigned s0 = (unsigned)min(start, (unsigned long long)p.rec_cap);
+            p.blk_start[b] = s0;
+            p.blk_cursor[b] = s0;
+            p.blk_end[b] = (unsigned)min(end, (unsigned long long)p.rec_cap);
+        }
+        carry += tot1;
+    }
+}
+
+// ------------------------------------------------------------ part_plan2
+// One CTA: the rows each block holds (its cursor, at most its room) split
+// into work items of at most ITEM rows, ceil(c / m) each.
+__global__ void __launch_bounds__(PLAN_THREADS) part_plan2(const __grid_constant__ Params p) {
+    __shared__ unsigned ws2[32];
+    __shared__ unsigned tot2;
+    unsigned carry2 = 0;
+    for (int r0 = 0; r0 < p.nblk; r0 += PLAN_THREADS) {
+        const int b = r0 + threadIdx.x;
+        unsigned c = 0, o1 = 0;
+        if (b < p.nblk) {
+            o1 = p.blk_start[b];
+            c = min(p.blk_cursor[b], p.blk_end[b]) - o1;
+        }
         const unsigned m = (unsigned)((c + (unsigned)ITEM - 1) / (unsigned)ITEM);
-        const unsigned o1 = block_scan<PLAN_THREADS>(c, ws1, &tot1) + carry1;
         const unsigned o2 = block_scan<PLAN_THREADS>(m, ws2, &tot2) + carry2;
         if (b < p.nblk) {
-            p.blk_start[b] = o1;
-            p.blk_cursor[b] = o1;
             const unsigned sz = m ? (c + m - 1) / m : 0u;
             for (unsigned j = 0; j < m; ++j) {
                 const unsigned lo = j * sz, hi = min(c, lo + sz);
                 p.items[o2 + j] = make_int4(b, (int)(o1 + lo), (int)(o1 + hi), m == 1 ? 1 : 0);
             }
         }
-        carry1 += tot1;
         carry2 += tot2;
     }
     if (threadIdx.x == 0) {
-        p.blk_start[p.nblk] = carry1;
         p.counters[0] = carry2;
         p.counters[1] = 0;
+    }
+}
+
+__device__ __forceinline__ Rec decode(const uint4 q) {
+    Rec r;
+    r.v = __longlong_as_double((long long)(((unsigned long long)q.y << 32) | q.x));
+    r.row = q.z;
+    r.lpix = (uint16_t)(q.w & 0xffffu);
+    r.cat = (uint8_t)((q.w >> 16) & 0xffu);
+    r.pad = 0;
+    return r;
+}
+
+// A row whose block has no room left: its appends go straight into the bases
+// with L2 atomics, as the generic kernel does (reductions combine in any
+// order, so the result does not depend on which rows take this path).
+static __device__ __noinline__ void apply_direct(const Params *pp, int blk, uint4 q) {
+    const Params &p = *pp;
+    const Rec r = decode(q);
+    const unsigned lx = r.lpix & ((1u << p.bw_log) - 1), ly = (unsigned)r.lpix >> p.bw_log;
+    const int64_t gpix = (int64_t)(((blk / p.bx) << p.bh_log) + (int)ly) * p.W + ((blk % p.bx) << p.bw_log) + lx;
+    const bool has = !isnull(r.v);
+    const long long key = f64_key(r.v);
+    const long long row = p.row0 + (long long)r.row;
+    for (int b = 0; b < p.nbases; ++b) {
+        const PBase &B = p.bases[b];
+        if (B.has_col && !has) continue;
+        int64_t cell = gpix;
+        if (B.has_cat) {
+            if (r.cat == CAT_NONE) continue;
+            cell = gpix * B.ncat + r.cat;
+        }
+        switch (B.op) {
+        case DSGB_BASE_COUNT: atomicAdd((unsigned *)B.agg + cell, 1u); break;
+        case DSGB_BASE_ANY: ((volatile uint8_t *)B.agg)[cell] = 1; break;
+        case DSGB_BASE_SUM: atomicAdd((double *)B.agg + cell, r.v); break;
+        case DSGB_BASE_MAX: atomic_max_key((long long *)B.agg + cell, key); break;
+        case DSGB_BASE_MIN: atomic_min_key((long long *)B.agg + cell, key); break;
+        case DSGB_BASE_MIN_ROW: atomic_min_key((long long *)B.agg + cell, row); break;
+        case DSGB_BASE_MAX_ROW: atomic_max_key((long long *)B.agg + cell, row); break;
+        case DSGB_BASE_ARGMAX: pair_update<true>((long long *)B.agg + 2 * cell, key, row); break;
+        case DSGB_BASE_ARGMIN: pair_update<false>((long long *)B.agg + 2 * cell, key, row); break;
+        default: break;
+        }
     }
 }
 
@@ -383,9 +463,8 @@ __global__ void __launch_bounds__(SC_THREADS, 2) part_scatter(const __grid_const
             const unsigned e = sblk[i];
             if (e >= (unsigned)p.nblk) { raise_status(DSGB_STATUS_INDEX); continue; }
             const unsigned dst = delta[e] + i;
-            // both passes bin alike, so every run stays inside its block's range
-            if (dst < p.n) __stcg((uint4 *)(p.recs + dst), q);
-            else raise_status(DSGB_STATUS_INDEX);
+            if (dst < __ldg(p.blk_end + e)) __stcg((uint4 *)(p.recs + dst), q);
+            else apply_direct(&p, e, q);          // the block's room is full
         }
         for (int j = 0; j < per; ++j) {
             const int e = e0 + j;
@@ -406,8 +485,10 @@ __global__ void __launch_bounds__(SC_THREADS, 2) part_scatter(const __grid_const
             r.cat = load_code(p, i);
             r.pad = 0;
             const unsigned dst = atomicAdd(&p.blk_cursor[e], 1u);
-            if (dst < p.n) p.recs[dst] = r;
-            else raise_status(DSGB_STATUS_INDEX);
+            if (dst < p.blk_end[e]) p.recs[dst] = r;
+            else apply_direct(&p, e, make_uint4((unsigned)__double_as_longlong(r.v),
+                                                (unsigned)((unsigned long long)__double_as_longlong(r.v) >> 32),
+                                                r.row, (unsigned)r.lpix | ((unsigned)r.cat << 16)));
         }
     }
 }
@@ -491,15 +572,6 @@ __device__ __forceinline__ void init_state(const Params &p, unsigned char *sm, i
     }
 }
 
-__device__ __forceinline__ Rec decode(const uint4 q) {
-    Rec r;
-    r.v = __longlong_as_double((long long)(((unsigned long long)q.y << 32) | q.x));
-    r.row = q.z;
-    r.lpix = (uint16_t)(q.w & 0xffffu);
-    r.cat = (uint8_t)((q.w >> 16) & 0xffu);
-    r.pad = 0;
-    return r;
-}
 
 // One record into every base's block state: the common kinds first, by
 // warp-uniform tests of fast_mask, then the rest by the generic loop.
@@ -678,7 +750,7 @@ __global__ void __launch_bounds__(RD_THREADS, 1) part_reduce(const __grid_consta
         const int it = s_item;
         if ((unsigned)it >= nitems) break;
         const int4 item = p.items[it];
-        if (item.x < 0 || item.x >= p.nblk || item.y < 0 || item.y > item.z || (unsigned)item.z > p.blk_start[p.nblk]) {
+        if (item.x < 0 || item.x >= p.nblk || item.y < 0 || item.y > item.z || (int64_t)item.z > p.rec_cap) {
             raise_status(DSGB_STATUS_INDEX);
             __syncthreads();
             continue;
@@ -758,6 +830,17 @@ static bool geometry(int bpp, int W, int H, int &bw_log, int &bh_log, int &bx, i
 
 static size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
+// Records the workspace holds for a pass of `rows` rows over `nblk` blocks:
+// the rows, plus the blocks' margins (six standard deviations of a sampled
+// estimate and 64 rows each, at most 6 * sqrt(7 * nblk * rows) + 64 * nblk
+// together), plus 1/16 for the sampling error of the estimates' sum.
+static int64_t record_room(int64_t rows, int nblk) {
+    return rows + rows / 16 + 64 * (int64_t)nblk +
+           (int64_t)(6.0 * sqrt(7.0 * (double)nblk * (double)rows)) + 1024;
+}
+
+constexpr size_t BLK_ARRAYS = (size_t)4 * MAX_BLOCKS * 4;     // count, start, cursor, end
+
 }  // namespace part
 
 // Workspace of the partitioned path for n rows (0 when the bases are not served).
@@ -768,8 +851,8 @@ size_t part_workspace_size(int64_t n, const dsgb_canvas *cv, const dsgb_base *ba
     const int bpp = pixel_bytes(bases, nbases, vcol, ccol, ncat);
     if (!geometry(bpp, cv->width, cv->height, bwl, bhl, bx, nblk)) return 0;
     const int64_t rows = std::min(n, CHUNK);
-    return align16((size_t)rows * sizeof(Rec)) + align16((size_t)MAX_ITEMS * sizeof(int4)) +
-           align16((size_t)(3 * MAX_BLOCKS + 1) * 4) + 16;
+    return align16((size_t)record_room(rows, nblk) * sizeof(Rec)) + align16((size_t)MAX_ITEMS * sizeof(int4)) +
+           BLK_ARRAYS + 16;
 }
 
 // DSGB_E_UNSUPPORTED when the case is not served (the caller takes the
@@ -788,17 +871,19 @@ int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws,
     memset(&p, 0, sizeof(p));
     if (!geometry(bpp, pp.width, pp.height, p.bw_log, p.bh_log, p.bx, p.nblk)) return DSGB_E_UNSUPPORTED;
     const int64_t rows = std::min(pp.n, CHUNK);
-    const size_t rec_bytes = align16((size_t)rows * sizeof(Rec));
+    p.rec_cap = record_room(rows, p.nblk);
+    const size_t rec_bytes = align16((size_t)p.rec_cap * sizeof(Rec));
     const size_t item_bytes = align16((size_t)MAX_ITEMS * sizeof(int4));
-    const size_t need = rec_bytes + item_bytes + align16((size_t)(3 * MAX_BLOCKS + 1) * 4) + 16;
+    const size_t need = rec_bytes + item_bytes + BLK_ARRAYS + 16;
     if (ws_bytes < need || ((uintptr_t)ws & 15u)) return DSGB_E_UNSUPPORTED;
     unsigned char *w = (unsigned char *)ws;
     p.recs = (Rec *)w;
     p.items = (int4 *)(w + rec_bytes);
     p.blk_count = (uint32_t *)(w + rec_bytes + item_bytes);
     p.blk_start = p.blk_count + MAX_BLOCKS;
-    p.blk_cursor = p.blk_start + MAX_BLOCKS + 1;
-    p.counters = (uint32_t *)(w + rec_bytes + item_bytes + align16((size_t)(3 * MAX_BLOCKS + 1) * 4));
+    p.blk_cursor = p.blk_start + MAX_BLOCKS;
+    p.blk_end = p.blk_cursor + MAX_BLOCKS;
+    p.counters = (uint32_t *)(w + rec_bytes + item_bytes + BLK_ARRAYS);
     p.W = pp.width; p.H = pp.height;
     p.ax = pp.ax; p.ay = pp.ay; p.bb = pp.bb;
     p.lean = edges_ok(pp.bb.xminf, pp.bb.xmaxf, pp.sx, pp.tx, pp.width) &&
@@ -880,7 +965,7 @@ int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws,
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(part_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, p.nblk * 4);
+        e = cudaFuncSetAttribute(part_sample, cudaFuncAttributeMaxDynamicSharedMemorySize, p.nblk * 4);
     if (e != cudaSuccess) return cuda_status(e, "points part: shared memory attribute");
     int sc_per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sc_per_sm, scatter, SC_THREADS, sc_smem);
@@ -904,11 +989,14 @@ int launch_points_part(const PointsParams &pp, const dsgb_base *bases, void *ws,
         e = cudaMemsetAsync(p.blk_count, 0, (size_t)p.nblk * 4, st);
         if (e != cudaSuccess) return cuda_status(e, "points part: memset");
         const int64_t n4 = m >> 2;
-        int hist_grid = (int)std::min<int64_t>((int64_t)sms * 8, std::max<int64_t>(1, (n4 + HIST_THREADS - 1) / HIST_THREADS));
-        part_hist<<<hist_grid, HIST_THREADS, (size_t)p.nblk * 4, st>>>(p);
-        part_plan<<<1, PLAN_THREADS, 0, st>>>(p);
+        const int64_t ns = n4 >> SAMPLE_LOG;
+        const int sample_grid =
+            (int)std::min<int64_t>((int64_t)sms * 8, std::max<int64_t>(1, (ns + HIST_THREADS - 1) / HIST_THREADS));
+        part_sample<<<sample_grid, HIST_THREADS, (size_t)p.nblk * 4, st>>>(p);
+        part_plan1<<<1, PLAN_THREADS, 0, st>>>(p);
         const int sc_grid = (int)std::min<int64_t>((int64_t)sms * sc_per_sm, std::max<int64_t>(1, n4 / SC_THREADS));
         scatter<<<sc_grid, SC_THREADS, sc_smem, st>>>(p);
+        part_plan2<<<1, PLAN_THREADS, 0, st>>>(p);
         part_reduce<<<sms, RD_THREADS, p.state_bytes, st>>>(p);
         DSGB_CHECK_LAUNCH("points part: launch");
     }

@@ -160,3 +160,20 @@ def test_part_matches_generic_kernels_past_one_pass():
             assert_same(a[k], b[k], what=k)
     assert int(a["count"].sum()) > 0.95 * n
     assert a["where_row"].max() > (1 << 27)
+
+
+def test_part_rows_past_a_blocks_room_take_the_direct_path():
+    """The block rooms come from a sample of one tile of 1,024 rows in eight.
+    Rows laid out so that the sampled tiles fall left of x = 0 and every other
+    row right of it: the right half's blocks get the minimum room and most of
+    their rows go straight to the bases (L2 atomics).  Equal to the oracle."""
+    n = (1 << 21) + 3
+    cols = _cols(n, seed=31)
+    tile = np.arange(n) // 1024
+    x = np.abs(cols["x"]).astype(np.float32)
+    cols["x"] = np.where(tile % 8 == 0, -x, x).astype(np.float32)
+    canvas = dict(plot_width=1024, plot_height=1024, x_range=(-4.0, 4.0), y_range=(-4.0, 4.0))
+    agg = _summary()
+    got = to_numpy(ds.Canvas(**canvas).points(frame_from_numpy(cols, CATS), "x", "y", agg))
+    _check(got, run_points(cols, CATS, agg, canvas))
+    assert got["count"][:, 600:].sum() > 0.8 * n * 7 / 8 / 2
