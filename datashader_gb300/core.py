@@ -249,6 +249,9 @@ def as_frame(source):
 
 # -------------------------------------------------------------------- axes
 
+_INDEX_CACHE = {}
+
+
 class Axis:
     """core.py:45-111."""
 
@@ -260,10 +263,19 @@ class Axis:
         return s, t
 
     def compute_index(self, st, n):
-        """core.py:83-99: pixel-centre coordinates."""
-        px = np.arange(n) + 0.5
-        s, t = st
-        return self.inverse_mapper((px - t) / s)
+        """core.py:83-99: pixel-centre coordinates (read-only arrays, built
+        once per axis type, scale / translate and size)."""
+        key = (type(self), float(st[0]), float(st[1]), int(n))
+        c = _INDEX_CACHE.get(key)
+        if c is None:
+            px = np.arange(n) + 0.5
+            s, t = st
+            c = self.inverse_mapper((px - t) / s)
+            c.flags.writeable = False
+            if len(_INDEX_CACHE) > 256:
+                _INDEX_CACHE.clear()
+            _INDEX_CACHE[key] = c
+        return c
 
     def validate(self, range):
         pass
@@ -705,8 +717,6 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
     width, height = canvas.plot_width, canvas.plot_height
     x_st = canvas.x_axis.compute_scale_and_translate(x_range, width)
     y_st = canvas.y_axis.compute_scale_and_translate(y_range, height)
-    x_axis = canvas.x_axis.compute_index(x_st, width)
-    y_axis = canvas.y_axis.compute_index(y_st, height)
     ex = Executor(frame, plan, glyph)
     ex.allocate(height, width, frame.device)
     cv = N.CanvasDesc(width, height, int(canvas.x_axis.is_log), int(canvas.y_axis.is_log),
@@ -778,7 +788,9 @@ def gpu_pipeline(frame, canvas, glyph, agg, *, antialias=False, flags=0, stream=
                               ex.bases, len(plan.bases), ex.outs, ex.nouts,
                               ws.data_ptr() if ws is not None else None, wsz, flags, stream)
         N.check(rc, "dsgb_points_ws")
-    coords = {glyph.x_label: x_axis, glyph.y_label: y_axis}
+    # the coordinates are built while the kernels run
+    coords = {glyph.x_label: canvas.x_axis.compute_index(x_st, width),
+              glyph.y_label: canvas.y_axis.compute_index(y_st, height)}
     dims = [glyph.y_label, glyph.x_label]
     with _NvtxRange("dsgb results"):
         return _results(plan, ex, coords, dims, dict(x_range=x_range, y_range=y_range))
