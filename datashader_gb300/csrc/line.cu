@@ -12,6 +12,7 @@
 // separately and the coverage values are bit-identical to the reference's.
 // Only the order of the floating-point accumulation differs (atomics).
 #include "dsgb_internal.cuh"
+#include "f64cmp.cuh"
 
 #include <cmath>
 
@@ -27,6 +28,7 @@ struct LineParams {
     double sx, tx, sy, ty;
     double xmin, xmax, ymin, ymax;
     double line_width;
+    int64_t aa_nx, aa_ny;   // round((xmax - xmin) * sx), round((ymax - ymin) * sy) (line.py:1070-1071)
     int32_t plot_start, overwrite, use_2_stage;
     int64_t field_mod;      // > 0: appends carry a visit key (row = key % field_mod); 0: the row itself
     int32_t debug;          // DSGB_FLAG_DEBUG_CHECKS
@@ -104,18 +106,19 @@ __device__ void line_append(const LineParams &p, int64_t key, long long x, long 
     }
 }
 
-// line.py:783-800
+// line.py:783-800.  Comparisons by integer operations (f64cmp.cuh), IEEE
+// results for every input.
 __device__ __forceinline__ bool clipt(double p, double q, double &t0, double &t1) {
     bool accept = true;
-    if (p < 0 && q < 0) {
+    if (f64_lt0(p) && f64_lt0(q)) {
         double r = q / p;
-        if (r > t1) accept = false;
-        else if (r > t0) t0 = r;
-    } else if (p > 0 && q < p) {
+        if (f64_lt(t1, r)) accept = false;
+        else if (f64_lt(t0, r)) t0 = r;
+    } else if (f64_gt0(p) && f64_lt(q, p)) {
         double r = q / p;
-        if (r < t0) accept = false;
-        else if (r < t1) t1 = r;
-    } else if (q < 0) {
+        if (f64_lt(r, t0)) accept = false;
+        else if (f64_lt(r, t1)) t1 = r;
+    } else if (f64_lt0(q)) {
         accept = false;
     }
     return accept;
@@ -125,10 +128,10 @@ __device__ __forceinline__ bool clipt(double p, double q, double &t0, double &t1
 __device__ __forceinline__ void liang_barsky(double xmin, double xmax, double ymin, double ymax,
                                              double &x0, double &x1, double &y0, double &y1,
                                              bool &skip, bool &cs, bool &ce) {
-    if (x0 < xmin && x1 < xmin) skip = true;
-    else if (x0 > xmax && x1 > xmax) skip = true;
-    else if (y0 < ymin && y1 < ymin) skip = true;
-    else if (y0 > ymax && y1 > ymax) skip = true;
+    if (f64_lt(x0, xmin) && f64_lt(x1, xmin)) skip = true;
+    else if (f64_lt(xmax, x0) && f64_lt(xmax, x1)) skip = true;
+    else if (f64_lt(y0, ymin) && f64_lt(y1, ymin)) skip = true;
+    else if (f64_lt(ymax, y0) && f64_lt(ymax, y1)) skip = true;
     double t0 = 0, t1 = 1;
     double dx1 = x1 - x0;
     if (!clipt(-dx1, x0 - xmin, t0, t1)) skip = true;
@@ -136,25 +139,13 @@ __device__ __forceinline__ void liang_barsky(double xmin, double xmax, double ym
     double dy1 = y1 - y0;
     if (!clipt(-dy1, y0 - ymin, t0, t1)) skip = true;
     if (!clipt(dy1, ymax - y0, t0, t1)) skip = true;
-    if (t1 < 1) { ce = true; x1 = x0 + t1 * dx1; y1 = y0 + t1 * dy1; } else ce = false;
-    if (t0 > 0) { cs = true; x0 = x0 + t0 * dx1; y0 = y0 + t0 * dy1; } else cs = false;
+    if (f64_lt(t1, 1.0)) { ce = true; x1 = x0 + t1 * dx1; y1 = y0 + t1 * dy1; } else ce = false;
+    if (f64_gt0(t0)) { cs = true; x0 = x0 + t0 * dx1; y0 = y0 + t0 * dy1; } else cs = false;
 }
 
-__device__ __forceinline__ double clampd(double x, double lo, double hi) {
-    double m = x < hi ? x : hi;
-    return lo > m ? lo : m;
-}
-__device__ __forceinline__ long long clampi(long long x, long long lo, long long hi) {
-    long long m = x < hi ? x : hi;
-    return lo > m ? lo : m;
-}
-// line.py:808-811
-__device__ __forceinline__ double linearstep(double e0, double e1, double x) {
-    return clampd((x - e0) / (e1 - e0), 0.0, 1.0);
-}
 // line.py:814-821
 __device__ __forceinline__ double x_intercept(double y, double cx0, double cy0, double cx1, double cy1) {
-    if (cy0 == cy1) return cx1;
+    if (f64_eq(cy0, cy1)) return cx1;
     double frac = (y - cy0) / (cy1 - cy0);
     return cx0 + frac * (cx1 - cx0);
 }
@@ -171,8 +162,8 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
                                double x0, double x1, double y0, double y1,
                                bool segment_start, bool segment_end, double xm, double ym,
                                long long nx, long long ny) {
-    if (x0 == x1 && y0 == y1) return;
-    const bool flip_xy = fabs(x0 - x1) < fabs(y0 - y1);
+    if (f64_eq(x0, x1) && f64_eq(y0, y1)) return;
+    const bool flip_xy = f64_abs_lt(x0 - x1, y0 - y1);
     if (flip_xy) {
         double t;
         t = x0; x0 = y0; y0 = t;
@@ -183,7 +174,7 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
     if (line_width < 1.0) { scale *= line_width; line_width = 1.0; }
     const double aa = 1.0;
     const double halfwidth = 0.5 * (line_width + aa);
-    const bool flip_order = y1 < y0 || (y1 == y0 && x1 < x0);
+    const bool flip_order = f64_lt(y1, y0) || (f64_eq(y1, y0) && f64_lt(x1, x0));
     double alongx = x1 - x0;
     double alongy = y1 - y0;
     const double length = sqrt(sq(alongx) + sq(alongy));
@@ -215,13 +206,13 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
     }
     long long xmaxi = nx - 1, ymaxi = ny - 1;
     if (flip_xy) { long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
-    const int lowindex = flip_order ? (x0 > x1 ? 0 : 1) : (x1 > x0 ? 0 : 1);
+    const int lowindex = flip_order ? (f64_lt(x1, x0) ? 0 : 1) : (f64_lt(x0, x1) ? 0 : 1);
     double prev_alongx = 0, prev_alongy = 0, prev_length = 0, prev_rightx = 0, prev_righty = 0;
     if (!overwrite && !segment_start) {
         prev_alongx = x0 - xm;
         prev_alongy = y0 - ym;
         prev_length = sqrt(sq(prev_alongx) + sq(prev_alongy));
-        if (prev_length > 0.0) {
+        if (f64_gt0(prev_length)) {
             prev_alongx /= prev_length;
             prev_alongy /= prev_length;
             prev_rightx = prev_alongy;
@@ -230,49 +221,60 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
             overwrite = true;
         }
     }
-    const long long ystart = clampi((long long)ceil(pick4(lowindex, by0, by1, by2, by3)), 0, ymaxi);
-    const long long yend = clampi((long long)floor(pick4((lowindex + 2) % 4, by0, by1, by2, by3)), 0, ymaxi);
+    // clampi((long long)ceil / floor(.), 0, max) by integer operations (nx, ny < 2^31)
+    const long long ystart = f64_ceil_clamp(pick4(lowindex, by0, by1, by2, by3), ymaxi);
+    const long long yend = f64_floor_clamp(pick4((lowindex + 2) % 4, by0, by1, by2, by3), ymaxi);
     int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
     const double lw_lo = 0.5 * (line_width - aa);
+    const double ls_den = halfwidth - lw_lo;           // linearstep's edge1 - edge0
+    const bool unit_den = ls_den == 1.0;               // x / 1.0 == x: the division is skipped
+    // The comparisons, the float64 pixel coordinates and the ceil / floor
+    // conversions are integer operations on the bit patterns (f64cmp.cuh),
+    // each with the IEEE result for the values that reach it: the float64
+    // pipe, which bounds this loop, then issues only the products, sums,
+    // square roots and divisions (none for the ramp when its denominator is
+    // exactly 1.0).  length >= +0 (or NaN), prev_length in (0, inf],
+    // halfwidth in [1, inf], and the coverage values lie in [+0, 1].
     for (long long y = ystart; y <= yend; ++y) {
-        const double yd = (double)y;
-        if (ll == lowindex && yd > pick4(lu, by0, by1, by2, by3)) { ll = lu; lu = (ll + 1) % 4; }
-        if (rl == lowindex && yd > pick4(ru, by0, by1, by2, by3)) { rl = ru; ru = (rl + 3) % 4; }
-        const long long xleft = clampi((long long)ceil(x_intercept(yd, pick4(ll, bx0, bx1, bx2, bx3),
-            pick4(ll, by0, by1, by2, by3), pick4(lu, bx0, bx1, bx2, bx3), pick4(lu, by0, by1, by2, by3))), 0, xmaxi);
-        const long long xright = clampi((long long)floor(x_intercept(yd, pick4(rl, bx0, bx1, bx2, bx3),
-            pick4(rl, by0, by1, by2, by3), pick4(ru, bx0, bx1, bx2, bx3), pick4(ru, by0, by1, by2, by3))), 0, xmaxi);
+        const double yd = f64_from_u32((unsigned)y);
+        if (ll == lowindex && f64_nonneg_gt(yd, pick4(lu, by0, by1, by2, by3))) { ll = lu; lu = (ll + 1) % 4; }
+        if (rl == lowindex && f64_nonneg_gt(yd, pick4(ru, by0, by1, by2, by3))) { rl = ru; ru = (rl + 3) % 4; }
+        const long long xleft = f64_ceil_clamp(x_intercept(yd, pick4(ll, bx0, bx1, bx2, bx3),
+            pick4(ll, by0, by1, by2, by3), pick4(lu, bx0, bx1, bx2, bx3), pick4(lu, by0, by1, by2, by3)), xmaxi);
+        const long long xright = f64_floor_clamp(x_intercept(yd, pick4(rl, bx0, bx1, bx2, bx3),
+            pick4(rl, by0, by1, by2, by3), pick4(ru, bx0, bx1, bx2, bx3), pick4(ru, by0, by1, by2, by3)), xmaxi);
         for (long long x = xleft; x <= xright; ++x) {
-            const double xd = (double)x;
+            const double xd = f64_from_u32((unsigned)x);         // 0 <= x < 2^31
             const double along = (xd - x0) * alongx + (yd - y0) * alongy;
             bool prev_correction = false;
             double distance;
-            if (along < 0.0) {
-                if (overwrite || segment_start || (xd - x0) * prev_alongx + (yd - y0) * prev_alongy > 0.0)
+            if (f64_lt0(along)) {
+                if (overwrite || segment_start || f64_gt0((xd - x0) * prev_alongx + (yd - y0) * prev_alongy))
                     distance = sqrt(sq(xd - x0) + sq(yd - y0));
                 else continue;
-            } else if (along > length) {
+            } else if (f64_gt_nonneg(along, length)) {
                 if (overwrite || segment_end) distance = sqrt(sq(xd - x1) + sq(yd - y1));
                 else continue;
             } else {
                 distance = fabs((xd - x0) * rightx + (yd - y0) * righty);
                 if (!overwrite && !segment_start) {
                     const double pd = (xd - x0) * prev_alongx + (yd - y0) * prev_alongy;
-                    if (-prev_length <= pd && pd <= 0.0 &&
-                        fabs((xd - x0) * prev_rightx + (yd - y0) * prev_righty) <= halfwidth)
+                    if (f64_in_neg_range(pd, prev_length) &&
+                        f64_abs_le((xd - x0) * prev_rightx + (yd - y0) * prev_righty, halfwidth))
                         prev_correction = true;
                 }
             }
-            double value = 1.0 - linearstep(lw_lo, halfwidth, distance);
+            // 1 - linearstep(lw_lo, halfwidth, distance), line.py:808-811
+            double value = f64_one_minus_clamp01(unit_den ? distance - lw_lo : (distance - lw_lo) / ls_den);
             value *= scale;
             double prev_value = 0.0;
             if (prev_correction) {
                 const double prev_distance = fabs((xd - x0) * prev_rightx + (yd - y0) * prev_righty);
-                prev_value = 1.0 - linearstep(lw_lo, halfwidth, prev_distance);
+                prev_value = f64_one_minus_clamp01(unit_den ? prev_distance - lw_lo : (prev_distance - lw_lo) / ls_den);
                 prev_value *= scale;
-                if (value <= prev_value) value = 0.0;
+                if (f64_le_nonneg(value, prev_value)) value = 0.0;
             }
-            if (value > 0.0) {
+            if (f64_gt0(value)) {
                 if (flip_xy) line_append<KEYED>(p, i, y, x, value, prev_value);
                 else line_append<KEYED>(p, i, x, y, value, prev_value);
             }
@@ -344,8 +346,7 @@ __device__ void draw_segment(const LineParams &p, int64_t row, double x0, double
         const double px1 = x1 * p.sx + p.tx - 0.5, py1 = y1 * p.sy + p.ty - 0.5;
         double pxm = 0.0, pym = 0.0;
         if (!segment_start) { pxm = xm * p.sx + p.tx - 0.5; pym = ym * p.sy + p.ty - 0.5; }
-        const long long nx = pyround((p.xmax - p.xmin) * p.sx);
-        const long long ny = pyround((p.ymax - p.ymin) * p.sy);
+        const long long nx = p.aa_nx, ny = p.aa_ny;          // pyround((xmax - xmin) * sx), on the host
         full_antialias<KEYED>(p, p.line_width, p.overwrite != 0, row, px0, px1, py0, py1,
                        segment_start, segment_end, pxm, pym, nx, ny);
     } else {
@@ -616,6 +617,16 @@ int build_line_params(LineParams &p, const dsgb_column *cols, int32_t ncols, int
     p.x_col = x_col; p.y_col = y_col; p.width = cv->width; p.height = cv->height;
     p.sx = cv->sx; p.tx = cv->tx; p.sy = cv->sy; p.ty = cv->ty;
     p.xmin = cv->xmin; p.xmax = cv->xmax; p.ymin = cv->ymin; p.ymax = cv->ymax;
+    // The antialiased scan's pixel counts (line.py:1070-1071, Python round:
+    // half to even, as rint), once here instead of per segment.  The
+    // kernels' integer ceil / floor take pixel indexes below 2^31.
+    const double span_x = (p.xmax - p.xmin) * p.sx, span_y = (p.ymax - p.ymin) * p.sy;
+    if (!(std::fabs(span_x) < 2147483648.0) || !(std::fabs(span_y) < 2147483648.0)) {
+        set_error("dsgb_line_axis0: the canvas spans (xmax - xmin) * sx and (ymax - ymin) * sy must be below 2^31 pixels");
+        return DSGB_E_INVALID;
+    }
+    p.aa_nx = (int64_t)std::rint(span_x);
+    p.aa_ny = (int64_t)std::rint(span_y);
     return DSGB_OK;
 }
 

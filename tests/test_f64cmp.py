@@ -1,0 +1,25 @@
+"""The float64 comparisons by integer operations of the antialiased line
+kernels (csrc/f64cmp.cuh), checked on the host: each helper against the IEEE
+operation it replaces over special values (signed zeros, subnormals, the
+largest finite, infinities, NaNs of both signs and several payloads) and
+random ones, and the uint32 -> float64 conversion against the C conversion."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "datashader_gb300", "csrc")
+
+
+def test_f64cmp_helpers_match_ieee(tmp_path):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not found")
+    exe = str(tmp_path / "f64cmp_check")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", f"-I{CSRC}",
+                    os.path.join(HERE, "f64cmp_check.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok")
