@@ -24,6 +24,7 @@
 // for rows that land on a pixel with a non-NaN value, 0 otherwise.
 #include "dsgb_internal.cuh"
 #include "binning.cuh"
+#include "f64cmp.cuh"
 
 #include <cmath>
 
@@ -58,25 +59,29 @@ __device__ __forceinline__ D3 operator/(D3 a, D3 b) {
 }
 __device__ __forceinline__ D3 dsqrt(D3 a) {
     const double r = sqrt(a.v);
-    const float k = r > 0.0 ? 0.5f / f32(r) : 0.0f;
+    const float k = f64_gt0(r) ? 0.5f / f32(r) : 0.0f;
     return D3{r, a.g0 * k, a.g1 * k, a.g2 * k};
 }
-__device__ __forceinline__ D3 dabs(D3 a) { return a.v < 0.0 ? -a : a; }
+__device__ __forceinline__ D3 dabs(D3 a) { return f64_lt0(a.v) ? -a : a; }
 __device__ __forceinline__ D3 dsq(D3 a) { return a * a; }
-// max(lo, min(x, hi)) as the forward computes it
-__device__ __forceinline__ D3 dclamp(D3 x, double lo, double hi) {
-    D3 m = x.v < hi ? x : dc(hi);
-    return lo > m.v ? dc(lo) : m;
+// max(0, min(x, 1)) with the comparisons m = x < 1 ? x : 1, 0 > m ? 0 : m,
+// classified on the bit pattern (f64cmp.cuh): x itself (with its tangents)
+// for [+0, 1) and -0.0, a constant 0 for negative x, a constant 1 for
+// [1, inf] and NaN.
+__device__ __forceinline__ D3 dclamp01(D3 x) {
+    const unsigned long long T = f64_bits(x.v);
+    if (T < F64_ONE || T == F64_SIGN) return x;
+    return f64_lt0(x.v) ? dc(0.0) : dc(1.0);
 }
 // den = edge1 - edge0, computed once per segment; exactly 1.0 skips the
 // division (x / 1.0 == x, and the constant divisor has no tangents), as in
 // the forward kernel.
 __device__ __forceinline__ D3 dlinearstep(double e0, double den, bool unit_den, D3 x) {
     const D3 d = x - dc(e0);
-    return dclamp(unit_den ? d : d / dc(den), 0.0, 1.0);
+    return dclamp01(unit_den ? d : d / dc(den));
 }
 __device__ __forceinline__ D3 dx_intercept(double y, D3 cx0, D3 cy0, D3 cx1, D3 cy1) {
-    if (cy0.v == cy1.v) return cx1;
+    if (f64_eq(cy0.v, cy1.v)) return cx1;
     const D3 frac = (dc(y) - cy0) / (cy1 - cy0);
     return cx0 + frac * (cx1 - cx0);
 }
@@ -86,23 +91,19 @@ __device__ __forceinline__ D3 dpick4(int i, const D3 &a0, const D3 &a1, const D3
     const D3 &hi = (i & 1) ? a3 : a2;
     return (i & 2) ? hi : lo;
 }
-__device__ __forceinline__ long long clampi_b(long long x, long long lo, long long hi) {
-    long long m = x < hi ? x : hi;
-    return lo > m ? lo : m;
-}
 
 // line.py:783-800 in duals
 __device__ __forceinline__ bool dclipt(D3 p, D3 q, D3 &t0, D3 &t1) {
     bool accept = true;
-    if (p.v < 0 && q.v < 0) {
+    if (f64_lt0(p.v) && f64_lt0(q.v)) {
         const D3 r = q / p;
-        if (r.v > t1.v) accept = false;
-        else if (r.v > t0.v) t0 = r;
-    } else if (p.v > 0 && q.v < p.v) {
+        if (f64_lt(t1.v, r.v)) accept = false;
+        else if (f64_lt(t0.v, r.v)) t0 = r;
+    } else if (f64_gt0(p.v) && f64_lt(q.v, p.v)) {
         const D3 r = q / p;
-        if (r.v < t0.v) accept = false;
-        else if (r.v < t1.v) t1 = r;
-    } else if (q.v < 0) {
+        if (f64_lt(r.v, t0.v)) accept = false;
+        else if (f64_lt(r.v, t1.v)) t1 = r;
+    } else if (f64_lt0(q.v)) {
         accept = false;
     }
     return accept;
@@ -115,6 +116,7 @@ struct BwdParams {
     double sx, tx, sy, ty;
     double xmin, xmax, ymin, ymax;
     double line_width;
+    int64_t aa_nx, aa_ny;   // round((xmax - xmin) * sx), round((ymax - ymin) * sy), on the host
     int32_t plot_start;
     const double *grad;
     const uint8_t *any;
@@ -128,8 +130,8 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
                                  double &gv, double &gy0, double &gy1, double &gy2) {
     double line_width = p.line_width;
     bool overwrite = false;
-    if (x0.v == x1.v && y0.v == y1.v) return;
-    const bool flip_xy = fabs(x0.v - x1.v) < fabs(y0.v - y1.v);
+    if (f64_eq(x0.v, x1.v) && f64_eq(y0.v, y1.v)) return;
+    const bool flip_xy = f64_abs_lt(x0.v - x1.v, y0.v - y1.v);
     if (flip_xy) {
         D3 t;
         t = x0; x0 = y0; y0 = t;
@@ -138,9 +140,10 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
     }
     double scale = 1.0;
     if (line_width < 1.0) { scale *= line_width; line_width = 1.0; }
+    const bool unit_scale = scale == 1.0;
     const double aa = 1.0;
     const double halfwidth = 0.5 * (line_width + aa);
-    const bool flip_order = y1.v < y0.v || (y1.v == y0.v && x1.v < x0.v);
+    const bool flip_order = f64_lt(y1.v, y0.v) || (f64_eq(y1.v, y0.v) && f64_lt(x1.v, x0.v));
     D3 alongx = x1 - x0, alongy = y1 - y0;
     const D3 length = dsqrt(dsq(alongx) + dsq(alongy));
     alongx = alongx / length;
@@ -171,13 +174,13 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
     }
     long long xmaxi = nx - 1, ymaxi = ny - 1;
     if (flip_xy) { long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
-    const int lowindex = flip_order ? (x0.v > x1.v ? 0 : 1) : (x1.v > x0.v ? 0 : 1);
+    const int lowindex = flip_order ? (f64_lt(x1.v, x0.v) ? 0 : 1) : (f64_lt(x0.v, x1.v) ? 0 : 1);
     D3 prev_alongx = dc(0), prev_alongy = dc(0), prev_length = dc(0), prev_rightx = dc(0), prev_righty = dc(0);
     if (!overwrite && !segment_start) {
         prev_alongx = x0 - xm;
         prev_alongy = y0 - ym;
         prev_length = dsqrt(dsq(prev_alongx) + dsq(prev_alongy));
-        if (prev_length.v > 0.0) {
+        if (f64_gt0(prev_length.v)) {
             prev_alongx = prev_alongx / prev_length;
             prev_alongy = prev_alongy / prev_length;
             prev_rightx = prev_alongy;
@@ -186,52 +189,52 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
             overwrite = true;
         }
     }
-    const long long ystart = clampi_b((long long)ceil(dpick4(lowindex, by0, by1, by2, by3).v), 0, ymaxi);
-    const long long yend = clampi_b((long long)floor(dpick4((lowindex + 2) % 4, by0, by1, by2, by3).v), 0, ymaxi);
+    const long long ystart = f64_ceil_clamp(dpick4(lowindex, by0, by1, by2, by3).v, ymaxi);
+    const long long yend = f64_floor_clamp(dpick4((lowindex + 2) % 4, by0, by1, by2, by3).v, ymaxi);
     int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
     const double lw_lo = 0.5 * (line_width - aa);
     const double ls_den = halfwidth - lw_lo;
     const bool unit_den = ls_den == 1.0;
     float ty0 = 0.0f, ty1 = 0.0f, ty2 = 0.0f;     // the y tangents of this segment, in float32
     for (long long y = ystart; y <= yend; ++y) {
-        const double yd = (double)y;
-        if (ll == lowindex && yd > dpick4(lu, by0, by1, by2, by3).v) { ll = lu; lu = (ll + 1) % 4; }
-        if (rl == lowindex && yd > dpick4(ru, by0, by1, by2, by3).v) { rl = ru; ru = (rl + 3) % 4; }
-        const long long xleft = clampi_b((long long)ceil(dx_intercept(yd, dpick4(ll, bx0, bx1, bx2, bx3),
-            dpick4(ll, by0, by1, by2, by3), dpick4(lu, bx0, bx1, bx2, bx3), dpick4(lu, by0, by1, by2, by3)).v), 0, xmaxi);
-        const long long xright = clampi_b((long long)floor(dx_intercept(yd, dpick4(rl, bx0, bx1, bx2, bx3),
-            dpick4(rl, by0, by1, by2, by3), dpick4(ru, bx0, bx1, bx2, bx3), dpick4(ru, by0, by1, by2, by3)).v), 0, xmaxi);
+        const double yd = f64_from_u32((unsigned)y);
+        if (ll == lowindex && f64_nonneg_gt(yd, dpick4(lu, by0, by1, by2, by3).v)) { ll = lu; lu = (ll + 1) % 4; }
+        if (rl == lowindex && f64_nonneg_gt(yd, dpick4(ru, by0, by1, by2, by3).v)) { rl = ru; ru = (rl + 3) % 4; }
+        const long long xleft = f64_ceil_clamp(dx_intercept(yd, dpick4(ll, bx0, bx1, bx2, bx3),
+            dpick4(ll, by0, by1, by2, by3), dpick4(lu, bx0, bx1, bx2, bx3), dpick4(lu, by0, by1, by2, by3)).v, xmaxi);
+        const long long xright = f64_floor_clamp(dx_intercept(yd, dpick4(rl, bx0, bx1, bx2, bx3),
+            dpick4(rl, by0, by1, by2, by3), dpick4(ru, bx0, bx1, bx2, bx3), dpick4(ru, by0, by1, by2, by3)).v, xmaxi);
         for (long long x = xleft; x <= xright; ++x) {
-            const D3 xd = dc((double)x), ydd = dc(yd);
+            const D3 xd = dc(f64_from_u32((unsigned)x)), ydd = dc(yd);
             const D3 along = (xd - x0) * alongx + (ydd - y0) * alongy;
             bool prev_correction = false;
             D3 distance;
-            if (along.v < 0.0) {
-                if (overwrite || segment_start || ((xd - x0) * prev_alongx + (ydd - y0) * prev_alongy).v > 0.0)
+            if (f64_lt0(along.v)) {
+                if (overwrite || segment_start || f64_gt0(((xd - x0) * prev_alongx + (ydd - y0) * prev_alongy).v))
                     distance = dsqrt(dsq(xd - x0) + dsq(ydd - y0));
                 else continue;
-            } else if (along.v > length.v) {
+            } else if (f64_gt_nonneg(along.v, length.v)) {
                 if (overwrite || segment_end) distance = dsqrt(dsq(xd - x1) + dsq(ydd - y1));
                 else continue;
             } else {
                 distance = dabs((xd - x0) * rightx + (ydd - y0) * righty);
                 if (!overwrite && !segment_start) {
                     const D3 pd = (xd - x0) * prev_alongx + (ydd - y0) * prev_alongy;
-                    if (-prev_length.v <= pd.v && pd.v <= 0.0 &&
-                        dabs((xd - x0) * prev_rightx + (ydd - y0) * prev_righty).v <= halfwidth)
+                    if (f64_in_neg_range(pd.v, prev_length.v) &&
+                        f64_abs_le(((xd - x0) * prev_rightx + (ydd - y0) * prev_righty).v, halfwidth))
                         prev_correction = true;
                 }
             }
             D3 value = dc(1.0) - dlinearstep(lw_lo, ls_den, unit_den, distance);
-            value = value * dc(scale);
+            if (!unit_scale) value = value * dc(scale);      // x * 1.0 == x
             D3 prev_value = dc(0.0);
             if (prev_correction) {
                 const D3 prev_distance = dabs((xd - x0) * prev_rightx + (ydd - y0) * prev_righty);
                 prev_value = dc(1.0) - dlinearstep(lw_lo, ls_den, unit_den, prev_distance);
-                prev_value = prev_value * dc(scale);
-                if (value.v <= prev_value.v) value = dc(0.0);
+                if (!unit_scale) prev_value = prev_value * dc(scale);
+                if (f64_le_nonneg(value.v, prev_value.v)) value = dc(0.0);
             }
-            if (value.v > 0.0) {
+            if (f64_gt0(value.v)) {
                 const long long xx = flip_xy ? y : x, yy = flip_xy ? x : y;
                 if (xx < 0 || yy < 0 || xx >= p.width || yy >= p.height) continue;
                 const int64_t pix = yy * (int64_t)p.width + xx;
@@ -274,10 +277,10 @@ __global__ void __launch_bounds__(256, 1) line_backward_kernel(const BwdParams p
         D3 y0 = D3{yv0, 0.0f, 1.0f, 0.0f}, y1 = D3{yv1, 0.0f, 0.0f, 1.0f};
         // line.py:734-780 (Liang-Barsky) in duals
         bool skip = false;
-        if (x0.v < p.xmin && x1.v < p.xmin) skip = true;
-        else if (x0.v > p.xmax && x1.v > p.xmax) skip = true;
-        else if (y0.v < p.ymin && y1.v < p.ymin) skip = true;
-        else if (y0.v > p.ymax && y1.v > p.ymax) skip = true;
+        if (f64_lt(x0.v, p.xmin) && f64_lt(x1.v, p.xmin)) skip = true;
+        else if (f64_lt(p.xmax, x0.v) && f64_lt(p.xmax, x1.v)) skip = true;
+        else if (f64_lt(y0.v, p.ymin) && f64_lt(y1.v, p.ymin)) skip = true;
+        else if (f64_lt(p.ymax, y0.v) && f64_lt(p.ymax, y1.v)) skip = true;
         D3 t0 = dc(0.0), t1 = dc(1.0);
         const D3 dx1 = x1 - x0;
         if (!dclipt(-dx1, x0 - dc(p.xmin), t0, t1)) skip = true;
@@ -287,8 +290,8 @@ __global__ void __launch_bounds__(256, 1) line_backward_kernel(const BwdParams p
         if (!dclipt(dy1, dc(p.ymax) - y0, t0, t1)) skip = true;
         if (skip) continue;
         bool cs = false;
-        if (t1.v < 1) { x1 = x0 + t1 * dx1; y1 = y0 + t1 * dy1; }
-        if (t0.v > 0) { cs = true; x0 = x0 + t0 * dx1; y0 = y0 + t0 * dy1; }
+        if (f64_lt(t1.v, 1.0)) { x1 = x0 + t1 * dx1; y1 = y0 + t1 * dy1; }
+        if (f64_gt0(t0.v)) { cs = true; x0 = x0 + t0 * dx1; y0 = y0 + t0 * dy1; }
         segment_start = segment_start || cs;
         // line.py:723-726 (no snap) in duals
         const D3 sxd = dc(p.sx), txd = dc(p.tx), syd = dc(p.sy), tyd = dc(p.ty), half = dc(0.5);
@@ -299,15 +302,14 @@ __global__ void __launch_bounds__(256, 1) line_backward_kernel(const BwdParams p
             pxm = dc(xmv) * sxd + txd - half;
             pym = D3{ymv, 1.0f, 0.0f, 0.0f} * syd + tyd - half;
         }
-        const long long nx = (long long)rint((p.xmax - p.xmin) * p.sx);
-        const long long ny = (long long)rint((p.ymax - p.ymin) * p.sy);
+        const long long nx = p.aa_nx, ny = p.aa_ny;
         double gv = 0.0, gy0 = 0.0, gy1 = 0.0, gy2 = 0.0;
         segment_backward(p, i, px0, px1, py0, py1, segment_start, segment_end, pxm, pym, nx, ny, field,
                          gv, gy0, gy1, gy2);
         p.grad_v[i] = gv;   // only segment i appends row i's value
-        if (gy0 != 0.0) atomicAdd(&p.grad_y[im], gy0);
-        if (gy1 != 0.0) atomicAdd(&p.grad_y[i], gy1);
-        if (gy2 != 0.0) atomicAdd(&p.grad_y[i + 1], gy2);
+        if (f64_bits(gy0) & F64_MAG) atomicAdd(&p.grad_y[im], gy0);      // gy != 0.0 (NaN included)
+        if (f64_bits(gy1) & F64_MAG) atomicAdd(&p.grad_y[i], gy1);
+        if (f64_bits(gy2) & F64_MAG) atomicAdd(&p.grad_y[i + 1], gy2);
     }
 }
 
@@ -366,6 +368,13 @@ extern "C" int dsgb_line_axis0_backward_ws(const dsgb_column *cols, int32_t ncol
     p.sx = canvas->sx; p.tx = canvas->tx; p.sy = canvas->sy; p.ty = canvas->ty;
     p.xmin = canvas->xmin; p.xmax = canvas->xmax; p.ymin = canvas->ymin; p.ymax = canvas->ymax;
     p.line_width = line_width; p.plot_start = plot_start;
+    const double span_x = (p.xmax - p.xmin) * p.sx, span_y = (p.ymax - p.ymin) * p.sy;
+    if (!(std::fabs(span_x) < 2147483648.0) || !(std::fabs(span_y) < 2147483648.0)) {
+        set_error("dsgb_line_axis0_backward: the canvas spans (xmax - xmin) * sx and (ymax - ymin) * sy must be below 2^31 pixels");
+        return DSGB_E_INVALID;
+    }
+    p.aa_nx = (int64_t)std::rint(span_x);     // Python round: half to even, as rint
+    p.aa_ny = (int64_t)std::rint(span_y);
     p.grad = grad_agg; p.any = agg_any; p.grad_v = grad_v; p.grad_y = grad_y;
     cudaStream_t st = as_stream(stream);
     cudaError_t e = cudaMemsetAsync(grad_y, 0, (size_t)n * 8, st);
