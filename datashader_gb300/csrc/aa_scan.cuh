@@ -1,0 +1,86 @@
+// aa_scan.cuh -- the pixel span of one scanline of the antialiased line's
+// rectangle (line.py:814-821 x_intercept, and the ceil / floor that follow it
+// at line.py:921-926) without a float64 division in the common case.
+//
+// The span ends are ceil(x) and floor(x) of the float64 intercept
+//     x = cx0 + ((y - cy0) / (cy1 - cy0)) * (cx1 - cx0).
+// Only the integers next to x matter.  The intercept is first computed in
+// float32, with a bound B on its distance from the float64 value (first-
+// order error analysis of each float32 rounding, each conversion of an input
+// and the float64 result's own roundings, times a margin of 4); when the
+// float32 value lies farther than B from every integer, the integer on
+// either side of it is the float64 value's too.  Otherwise, or when an input
+// is not finite, the float64 expression is evaluated as the reference does.
+// The float32 work runs on the FMA pipe; the float64 division it replaces
+// takes several passes through the float64 pipe, which bounds the kernels.
+#pragma once
+
+#include "f64cmp.cuh"
+
+#include <cmath>
+
+namespace dsgb {
+
+// x_intercept in float64, the reference's operations in order (compiled
+// without multiply-add contraction).
+F64CMP_FN double aa_x_intercept(double y, double cx0, double cy0, double cx1, double cy1) {
+    if (f64_eq(cy0, cy1)) return cx1;
+    const double frac = (y - cy0) / (cy1 - cy0);
+    return cx0 + frac * (cx1 - cx0);
+}
+
+// The float32 intercept xf for scanline y (an integer below 2^24, exact in
+// float32) and whether it is provably on the same side of every integer as
+// aa_x_intercept (cy0 != cy1 is the caller's case).
+//
+// Error terms (u = 2^-24, R = the exact real value of each quantity):
+//   Nf = y - Y0f:        |Nf - N_R| <= u (|Y0| + |Nf|)
+//   Df = Y1f - Y0f:      |Df - D_R| <= u (|Y0| + |Y1| + |Df|) <= |Df| / 8  (checked)
+//   Xd = X1f - X0f:      |Xd - X_R| <= u (|X0| + |X1| + |Xd|)
+//   Ff = Nf * (1 / Df):  |Ff - F_R| <= (|Nf - N_R| + |F_R| |Df - D_R|) / |Df| + 2 u |Ff|
+//   Pf = Ff * Xd:        |Pf - P_R| <= |Ff - F_R| |Xd| + |F_R| |Xd - X_R| + u |Pf|
+//   xf = X0f + Pf:       |xf - x_R| <= u |X0| + |Pf - P_R| + u |xf|
+// with |F_R| <= |Ff| + 1 under the checked bound on Df.  The float64 value's
+// own error is below 2^-50 of the same magnitudes, inside the margin.
+F64CMP_FN bool aa_x_intercept_f32(unsigned y, double cx0, double cy0, double cx1, double cy1, float &xf) {
+    const float u = 5.9604645e-08f;                       // 2^-24
+    if (y >= (1u << 24)) return false;
+    const float yf = (float)y;
+    const float X0 = (float)cx0, X1 = (float)cx1, Y0 = (float)cy0, Y1 = (float)cy1;
+    const float Nf = yf - Y0, Df = Y1 - Y0, Xd = X1 - X0;
+    const float aX0 = fabsf(X0), aX1 = fabsf(X1), aY0 = fabsf(Y0), aY1 = fabsf(Y1);
+    const float aDf = fabsf(Df), aXd = fabsf(Xd), aNf = fabsf(Nf);
+    const float eD = u * (aY0 + aY1 + aDf);
+    if (!(8.0f * eD <= aDf)) return false;                // also Df == 0, NaN, infinities
+    const float If = 1.0f / Df;
+    const float Ff = Nf * If;
+    const float Pf = Ff * Xd;
+    xf = X0 + Pf;
+    const float aIf = fabsf(If), aFf = fabsf(Ff), Fr = aFf + 1.0f;
+    const float eF = (u * (aY0 + aNf) + Fr * eD) * aIf + 2.0f * u * aFf;
+    const float eP = eF * aXd + Fr * u * (aX0 + aX1 + aXd) + u * fabsf(Pf);
+    const float e = u * aX0 + eP + u * fabsf(xf);
+    const float bound = 4.0f * e + u;
+    const float dist = fminf(xf - floorf(xf), ceilf(xf) - xf);
+    return dist > bound;                                  // false for NaN
+}
+
+// max(0, min(ceil(x), hi)) (CEIL) or max(0, min(floor(x), hi)) of the
+// intercept x, for hi < 2^31 and y < 2^31: integer operations for a
+// horizontal edge, the float32 intercept when it is decisive, the float64
+// expression otherwise.
+template <bool CEIL>
+F64CMP_FN long long aa_scan_bound(unsigned y, double yd, double cx0, double cy0, double cx1, double cy1,
+                                  long long hi) {
+    if (f64_eq(cy0, cy1)) return CEIL ? f64_ceil_clamp(cx1, hi) : f64_floor_clamp(cx1, hi);
+    float xf;
+    if (aa_x_intercept_f32(y, cx0, cy0, cx1, cy1, xf)) {   // |xf| < 2^23 here
+        long long c = (long long)(CEIL ? ceilf(xf) : floorf(xf));
+        c = c < hi ? c : hi;
+        return c > 0 ? c : 0;
+    }
+    const double x = aa_x_intercept(yd, cx0, cy0, cx1, cy1);
+    return CEIL ? f64_ceil_clamp(x, hi) : f64_floor_clamp(x, hi);
+}
+
+}  // namespace dsgb

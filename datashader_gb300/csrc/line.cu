@@ -13,6 +13,7 @@
 // Only the order of the floating-point accumulation differs (atomics).
 #include "dsgb_internal.cuh"
 #include "f64cmp.cuh"
+#include "aa_scan.cuh"
 
 #include <cmath>
 
@@ -143,12 +144,6 @@ __device__ __forceinline__ void liang_barsky(double xmin, double xmax, double ym
     if (f64_gt0(t0)) { cs = true; x0 = x0 + t0 * dx1; y0 = y0 + t0 * dy1; } else cs = false;
 }
 
-// line.py:814-821
-__device__ __forceinline__ double x_intercept(double y, double cx0, double cy0, double cx1, double cy1) {
-    if (f64_eq(cy0, cy1)) return cx1;
-    double frac = (y - cy0) / (cy1 - cy0);
-    return cx0 + frac * (cx1 - cx0);
-}
 __device__ __forceinline__ double sq(double v) { return v * v; }
 // element i (0..3) of four scalars, by selects
 __device__ __forceinline__ double pick4(int i, double a0, double a1, double a2, double a3) {
@@ -239,10 +234,11 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
         const double yd = f64_from_u32((unsigned)y);
         if (ll == lowindex && f64_nonneg_gt(yd, pick4(lu, by0, by1, by2, by3))) { ll = lu; lu = (ll + 1) % 4; }
         if (rl == lowindex && f64_nonneg_gt(yd, pick4(ru, by0, by1, by2, by3))) { rl = ru; ru = (rl + 3) % 4; }
-        const long long xleft = f64_ceil_clamp(x_intercept(yd, pick4(ll, bx0, bx1, bx2, bx3),
-            pick4(ll, by0, by1, by2, by3), pick4(lu, bx0, bx1, bx2, bx3), pick4(lu, by0, by1, by2, by3)), xmaxi);
-        const long long xright = f64_floor_clamp(x_intercept(yd, pick4(rl, bx0, bx1, bx2, bx3),
-            pick4(rl, by0, by1, by2, by3), pick4(ru, bx0, bx1, bx2, bx3), pick4(ru, by0, by1, by2, by3)), xmaxi);
+        // clampi(ceil / floor(x_intercept(...)), 0, max), line.py:921-926 (aa_scan.cuh)
+        const long long xleft = aa_scan_bound<true>((unsigned)y, yd, pick4(ll, bx0, bx1, bx2, bx3),
+            pick4(ll, by0, by1, by2, by3), pick4(lu, bx0, bx1, bx2, bx3), pick4(lu, by0, by1, by2, by3), xmaxi);
+        const long long xright = aa_scan_bound<false>((unsigned)y, yd, pick4(rl, bx0, bx1, bx2, bx3),
+            pick4(rl, by0, by1, by2, by3), pick4(ru, bx0, bx1, bx2, bx3), pick4(ru, by0, by1, by2, by3), xmaxi);
         for (long long x = xleft; x <= xright; ++x) {
             const double xd = f64_from_u32((unsigned)x);         // 0 <= x < 2^31
             const double along = (xd - x0) * alongx + (yd - y0) * alongy;

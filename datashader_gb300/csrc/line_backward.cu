@@ -25,6 +25,7 @@
 #include "dsgb_internal.cuh"
 #include "binning.cuh"
 #include "f64cmp.cuh"
+#include "aa_scan.cuh"
 
 #include <cmath>
 
@@ -79,11 +80,6 @@ __device__ __forceinline__ D3 dclamp01(D3 x) {
 __device__ __forceinline__ D3 dlinearstep(double e0, double den, bool unit_den, D3 x) {
     const D3 d = x - dc(e0);
     return dclamp01(unit_den ? d : d / dc(den));
-}
-__device__ __forceinline__ D3 dx_intercept(double y, D3 cx0, D3 cy0, D3 cx1, D3 cy1) {
-    if (f64_eq(cy0.v, cy1.v)) return cx1;
-    const D3 frac = (dc(y) - cy0) / (cy1 - cy0);
-    return cx0 + frac * (cx1 - cx0);
 }
 // element i (0..3) of four duals, by selects
 __device__ __forceinline__ D3 dpick4(int i, const D3 &a0, const D3 &a1, const D3 &a2, const D3 &a3) {
@@ -200,10 +196,11 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
         const double yd = f64_from_u32((unsigned)y);
         if (ll == lowindex && f64_nonneg_gt(yd, dpick4(lu, by0, by1, by2, by3).v)) { ll = lu; lu = (ll + 1) % 4; }
         if (rl == lowindex && f64_nonneg_gt(yd, dpick4(ru, by0, by1, by2, by3).v)) { rl = ru; ru = (rl + 3) % 4; }
-        const long long xleft = f64_ceil_clamp(dx_intercept(yd, dpick4(ll, bx0, bx1, bx2, bx3),
-            dpick4(ll, by0, by1, by2, by3), dpick4(lu, bx0, bx1, bx2, bx3), dpick4(lu, by0, by1, by2, by3)).v, xmaxi);
-        const long long xright = f64_floor_clamp(dx_intercept(yd, dpick4(rl, bx0, bx1, bx2, bx3),
-            dpick4(rl, by0, by1, by2, by3), dpick4(ru, bx0, bx1, bx2, bx3), dpick4(ru, by0, by1, by2, by3)).v, xmaxi);
+        // the span ends are integers: only the intercept's value matters (aa_scan.cuh)
+        const long long xleft = aa_scan_bound<true>((unsigned)y, yd, dpick4(ll, bx0, bx1, bx2, bx3).v,
+            dpick4(ll, by0, by1, by2, by3).v, dpick4(lu, bx0, bx1, bx2, bx3).v, dpick4(lu, by0, by1, by2, by3).v, xmaxi);
+        const long long xright = aa_scan_bound<false>((unsigned)y, yd, dpick4(rl, bx0, bx1, bx2, bx3).v,
+            dpick4(rl, by0, by1, by2, by3).v, dpick4(ru, bx0, bx1, bx2, bx3).v, dpick4(ru, by0, by1, by2, by3).v, xmaxi);
         for (long long x = xleft; x <= xright; ++x) {
             const D3 xd = dc(f64_from_u32((unsigned)x)), ydd = dc(yd);
             const D3 along = (xd - x0) * alongx + (ydd - y0) * alongy;
