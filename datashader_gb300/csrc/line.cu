@@ -178,26 +178,19 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
     const double rightx = alongy;
     const double righty = -alongx;
     // the four corners (bx[k], by[k]) as scalars: they are picked by a run-time
-    // index per scanline, which an array would leave in local memory
+    // index per scanline, which an array would leave in local memory.  With
+    // rightx = alongy and righty = -alongx the eight products
+    // halfwidth * (+-right +- along) are +-ca and +-cb (round to nearest is
+    // symmetric, so each is the same value; only the sign of a zero may
+    // differ, which the corners' one use, the scan bounds, does not see).
     double bx0, bx1, bx2, bx3, by0, by1, by2, by3;
+    const double ca = halfwidth * (rightx - alongx), cb = halfwidth * (rightx + alongx);
     if (flip_order) {
-        bx0 = x1 - halfwidth * (rightx - alongx);
-        bx1 = x1 - halfwidth * (-rightx - alongx);
-        bx2 = x0 - halfwidth * (-rightx + alongx);
-        bx3 = x0 - halfwidth * (rightx + alongx);
-        by0 = y1 - halfwidth * (righty - alongy);
-        by1 = y1 - halfwidth * (-righty - alongy);
-        by2 = y0 - halfwidth * (-righty + alongy);
-        by3 = y0 - halfwidth * (righty + alongy);
+        bx0 = x1 - ca; bx1 = x1 + cb; bx2 = x0 + ca; bx3 = x0 - cb;
+        by0 = y1 + cb; by1 = y1 + ca; by2 = y0 - cb; by3 = y0 - ca;
     } else {
-        bx0 = x0 + halfwidth * (rightx - alongx);
-        bx1 = x0 + halfwidth * (-rightx - alongx);
-        bx2 = x1 + halfwidth * (-rightx + alongx);
-        bx3 = x1 + halfwidth * (rightx + alongx);
-        by0 = y0 + halfwidth * (righty - alongy);
-        by1 = y0 + halfwidth * (-righty - alongy);
-        by2 = y1 + halfwidth * (-righty + alongy);
-        by3 = y1 + halfwidth * (righty + alongy);
+        bx0 = x0 + ca; bx1 = x0 - cb; bx2 = x1 - ca; bx3 = x1 + cb;
+        by0 = y0 - cb; by1 = y0 - ca; by2 = y1 + cb; by3 = y1 + ca;
     }
     long long xmaxi = nx - 1, ymaxi = ny - 1;
     if (flip_xy) { long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
@@ -223,6 +216,11 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
     const double lw_lo = 0.5 * (line_width - aa);
     const double ls_den = halfwidth - lw_lo;           // linearstep's edge1 - edge0
     const bool unit_den = ls_den == 1.0;               // x / 1.0 == x: the division is skipped
+    // A cap pixel whose squared distance d2 (>= +0 or NaN) is at least
+    // halfwidth^2 rounded up has sqrt(d2) >= halfwidth (the square root and
+    // its rounding are monotone; halfwidth is a float64), so linearstep is 1
+    // and its coverage 0: it appends nothing and the square root is skipped.
+    const unsigned long long cap_far = f64_bits(__dmul_ru(halfwidth, halfwidth));
     // The comparisons, the float64 pixel coordinates and the ceil / floor
     // conversions are integer operations on the bit patterns (f64cmp.cuh),
     // each with the IEEE result for the values that reach it: the float64
@@ -245,12 +243,16 @@ __device__ void full_antialias(const LineParams &p, double line_width, bool over
             bool prev_correction = false;
             double distance;
             if (f64_lt0(along)) {
-                if (overwrite || segment_start || f64_gt0((xd - x0) * prev_alongx + (yd - y0) * prev_alongy))
-                    distance = sqrt(sq(xd - x0) + sq(yd - y0));
-                else continue;
+                if (!(overwrite || segment_start || f64_gt0((xd - x0) * prev_alongx + (yd - y0) * prev_alongy)))
+                    continue;
+                const double d2 = sq(xd - x0) + sq(yd - y0);
+                if (f64_bits(d2) >= cap_far) continue;
+                distance = sqrt(d2);
             } else if (f64_gt_nonneg(along, length)) {
-                if (overwrite || segment_end) distance = sqrt(sq(xd - x1) + sq(yd - y1));
-                else continue;
+                if (!(overwrite || segment_end)) continue;
+                const double d2 = sq(xd - x1) + sq(yd - y1);
+                if (f64_bits(d2) >= cap_far) continue;
+                distance = sqrt(d2);
             } else {
                 distance = fabs((xd - x0) * rightx + (yd - y0) * righty);
                 if (!overwrite && !segment_start) {

@@ -81,10 +81,9 @@ __device__ __forceinline__ D3 dlinearstep(double e0, double den, bool unit_den, 
     const D3 d = x - dc(e0);
     return dclamp01(unit_den ? d : d / dc(den));
 }
-// element i (0..3) of four duals, by selects
-__device__ __forceinline__ D3 dpick4(int i, const D3 &a0, const D3 &a1, const D3 &a2, const D3 &a3) {
-    const D3 &lo = (i & 1) ? a1 : a0;
-    const D3 &hi = (i & 1) ? a3 : a2;
+// element i (0..3) of four scalars, by selects
+__device__ __forceinline__ double pick4_b(int i, double a0, double a1, double a2, double a3) {
+    const double lo = (i & 1) ? a1 : a0, hi = (i & 1) ? a3 : a2;
     return (i & 2) ? hi : lo;
 }
 
@@ -145,28 +144,16 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
     alongx = alongx / length;
     alongy = alongy / length;
     const D3 rightx = alongy, righty = -alongx;
-    const D3 hw = dc(halfwidth);
-    // corners as scalars (picked per scanline by a run-time index: an array
-    // would live in local memory)
-    D3 bx0, bx1, bx2, bx3, by0, by1, by2, by3;
+    // the corners only bound the scan (integers): plain float64 values, as
+    // the forward kernel computes them (+-ca, +-cb shared)
+    double bx0, bx1, bx2, bx3, by0, by1, by2, by3;
+    const double ca = halfwidth * (rightx.v - alongx.v), cb = halfwidth * (rightx.v + alongx.v);
     if (flip_order) {
-        bx0 = x1 - hw * (rightx - alongx);
-        bx1 = x1 - hw * (-rightx - alongx);
-        bx2 = x0 - hw * (-rightx + alongx);
-        bx3 = x0 - hw * (rightx + alongx);
-        by0 = y1 - hw * (righty - alongy);
-        by1 = y1 - hw * (-righty - alongy);
-        by2 = y0 - hw * (-righty + alongy);
-        by3 = y0 - hw * (righty + alongy);
+        bx0 = x1.v - ca; bx1 = x1.v + cb; bx2 = x0.v + ca; bx3 = x0.v - cb;
+        by0 = y1.v + cb; by1 = y1.v + ca; by2 = y0.v - cb; by3 = y0.v - ca;
     } else {
-        bx0 = x0 + hw * (rightx - alongx);
-        bx1 = x0 + hw * (-rightx - alongx);
-        bx2 = x1 + hw * (-rightx + alongx);
-        bx3 = x1 + hw * (rightx + alongx);
-        by0 = y0 + hw * (righty - alongy);
-        by1 = y0 + hw * (-righty - alongy);
-        by2 = y1 + hw * (-righty + alongy);
-        by3 = y1 + hw * (righty + alongy);
+        bx0 = x0.v + ca; bx1 = x0.v - cb; bx2 = x1.v - ca; bx3 = x1.v + cb;
+        by0 = y0.v - cb; by1 = y0.v - ca; by2 = y1.v + cb; by3 = y1.v + ca;
     }
     long long xmaxi = nx - 1, ymaxi = ny - 1;
     if (flip_xy) { long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
@@ -185,34 +172,40 @@ __device__ void segment_backward(const BwdParams &p, int64_t i, D3 x0, D3 x1, D3
             overwrite = true;
         }
     }
-    const long long ystart = f64_ceil_clamp(dpick4(lowindex, by0, by1, by2, by3).v, ymaxi);
-    const long long yend = f64_floor_clamp(dpick4((lowindex + 2) % 4, by0, by1, by2, by3).v, ymaxi);
+    const long long ystart = f64_ceil_clamp(pick4_b(lowindex, by0, by1, by2, by3), ymaxi);
+    const long long yend = f64_floor_clamp(pick4_b((lowindex + 2) % 4, by0, by1, by2, by3), ymaxi);
     int ll = lowindex, lu = (ll + 1) % 4, rl = lowindex, ru = (rl + 3) % 4;
     const double lw_lo = 0.5 * (line_width - aa);
     const double ls_den = halfwidth - lw_lo;
     const bool unit_den = ls_den == 1.0;
+    // cap pixels at distance >= halfwidth append nothing (as in the forward kernel)
+    const unsigned long long cap_far = f64_bits(__dmul_ru(halfwidth, halfwidth));
     float ty0 = 0.0f, ty1 = 0.0f, ty2 = 0.0f;     // the y tangents of this segment, in float32
     for (long long y = ystart; y <= yend; ++y) {
         const double yd = f64_from_u32((unsigned)y);
-        if (ll == lowindex && f64_nonneg_gt(yd, dpick4(lu, by0, by1, by2, by3).v)) { ll = lu; lu = (ll + 1) % 4; }
-        if (rl == lowindex && f64_nonneg_gt(yd, dpick4(ru, by0, by1, by2, by3).v)) { rl = ru; ru = (rl + 3) % 4; }
+        if (ll == lowindex && f64_nonneg_gt(yd, pick4_b(lu, by0, by1, by2, by3))) { ll = lu; lu = (ll + 1) % 4; }
+        if (rl == lowindex && f64_nonneg_gt(yd, pick4_b(ru, by0, by1, by2, by3))) { rl = ru; ru = (rl + 3) % 4; }
         // the span ends are integers: only the intercept's value matters (aa_scan.cuh)
-        const long long xleft = aa_scan_bound<true>((unsigned)y, yd, dpick4(ll, bx0, bx1, bx2, bx3).v,
-            dpick4(ll, by0, by1, by2, by3).v, dpick4(lu, bx0, bx1, bx2, bx3).v, dpick4(lu, by0, by1, by2, by3).v, xmaxi);
-        const long long xright = aa_scan_bound<false>((unsigned)y, yd, dpick4(rl, bx0, bx1, bx2, bx3).v,
-            dpick4(rl, by0, by1, by2, by3).v, dpick4(ru, bx0, bx1, bx2, bx3).v, dpick4(ru, by0, by1, by2, by3).v, xmaxi);
+        const long long xleft = aa_scan_bound<true>((unsigned)y, yd, pick4_b(ll, bx0, bx1, bx2, bx3),
+            pick4_b(ll, by0, by1, by2, by3), pick4_b(lu, bx0, bx1, bx2, bx3), pick4_b(lu, by0, by1, by2, by3), xmaxi);
+        const long long xright = aa_scan_bound<false>((unsigned)y, yd, pick4_b(rl, bx0, bx1, bx2, bx3),
+            pick4_b(rl, by0, by1, by2, by3), pick4_b(ru, bx0, bx1, bx2, bx3), pick4_b(ru, by0, by1, by2, by3), xmaxi);
         for (long long x = xleft; x <= xright; ++x) {
             const D3 xd = dc(f64_from_u32((unsigned)x)), ydd = dc(yd);
             const D3 along = (xd - x0) * alongx + (ydd - y0) * alongy;
             bool prev_correction = false;
             D3 distance;
             if (f64_lt0(along.v)) {
-                if (overwrite || segment_start || f64_gt0(((xd - x0) * prev_alongx + (ydd - y0) * prev_alongy).v))
-                    distance = dsqrt(dsq(xd - x0) + dsq(ydd - y0));
-                else continue;
+                if (!(overwrite || segment_start || f64_gt0(((xd - x0) * prev_alongx + (ydd - y0) * prev_alongy).v)))
+                    continue;
+                const D3 d2 = dsq(xd - x0) + dsq(ydd - y0);
+                if (f64_bits(d2.v) >= cap_far) continue;
+                distance = dsqrt(d2);
             } else if (f64_gt_nonneg(along.v, length.v)) {
-                if (overwrite || segment_end) distance = dsqrt(dsq(xd - x1) + dsq(ydd - y1));
-                else continue;
+                if (!(overwrite || segment_end)) continue;
+                const D3 d2 = dsq(xd - x1) + dsq(ydd - y1);
+                if (f64_bits(d2.v) >= cap_far) continue;
+                distance = dsqrt(d2);
             } else {
                 distance = dabs((xd - x0) * rightx + (ydd - y0) * righty);
                 if (!overwrite && !segment_start) {
