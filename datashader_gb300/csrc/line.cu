@@ -382,13 +382,16 @@ constexpr int LINE_ORDER_TILE = 4096;
 
 static size_t line_ws_align(size_t v) { return (v + 255) / 256 * 256; }
 
+// The estimate only orders the segments (any deterministic one draws the
+// same pixels): float32 after the two float64 differences, off the float64
+// pipe that bounds the drawing kernels.
 __device__ __forceinline__ int line_work_bucket(const LineWorkArgs &p, int64_t i) {
     const double x0 = load_f64(p.X, i), y0 = load_f64(p.Y, i), x1 = load_f64(p.X, i + 1), y1 = load_f64(p.Y, i + 1);
     if (isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1)) return 0;
-    const double pad = p.line_width + 2.0;
-    const double w = (fabs((x1 - x0) * p.sx) + pad) * (fabs((y1 - y0) * p.sy) + pad);
-    if (!(w < 2.0 * (LINE_WORK_BUCKETS - 1))) return LINE_WORK_BUCKETS - 1;
-    return (int)(w * 0.5);
+    const float pad = (float)p.line_width + 2.0f;
+    const float w = (fabsf((float)(x1 - x0) * (float)p.sx) + pad) * (fabsf((float)(y1 - y0) * (float)p.sy) + pad);
+    if (!(w < 2.0f * (LINE_WORK_BUCKETS - 1))) return LINE_WORK_BUCKETS - 1;
+    return (int)(w * 0.5f);
 }
 
 __global__ void __launch_bounds__(256) line_work_hist(const LineWorkArgs p, unsigned *hist) {
@@ -408,17 +411,22 @@ __global__ void line_work_scan(const unsigned *hist, unsigned *cursor) {
 
 __global__ void __launch_bounds__(256) line_work_order(const LineWorkArgs p, unsigned *cursor, unsigned *order) {
     __shared__ unsigned h[LINE_WORK_BUCKETS];
+    __shared__ unsigned char bk[LINE_ORDER_TILE];      // each segment's bucket, computed once
     if (threadIdx.x < LINE_WORK_BUCKETS) h[threadIdx.x] = 0;
     __syncthreads();
     const int64_t s0 = (int64_t)blockIdx.x * LINE_ORDER_TILE;
     const int64_t s1 = s0 + LINE_ORDER_TILE < p.n - 1 ? s0 + LINE_ORDER_TILE : p.n - 1;
-    for (int64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) atomicAdd(&h[line_work_bucket(p, i)], 1u);
+    for (int64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+        const int b = line_work_bucket(p, i);
+        bk[i - s0] = (unsigned char)b;
+        atomicAdd(&h[b], 1u);
+    }
     __syncthreads();
     if (threadIdx.x < LINE_WORK_BUCKETS && h[threadIdx.x])
         h[threadIdx.x] = atomicAdd(&cursor[threadIdx.x], h[threadIdx.x]);
     __syncthreads();
     for (int64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x)
-        order[atomicAdd(&h[line_work_bucket(p, i)], 1u)] = (unsigned)i;
+        order[atomicAdd(&h[bk[i - s0]], 1u)] = (unsigned)i;
 }
 
 size_t line_work_order_bytes(int64_t n) {
