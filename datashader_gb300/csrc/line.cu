@@ -464,6 +464,307 @@ __global__ void __launch_bounds__(256, 1) line_axis0_ordered_kernel(const LinePa
     }
 }
 
+// ---- antialiased LineAxis0, pixels queued by case.  In the kernels above a
+// warp's 32 segments scan their pixels together, and each pixel takes one of
+// three float64 paths (before the segment, after it, beside it) or none, so
+// the float64 pipe issues every path for the whole warp with half the lanes
+// idle.  Here each lane scans its segment's pixels and classifies them in
+// float32 with an error bound; the pixels go to per-warp queues in shared
+// memory by case (cap, side, or exact when the bound does not decide), and
+// the warp works off each queue 32 pixels at a time, every lane on the same
+// float64 path.  Same arithmetic as full_antialias on the same values.
+constexpr int AAQ_CAP = 64;                // per queue and warp: < 32 queued + 32 added in one round
+
+struct AASeg {                             // a segment in the flipped frame (line.py:840-906)
+    double x0, y0, x1, y1;
+    double ax, ay, len;                    // alongx, alongy, length
+    double pax, pay, plen;                 // prev_alongx, prev_alongy, prev_length
+    long long row;
+    unsigned flags;                        // AAF_*
+};
+constexpr unsigned AAF_OVERWRITE = 1u, AAF_START = 2u, AAF_END = 4u, AAF_FLIP = 8u, AAF_PREV = 16u;
+
+struct AAConsts {                          // uniform per launch
+    double halfwidth, lw_lo, ls_den, scale;
+    bool unit_den;
+    unsigned long long cap_far;
+};
+
+__device__ __forceinline__ AAConsts aa_consts(double line_width) {
+    AAConsts c;
+    c.scale = 1.0;
+    if (line_width < 1.0) { c.scale *= line_width; line_width = 1.0; }
+    c.halfwidth = 0.5 * (line_width + 1.0);
+    c.lw_lo = 0.5 * (line_width - 1.0);
+    c.ls_den = c.halfwidth - c.lw_lo;
+    c.unit_den = c.ls_den == 1.0;
+    c.cap_far = f64_bits(__dmul_ru(c.halfwidth, c.halfwidth));
+    return c;
+}
+
+// 1 - linearstep(lw_lo, halfwidth, d), times scale
+__device__ __forceinline__ double aa_ramp(const AAConsts &c, double d) {
+    return f64_one_minus_clamp01(c.unit_den ? d - c.lw_lo : (d - c.lw_lo) / c.ls_den) * c.scale;
+}
+
+// The pixel of full_antialias's inner loop, all cases (the exact queue):
+// value and prev_value (value 0: nothing appended).
+static __device__ __noinline__ double2 aa_pixel_exact(const AAConsts c, const AASeg &S, long long x, long long y) {
+    const double xd = f64_from_u32((unsigned)x), yd = f64_from_u32((unsigned)y);
+    const bool overwrite = S.flags & AAF_OVERWRITE, start = S.flags & AAF_START, end = S.flags & AAF_END;
+    const double along = (xd - S.x0) * S.ax + (yd - S.y0) * S.ay;
+    bool prev_correction = false;
+    double distance;
+    if (f64_lt0(along)) {
+        if (!(overwrite || start || f64_gt0((xd - S.x0) * S.pax + (yd - S.y0) * S.pay))) return make_double2(0.0, 0.0);
+        const double d2 = sq(xd - S.x0) + sq(yd - S.y0);
+        if (f64_bits(d2) >= c.cap_far) return make_double2(0.0, 0.0);
+        distance = sqrt(d2);
+    } else if (f64_gt_nonneg(along, S.len)) {
+        if (!(overwrite || end)) return make_double2(0.0, 0.0);
+        const double d2 = sq(xd - S.x1) + sq(yd - S.y1);
+        if (f64_bits(d2) >= c.cap_far) return make_double2(0.0, 0.0);
+        distance = sqrt(d2);
+    } else {
+        distance = fabs((xd - S.x0) * S.ay + (yd - S.y0) * -S.ax);
+        if (S.flags & AAF_PREV) {
+            const double pd = (xd - S.x0) * S.pax + (yd - S.y0) * S.pay;
+            if (f64_in_neg_range(pd, S.plen) && f64_abs_le((xd - S.x0) * S.pay + (yd - S.y0) * -S.pax, c.halfwidth))
+                prev_correction = true;
+        }
+    }
+    double value = aa_ramp(c, distance);
+    double prev_value = 0.0;
+    if (prev_correction) {
+        prev_value = aa_ramp(c, fabs((xd - S.x0) * S.pay + (yd - S.y0) * -S.pax));
+        if (f64_le_nonneg(value, prev_value)) value = 0.0;
+    }
+    return make_double2(value, prev_value);
+}
+
+// A cap pixel (classified before or after the segment, with the cap drawn).
+__device__ __forceinline__ double2 aa_pixel_cap(const AAConsts &c, const AASeg &S, long long x, long long y,
+                                                bool before) {
+    const double xd = f64_from_u32((unsigned)x), yd = f64_from_u32((unsigned)y);
+    const double d2 = before ? sq(xd - S.x0) + sq(yd - S.y0) : sq(xd - S.x1) + sq(yd - S.y1);
+    if (f64_bits(d2) >= c.cap_far) return make_double2(0.0, 0.0);
+    return make_double2(aa_ramp(c, sqrt(d2)), 0.0);
+}
+
+// A pixel beside the segment (0 <= along <= length).
+__device__ __forceinline__ double2 aa_pixel_side(const AAConsts &c, const AASeg &S, long long x, long long y) {
+    const double xd = f64_from_u32((unsigned)x), yd = f64_from_u32((unsigned)y);
+    double value = aa_ramp(c, fabs((xd - S.x0) * S.ay + (yd - S.y0) * -S.ax));
+    double prev_value = 0.0;
+    if (S.flags & AAF_PREV) {
+        const double pd = (xd - S.x0) * S.pax + (yd - S.y0) * S.pay;
+        const double q = (xd - S.x0) * S.pay + (yd - S.y0) * -S.pax;
+        if (f64_in_neg_range(pd, S.plen) && f64_abs_le(q, c.halfwidth)) {
+            prev_value = aa_ramp(c, fabs(q));
+            if (f64_le_nonneg(value, prev_value)) value = 0.0;
+        }
+    }
+    return make_double2(value, prev_value);
+}
+
+// One queue item of kind `which` (0 cap, 1 side, 2 exact), appended when its
+// value is positive: the queue drains share this one append site.
+__device__ __forceinline__ void aa_item_work(const LineParams &p, const AAConsts &c, const AASeg *segs, int which,
+                                             unsigned long long it) {
+    const AASeg &S = segs[(it >> 48) & 31u];
+    const long long x = (long long)(it & 0xFFFFFFu), y = (long long)((it >> 24) & 0xFFFFFFu);
+    double2 v;
+    if (which == 0) v = aa_pixel_cap(c, S, x, y, (it >> 53) & 1u);
+    else if (which == 1) v = aa_pixel_side(c, S, x, y);
+    else v = aa_pixel_exact(c, S, x, y);
+    if (f64_gt0(v.x)) {
+        const bool flip = S.flags & AAF_FLIP;
+        line_append<false>(p, S.row, flip ? y : x, flip ? x : y, v.x, v.y);
+    }
+}
+
+// Queue items: x (24 bits), y (24 bits), the warp lane of the segment (5
+// bits), before / after for caps (1 bit).
+__device__ __forceinline__ unsigned long long aa_item(long long x, long long y, int lane, bool before) {
+    return (unsigned long long)x | ((unsigned long long)y << 24) | ((unsigned long long)lane << 48) |
+           ((unsigned long long)before << 53);
+}
+
+enum { AAK_NONE = 0, AAK_CAP = 1, AAK_SIDE = 2, AAK_EXACT = 3 };
+
+__global__ void __launch_bounds__(256, 1) line_axis0_queued_kernel(const LineParams p, const unsigned *order) {
+    __shared__ AASeg seg_s[8][32];
+    __shared__ unsigned long long q_s[8][3][AAQ_CAP];
+    const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    AASeg *segs = seg_s[warp];
+    unsigned long long *qcap = q_s[warp][0], *qside = q_s[warp][1], *qexact = q_s[warp][2];
+    const AAConsts c = aa_consts(p.line_width);
+    const float u = 5.9604645e-08f;            // 2^-24
+    const int64_t nseg = p.n - 1;
+    const int64_t nbatches = (nseg + 31) / 32;
+    const int64_t warps_total = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; b < nbatches; b += warps_total) {
+        const int64_t k = b * 32 + lane;
+        // ---- set-up: draw_segment (line.py:1033-1097) and full_antialias up to the scan
+        bool active = false;
+        AASeg S;
+        long long cy = 0, cyend = -1, cx = 1, cxr = 0, xmaxi = 0;
+        int ll = 0, lu = 1, rl = 0, ru = 3, lowindex = 0;
+        double bx0 = 0, bx1 = 0, bx2 = 0, bx3 = 0, by0 = 0, by1 = 0, by2 = 0, by3 = 0;
+        float fx0 = 0.f, fy0 = 0.f, fax = 0.f, fay = 0.f, flen = 0.f, fpax = 0.f, fpay = 0.f;
+        if (k < nseg) {
+            const int64_t i = order[k];
+            double x0 = load_f64(X, i), y0 = load_f64(Y, i);
+            double x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
+            const int64_t im = i > 0 ? i - 1 : p.n - 1;
+            bool segment_start = (i == 0) ? (p.plot_start != 0)
+                                          : (isnull(load_f64(X, im)) || isnull(load_f64(Y, im)));
+            const bool segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
+            double xm = 0.0, ym = 0.0;
+            if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, im); ym = load_f64(Y, im); }
+            bool skip = isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1);
+            bool cs = false, ce = false;
+            liang_barsky(p.xmin, p.xmax, p.ymin, p.ymax, x0, x1, y0, y1, skip, cs, ce);
+            segment_start = segment_start || cs;
+            double px0 = x0 * p.sx + p.tx - 0.5, py0 = y0 * p.sy + p.ty - 0.5;
+            double px1 = x1 * p.sx + p.tx - 0.5, py1 = y1 * p.sy + p.ty - 0.5;
+            double pxm = 0.0, pym = 0.0;
+            if (!segment_start) { pxm = xm * p.sx + p.tx - 0.5; pym = ym * p.sy + p.ty - 0.5; }
+            if (!skip && !(f64_eq(px0, px1) && f64_eq(py0, py1))) {
+                bool overwrite = p.overwrite != 0;
+                const bool flip_xy = f64_abs_lt(px0 - px1, py0 - py1);
+                if (flip_xy) {
+                    double t;
+                    t = px0; px0 = py0; py0 = t;
+                    t = px1; px1 = py1; py1 = t;
+                    t = pxm; pxm = pym; pym = t;
+                }
+                const bool flip_order = f64_lt(py1, py0) || (f64_eq(py1, py0) && f64_lt(px1, px0));
+                double alongx = px1 - px0, alongy = py1 - py0;
+                const double length = sqrt(sq(alongx) + sq(alongy));
+                alongx /= length;
+                alongy /= length;
+                const double ca = c.halfwidth * (alongy - alongx), cb = c.halfwidth * (alongy + alongx);
+                if (flip_order) {
+                    bx0 = px1 - ca; bx1 = px1 + cb; bx2 = px0 + ca; bx3 = px0 - cb;
+                    by0 = py1 + cb; by1 = py1 + ca; by2 = py0 - cb; by3 = py0 - ca;
+                } else {
+                    bx0 = px0 + ca; bx1 = px0 - cb; bx2 = px1 - ca; bx3 = px1 + cb;
+                    by0 = py0 - cb; by1 = py0 - ca; by2 = py1 + cb; by3 = py1 + ca;
+                }
+                xmaxi = p.aa_nx - 1;
+                long long ymaxi = p.aa_ny - 1;
+                if (flip_xy) { const long long t = xmaxi; xmaxi = ymaxi; ymaxi = t; }
+                lowindex = flip_order ? (f64_lt(px1, px0) ? 0 : 1) : (f64_lt(px0, px1) ? 0 : 1);
+                double pax = 0.0, pay = 0.0, plen = 0.0;
+                if (!overwrite && !segment_start) {
+                    pax = px0 - pxm;
+                    pay = py0 - pym;
+                    plen = sqrt(sq(pax) + sq(pay));
+                    if (f64_gt0(plen)) {
+                        pax /= plen;
+                        pay /= plen;
+                    } else {
+                        overwrite = true;
+                    }
+                }
+                S.x0 = px0; S.y0 = py0; S.x1 = px1; S.y1 = py1;
+                S.ax = alongx; S.ay = alongy; S.len = length;
+                S.pax = pax; S.pay = pay; S.plen = plen;
+                S.row = i;
+                S.flags = (overwrite ? AAF_OVERWRITE : 0u) | (segment_start ? AAF_START : 0u) |
+                          (segment_end ? AAF_END : 0u) | (flip_xy ? AAF_FLIP : 0u) |
+                          (!overwrite && !segment_start ? AAF_PREV : 0u);
+                cy = f64_ceil_clamp(pick4(lowindex, by0, by1, by2, by3), ymaxi) - 1;
+                cyend = f64_floor_clamp(pick4((lowindex + 2) % 4, by0, by1, by2, by3), ymaxi);
+                ll = lowindex; lu = (ll + 1) % 4; rl = lowindex; ru = (rl + 3) % 4;
+                fx0 = (float)px0; fy0 = (float)py0; fax = (float)alongx; fay = (float)alongy; flen = (float)length;
+                fpax = (float)pax; fpay = (float)pay;
+                active = true;
+                segs[lane] = S;
+            }
+        }
+        __syncwarp();
+        const bool cap_before = active && (S.flags & (AAF_OVERWRITE | AAF_START));
+        const bool cap_after = active && (S.flags & (AAF_OVERWRITE | AAF_END));
+        int ncap = 0, nside = 0, nexact = 0;          // warp-uniform queue lengths
+        while (__any_sync(0xffffffffu, active)) {
+            // ---- one pixel per lane: the next of its scan (line.py:908-981 loop order)
+            int kind = AAK_NONE;
+            long long px = 0, py = 0;
+            bool before = false;
+            while (active) {
+                if (cx <= cxr) { px = cx; py = cy; ++cx; kind = AAK_EXACT; break; }
+                if (++cy > cyend) { active = false; break; }
+                const double yd = f64_from_u32((unsigned)cy);
+                if (ll == lowindex && f64_nonneg_gt(yd, pick4(lu, by0, by1, by2, by3))) { ll = lu; lu = (ll + 1) % 4; }
+                if (rl == lowindex && f64_nonneg_gt(yd, pick4(ru, by0, by1, by2, by3))) { rl = ru; ru = (rl + 3) % 4; }
+                cx = aa_scan_bound<true>((unsigned)cy, yd, pick4(ll, bx0, bx1, bx2, bx3), pick4(ll, by0, by1, by2, by3),
+                                         pick4(lu, bx0, bx1, bx2, bx3), pick4(lu, by0, by1, by2, by3), xmaxi);
+                cxr = aa_scan_bound<false>((unsigned)cy, yd, pick4(rl, bx0, bx1, bx2, bx3), pick4(rl, by0, by1, by2, by3),
+                                           pick4(ru, bx0, bx1, bx2, bx3), pick4(ru, by0, by1, by2, by3), xmaxi);
+            }
+            if (kind != AAK_NONE) {
+                // float32 classification: along = dx*ax + dy*ay against 0 and length, and
+                // the previous direction's dot for a start cap.  Each test is decided
+                // only when the float32 value is farther from the threshold than four
+                // times its first-order error bound (the float32 roundings of the inputs,
+                // the difference, the products and the sum; the float64 value's own
+                // error is far below); otherwise the pixel goes to the exact queue.
+                const float xf = (float)px, yf = (float)py;   // < 2^24: exact
+                const float dxf = __fsub_rn(xf, fx0), dyf = __fsub_rn(yf, fy0);
+                const float mx = fabsf(fx0) + 3.0f * fabsf(dxf), my = fabsf(fy0) + 3.0f * fabsf(dyf);
+                const float af = __fadd_rn(__fmul_rn(dxf, fax), __fmul_rn(dyf, fay));
+                const float ba = 4.0f * u * (mx * fabsf(fax) + my * fabsf(fay) + fabsf(af)) + 1e-30f;
+                if (af < -ba) {
+                    if (cap_before) {
+                        kind = AAK_CAP; before = true;
+                    } else {
+                        const float pf = __fadd_rn(__fmul_rn(dxf, fpax), __fmul_rn(dyf, fpay));
+                        const float bp = 4.0f * u * (mx * fabsf(fpax) + my * fabsf(fpay) + fabsf(pf)) + 1e-30f;
+                        if (pf > bp) { kind = AAK_CAP; before = true; }
+                        else if (pf < -bp) kind = AAK_NONE;
+                    }
+                } else if (af > ba) {
+                    const float dl = __fsub_rn(af, flen);
+                    const float bl = ba + 4.0f * u * (flen + fabsf(dl));
+                    if (dl > bl) kind = cap_after ? AAK_CAP : AAK_NONE;
+                    else if (dl < -bl) kind = AAK_SIDE;
+                }
+            }
+            // ---- append to the queues (lane order within a round)
+            const unsigned long long item = aa_item(px, py, lane, before);
+            unsigned m = __ballot_sync(0xffffffffu, kind == AAK_CAP);
+            if (kind == AAK_CAP) qcap[ncap + __popc(m & lt_mask)] = item;
+            ncap += __popc(m);
+            m = __ballot_sync(0xffffffffu, kind == AAK_SIDE);
+            if (kind == AAK_SIDE) qside[nside + __popc(m & lt_mask)] = item;
+            nside += __popc(m);
+            m = __ballot_sync(0xffffffffu, kind == AAK_EXACT);
+            if (kind == AAK_EXACT) qexact[nexact + __popc(m & lt_mask)] = item;
+            nexact += __popc(m);
+            __syncwarp();
+            // ---- work off full rounds of 32, every lane on the same path (one
+            // round a pass; after the last pixels, the partial rounds too)
+            const bool last = !__any_sync(0xffffffffu, active);
+            while (true) {
+                int which, cnt;
+                if (ncap >= 32 || (last && ncap > 0)) { which = 0; cnt = ncap; }
+                else if (nside >= 32 || (last && nside > 0)) { which = 1; cnt = nside; }
+                else if (nexact >= 32 || (last && nexact > 0)) { which = 2; cnt = nexact; }
+                else break;
+                const int take = cnt < 32 ? cnt : 32;
+                const int from = cnt - take;
+                if (which == 0) ncap = from; else if (which == 1) nside = from; else nexact = from;
+                if (lane < take) aa_item_work(p, c, segs, which, q_s[warp][which][from + lane]);
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // Multi-line layouts over float64 vertex arrays.
 //   LAYOUT 1, LineAxis0Multi (line.py:1152-1242): xs, ys [nrows][nlines];
 //       line j runs down the rows; segment (i, j) appends row i; the
@@ -711,7 +1012,9 @@ static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, in
             a.sx = p.sx; a.sy = p.sy; a.line_width = line_width;
             order = build_line_work_order(a, workspace, ws_bytes, st);
         }
-        if (order) {
+        if (order && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24)) {
+            line_axis0_queued_kernel<<<(unsigned)((int64_t)sms * 2), 256, 0, st>>>(p, order);
+        } else if (order) {
             line_axis0_ordered_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, order);
         } else {
             line_axis0_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
