@@ -1,6 +1,7 @@
 // aa_scan.cuh -- the pixel span of one scanline of the antialiased line's
 // rectangle (line.py:814-821 x_intercept, and the ceil / floor that follow it
-// at line.py:921-926) without a float64 division in the common case.
+// at line.py:921-926) without a float64 division in the common case, and
+// the case of each scanned pixel decided in float32 where that is exact.
 //
 // The span ends are ceil(x) and floor(x) of the float64 intercept
 //     x = cx0 + ((y - cy0) / (cy1 - cy0)) * (cx1 - cx0).
@@ -81,6 +82,48 @@ F64CMP_FN long long aa_scan_bound(unsigned y, double yd, double cx0, double cy0,
     }
     const double x = aa_x_intercept(yd, cx0, cy0, cx1, cy1);
     return CEIL ? f64_ceil_clamp(x, hi) : f64_floor_clamp(x, hi);
+}
+
+// ---- the case of a scanned pixel, decided in float32 (the queued line
+// kernel).  along = (x - x0) * ax + (y - y0) * ay against 0 and the length,
+// and for a start cap the previous direction's dot (x - x0) * pax +
+// (y - y0) * pay against 0 (line.py:930-950).  Each test is decided only
+// when the float32 value is farther from its threshold than four times its
+// first-order error bound: u = 2^-24 for each of the conversions of x0, y0,
+// the direction and the length, the differences, the products and the sum
+// (|x0| + 3 |dx|) |ax| + (|y0| + 3 |dy|) |ay| + |along|; the float64 value's
+// own roundings are 2^-29 of that.  Otherwise the answer is AAC_EXACT and
+// the float64 tests decide.
+struct AAClassF {                          // float32 images of the segment's float64 values
+    float x0, y0, ax, ay, len, pax, pay;
+};
+
+enum { AAC_NONE = 0, AAC_CAP_BEFORE = 1, AAC_CAP_AFTER = 2, AAC_SIDE = 3, AAC_EXACT = 4 };
+
+// x, y below 2^24 (exact in float32).  cap_before: the start cap is drawn
+// whatever the previous direction (overwrite or a segment start); cap_after:
+// the end cap is drawn (overwrite or a segment end).
+F64CMP_FN int aa_classify(unsigned x, unsigned y, const AAClassF &k, bool cap_before, bool cap_after) {
+    const float u = 5.9604645e-08f;                       // 2^-24
+    const float dx = (float)x - k.x0, dy = (float)y - k.y0;
+    const float mx = fabsf(k.x0) + 3.0f * fabsf(dx), my = fabsf(k.y0) + 3.0f * fabsf(dy);
+    const float along = dx * k.ax + dy * k.ay;
+    const float ba = 4.0f * u * (mx * fabsf(k.ax) + my * fabsf(k.ay) + fabsf(along)) + 1e-30f;
+    if (along < -ba) {
+        if (cap_before) return AAC_CAP_BEFORE;
+        const float pd = dx * k.pax + dy * k.pay;
+        const float bp = 4.0f * u * (mx * fabsf(k.pax) + my * fabsf(k.pay) + fabsf(pd)) + 1e-30f;
+        if (pd > bp) return AAC_CAP_BEFORE;
+        if (pd < -bp) return AAC_NONE;
+        return AAC_EXACT;
+    }
+    if (along > ba) {
+        const float dl = along - k.len;
+        const float bl = ba + 4.0f * u * (k.len + fabsf(dl));
+        if (dl > bl) return cap_after ? AAC_CAP_AFTER : AAC_NONE;
+        if (dl < -bl) return AAC_SIDE;
+    }
+    return AAC_EXACT;                                     // also NaN and infinite values
 }
 
 }  // namespace dsgb

@@ -601,7 +601,6 @@ __global__ void __launch_bounds__(256, 1) line_axis0_queued_kernel(const LinePar
     AASeg *segs = seg_s[warp];
     unsigned long long *qcap = q_s[warp][0], *qside = q_s[warp][1], *qexact = q_s[warp][2];
     const AAConsts c = aa_consts(p.line_width);
-    const float u = 5.9604645e-08f;            // 2^-24
     const int64_t nseg = p.n - 1;
     const int64_t nbatches = (nseg + 31) / 32;
     const int64_t warps_total = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -613,7 +612,7 @@ __global__ void __launch_bounds__(256, 1) line_axis0_queued_kernel(const LinePar
         long long cy = 0, cyend = -1, cx = 1, cxr = 0, xmaxi = 0;
         int ll = 0, lu = 1, rl = 0, ru = 3, lowindex = 0;
         double bx0 = 0, bx1 = 0, bx2 = 0, bx3 = 0, by0 = 0, by1 = 0, by2 = 0, by3 = 0;
-        float fx0 = 0.f, fy0 = 0.f, fax = 0.f, fay = 0.f, flen = 0.f, fpax = 0.f, fpay = 0.f;
+        AAClassF kf = AAClassF{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (k < nseg) {
             const int64_t i = order[k];
             double x0 = load_f64(X, i), y0 = load_f64(Y, i);
@@ -680,8 +679,7 @@ __global__ void __launch_bounds__(256, 1) line_axis0_queued_kernel(const LinePar
                 cy = f64_ceil_clamp(pick4(lowindex, by0, by1, by2, by3), ymaxi) - 1;
                 cyend = f64_floor_clamp(pick4((lowindex + 2) % 4, by0, by1, by2, by3), ymaxi);
                 ll = lowindex; lu = (ll + 1) % 4; rl = lowindex; ru = (rl + 3) % 4;
-                fx0 = (float)px0; fy0 = (float)py0; fax = (float)alongx; fay = (float)alongy; flen = (float)length;
-                fpax = (float)pax; fpay = (float)pay;
+                kf = AAClassF{(float)px0, (float)py0, (float)alongx, (float)alongy, (float)length, (float)pax, (float)pay};
                 active = true;
                 segs[lane] = S;
             }
@@ -707,31 +705,12 @@ __global__ void __launch_bounds__(256, 1) line_axis0_queued_kernel(const LinePar
                                            pick4(ru, bx0, bx1, bx2, bx3), pick4(ru, by0, by1, by2, by3), xmaxi);
             }
             if (kind != AAK_NONE) {
-                // float32 classification: along = dx*ax + dy*ay against 0 and length, and
-                // the previous direction's dot for a start cap.  Each test is decided
-                // only when the float32 value is farther from the threshold than four
-                // times its first-order error bound (the float32 roundings of the inputs,
-                // the difference, the products and the sum; the float64 value's own
-                // error is far below); otherwise the pixel goes to the exact queue.
-                const float xf = (float)px, yf = (float)py;   // < 2^24: exact
-                const float dxf = __fsub_rn(xf, fx0), dyf = __fsub_rn(yf, fy0);
-                const float mx = fabsf(fx0) + 3.0f * fabsf(dxf), my = fabsf(fy0) + 3.0f * fabsf(dyf);
-                const float af = __fadd_rn(__fmul_rn(dxf, fax), __fmul_rn(dyf, fay));
-                const float ba = 4.0f * u * (mx * fabsf(fax) + my * fabsf(fay) + fabsf(af)) + 1e-30f;
-                if (af < -ba) {
-                    if (cap_before) {
-                        kind = AAK_CAP; before = true;
-                    } else {
-                        const float pf = __fadd_rn(__fmul_rn(dxf, fpax), __fmul_rn(dyf, fpay));
-                        const float bp = 4.0f * u * (mx * fabsf(fpax) + my * fabsf(fpay) + fabsf(pf)) + 1e-30f;
-                        if (pf > bp) { kind = AAK_CAP; before = true; }
-                        else if (pf < -bp) kind = AAK_NONE;
-                    }
-                } else if (af > ba) {
-                    const float dl = __fsub_rn(af, flen);
-                    const float bl = ba + 4.0f * u * (flen + fabsf(dl));
-                    if (dl > bl) kind = cap_after ? AAK_CAP : AAK_NONE;
-                    else if (dl < -bl) kind = AAK_SIDE;
+                switch (aa_classify((unsigned)px, (unsigned)py, kf, cap_before, cap_after)) {
+                case AAC_NONE: kind = AAK_NONE; break;
+                case AAC_CAP_BEFORE: kind = AAK_CAP; before = true; break;
+                case AAC_CAP_AFTER: kind = AAK_CAP; break;
+                case AAC_SIDE: kind = AAK_SIDE; break;
+                default: kind = AAK_EXACT; break;
                 }
             }
             // ---- append to the queues (lane order within a round)

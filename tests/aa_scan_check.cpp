@@ -4,7 +4,10 @@
 // intercept is placed within 1e-15 ... 1e-3 of an integer, near-horizontal
 // and near-vertical edges and large coordinates.  Prints "ok" with the share
 // of calls that fell back to float64, or the first mismatch, and exits 1 on
-// a mismatch.  Compiled with g++ -ffp-contract=off by tests/test_f64cmp.py.
+// a mismatch.  Then the float32 pixel classification against the float64
+// tests over random and axis-aligned segments (along exactly 0 on integer
+// endpoints), every pixel of their bounding boxes.  Compiled with g++
+// -ffp-contract=off by tests/test_f64cmp.py.
 #define __host__
 #define __device__
 #define __forceinline__ inline
@@ -78,6 +81,50 @@ int main() {
         if (check(y, cx0, cy0, cx1, cy1, 2147483647ll)) return 1;
         if (check(y, std::floor(cx0), (double)y, std::floor(cx0) + 2.0, (double)y + 1.0, 2147483647ll)) return 1;
     }
-    std::printf("ok %lld calls, %.4f float32-decided\n", n_calls, (double)n_fast / (double)n_calls);
+    // the pixel classification: every decided case equals the float64 tests' case
+    long long n_pix = 0, n_dec = 0;
+    for (int i = 0; i < 300000; ++i) {
+        const bool axis = i % 7 == 0;                     // axis-aligned, integer endpoints: along hits 0 exactly
+        const double x0 = axis ? std::floor(pos(rng)) : pos(rng), y0 = axis ? std::floor(pos(rng)) : pos(rng);
+        const double len0 = 0.05 * std::pow(400.0, unit(rng)), a = axis ? 1.5707963267948966 * (rng() % 4) : ang(rng);
+        const double dx = axis ? std::round(len0 * std::cos(a)) + (std::cos(a) > 0.5 ? 1 : 0) : len0 * std::cos(a);
+        const double dy = axis ? std::round(len0 * std::sin(a)) : len0 * std::sin(a);
+        const double x1 = x0 + dx, y1 = y0 + dy;
+        double ax = x1 - x0, ay = y1 - y0;
+        const double len = std::sqrt(ax * ax + ay * ay);
+        if (!(len > 0.0)) continue;
+        ax /= len;
+        ay /= len;
+        const double pa = ang(rng);
+        double pax = std::cos(pa), pay = std::sin(pa);
+        const double plen = std::sqrt(pax * pax + pay * pay);
+        pax /= plen;
+        pay /= plen;
+        const bool cap_before = rng() % 3 == 0, cap_after = rng() % 3 == 0;
+        const AAClassF k{(float)x0, (float)y0, (float)ax, (float)ay, (float)len, (float)pax, (float)pay};
+        const long long xa = (long long)std::floor(std::fmin(x0, x1)) - 3, xb = (long long)std::ceil(std::fmax(x0, x1)) + 3;
+        const long long ya = (long long)std::floor(std::fmin(y0, y1)) - 3, yb = (long long)std::ceil(std::fmax(y0, y1)) + 3;
+        for (long long yy = ya; yy <= yb; ++yy)
+            for (long long xx = xa; xx <= xb; ++xx) {
+                if (xx < 0 || yy < 0) continue;
+                const double xd = (double)xx, yd = (double)yy;
+                const double along = (xd - x0) * ax + (yd - y0) * ay;
+                int want;
+                if (along < 0.0) want = (cap_before || (xd - x0) * pax + (yd - y0) * pay > 0.0) ? AAC_CAP_BEFORE : AAC_NONE;
+                else if (along > len) want = cap_after ? AAC_CAP_AFTER : AAC_NONE;
+                else want = AAC_SIDE;
+                const int got = aa_classify((unsigned)xx, (unsigned)yy, k, cap_before, cap_after);
+                n_pix += 1;
+                if (got == AAC_EXACT) continue;
+                n_dec += 1;
+                if (got != want) {
+                    std::printf("classify mismatch x=%lld y=%lld x0=%a y0=%a ax=%a ay=%a len=%a got %d want %d\n", xx, yy,
+                                x0, y0, ax, ay, len, got, want);
+                    return 1;
+                }
+            }
+    }
+    std::printf("ok %lld calls, %.4f float32-decided; %lld pixels, %.4f classified in float32\n", n_calls,
+                (double)n_fast / (double)n_calls, n_pix, (double)n_dec / (double)n_pix);
     return 0;
 }

@@ -4,7 +4,8 @@ operation it replaces over special values (signed zeros, subnormals, the
 largest finite, infinities, NaNs of both signs and several payloads) and
 random ones, and the uint32 -> float64 conversion against the C conversion.
 The scanline span ends decided by the float32 intercept (csrc/aa_scan.cuh)
-against the float64 intercept's ceil / floor."""
+against the float64 intercept's ceil / floor, and the float32 pixel
+classification of the queued line kernel against the float64 tests."""
 import os
 import shutil
 import subprocess
@@ -42,5 +43,6 @@ def _run_check(tmp_path, src):
 
 def test_aa_scan_span_matches_float64(tmp_path):
     out = _run_check(tmp_path, "aa_scan_check.cpp")
-    share = float(out.split()[-2])
+    share = float(out.split()[3])
     assert share > 0.5, out          # most scanline ends are decided in float32
+    assert float(out.split()[-4]) > 0.9, out    # and most pixels are classified in float32
