@@ -991,7 +991,7 @@ static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, in
             a.sx = p.sx; a.sy = p.sy; a.line_width = line_width;
             order = build_line_work_order(a, workspace, ws_bytes, st);
         }
-        if (order && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24)) {
+        if (order && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
             line_axis0_queued_kernel<<<(unsigned)((int64_t)sms * 2), 256, 0, st>>>(p, order);
         } else if (order) {
             line_axis0_ordered_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, order);

@@ -130,7 +130,9 @@ typedef struct {
 /* Flags. */
 #define DSGB_FLAG_NO_INIT      0x1u  /* accumulate into the bases as they are */
 #define DSGB_FLAG_NO_FINALIZE  0x2u  /* skip the finalize step */
-#define DSGB_FLAG_EXACT_BIN    0x4u  /* always bin in float64 (disable the float32 fast path) */
+#define DSGB_FLAG_EXACT_BIN    0x4u  /* always bin in float64 (disable the float32 fast path);
+                                       * dsgb_line_axis0_ws: antialiased pixels scanned per
+                                       * segment, without the float32 classification */
 #define DSGB_FLAG_WARP_AGG     0x8u  /* warp-level pre-aggregation of identical pixels */
 #define DSGB_FLAG_DETERMINISTIC 0x10u /* float64 sums in row order (bit-identical to the
                                          reference's CPU loop and run to run); needs the

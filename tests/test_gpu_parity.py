@@ -201,6 +201,38 @@ def test_line_aa_reductions_vs_oracle(agg_name):
             assert_same(g, r, what=str(k))
 
 
+@pytest.mark.parametrize("line_width", [1.5, 0.5, 3.0])
+def test_line_aa_queued_matches_per_segment_kernel(line_width):
+    """The antialiased forward with pixels classified in float32 and worked off
+    by case against the per-segment scan (DSGB_FLAG_EXACT_BIN): the same pixels
+    and coverage, float64 sums in another atomic order.  Time series, plus a
+    staircase of axis-aligned steps between pixel centres, where the along /
+    length and previous-direction tests meet their thresholds exactly."""
+    from datashader_gb300 import _native as N_
+    from datashader_gb300.core import gpu_pipeline
+    from datashader_gb300.glyphs import LineAxis0
+    cols = _series(30, 500, seed=7)
+    ylo, yhi = float(np.nanmin(cols["y"])), float(np.nanmax(cols["y"]))
+    k = np.arange(500)
+    px, py = 50 + (k + 1) // 2, 20 + k // 2          # unit steps right / up between pixel centres
+    stair = {"x": (px + 0.5) / 400.0, "y": ylo + (py + 0.5) * (yhi - ylo) / 300.0, "v": np.linspace(0.0, 1.0, k.size)}
+    cols = {c: np.concatenate([cols[c], [np.nan], stair[c]]) for c in cols}
+    frame = frame_from_numpy(cols)
+    cv = ds.Canvas(plot_width=400, plot_height=300, x_range=(0.0, 1.0), y_range=(ylo, yhi))
+    glyph = LineAxis0("x", "y")
+    glyph.set_line_width(line_width)
+    agg = ds.summary(c=ds.count(), s=ds.sum("v"), m=ds.max("v"))
+    a = to_numpy(gpu_pipeline(frame, cv, glyph, agg, antialias=True))
+    b = to_numpy(gpu_pipeline(frame, cv, glyph, agg, antialias=True, flags=N_.FLAG_EXACT_BIN))
+    assert_same(a["m"], b["m"], what="max")
+    for key in ("c", "s"):
+        if a[key].dtype == np.float32:     # float32 coverage sums: atomic order at float32 rounding
+            assert_same(a[key], b[key], rtol=3e-7, atol=1e-7, what=key)
+        else:
+            assert_same(a[key], b[key], rtol=RTOL_SUM, atol=1e-13, what=key)
+    assert np.nansum(a["c"]) > 1000
+
+
 def test_line_bresenham_vs_oracle():
     cols = _series(30, 500, seed=3)
     canvas = dict(plot_width=300, plot_height=150)
