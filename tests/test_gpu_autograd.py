@@ -141,8 +141,11 @@ def test_points_adjoint_vs_finite_differences(mean):
 
 def test_line_adjoint_work_order_matches_row_order():
     """The adjoint with a workspace recomputes segments in work order; without
-    one, in row order.  dL/dv is a plain store per segment (bit-identical);
-    dL/dy sums float64 atomics in another order (1e-12 relative)."""
+    one, in row order.  The pixels of a warp's 32 segments are worked off by
+    case, so a segment's dL/dv terms (float64) and its float32 tangent terms
+    are summed in an order that depends on its warp's other segments: equal
+    up to float64 rounding (dL/dv, 1e-12 relative) and float32 rounding of
+    the tangent sums (dL/dy, 1e-5 relative)."""
     import ctypes
     from datashader_gb300 import _native as N
     from datashader_gb300.autograd import _canvas_desc
@@ -174,8 +177,8 @@ def test_line_adjoint_work_order_matches_row_order():
                                                None, gv.data_ptr(), gy.data_ptr(), st), "dsgb_line_axis0_backward")
         out.append((gv.cpu().numpy(), gy.cpu().numpy()))
     (gv0, gy0), (gv1, gy1) = out
-    assert np.array_equal(gv0, gv1)
-    np.testing.assert_allclose(gy1, gy0, rtol=1e-12, atol=1e-12 * np.abs(gy0).max())
+    np.testing.assert_allclose(gv1, gv0, rtol=1e-12, atol=1e-12 * np.abs(gv0).max())
+    np.testing.assert_allclose(gy1, gy0, rtol=1e-5, atol=1e-6 * np.abs(gy0).max())
     assert np.abs(gv0).max() > 0 and np.abs(gy0).max() > 0
 
 
@@ -220,5 +223,7 @@ def test_line_adjoint_strided_inputs():
     Ys = big[:, 1].detach().requires_grad_(True)
     Vs = big[:, 2].detach().requires_grad_(True)
     (torch.nan_to_num(ag.line_sum(big[:, 0], Ys, Vs, cvs)) * w).sum().backward()
-    assert torch.equal(Vs.grad, V.grad)
-    torch.testing.assert_close(Ys.grad, Y.grad, rtol=1e-12, atol=1e-12 * float(Y.grad.abs().max()))
+    # the work order's ties fall by atomics, and a segment's dL/dv terms sum in
+    # an order set by its warp's other segments: equal up to rounding
+    torch.testing.assert_close(Vs.grad, V.grad, rtol=1e-12, atol=1e-12 * float(V.grad.abs().max()))
+    torch.testing.assert_close(Ys.grad, Y.grad, rtol=1e-5, atol=1e-6 * float(Y.grad.abs().max()))
