@@ -66,11 +66,26 @@ F64CMP_FN bool aa_x_intercept_f32(unsigned y, double cx0, double cy0, double cx1
     return dist > bound;                                  // false for NaN
 }
 
+// The float64 fallback, out of line on the device (OUT_OF_LINE): it runs for
+// about one scanline end in a hundred, and inlined twice into a scan loop it
+// costs instruction-cache room; where the call's register saves cost more
+// (the adjoint's dual-number loop spills around it), it stays inline.
+#if defined(__CUDACC__)
+#define AA_COLD_FN __host__ __device__ __noinline__
+#else
+#define AA_COLD_FN inline
+#endif
+template <bool CEIL>
+AA_COLD_FN long long aa_scan_bound_f64(double yd, double cx0, double cy0, double cx1, double cy1, long long hi) {
+    const double x = aa_x_intercept(yd, cx0, cy0, cx1, cy1);
+    return CEIL ? f64_ceil_clamp(x, hi) : f64_floor_clamp(x, hi);
+}
+
 // max(0, min(ceil(x), hi)) (CEIL) or max(0, min(floor(x), hi)) of the
 // intercept x, for hi < 2^31 and y < 2^31: integer operations for a
 // horizontal edge, the float32 intercept when it is decisive, the float64
 // expression otherwise.
-template <bool CEIL>
+template <bool CEIL, bool OUT_OF_LINE = false>
 F64CMP_FN long long aa_scan_bound(unsigned y, double yd, double cx0, double cy0, double cx1, double cy1,
                                   long long hi) {
     if (f64_eq(cy0, cy1)) return CEIL ? f64_ceil_clamp(cx1, hi) : f64_floor_clamp(cx1, hi);
@@ -80,6 +95,7 @@ F64CMP_FN long long aa_scan_bound(unsigned y, double yd, double cx0, double cy0,
         c = c < hi ? c : hi;
         return c > 0 ? c : 0;
     }
+    if (OUT_OF_LINE) return aa_scan_bound_f64<CEIL>(yd, cx0, cy0, cx1, cy1, hi);
     const double x = aa_x_intercept(yd, cx0, cy0, cx1, cy1);
     return CEIL ? f64_ceil_clamp(x, hi) : f64_floor_clamp(x, hi);
 }

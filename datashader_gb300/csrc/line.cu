@@ -699,9 +699,9 @@ __global__ void __launch_bounds__(256, 1) line_axis0_queued_kernel(const LinePar
                 const double yd = f64_from_u32((unsigned)cy);
                 if (ll == lowindex && f64_nonneg_gt(yd, pick4(lu, by0, by1, by2, by3))) { ll = lu; lu = (ll + 1) % 4; }
                 if (rl == lowindex && f64_nonneg_gt(yd, pick4(ru, by0, by1, by2, by3))) { rl = ru; ru = (rl + 3) % 4; }
-                cx = aa_scan_bound<true>((unsigned)cy, yd, pick4(ll, bx0, bx1, bx2, bx3), pick4(ll, by0, by1, by2, by3),
+                cx = aa_scan_bound<true, true>((unsigned)cy, yd, pick4(ll, bx0, bx1, bx2, bx3), pick4(ll, by0, by1, by2, by3),
                                          pick4(lu, bx0, bx1, bx2, bx3), pick4(lu, by0, by1, by2, by3), xmaxi);
-                cxr = aa_scan_bound<false>((unsigned)cy, yd, pick4(rl, bx0, bx1, bx2, bx3), pick4(rl, by0, by1, by2, by3),
+                cxr = aa_scan_bound<false, true>((unsigned)cy, yd, pick4(rl, bx0, bx1, bx2, bx3), pick4(rl, by0, by1, by2, by3),
                                            pick4(ru, bx0, bx1, bx2, bx3), pick4(ru, by0, by1, by2, by3), xmaxi);
             }
             if (kind != AAK_NONE) {
