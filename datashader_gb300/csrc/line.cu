@@ -592,7 +592,7 @@ __device__ __forceinline__ unsigned long long aa_item(long long x, long long y, 
 
 enum { AAK_NONE = 0, AAK_CAP = 1, AAK_SIDE = 2, AAK_EXACT = 3 };
 
-__global__ void __launch_bounds__(256, 1) line_axis0_queued_kernel(const LineParams p, const unsigned *order) {
+__global__ void __launch_bounds__(256, 3) line_axis0_queued_kernel(const LineParams p, const unsigned *order) {
     __shared__ AASeg seg_s[8][32];
     __shared__ unsigned long long q_s[8][3][AAQ_CAP];
     const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
@@ -992,7 +992,7 @@ static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, in
             order = build_line_work_order(a, workspace, ws_bytes, st);
         }
         if (order && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
-            line_axis0_queued_kernel<<<(unsigned)((int64_t)sms * 2), 256, 0, st>>>(p, order);
+            line_axis0_queued_kernel<<<(unsigned)((int64_t)sms * 3), 256, 0, st>>>(p, order);   // three blocks an SM (80 registers)
         } else if (order) {
             line_axis0_ordered_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, order);
         } else {
