@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(256, 3) line_axis0_queued_kernel(const LinePar
         double bx0 = 0, bx1 = 0, bx2 = 0, bx3 = 0, by0 = 0, by1 = 0, by2 = 0, by3 = 0;
         AAClassF kf = AAClassF{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (k < nseg) {
-            const int64_t i = order[k];
+            const int64_t i = order ? (int64_t)order[k] : k;   // no order: row order
             double x0 = load_f64(X, i), y0 = load_f64(Y, i);
             double x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
             const int64_t im = i > 0 ? i - 1 : p.n - 1;
@@ -991,7 +991,10 @@ static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, in
             a.sx = p.sx; a.sy = p.sy; a.line_width = line_width;
             order = build_line_work_order(a, workspace, ws_bytes, st);
         }
-        if (order && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
+        // antialiased: pixels queued by case, segments in work order when the
+        // workspace holds it (else in row order); canvases past 2^24 pixels a
+        // side, or DSGB_FLAG_EXACT_BIN, scan per segment
+        if (line_width > 0.0 && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
             line_axis0_queued_kernel<<<(unsigned)((int64_t)sms * 3), 256, 0, st>>>(p, order);   // three blocks an SM (80 registers)
         } else if (order) {
             line_axis0_ordered_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, order);

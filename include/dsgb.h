@@ -268,7 +268,9 @@ int dsgb_combine(const dsgb_base *dst, const dsgb_base *src, int32_t nbases, int
 /* ---- Canvas.line, LineAxis0 glyph ----------------------------------------
  * Replaces line.py:59-103 + 1033-1149.  line_width == 0 draws Bresenham
  * lines, > 0 antialiased lines; overwrite / use_2_stage_agg follow
- * antialias.py:30-58 (two_stage_agg) for the reductions in `bases`. */
+ * antialias.py:30-58 (two_stage_agg) for the reductions in `bases`.
+ * Antialiased pixels are classified in float32 and worked off by case
+ * (segments in row order here, in work order with dsgb_line_axis0_ws). */
 int dsgb_line_axis0(const dsgb_column *cols, int32_t ncols, int64_t n, int64_t row_offset,
                     int32_t x_col, int32_t y_col, const dsgb_canvas *canvas,
                     double line_width, int32_t plot_start, int32_t overwrite,

@@ -233,6 +233,52 @@ def test_line_aa_queued_matches_per_segment_kernel(line_width):
     assert np.nansum(a["c"]) > 1000
 
 
+def test_line_aa_without_workspace_matches_workspace():
+    """dsgb_line_axis0 without a workspace draws the segments in row order
+    (the queued scan without the work order); with one, in work order: the
+    same pixels and coverage, float sums in another atomic order."""
+    import ctypes
+    from datashader_gb300 import _native as N_
+    from datashader_gb300.autograd import _canvas_desc
+    from datashader_gb300.compiler import compile_plan
+    from datashader_gb300.core import Executor
+    from datashader_gb300.glyphs import LineAxis0
+    cols = _series(25, 400, seed=13)
+    frame = frame_from_numpy(cols)
+    ylo, yhi = float(np.nanmin(cols["y"])), float(np.nanmax(cols["y"]))
+    cv = ds.Canvas(plot_width=300, plot_height=200, x_range=(0.0, 1.0), y_range=(ylo, yhi))
+    cd = _canvas_desc(cv, cv.x_range, cv.y_range)
+    glyph = LineAxis0("x", "y")
+    glyph.set_line_width(1.5)
+    agg = ds.summary(c=ds.count(), s=ds.sum("v"), m=ds.max("v"))
+    L = N_.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    n = len(frame)
+    got = []
+    for with_ws in (False, True):
+        plan = compile_plan(agg, frame, antialias=True)
+        ex = Executor(frame, plan, glyph)
+        ex.allocate(200, 300, torch.device("cuda"))
+        args = (ex.cols, len(ex.names), n, 0, 0, 1, ctypes.byref(cd), 1.5, 1, int(plan.overwrite),
+                int(plan.use_2_stage), ex.bases, len(plan.bases), ex.outs, ex.nouts)
+        if with_ws:
+            wsz = int(L.dsgb_line_workspace_size(n))
+            ws = torch.empty(wsz, dtype=torch.uint8, device="cuda")
+            N_.check(L.dsgb_line_axis0_ws(*args, ws.data_ptr(), wsz, 0, st), "dsgb_line_axis0_ws")
+        else:
+            N_.check(L.dsgb_line_axis0(*args, 0, st), "dsgb_line_axis0")
+        torch.cuda.synchronize()
+        got.append([t.cpu().numpy().copy() for t in ex.out_tensors])
+    for a, b in zip(*got):
+        if a.dtype == np.float32:
+            assert_same(a, b, rtol=3e-7, atol=1e-7)
+        elif a.dtype.kind == "f":
+            assert_same(a, b, rtol=RTOL_SUM, atol=1e-13)
+        else:
+            assert_same(a, b)
+    assert sum(float(np.nansum(a)) for a in got[0]) > 0
+
+
 def test_line_bresenham_vs_oracle():
     cols = _series(30, 500, seed=3)
     canvas = dict(plot_width=300, plot_height=150)
