@@ -464,6 +464,14 @@ __global__ void __launch_bounds__(256, 1) line_axis0_ordered_kernel(const LinePa
     }
 }
 
+// The vertex arrays of the multi-line layouts (see lines_kernel below).
+struct LinesGeom {
+    const double *xs, *ys;
+    int64_t nrows, nv;      // LAYOUT 1: nv = lines; LAYOUT 2: nv = vertices per line
+    int64_t xrow, yrow;     // LAYOUT 2: row strides of xs and ys (0 = shared by all rows)
+    int64_t only_line;      // >= 0: draw this line alone (two-stage plans); -1: every line
+};
+
 // ---- antialiased LineAxis0, pixels queued by case.  In the kernels above a
 // warp's 32 segments scan their pixels together, and each pixel takes one of
 // three float64 paths (before the segment, after it, beside it) or none, so
@@ -569,6 +577,7 @@ __device__ __forceinline__ double2 aa_pixel_side(const AAConsts &c, const AASeg 
 
 // One queue item of kind `which` (0 cap, 1 side, 2 exact), appended when its
 // value is positive: the queue drains share this one append site.
+template <bool KEYED>
 __device__ __forceinline__ void aa_item_work(const LineParams &p, const AAConsts &c, const AASeg *segs, int which,
                                              unsigned long long it) {
     const AASeg &S = segs[(it >> 48) & 31u];
@@ -579,7 +588,7 @@ __device__ __forceinline__ void aa_item_work(const LineParams &p, const AAConsts
     else v = aa_pixel_exact(c, S, x, y);
     if (f64_gt0(v.x)) {
         const bool flip = S.flags & AAF_FLIP;
-        line_append<false>(p, S.row, flip ? y : x, flip ? x : y, v.x, v.y);
+        line_append<KEYED>(p, S.row, flip ? y : x, flip ? x : y, v.x, v.y);
     }
 }
 
@@ -592,7 +601,12 @@ __device__ __forceinline__ unsigned long long aa_item(long long x, long long y, 
 
 enum { AAK_NONE = 0, AAK_CAP = 1, AAK_SIDE = 2, AAK_EXACT = 3 };
 
-__global__ void __launch_bounds__(256, 3) line_axis0_queued_kernel(const LineParams p, const unsigned *order) {
+// SRC 0: LineAxis0 rows (line_axis0_kernel's segments, in `order` or row
+// order); SRC 1 / 2: the multi-line layouts of lines_kernel (every line),
+// KEYED appends carrying LineAxis0Multi's visit keys.
+template <int SRC, bool KEYED>
+__global__ void __launch_bounds__(256, 3) aa_queued_kernel(const LineParams p, const unsigned *order, const LinesGeom g,
+                                                           const int64_t nseg) {
     __shared__ AASeg seg_s[8][32];
     __shared__ unsigned long long q_s[8][3][AAQ_CAP];
     const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
@@ -601,7 +615,6 @@ __global__ void __launch_bounds__(256, 3) line_axis0_queued_kernel(const LinePar
     AASeg *segs = seg_s[warp];
     unsigned long long *qcap = q_s[warp][0], *qside = q_s[warp][1], *qexact = q_s[warp][2];
     const AAConsts c = aa_consts(p.line_width);
-    const int64_t nseg = p.n - 1;
     const int64_t nbatches = (nseg + 31) / 32;
     const int64_t warps_total = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; b < nbatches; b += warps_total) {
@@ -614,15 +627,38 @@ __global__ void __launch_bounds__(256, 3) line_axis0_queued_kernel(const LinePar
         double bx0 = 0, bx1 = 0, bx2 = 0, bx3 = 0, by0 = 0, by1 = 0, by2 = 0, by3 = 0;
         AAClassF kf = AAClassF{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (k < nseg) {
-            const int64_t i = order ? (int64_t)order[k] : k;   // no order: row order
-            double x0 = load_f64(X, i), y0 = load_f64(Y, i);
-            double x1 = load_f64(X, i + 1), y1 = load_f64(Y, i + 1);
-            const int64_t im = i > 0 ? i - 1 : p.n - 1;
-            bool segment_start = (i == 0) ? (p.plot_start != 0)
-                                          : (isnull(load_f64(X, im)) || isnull(load_f64(Y, im)));
-            const bool segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
-            double xm = 0.0, ym = 0.0;
-            if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, im); ym = load_f64(Y, im); }
+            // the segment, its neighbours' NaN tests and its previous vertex,
+            // as line_axis0_kernel / lines_kernel read them
+            int64_t i;                                       // the append key (row, or visit key)
+            double x0, y0, x1, y1, xm = 0.0, ym = 0.0;
+            bool segment_start, segment_end;
+            if (SRC == 0) {
+                i = order ? (int64_t)order[k] : k;           // no order: row order
+                x0 = load_f64(X, i); y0 = load_f64(Y, i);
+                x1 = load_f64(X, i + 1); y1 = load_f64(Y, i + 1);
+                const int64_t im = i > 0 ? i - 1 : p.n - 1;
+                segment_start = (i == 0) ? (p.plot_start != 0) : (isnull(load_f64(X, im)) || isnull(load_f64(Y, im)));
+                segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
+                if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, im); ym = load_f64(Y, im); }
+            } else if (SRC == 1) {                           // line j down the rows (line.py:1152-1242)
+                const int64_t r = k / g.nv, j = k - r * g.nv;
+                const double *Xp = g.xs + j, *Yp = g.ys + j;
+                const int64_t st = g.nv;
+                x0 = Xp[r * st]; y0 = Yp[r * st]; x1 = Xp[(r + 1) * st]; y1 = Yp[(r + 1) * st];
+                const int64_t rm = r > 0 ? r - 1 : g.nrows - 1;
+                segment_start = (r == 0) ? (p.plot_start != 0) : (isnull(Xp[rm * st]) || isnull(Yp[rm * st]));
+                segment_end = (r == g.nrows - 2) || isnull(Xp[(r + 2) * st]) || isnull(Yp[(r + 2) * st]);
+                if (!(segment_start || p.use_2_stage)) { xm = Xp[rm * st]; ym = Yp[rm * st]; }
+                i = KEYED ? j * p.field_mod + r : r;        // line j's appends after lines 0 .. j-1
+            } else {                                         // row r along its vertices (line.py:1244-1437)
+                const int64_t r = k / (g.nv - 1), j = k - r * (g.nv - 1);
+                const double *Xp = g.xs + r * g.xrow, *Yp = g.ys + r * g.yrow;
+                x0 = Xp[j]; x1 = Xp[j + 1]; y0 = Yp[j]; y1 = Yp[j + 1];
+                segment_start = (j == 0) || isnull(Xp[j - 1]) || isnull(Yp[j - 1]);
+                segment_end = (j == g.nv - 2) || isnull(Xp[j + 2]) || isnull(Yp[j + 2]);
+                if (!(segment_start || p.use_2_stage)) { xm = Xp[j - 1]; ym = Yp[j - 1]; }
+                i = r;
+            }
             bool skip = isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1);
             bool cs = false, ce = false;
             liang_barsky(p.xmin, p.xmax, p.ymin, p.ymax, x0, x1, y0, y1, skip, cs, ce);
@@ -737,7 +773,7 @@ __global__ void __launch_bounds__(256, 3) line_axis0_queued_kernel(const LinePar
                 const int take = cnt < 32 ? cnt : 32;
                 const int from = cnt - take;
                 if (which == 0) ncap = from; else if (which == 1) nside = from; else nexact = from;
-                if (lane < take) aa_item_work(p, c, segs, which, q_s[warp][which][from + lane]);
+                if (lane < take) aa_item_work<KEYED>(p, c, segs, which, q_s[warp][which][from + lane]);
             }
             __syncwarp();
         }
@@ -755,12 +791,6 @@ __global__ void __launch_bounds__(256, 3) line_axis0_queued_kernel(const LinePar
 //       segment (i, j) appends row i; a segment starts at j == 0 or after a
 //       NaN.
 // Consecutive threads take consecutive array elements (coalesced loads).
-struct LinesGeom {
-    const double *xs, *ys;
-    int64_t nrows, nv;      // LAYOUT 1: nv = lines; LAYOUT 2: nv = vertices per line
-    int64_t xrow, yrow;     // LAYOUT 2: row strides of xs and ys (0 = shared by all rows)
-    int64_t only_line;      // >= 0: draw this line alone (two-stage plans); -1: every line
-};
 
 template <int LAYOUT>
 __global__ void __launch_bounds__(256, 1) lines_kernel(const LineParams p, const LinesGeom g) {
@@ -995,7 +1025,8 @@ static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, in
         // workspace holds it (else in row order); canvases past 2^24 pixels a
         // side, or DSGB_FLAG_EXACT_BIN, scan per segment
         if (line_width > 0.0 && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
-            line_axis0_queued_kernel<<<(unsigned)((int64_t)sms * 3), 256, 0, st>>>(p, order);   // three blocks an SM (80 registers)
+            // three blocks an SM (80 registers)
+            aa_queued_kernel<0, false><<<(unsigned)((int64_t)sms * 3), 256, 0, st>>>(p, order, LinesGeom{}, n - 1);
         } else if (order) {
             line_axis0_ordered_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, order);
         } else {
@@ -1054,8 +1085,17 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
         if (sms <= 0) sms = 148;
         int64_t blocks = (nseg + 255) / 256;
         if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
-        if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(p, g);
-        else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(p, g);
+        if (line_width > 0.0 && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
+            // antialiased: pixels queued by case (the LineAxis0 kernel's machinery)
+            const unsigned qblocks = (unsigned)((int64_t)sms * 3);
+            if (layout == 2) aa_queued_kernel<2, false><<<qblocks, 256, 0, st>>>(p, nullptr, g, nseg);
+            else if (p.field_mod > 0) aa_queued_kernel<1, true><<<qblocks, 256, 0, st>>>(p, nullptr, g, nseg);
+            else aa_queued_kernel<1, false><<<qblocks, 256, 0, st>>>(p, nullptr, g, nseg);
+        } else if (layout == 1) {
+            lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(p, g);
+        } else {
+            lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(p, g);
+        }
         DSGB_CHECK_LAUNCH("lines kernel");
     }
     if (p.field_mod > 0) {

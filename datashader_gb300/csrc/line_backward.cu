@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(256, 1) line_backward_kernel(const BwdParams p
     }
 }
 
-// ---- the adjoint with pixels queued by case (as line_axis0_queued_kernel):
+// ---- the adjoint with pixels queued by case (as aa_queued_kernel, line.cu):
 // each lane scans its segment and classifies the pixels in float32
 // (aa_classify, the value's float64 tests reproduced), the warp works off its
 // per-case queues 32 pixels at a time with every lane on one dual-number
