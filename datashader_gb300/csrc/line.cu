@@ -464,7 +464,13 @@ __global__ void __launch_bounds__(256, 1) line_axis0_ordered_kernel(const LinePa
     }
 }
 
-// The vertex arrays of the multi-line layouts (see lines_kernel below).
+// The vertex arrays of the multi-line layouts and of ragged rows (see
+// lines_kernel and lines_ragged_kernel below).
+struct RaggedGeom {
+    const double *xf, *yf;
+    const int64_t *xs, *ys;
+    int64_t nrows, nx, ny;
+};
 struct LinesGeom {
     const double *xs, *ys;
     int64_t nrows, nv;      // LAYOUT 1: nv = lines; LAYOUT 2: nv = vertices per line
@@ -603,10 +609,11 @@ enum { AAK_NONE = 0, AAK_CAP = 1, AAK_SIDE = 2, AAK_EXACT = 3 };
 
 // SRC 0: LineAxis0 rows (line_axis0_kernel's segments, in `order` or row
 // order); SRC 1 / 2: the multi-line layouts of lines_kernel (every line),
-// KEYED appends carrying LineAxis0Multi's visit keys.
+// KEYED appends carrying LineAxis0Multi's visit keys; SRC 3: ragged rows
+// (lines_ragged_kernel's segments, one a flat x vertex, `rg`).
 template <int SRC, bool KEYED>
 __global__ void __launch_bounds__(256, 3) aa_queued_kernel(const LineParams p, const unsigned *order, const LinesGeom g,
-                                                           const int64_t nseg) {
+                                                           const RaggedGeom rg, const int64_t nseg) {
     __shared__ AASeg seg_s[8][32];
     __shared__ unsigned long long q_s[8][3][AAQ_CAP];
     const ColumnRef X = p.cols[p.x_col], Y = p.cols[p.y_col];
@@ -629,9 +636,9 @@ __global__ void __launch_bounds__(256, 3) aa_queued_kernel(const LineParams p, c
         if (k < nseg) {
             // the segment, its neighbours' NaN tests and its previous vertex,
             // as line_axis0_kernel / lines_kernel read them
-            int64_t i;                                       // the append key (row, or visit key)
-            double x0, y0, x1, y1, xm = 0.0, ym = 0.0;
-            bool segment_start, segment_end;
+            int64_t i = 0;                                   // the append key (row, or visit key)
+            double x0 = 0.0, y0 = 0.0, x1 = 0.0, y1 = 0.0, xm = 0.0, ym = 0.0;
+            bool segment_start = false, segment_end = false, have_seg = true;
             if (SRC == 0) {
                 i = order ? (int64_t)order[k] : k;           // no order: row order
                 x0 = load_f64(X, i); y0 = load_f64(Y, i);
@@ -650,6 +657,28 @@ __global__ void __launch_bounds__(256, 3) aa_queued_kernel(const LineParams p, c
                 segment_end = (r == g.nrows - 2) || isnull(Xp[(r + 2) * st]) || isnull(Yp[(r + 2) * st]);
                 if (!(segment_start || p.use_2_stage)) { xm = Xp[rm * st]; ym = Yp[rm * st]; }
                 i = KEYED ? j * p.field_mod + r : r;        // line j's appends after lines 0 .. j-1
+            } else if (SRC == 3) {                           // ragged row (line.py:1538-1612)
+                int64_t lo = 0, hi = rg.nrows - 1;
+                while (lo < hi) {
+                    const int64_t mid = (lo + hi + 1) >> 1;
+                    if (rg.xs[mid] <= k) lo = mid; else hi = mid - 1;
+                }
+                const bool last = lo == rg.nrows - 1;
+                const int64_t xa = min(max(rg.xs[lo], (int64_t)0), rg.nx);
+                const int64_t xb = max(min(last ? rg.nx : rg.xs[lo + 1], rg.nx), xa);
+                const int64_t ya = min(max(rg.ys[lo], (int64_t)0), rg.ny);
+                const int64_t yb = max(min(last ? rg.ny : rg.ys[lo + 1], rg.ny), ya);
+                const int64_t len = min(xb - xa, yb - ya);
+                const int64_t j = k - xa;
+                have_seg = j >= 0 && j + 1 < len;
+                if (have_seg) {
+                    const double *Xp = rg.xf + xa, *Yp = rg.yf + ya;
+                    x0 = Xp[j]; y0 = Yp[j]; x1 = Xp[j + 1]; y1 = Yp[j + 1];
+                    segment_start = (j == 0) || isnull(Xp[j - 1]) || isnull(Yp[j - 1]);
+                    segment_end = (j == len - 2) || isnull(Xp[j + 2]) || isnull(Yp[j + 2]);
+                    if (!(segment_start || p.use_2_stage)) { xm = Xp[j - 1]; ym = Yp[j - 1]; }
+                }
+                i = lo;
             } else {                                         // row r along its vertices (line.py:1244-1437)
                 const int64_t r = k / (g.nv - 1), j = k - r * (g.nv - 1);
                 const double *Xp = g.xs + r * g.xrow, *Yp = g.ys + r * g.yrow;
@@ -659,7 +688,7 @@ __global__ void __launch_bounds__(256, 3) aa_queued_kernel(const LineParams p, c
                 if (!(segment_start || p.use_2_stage)) { xm = Xp[j - 1]; ym = Yp[j - 1]; }
                 i = r;
             }
-            bool skip = isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1);
+            bool skip = !have_seg || isnull(x0) || isnull(y0) || isnull(x1) || isnull(y1);
             bool cs = false, ce = false;
             liang_barsky(p.xmin, p.xmax, p.ymin, p.ymax, x0, x1, y0, y1, skip, cs, ce);
             segment_start = segment_start || cs;
@@ -832,11 +861,6 @@ __global__ void __launch_bounds__(256, 1) lines_kernel(const LineParams p, const
 // thread per flat x vertex finds its row by bisection over the starts (non-
 // decreasing); the slices are clamped to the arrays, so malformed starts
 // cannot read outside them.
-struct RaggedGeom {
-    const double *xf, *yf;
-    const int64_t *xs, *ys;
-    int64_t nrows, nx, ny;
-};
 
 __global__ void __launch_bounds__(256, 1) lines_ragged_kernel(const LineParams p, const RaggedGeom g) {
     for (int64_t k = gtid(); k < g.nx; k += gstride()) {
@@ -1026,7 +1050,8 @@ static int line_axis0_impl(const dsgb_column *cols, int32_t ncols, int64_t n, in
         // side, or DSGB_FLAG_EXACT_BIN, scan per segment
         if (line_width > 0.0 && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
             // three blocks an SM (80 registers)
-            aa_queued_kernel<0, false><<<(unsigned)((int64_t)sms * 3), 256, 0, st>>>(p, order, LinesGeom{}, n - 1);
+            aa_queued_kernel<0, false><<<(unsigned)((int64_t)sms * 3), 256, 0, st>>>(p, order, LinesGeom{}, RaggedGeom{},
+                                                                                     n - 1);
         } else if (order) {
             line_axis0_ordered_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, order);
         } else {
@@ -1088,9 +1113,9 @@ extern "C" int dsgb_lines(const dsgb_column *cols, int32_t ncols, int64_t nrows,
         if (line_width > 0.0 && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
             // antialiased: pixels queued by case (the LineAxis0 kernel's machinery)
             const unsigned qblocks = (unsigned)((int64_t)sms * 3);
-            if (layout == 2) aa_queued_kernel<2, false><<<qblocks, 256, 0, st>>>(p, nullptr, g, nseg);
-            else if (p.field_mod > 0) aa_queued_kernel<1, true><<<qblocks, 256, 0, st>>>(p, nullptr, g, nseg);
-            else aa_queued_kernel<1, false><<<qblocks, 256, 0, st>>>(p, nullptr, g, nseg);
+            if (layout == 2) aa_queued_kernel<2, false><<<qblocks, 256, 0, st>>>(p, nullptr, g, RaggedGeom{}, nseg);
+            else if (p.field_mod > 0) aa_queued_kernel<1, true><<<qblocks, 256, 0, st>>>(p, nullptr, g, RaggedGeom{}, nseg);
+            else aa_queued_kernel<1, false><<<qblocks, 256, 0, st>>>(p, nullptr, g, RaggedGeom{}, nseg);
         } else if (layout == 1) {
             lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(p, g);
         } else {
@@ -1374,7 +1399,14 @@ extern "C" int dsgb_lines_ragged(const dsgb_column *cols, int32_t ncols, int64_t
         if (rc) return rc;
     }
     if (nrows > 0 && nx > 1 && nbases > 0) {
-        lines_ragged_kernel<<<grid_of(nx), 256, 0, st>>>(p, g);
+        if (p.line_width > 0.0 && p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN)) {
+            // antialiased: pixels queued by case (one segment a flat x vertex)
+            int sms = sm_count();
+            if (sms <= 0) sms = 148;
+            aa_queued_kernel<3, false><<<(unsigned)((int64_t)sms * 3), 256, 0, st>>>(p, nullptr, LinesGeom{}, g, nx);
+        } else {
+            lines_ragged_kernel<<<grid_of(nx), 256, 0, st>>>(p, g);
+        }
         DSGB_CHECK_LAUNCH("lines ragged kernel");
     }
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
