@@ -648,7 +648,8 @@ __global__ void __launch_bounds__(256, 3) aa_queued_kernel(const LineParams p, c
                 segment_end = (i == p.n - 2) || isnull(load_f64(X, i + 2)) || isnull(load_f64(Y, i + 2));
                 if (!(segment_start || p.use_2_stage)) { xm = load_f64(X, im); ym = load_f64(Y, im); }
             } else if (SRC == 1) {                           // line j down the rows (line.py:1152-1242)
-                const int64_t r = k / g.nv, j = k - r * g.nv;
+                const bool one = g.only_line >= 0;           // one line alone (two-stage plans)
+                const int64_t r = one ? k : k / g.nv, j = one ? g.only_line : k - r * g.nv;
                 const double *Xp = g.xs + j, *Yp = g.ys + j;
                 const int64_t st = g.nv;
                 x0 = Xp[r * st]; y0 = Yp[r * st]; x1 = Xp[(r + 1) * st]; y1 = Yp[(r + 1) * st];
@@ -680,7 +681,8 @@ __global__ void __launch_bounds__(256, 3) aa_queued_kernel(const LineParams p, c
                 }
                 i = lo;
             } else {                                         // row r along its vertices (line.py:1244-1437)
-                const int64_t r = k / (g.nv - 1), j = k - r * (g.nv - 1);
+                const bool one = g.only_line >= 0;
+                const int64_t r = one ? g.only_line : k / (g.nv - 1), j = one ? k : k - r * (g.nv - 1);
                 const double *Xp = g.xs + r * g.xrow, *Yp = g.ys + r * g.yrow;
                 x0 = Xp[j]; x1 = Xp[j + 1]; y0 = Yp[j]; y1 = Yp[j + 1];
                 segment_start = (j == 0) || isnull(Xp[j - 1]) || isnull(Yp[j - 1]);
@@ -1316,11 +1318,23 @@ extern "C" int dsgb_lines_2stage(const dsgb_column *cols, int32_t ncols, int64_t
     int64_t blocks = (nseg + 255) / 256;
     if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
     if (blocks < 1) blocks = 1;
+    // antialiased (always, in a two-stage plan): pixels queued by case, one
+    // line a launch, the grid sized to the line's 32-segment batches
+    const bool queued = p.aa_nx <= (1 << 24) && p.aa_ny <= (1 << 24) && !(flags & DSGB_FLAG_EXACT_BIN);
+    int64_t qblocks = ((nseg + 31) / 32 + 7) / 8;
+    if (qblocks > (int64_t)sms * 3) qblocks = (int64_t)sms * 3;
+    if (qblocks < 1) qblocks = 1;
     rc = run_two_stage(p, bases, nbases, folds, line_aggs, nseg > 0 ? (layout == 1 ? nv : nrows) : 0, ncells, st,
                        [&](const LineParams &pp, int64_t L) {
                            g.only_line = L;
-                           if (layout == 1) lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(pp, g);
-                           else lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(pp, g);
+                           if (queued && layout == 1)
+                               aa_queued_kernel<1, false><<<(unsigned)qblocks, 256, 0, st>>>(pp, nullptr, g, RaggedGeom{}, nseg);
+                           else if (queued)
+                               aa_queued_kernel<2, false><<<(unsigned)qblocks, 256, 0, st>>>(pp, nullptr, g, RaggedGeom{}, nseg);
+                           else if (layout == 1)
+                               lines_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(pp, g);
+                           else
+                               lines_kernel<2><<<(unsigned)blocks, 256, 0, st>>>(pp, g);
                        });
     if (rc) return rc;
     if (!(flags & DSGB_FLAG_NO_FINALIZE) && nouts > 0)
